@@ -1,0 +1,165 @@
+/*
+ * C-ABI of the GB300 query hot path for RhyDB/SILO sequence tables.
+ *
+ * The entry points replace the reference's filter / count / mutations path:
+ *   rhy_table_from_raw   ingestion of a partition: SequenceColumn::appendChunk + finalize
+ *                        (src/rhydb/storage/column/sequence_column.cpp:100-212) and the
+ *                        dictionary / date columns the metadata leaves read;
+ *   rhy_open             upload of the partition image to HBM (no reference counterpart: the
+ *                        reference evaluates on host memory);
+ *   rhy_plan             ScalarExpression::rewrite(table, NONE) + compile(table)
+ *                        (src/rhydb/query_engine/scalar_expressions/scalar_expression.h:81-90);
+ *   rhy_eval             computeFilter (src/rhydb/query_engine/operators/compute_filter.cpp:14-21)
+ *                        = Database::getFilteredBitmap (src/rhydb/database.cpp:259-283);
+ *   rhy_count            CountFilterNode (src/rhydb/query_engine/operators/count_filter_node.cpp:35-71);
+ *   rhy_mutations        calculateMutationsPerPosition
+ *                        (src/rhydb/query_engine/operators/mutations_node.cpp:269-288);
+ *   rhy_mutation_rows    addMutationsToOutput (mutations_node.cpp:292-366);
+ *   rhy_count_batch /
+ *   rhy_mutations_batch  many queries per launch (no reference counterpart: the reference runs one
+ *                        query per worker thread, app/src/api.cpp:39-51).
+ *
+ * Conventions: every function returns RHY_OK (0) or an error code and never throws; the message
+ * of the last error on the calling thread is returned by rhy_last_error(). Output buffers are
+ * owned by the caller. Calls on one device handle are serialised by the handle; `stream` is a
+ * cudaStream_t or NULL for the handle's own stream. Row sets are dense bitmaps: chunk k (2^16
+ * rows, global row ids k << 16 ...) occupies 2048 uint32 words.
+ */
+#ifndef RHYDB_GPU_H
+#define RHYDB_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+   RHY_OK = 0,
+   RHY_ILLEGAL_QUERY = 1,   /* IllegalQueryException in the reference */
+   RHY_COMPILATION = 2,     /* QueryCompilationException in the reference */
+   RHY_CUDA = 3,
+   RHY_INVALID_ARGUMENT = 4,
+   RHY_INTERNAL = 5
+};
+
+typedef struct RhyTable RhyTable;
+typedef struct RhyDevice RhyDevice;
+
+/* Raw input: each aligned sequence is the column's reference with sorted, non-overlapping runs
+ * (pos, len, char) applied; missing symbols (N / X) inside runs become coverage information. */
+typedef struct {
+   const char* name;
+   int kind;                 /* 0 = nucleotide, 1 = amino acid */
+   const char* reference;    /* L characters */
+   uint32_t L;
+   const uint8_t* is_null;   /* n_rows */
+   const uint64_t* row_off;  /* n_rows + 1 */
+   const uint32_t* run_pos;
+   const uint32_t* run_len;
+   const char* run_char;
+} RhyRawSeqColumn;
+
+typedef struct {
+   const char* name;
+   uint32_t n_values;
+   const char* const* values; /* dictionary */
+   const uint32_t* ids;       /* n_rows, UINT32_MAX = null */
+} RhyRawDictColumn;
+
+typedef struct {
+   const char* name;
+   const int32_t* days;       /* n_rows, INT32_MIN = null */
+} RhyRawDateColumn;
+
+typedef struct {
+   uint32_t n_rows;
+   uint32_t n_seq, n_dict, n_date;
+   const RhyRawSeqColumn* seq;
+   const RhyRawDictColumn* dict;
+   const RhyRawDateColumn* date;
+} RhyRawTable;
+
+typedef struct {
+   uint64_t seed;
+   uint32_t n_rows;
+   uint32_t genome_len;
+   uint32_t pool_sites;
+   uint32_t n_aa_genes;      /* 0 or 12 (9,700 aa) */
+   double null_fraction;
+   uint32_t threads;         /* 0 = all hardware threads */
+} RhyGenConfig;
+
+typedef struct {
+   uint32_t n_rows;
+   uint32_t n_chunks;
+   uint32_t n_seq, n_dict, n_date;
+} RhyTableInfo;
+
+typedef struct {
+   uint32_t L;
+   uint32_t n_symbols;
+   uint32_t kind;
+   uint32_t flipped_positions;
+   uint64_t n_containers;
+   uint64_t payload_bytes;
+   uint64_t n_array, n_bitset, n_run;
+   uint64_t n_missing_intervals;
+   uint64_t n_coverage_exceptions;
+   uint64_t n_null_rows;
+} RhySeqColumnInfo;
+
+typedef struct {
+   uint32_t position;        /* 1-based */
+   char from;                /* global reference symbol */
+   char to;
+   uint32_t count;
+   uint32_t coverage;        /* total over the valid mutation symbols */
+   double proportion;
+} RhyMutationRow;
+
+const char* rhy_last_error(void);
+
+/* ---- tables (host) ---- */
+int rhy_generate(const RhyGenConfig* cfg, RhyTable** out);
+int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out);
+int rhy_table_info(const RhyTable* t, RhyTableInfo* out);
+int rhy_seq_column_info(const RhyTable* t, uint32_t column, RhySeqColumnInfo* out);
+int rhy_seq_column_name(const RhyTable* t, uint32_t column, char* buf, size_t cap);
+/* Views of the raw input of a generated table (valid until rhy_table_free). */
+int rhy_table_raw(const RhyTable* t, RhyRawTable* out);
+/* Local reference symbols (after adaptation) as characters, L bytes. */
+int rhy_local_reference(const RhyTable* t, uint32_t column, char* out, size_t cap);
+/* Vertical-index containers of a column in storage order (chunk, position, symbol): position,
+ * chunk, symbol, cardinality and encoding (0 array, 1 bitset, 2 run). Pass cap = 0 to size. */
+int rhy_seq_containers(const RhyTable* t, uint32_t column, uint32_t* pos, uint16_t* chunk, uint8_t* sym, uint32_t* card,
+                       uint8_t* type, size_t cap, size_t* n);
+/* Newline-separated seeded random filter expressions; *needed receives the byte count (incl. NUL). */
+int rhy_generate_queries(const RhyTable* t, uint64_t seed, uint32_t n, uint32_t max_depth, uint32_t max_nof_children,
+                         int use_aa, int use_metadata, char* buf, size_t cap, size_t* needed);
+void rhy_table_free(RhyTable* t);
+
+/* ---- planning ---- */
+/* Operator tree of rewrite(NONE) + compile as text, and the device program length / stack depth. */
+int rhy_plan(const RhyTable* t, const char* expr, char* tree_buf, size_t cap, uint32_t* n_instr, uint32_t* depth);
+
+/* ---- device ---- */
+int rhy_open(const RhyTable* t, int device, RhyDevice** out);
+int rhy_set_tile_bits(RhyDevice* d, uint32_t tile_bits);
+int rhy_device_bytes(const RhyDevice* d, uint64_t* out);
+int rhy_count(RhyDevice* d, const char* expr, void* stream, uint64_t* out);
+/* out_bits: n_chunks * 2048 words (may be NULL); out_count may be NULL. */
+int rhy_eval(RhyDevice* d, const char* expr, void* stream, uint32_t* out_bits, uint64_t* out_count);
+/* counts: n_symbols * L words, counts[symbol * L + position]; filter_count may be NULL. */
+int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream, uint32_t* counts, uint64_t* filter_count);
+/* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */
+int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,
+                      RhyMutationRow* rows, size_t cap, size_t* n_rows);
+void rhy_close(RhyDevice* d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RHYDB_GPU_H */

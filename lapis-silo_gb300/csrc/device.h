@@ -1,0 +1,106 @@
+// Device-resident table image and the kernel launch interface.
+//
+// HBM layout of one partition (all arrays written once at open and read-only afterwards):
+//   sequence column: container descriptors (16 B, sorted by chunk, position, symbol), a u16
+//   payload arena (arrays, 8 KiB bitsets on 16-byte boundaries, run pairs), the (chunk, position)
+//   offset table, per-chunk coverage exceptions, missing-interval buckets per 128-position block,
+//   a dense null-row bitmap (8 KiB per chunk) and the local reference;
+//   dictionary column: the inverted index in the same container format, keyed by value id;
+//   date column: one int32 per row (chunk stride 2^16).
+// Row sets are dense bitmaps of 2^16 bits (8 KiB) per chunk.
+#pragma once
+
+#include <cstdint>
+
+#include "program.h"
+#include "table.h"
+
+namespace rhygpu {
+
+constexpr int MAX_SEQ_COLS = 32;
+constexpr int MAX_DICT_COLS = 8;
+constexpr int MAX_DATE_COLS = 8;
+
+struct DevSeqCol {
+   const CtrDesc* ctrs;
+   const uint16_t* payload;
+   const uint32_t* off;        // nchunks * L + 1
+   const CovExc* exc;
+   const uint32_t* exc_off;    // nchunks + 1
+   const NRunEntry* nblk;
+   const uint32_t* nblk_off;   // nblocks * nchunks + 1
+   const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
+   const uint8_t* local_ref;   // L
+   uint32_t L;
+   uint32_t nblocks;
+   uint32_t nsym;
+   uint32_t nctrs;
+};
+
+struct DevDictCol {
+   const CtrDesc* ctrs;
+   const uint16_t* payload;
+   const uint32_t* off;        // nchunks * nkeys + 1
+   uint32_t nkeys;
+   uint32_t pad;
+};
+
+struct DevDateCol {
+   const int32_t* days;        // nchunks * CHUNK_ROWS
+};
+
+struct DevTable {
+   uint32_t nchunks;
+   uint32_t n_rows;
+   const uint32_t* chunk_sizes;
+   DevSeqCol seq[MAX_SEQ_COLS];
+   DevDictCol dict[MAX_DICT_COLS];
+   DevDateCol date[MAX_DATE_COLS];
+};
+
+// A slice of one column's containers for the mutations pass: containers [begin, end) of chunk v.
+struct MutPart {
+   uint32_t v;
+   uint32_t begin;
+   uint32_t end;
+   uint32_t pad;
+};
+
+// One unit of the batched filter kernel: tile `tile` of query `query`.
+struct WorkItem {
+   uint32_t query;
+   uint32_t tile;
+};
+
+struct QueryDesc {
+   uint32_t code_off;     // offset of the program in the shared instruction buffer
+   uint32_t code_len;
+   uint32_t out_tiles;    // 1 = write the row set to the query's output tiles
+   uint32_t pad;
+};
+
+// ---- launchers (kernels.cu) ----
+// tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth.
+void launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode, uint32_t tile_bits,
+                   uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count, int* d_err, void* stream);
+
+// Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.
+void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
+                         const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
+                         uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
+                         uint32_t* d_next, uint32_t grid, int* d_err, void* stream);
+
+// Mutations. counts: nsym * L u32 (zeroed by the caller). scratch: 3 * (L + 1) u32 (zeroed by the caller).
+// The filter count decides on the device between the full path (|F| == rows: stored cardinalities),
+// the empty path and the mixed path, so no host round trip sits between filter and mutations.
+void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
+                      const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filter,
+                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream);
+
+// Batched mutations over nq filters (query-major dense tiles), counts[q][nsym][L].
+void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
+                            const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filters, uint32_t nq,
+                            const unsigned long long* d_filter_counts, uint32_t* d_counts, uint32_t* d_scratch,
+                            void* stream);
+
+}  // namespace rhygpu

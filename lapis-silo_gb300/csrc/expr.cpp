@@ -1,0 +1,1028 @@
+// Expression parsing, rewrite, compile and lowering (see expr.h).
+#include "expr.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <map>
+
+namespace rhygpu {
+
+// =============================================================================================
+// Expression basics
+
+ExprPtr Expr::clone() const {
+   auto e = std::make_unique<Expr>();
+   e->kind = kind;
+   for (const auto& c : children) e->children.push_back(c->clone());
+   e->column = column;
+   e->pos = pos;
+   e->sym = sym;
+   e->symmask = symmask;
+   e->n = n;
+   e->exact = exact;
+   e->value = value;
+   e->has_from = has_from;
+   e->has_to = has_to;
+   e->from = from;
+   e->to = to;
+   e->truth = truth;
+   e->sym_kind = sym_kind;
+   return e;
+}
+
+std::string Expr::to_string() const {
+   auto join = [&](const char* name) {
+      std::string s = name;
+      s += "(";
+      for (size_t i = 0; i < children.size(); ++i) {
+         if (i) s += ",";
+         s += children[i]->to_string();
+      }
+      return s + ")";
+   };
+   const Alphabet& A = alphabet(sym_kind);
+   switch (kind) {
+      case EK::AND: return join("And");
+      case EK::OR: return join("Or");
+      case EK::NOT: return "Not(" + children[0]->to_string() + ")";
+      case EK::MAYBE: return "Maybe(" + children[0]->to_string() + ")";
+      case EK::EXACT: return "Exact(" + children[0]->to_string() + ")";
+      case EK::NOF: {
+         std::string s = "NOf(" + std::to_string(n) + (exact ? ",exactly" : ",atleast");
+         for (const auto& c : children) s += "," + c->to_string();
+         return s + ")";
+      }
+      case EK::SYM_EQ:
+         return "SymEq(" + column + "," + std::to_string(pos + 1) + "," + (sym < 0 ? '.' : A.chars[sym]) + ")";
+      case EK::HAS_MUT: return "HasMut(" + column + "," + std::to_string(pos + 1) + ")";
+      case EK::SYM_IN_SET: {
+         std::string s = "SymInSet(" + column + "," + std::to_string(pos + 1) + ",";
+         for (uint32_t i = 0; i < A.count; ++i)
+            if (symmask >> i & 1) s += A.chars[i];
+         return s + ")";
+      }
+      case EK::STR_EQ: return "StrEq(" + column + "," + value + ")";
+      case EK::DATE_BETWEEN:
+         return "DateBetween(" + column + "," + (has_from ? std::to_string(from) : "*") + "," +
+                (has_to ? std::to_string(to) : "*") + ")";
+      case EK::BOOL: return truth ? "True" : "False";
+   }
+   return "?";
+}
+
+// =============================================================================================
+// Parser
+
+namespace {
+
+struct Parser {
+   const std::string& s;
+   const TableImage& t;
+   size_t i = 0;
+
+   [[noreturn]] void fail(const std::string& msg) const {
+      throw IllegalQuery("cannot parse expression at offset " + std::to_string(i) + ": " + msg);
+   }
+   void ws() {
+      while (i < s.size() && std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+   }
+   bool eat(char c) {
+      ws();
+      if (i < s.size() && s[i] == c) {
+         ++i;
+         return true;
+      }
+      return false;
+   }
+   void expect(char c) {
+      if (!eat(c)) fail(std::string("expected '") + c + "'");
+   }
+   std::string token() {
+      ws();
+      size_t b = i;
+      while (i < s.size() && s[i] != ',' && s[i] != '(' && s[i] != ')' && !std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+      if (b == i) fail("expected a token");
+      return s.substr(b, i - b);
+   }
+   long long integer() {
+      const std::string tok = token();
+      try {
+         size_t used = 0;
+         long long v = std::stoll(tok, &used);
+         if (used != tok.size()) fail("expected an integer, got '" + tok + "'");
+         return v;
+      } catch (const std::logic_error&) {
+         fail("expected an integer, got '" + tok + "'");
+      }
+   }
+   uint32_t position() {
+      const long long p = integer();
+      if (p < 1 || p > 0xFFFFFFFFll) fail("positions are 1-based");
+      return static_cast<uint32_t>(p - 1);
+   }
+
+   ExprPtr node(EK k) {
+      auto e = std::make_unique<Expr>();
+      e->kind = k;
+      return e;
+   }
+
+   void seq_column(Expr& e) {
+      e.column = token();
+      const int c = t.find_seq(e.column);
+      if (c < 0) throw IllegalQuery("the database does not contain the sequence column '" + e.column + "'");
+      e.sym_kind = t.seq[c].kind;
+   }
+
+   ExprPtr parse() {
+      const std::string name = token();
+      if (name == "True" || name == "False") {
+         auto e = node(EK::BOOL);
+         e->truth = name == "True";
+         return e;
+      }
+      expect('(');
+      ExprPtr e;
+      if (name == "And" || name == "Or") {
+         e = node(name == "And" ? EK::AND : EK::OR);
+         if (!eat(')')) {
+            do {
+               e->children.push_back(parse());
+            } while (eat(','));
+            expect(')');
+         }
+         return e;
+      }
+      if (name == "Not" || name == "Maybe" || name == "Exact") {
+         e = node(name == "Not" ? EK::NOT : name == "Maybe" ? EK::MAYBE : EK::EXACT);
+         e->children.push_back(parse());
+      } else if (name == "NOf") {
+         e = node(EK::NOF);
+         const long long n = integer();
+         if (n < -1000000 || n > 1000000) fail("NOf count out of range");
+         e->n = static_cast<int>(n);
+         expect(',');
+         const std::string mode = token();
+         if (mode != "exactly" && mode != "atleast") fail("NOf mode must be exactly or atleast");
+         e->exact = mode == "exactly";
+         while (eat(',')) e->children.push_back(parse());
+      } else if (name == "SymEq") {
+         e = node(EK::SYM_EQ);
+         seq_column(*e);
+         expect(',');
+         e->pos = position();
+         expect(',');
+         const std::string c = token();
+         if (c.size() != 1) fail("a symbol is a single character");
+         if (c[0] == '.') {
+            e->sym = -1;
+         } else {
+            e->sym = alphabet(e->sym_kind).sym(c[0]);
+            if (e->sym < 0) throw IllegalQuery("illegal symbol '" + c + "' for column " + e->column);
+         }
+      } else if (name == "HasMut") {
+         e = node(EK::HAS_MUT);
+         seq_column(*e);
+         expect(',');
+         e->pos = position();
+      } else if (name == "StrEq") {
+         e = node(EK::STR_EQ);
+         e->column = token();
+         expect(',');
+         e->value = token();
+      } else if (name == "DateBetween") {
+         e = node(EK::DATE_BETWEEN);
+         e->column = token();
+         expect(',');
+         if (eat('*')) {
+            e->has_from = false;
+         } else {
+            e->has_from = true;
+            e->from = static_cast<int32_t>(integer());
+         }
+         expect(',');
+         if (eat('*')) {
+            e->has_to = false;
+         } else {
+            e->has_to = true;
+            e->to = static_cast<int32_t>(integer());
+         }
+      } else {
+         fail("unknown function '" + name + "'");
+      }
+      expect(')');
+      return e;
+   }
+};
+
+}  // namespace
+
+ExprPtr parse_expression(const std::string& text, const TableImage& table) {
+   Parser p{text, table};
+   ExprPtr e = p.parse();
+   p.ws();
+   if (p.i != text.size()) p.fail("trailing characters");
+   return e;
+}
+
+// =============================================================================================
+// Rewrite (reference: and.cpp:154-162, or.cpp:173-192, negation.cpp:27-30, nof.cpp:217-257,
+// maybe.cpp:28-33, exact.cpp:28-33, symbol_equals.cpp:65-93, has_mutation.cpp:34-68)
+
+namespace {
+
+Ambiguity invert(Ambiguity m) {
+   if (m == Ambiguity::UPPER_BOUND) return Ambiguity::LOWER_BOUND;
+   if (m == Ambiguity::LOWER_BOUND) return Ambiguity::UPPER_BOUND;
+   return m;
+}
+
+const SeqColumnImage& seq_col(const TableImage& t, const std::string& name) {
+   const int c = t.find_seq(name);
+   if (c < 0) throw IllegalQuery("the database does not contain the sequence column '" + name + "'");
+   return t.seq[c];
+}
+
+}  // namespace
+
+ExprPtr rewrite(const Expr& e, const TableImage& t, Ambiguity mode) {
+   switch (e.kind) {
+      case EK::AND: {
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::AND;
+         for (const auto& c : e.children) out->children.push_back(rewrite(*c, t, mode));
+         return out;
+      }
+      case EK::OR: {
+         // collectChildren: flatten nested Or through a LIFO queue (or.cpp:26-57)
+         std::vector<const Expr*> collected, queue;
+         for (const auto& c : e.children) queue.push_back(c.get());
+         while (!queue.empty()) {
+            const Expr* cur = queue.back();
+            queue.pop_back();
+            if (cur->kind == EK::OR) {
+               for (const auto& c : cur->children) queue.push_back(c.get());
+            } else {
+               collected.push_back(cur);
+            }
+         }
+         std::vector<ExprPtr> rewritten;
+         for (const Expr* c : collected) rewritten.push_back(rewrite(*c, t, mode));
+         // algebraicSimplification (or.cpp:66-90)
+         std::vector<ExprPtr> non_trivial;
+         while (!rewritten.empty()) {
+            ExprPtr child = std::move(rewritten.back());
+            rewritten.pop_back();
+            if (child->kind == EK::BOOL) {
+               if (child->truth) {
+                  std::vector<ExprPtr> only;
+                  auto tr = std::make_unique<Expr>();
+                  tr->kind = EK::BOOL;
+                  tr->truth = true;
+                  only.push_back(std::move(tr));
+                  non_trivial = std::move(only);
+                  break;
+               }
+               continue;
+            }
+            if (child->kind == EK::OR) {
+               for (auto& g : child->children) rewritten.push_back(std::move(g));
+            } else {
+               non_trivial.push_back(std::move(child));
+            }
+         }
+         // merge SymbolInSet children per (column, position), nucleotide then amino acid (or.cpp:92-116)
+         for (SymKind kind : {SymKind::NUC, SymKind::AA}) {
+            std::vector<ExprPtr> next;
+            std::map<std::pair<std::string, uint32_t>, uint32_t> merged;
+            for (auto& c : non_trivial) {
+               if (c->kind == EK::SYM_IN_SET && c->sym_kind == kind) {
+                  merged[{c->column, c->pos}] |= c->symmask;
+               } else {
+                  next.push_back(std::move(c));
+               }
+            }
+            for (const auto& [key, mask] : merged) {
+               auto s = std::make_unique<Expr>();
+               s->kind = EK::SYM_IN_SET;
+               s->column = key.first;
+               s->pos = key.second;
+               s->symmask = mask;
+               s->sym_kind = kind;
+               next.push_back(std::move(s));
+            }
+            non_trivial = std::move(next);
+         }
+         if (non_trivial.size() == 1) return std::move(non_trivial[0]);
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::OR;
+         out->children = std::move(non_trivial);
+         return out;
+      }
+      case EK::NOT: {
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::NOT;
+         out->children.push_back(rewrite(*e.children[0], t, invert(mode)));
+         return out;
+      }
+      case EK::MAYBE: return rewrite(*e.children[0], t, Ambiguity::UPPER_BOUND);
+      case EK::EXACT: return rewrite(*e.children[0], t, Ambiguity::LOWER_BOUND);
+      case EK::NOF: {
+         auto rewrite_children = [&]() {
+            std::vector<ExprPtr> v;
+            for (const auto& c : e.children) v.push_back(rewrite(*c, t, mode));
+            return v;
+         };
+         if (mode != Ambiguity::NONE && e.exact && (e.n < 0 || static_cast<size_t>(e.n) < e.children.size())) {
+            auto at_least_k = std::make_unique<Expr>();
+            at_least_k->kind = EK::NOF;
+            at_least_k->children = rewrite_children();
+            at_least_k->n = e.n;
+            at_least_k->exact = false;
+            auto at_least_k1 = std::make_unique<Expr>();
+            at_least_k1->kind = EK::NOF;
+            at_least_k1->children = rewrite_children();
+            at_least_k1->n = e.n + 1;
+            at_least_k1->exact = false;
+            auto neg = std::make_unique<Expr>();
+            neg->kind = EK::NOT;
+            neg->children.push_back(std::move(at_least_k1));
+            auto out = std::make_unique<Expr>();
+            out->kind = EK::AND;
+            out->children.push_back(std::move(at_least_k));
+            out->children.push_back(std::move(neg));
+            return out;
+         }
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::NOF;
+         out->n = e.n;
+         out->exact = e.exact;
+         out->children = rewrite_children();
+         return out;
+      }
+      case EK::SYM_EQ: {
+         const SeqColumnImage& col = seq_col(t, e.column);
+         if (e.pos >= col.L)
+            throw IllegalQuery("SymbolEquals position is out of bounds " + std::to_string(e.pos + 1) + " > " + std::to_string(col.L));
+         const uint32_t symbol = e.sym < 0 ? col.global_ref[e.pos] : static_cast<uint32_t>(e.sym);
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::SYM_IN_SET;
+         out->column = e.column;
+         out->pos = e.pos;
+         out->sym_kind = col.kind;
+         out->symmask = mode == Ambiguity::UPPER_BOUND ? alphabet(col.kind).ambiguity[symbol] : (1u << symbol);
+         return out;
+      }
+      case EK::HAS_MUT: {
+         const SeqColumnImage& col = seq_col(t, e.column);
+         if (e.pos >= col.L)
+            throw IllegalQuery("HasMutation position is out of bounds " + std::to_string(e.pos + 1) + " > " + std::to_string(col.L));
+         const Alphabet& A = alphabet(col.kind);
+         const uint32_t ref = col.global_ref[e.pos];
+         uint32_t mask = A.all_mask;
+         if (mode == Ambiguity::UPPER_BOUND) {
+            mask &= ~(1u << ref);
+         } else {
+            mask &= ~A.ambiguity[ref];
+         }
+         auto out = std::make_unique<Expr>();
+         out->kind = EK::SYM_IN_SET;
+         out->column = e.column;
+         out->pos = e.pos;
+         out->sym_kind = col.kind;
+         out->symmask = mask;
+         return out;
+      }
+      case EK::SYM_IN_SET:
+         throw CompilationError("Cannot rewrite SymbolInSet - this expression should only be created during query rewrites");
+      case EK::STR_EQ:
+         if (t.find_dict(e.column) < 0) throw IllegalQuery("the database does not contain the indexed string column '" + e.column + "'");
+         return e.clone();
+      case EK::DATE_BETWEEN:
+         if (t.find_date(e.column) < 0) throw IllegalQuery("the database does not contain the date column '" + e.column + "'");
+         return e.clone();
+      case EK::BOOL: return e.clone();
+   }
+   throw CompilationError("unknown expression kind");
+}
+
+// =============================================================================================
+// Operators
+
+Pred Pred::negated() const {
+   Pred p = *this;
+   if (kind == COVERED) {
+      p.covered = !covered;
+      return p;
+   }
+   // reference: selection.h:127-157 (the comparator flips and nulls flip)
+   switch (cmp) {
+      case CMP_EQ: p.cmp = CMP_NE; break;
+      case CMP_NE: p.cmp = CMP_EQ; break;
+      case CMP_LT: p.cmp = CMP_GE; break;
+      case CMP_GE: p.cmp = CMP_LT; break;
+      case CMP_GT: p.cmp = CMP_LE; break;
+      case CMP_LE: p.cmp = CMP_GT; break;
+   }
+   p.with_nulls = !with_nulls;
+   return p;
+}
+
+namespace {
+
+OpPtr mk(OpT t) {
+   auto o = std::make_unique<Op>();
+   o->t = t;
+   return o;
+}
+OpPtr complement_of(OpPtr c) {
+   auto o = mk(OpT::COMPLEMENT);
+   o->children.push_back(std::move(c));
+   return o;
+}
+OpPtr intersection_of(std::vector<OpPtr> pos, std::vector<OpPtr> neg) {
+   // reference: intersection.cpp:18-41
+   if (pos.empty()) throw CompilationError("Compilation bug: Intersection without non-negated children is not allowed.");
+   if (pos.size() + neg.size() < 2) throw CompilationError("Compilation bug: Intersection needs at least two children.");
+   auto o = mk(OpT::INTERSECTION);
+   o->children = std::move(pos);
+   o->negated = std::move(neg);
+   return o;
+}
+OpPtr union_of(std::vector<OpPtr> c) {
+   auto o = mk(OpT::UNION);
+   o->children = std::move(c);
+   return o;
+}
+OpPtr scan_of(Leaf l) {
+   auto o = mk(OpT::INDEX_SCAN);
+   o->leaf = l;
+   return o;
+}
+OpPtr selection_of(OpPtr child, std::vector<Pred> preds) {
+   auto o = mk(OpT::SELECTION);
+   if (child) o->children.push_back(std::move(child));
+   o->preds = std::move(preds);
+   return o;
+}
+OpPtr threshold_of(std::vector<OpPtr> pos, std::vector<OpPtr> neg, int n, bool exact) {
+   // reference: threshold.cpp:18-41
+   if (static_cast<size_t>(n) >= pos.size() + neg.size())
+      throw CompilationError("Compilation Error: number_of_matchers must be less than the number of children of a threshold expression");
+   if (n == 0) throw CompilationError("Compilation Error: number_of_matchers must be greater than zero");
+   auto o = mk(OpT::THRESHOLD);
+   o->children = std::move(pos);
+   o->negated = std::move(neg);
+   o->n = n;
+   o->exact = exact;
+   return o;
+}
+
+// reference: symbol_in_set.cpp:105-264
+OpPtr compile_symbol_in_set(const TableImage& t, const Expr& e) {
+   const int ci = t.find_seq(e.column);
+   if (ci < 0) throw IllegalQuery("the database does not contain the sequence column '" + e.column + "'");
+   const SeqColumnImage& col = t.seq[ci];
+   if (e.pos >= col.L)
+      throw IllegalQuery("SymbolInSet position is out of bounds " + std::to_string(e.pos + 1) + " > " + std::to_string(col.L));
+   const Alphabet& A = alphabet(col.kind);
+   const uint32_t local_ref = col.local_ref[e.pos];
+   const bool has_ref = e.symmask >> local_ref & 1;
+   const bool has_missing = e.symmask >> A.missing & 1;
+   auto scan = [&](uint32_t mask) {
+      Leaf l;
+      l.kind = Leaf::SEQ;
+      l.col = ci;
+      l.pos = e.pos;
+      l.symmask = mask & A.all_mask;
+      return scan_of(l);
+   };
+   auto exclude_nulls = [&](OpPtr op) {
+      if (col.null_rows.empty()) return op;
+      Leaf l;
+      l.kind = Leaf::NULLS;
+      l.col = ci;
+      std::vector<OpPtr> pos, neg;
+      pos.push_back(std::move(op));
+      neg.push_back(scan_of(l));
+      return intersection_of(std::move(pos), std::move(neg));
+   };
+   Pred covered;
+   covered.kind = Pred::COVERED;
+   covered.col = ci;
+   covered.pos = e.pos;
+   if (has_ref && has_missing) {
+      return exclude_nulls(complement_of(scan(A.all_mask & ~e.symmask)));
+   }
+   if (has_missing) {
+      covered.covered = false;
+      std::vector<OpPtr> u;
+      u.push_back(selection_of(nullptr, {covered}));
+      u.push_back(scan(e.symmask));
+      return exclude_nulls(union_of(std::move(u)));
+   }
+   if (has_ref) {
+      covered.covered = true;
+      std::vector<OpPtr> pos, neg;
+      pos.push_back(selection_of(nullptr, {covered}));
+      neg.push_back(scan(A.all_mask & ~e.symmask & ~(1u << A.missing)));
+      return intersection_of(std::move(pos), std::move(neg));
+   }
+   return scan(e.symmask);
+}
+
+// NOf helpers (reference: nof.cpp:33-150)
+OpPtr nof_trivial(int n, std::vector<OpPtr>& pos, std::vector<OpPtr>& neg, bool exact) {
+   const int k = static_cast<int>(pos.size() + neg.size());
+   if (n > k) return mk(OpT::EMPTY);
+   if (n < 0) return exact ? mk(OpT::EMPTY) : mk(OpT::FULL);
+   if (n == 0) {
+      if (!exact) return mk(OpT::FULL);
+      if (k == 0) return mk(OpT::FULL);
+      if (k == 1) {
+         if (pos.empty()) return std::move(neg[0]);
+         return complement_of(std::move(pos[0]));
+      }
+      if (neg.empty()) return complement_of(union_of(std::move(pos)));
+      return intersection_of(std::move(neg), std::move(pos));
+   }
+   if (n == 1 && k == 1) {
+      if (neg.empty()) return std::move(pos[0]);
+      return complement_of(std::move(neg[0]));
+   }
+   return nullptr;
+}
+
+OpPtr nof_to_operator(int n, std::vector<OpPtr> pos, std::vector<OpPtr> neg, bool exact) {
+   if (OpPtr tmp = nof_trivial(n, pos, neg, exact)) return tmp;
+   const int k = static_cast<int>(pos.size() + neg.size());
+   if (n == k) {
+      if (pos.empty()) return complement_of(union_of(std::move(neg)));
+      return intersection_of(std::move(pos), std::move(neg));
+   }
+   if (n == 1 && !exact) {
+      if (neg.empty()) return union_of(std::move(pos));
+      return complement_of(intersection_of(std::move(neg), std::move(pos)));
+   }
+   return threshold_of(std::move(pos), std::move(neg), n, exact);
+}
+
+}  // namespace
+
+OpPtr negate(OpPtr op) {
+   switch (op->t) {
+      case OpT::EMPTY: return mk(OpT::FULL);
+      case OpT::FULL: return mk(OpT::EMPTY);
+      case OpT::COMPLEMENT: return std::move(op->children[0]);
+      case OpT::SELECTION:
+         if (op->children.empty() && op->preds.size() == 1) return selection_of(nullptr, {op->preds[0].negated()});
+         return complement_of(std::move(op));
+      default: return complement_of(std::move(op));
+   }
+}
+
+OpPtr compile(const Expr& e, const TableImage& t) {
+   switch (e.kind) {
+      case EK::AND: {
+         // reference: and.cpp:91-219
+         std::vector<OpPtr> unprocessed, pos, neg;
+         std::vector<Pred> preds;
+         for (const auto& c : e.children) unprocessed.push_back(compile(*c, t));
+         while (!unprocessed.empty()) {
+            OpPtr child = std::move(unprocessed.back());
+            unprocessed.pop_back();
+            if (child->t == OpT::FULL) continue;
+            if (child->t == OpT::EMPTY) return mk(OpT::EMPTY);
+            if (child->t == OpT::INTERSECTION) {
+               for (auto& g : child->children) pos.push_back(std::move(g));
+               for (auto& g : child->negated) neg.push_back(std::move(g));
+            } else if (child->t == OpT::COMPLEMENT) {
+               neg.push_back(negate(std::move(child)));
+            } else if (child->t == OpT::SELECTION) {
+               for (const auto& p : child->preds) preds.push_back(p);
+               if (!child->children.empty()) unprocessed.push_back(std::move(child->children[0]));
+            } else {
+               pos.push_back(std::move(child));
+            }
+         }
+         if (pos.empty() && neg.empty()) {
+            if (preds.empty()) return mk(OpT::FULL);
+            return selection_of(nullptr, std::move(preds));
+         }
+         OpPtr op;
+         if (pos.size() == 1 && neg.empty()) {
+            op = std::move(pos[0]);
+         } else if (neg.size() == 1 && pos.empty()) {
+            op = complement_of(std::move(neg[0]));
+         } else if (pos.empty()) {
+            op = complement_of(union_of(std::move(neg)));
+         } else {
+            op = intersection_of(std::move(pos), std::move(neg));
+         }
+         if (preds.empty()) return op;
+         return selection_of(std::move(op), std::move(preds));
+      }
+      case EK::OR: {
+         // reference: or.cpp:194-241
+         std::vector<OpPtr> filtered;
+         for (const auto& c : e.children) {
+            OpPtr child = compile(*c, t);
+            if (child->t == OpT::EMPTY) continue;
+            if (child->t == OpT::FULL) return mk(OpT::FULL);
+            if (child->t == OpT::UNION) {
+               for (auto& g : child->children) filtered.push_back(std::move(g));
+            } else {
+               filtered.push_back(std::move(child));
+            }
+         }
+         if (filtered.empty()) return mk(OpT::EMPTY);
+         if (filtered.size() == 1) return std::move(filtered[0]);
+         const bool any_complement =
+            std::any_of(filtered.begin(), filtered.end(), [](const OpPtr& o) { return o->t == OpT::COMPLEMENT; });
+         if (any_complement) {
+            // Complement::fromDeMorgan (complement.cpp:23-39)
+            std::vector<OpPtr> pos, neg;
+            for (auto& c : filtered) {
+               if (c->t == OpT::COMPLEMENT) {
+                  neg.push_back(negate(std::move(c)));
+               } else {
+                  pos.push_back(std::move(c));
+               }
+            }
+            return complement_of(intersection_of(std::move(neg), std::move(pos)));
+         }
+         return union_of(std::move(filtered));
+      }
+      case EK::NOT: return negate(compile(*e.children[0], t));
+      case EK::NOF: {
+         // reference: nof.cpp:183-215, 259-277
+         std::vector<OpPtr> pos, neg;
+         int n = e.n;
+         for (const auto& c : e.children) {
+            OpPtr child = compile(*c, t);
+            if (child->t == OpT::EMPTY) continue;
+            if (child->t == OpT::FULL) {
+               --n;
+               continue;
+            }
+            if (child->t == OpT::COMPLEMENT) {
+               neg.push_back(negate(std::move(child)));
+               continue;
+            }
+            pos.push_back(std::move(child));
+         }
+         if (n < 0) return e.exact ? mk(OpT::EMPTY) : mk(OpT::FULL);
+         return nof_to_operator(n, std::move(pos), std::move(neg), e.exact);
+      }
+      case EK::SYM_IN_SET: return compile_symbol_in_set(t, e);
+      case EK::STR_EQ: {
+         // reference: equals.cpp:174-187 (indexed string column -> IndexScan of the inverted index)
+         const int ci = t.find_dict(e.column);
+         if (ci < 0) throw IllegalQuery("the database does not contain the indexed string column '" + e.column + "'");
+         const DictColumnImage& d = t.dict[ci];
+         auto it = d.index.find(e.value);
+         if (it == d.index.end()) return mk(OpT::EMPTY);
+         bool any = false;
+         for (uint32_t v = 0; v < t.nchunks() && !any; ++v) {
+            const size_t slot = static_cast<size_t>(v) * d.inverted.nkeys + it->second;
+            any = d.inverted.off[slot + 1] > d.inverted.off[slot];
+         }
+         if (!any) return mk(OpT::EMPTY);
+         Leaf l;
+         l.kind = Leaf::DICT;
+         l.col = ci;
+         l.value = it->second;
+         return scan_of(l);
+      }
+      case EK::DATE_BETWEEN: {
+         // reference: date_between.cpp:61-89 (unsorted column -> Selection with two comparisons)
+         const int ci = t.find_date(e.column);
+         if (ci < 0) throw IllegalQuery("the database does not contain the date column '" + e.column + "'");
+         Pred lo, hi;
+         lo.kind = hi.kind = Pred::DATE;
+         lo.col = hi.col = ci;
+         lo.cmp = CMP_GE;
+         lo.value = e.has_from ? e.from : INT32_MIN;
+         hi.cmp = CMP_LE;
+         hi.value = e.has_to ? e.to : INT32_MAX;
+         return selection_of(nullptr, {lo, hi});
+      }
+      case EK::BOOL: return mk(e.truth ? OpT::FULL : OpT::EMPTY);
+      case EK::SYM_EQ: throw CompilationError("SymbolEquals should have been rewritten before compilation");
+      case EK::HAS_MUT: throw CompilationError("HasMutation expression must be eliminated in query rewrite phase");
+      case EK::MAYBE: throw CompilationError("Maybe expression must be elimitated in query rewrite phase");
+      case EK::EXACT: throw CompilationError("Exact expression must be elimitated in query rewrite phase");
+   }
+   throw CompilationError("unknown expression kind");
+}
+
+std::string Op::to_string() const {
+   auto list = [](const std::vector<OpPtr>& v) {
+      std::string s;
+      for (size_t i = 0; i < v.size(); ++i) {
+         if (i) s += ",";
+         s += v[i]->to_string();
+      }
+      return s;
+   };
+   switch (t) {
+      case OpT::EMPTY: return "Empty";
+      case OpT::FULL: return "Full";
+      case OpT::INDEX_SCAN:
+         if (leaf.kind == Leaf::SEQ) return "Scan(" + std::to_string(leaf.col) + "," + std::to_string(leaf.pos + 1) + ",0x" + [&] {
+                   char b[16];
+                   std::snprintf(b, sizeof b, "%x", leaf.symmask);
+                   return std::string(b);
+                }() + ")";
+         if (leaf.kind == Leaf::NULLS) return "Nulls(" + std::to_string(leaf.col) + ")";
+         return "Dict(" + std::to_string(leaf.col) + "," + std::to_string(leaf.value) + ")";
+      case OpT::INTERSECTION: return "Intersection(" + list(children) + ";not:" + list(negated) + ")";
+      case OpT::UNION: return "Union(" + list(children) + ")";
+      case OpT::COMPLEMENT: return "!" + children[0]->to_string();
+      case OpT::THRESHOLD:
+         return std::string("Threshold(") + (exact ? "=" : ">=") + std::to_string(n) + ";" + list(children) + ";not:" + list(negated) + ")";
+      case OpT::SELECTION: {
+         std::string s = "Select[";
+         for (size_t i = 0; i < preds.size(); ++i) {
+            if (i) s += ",";
+            const Pred& p = preds[i];
+            if (p.kind == Pred::COVERED) {
+               s += std::string(p.covered ? "" : "!") + "Covered(" + std::to_string(p.pos + 1) + ")";
+            } else {
+               s += "Date(" + std::to_string(p.cmp) + "," + std::to_string(p.value) + (p.with_nulls ? ",nulls" : "") + ")";
+            }
+         }
+         return s + "](" + list(children) + ")";
+      }
+   }
+   return "?";
+}
+
+// =============================================================================================
+// Estimation (rule based): container cardinalities for leaves, independence for combinations.
+
+Estimator rule_estimator(const TableImage& t) {
+   const double rows = std::max(1u, t.n_rows);
+   auto frac = [rows](double x) { return std::min(1.0, std::max(0.0, x / rows)); };
+   std::shared_ptr<std::function<double(const Op&)>> self = std::make_shared<std::function<double(const Op&)>>();
+   *self = [&t, rows, frac, self](const Op& op) -> double {
+      auto& rec = *self;
+      switch (op.t) {
+         case OpT::EMPTY: return 0.0;
+         case OpT::FULL: return rows;
+         case OpT::INDEX_SCAN: {
+            const ContainerSet* cs;
+            uint32_t key;
+            uint32_t mask = 1;
+            if (op.leaf.kind == Leaf::SEQ) {
+               cs = &t.seq[op.leaf.col].vertical;
+               key = op.leaf.pos;
+               mask = op.leaf.symmask;
+            } else if (op.leaf.kind == Leaf::NULLS) {
+               return static_cast<double>(t.seq[op.leaf.col].null_rows.size());
+            } else {
+               cs = &t.dict[op.leaf.col].inverted;
+               key = op.leaf.value;
+            }
+            double s = 0;
+            for (uint32_t v = 0; v < t.nchunks(); ++v) {
+               const size_t slot = static_cast<size_t>(v) * cs->nkeys + key;
+               for (uint32_t i = cs->off[slot]; i < cs->off[slot + 1]; ++i) {
+                  const CtrDesc& d = cs->ctrs[i];
+                  if (op.leaf.kind != Leaf::SEQ || (mask >> d.sym & 1)) s += d.card_m1 + 1.0;
+               }
+            }
+            return s;
+         }
+         case OpT::COMPLEMENT: return rows - rec(*op.children[0]);
+         case OpT::INTERSECTION: {
+            double f = 1;
+            for (const auto& c : op.children) f *= frac(rec(*c));
+            for (const auto& c : op.negated) f *= 1 - frac(rec(*c));
+            return f * rows;
+         }
+         case OpT::UNION: {
+            double f = 1;
+            for (const auto& c : op.children) f *= 1 - frac(rec(*c));
+            return (1 - f) * rows;
+         }
+         case OpT::SELECTION: {
+            double f = op.children.empty() ? 1.0 : frac(rec(*op.children[0]));
+            for (const auto& p : op.preds) {
+               if (p.kind == Pred::COVERED) {
+                  f *= p.covered ? 0.97 : 0.03;
+               } else {
+                  f *= 0.5;
+               }
+            }
+            return f * rows;
+         }
+         case OpT::THRESHOLD: {
+            // Poisson-binomial distribution of the number of matching children.
+            std::vector<double> dist(1, 1.0);
+            auto add = [&](double p) {
+               std::vector<double> nd(dist.size() + 1, 0.0);
+               for (size_t i = 0; i < dist.size(); ++i) {
+                  nd[i] += dist[i] * (1 - p);
+                  nd[i + 1] += dist[i] * p;
+               }
+               dist.swap(nd);
+            };
+            for (const auto& c : op.children) add(frac(rec(*c)));
+            for (const auto& c : op.negated) add(1 - frac(rec(*c)));
+            double f = 0;
+            if (op.exact) {
+               f = static_cast<size_t>(op.n) < dist.size() ? dist[op.n] : 0.0;
+            } else {
+               for (size_t i = op.n; i < dist.size(); ++i) f += dist[i];
+            }
+            return f * rows;
+         }
+      }
+      return rows;
+   };
+   return [self](const Op& op) { return (*self)(op); };
+}
+
+// =============================================================================================
+// Lowering
+
+namespace {
+
+struct Lowerer {
+   const Estimator& est;
+   const LowerOptions& opt;
+   Program prog;
+   uint32_t depth = 0;
+
+   void emit(uint8_t op, uint8_t col = 0, uint16_t flags = 0, uint32_t a = 0, uint32_t b = 0, uint32_t c = 0) {
+      if (prog.code.size() >= MAX_PROGRAM) throw IllegalQuery("filter program too large");
+      prog.code.push_back(Instr{op, col, flags, a, b, c});
+   }
+   void push() {
+      ++depth;
+      prog.max_depth = std::max(prog.max_depth, depth);
+   }
+   void pop(uint32_t n = 1) { depth -= n; }
+
+   std::vector<const Op*> order(const std::vector<OpPtr>& v, bool ascending) {
+      std::vector<std::pair<double, const Op*>> e;
+      for (const auto& c : v) e.emplace_back(opt.reorder ? est(*c) : 0.0, c.get());
+      if (opt.reorder) {
+         std::stable_sort(e.begin(), e.end(), [ascending](const auto& x, const auto& y) {
+            return ascending ? x.first < y.first : x.first > y.first;
+         });
+      }
+      std::vector<const Op*> out;
+      for (auto& x : e) out.push_back(x.second);
+      return out;
+   }
+
+   void pred(const Pred& p) {
+      if (p.kind == Pred::COVERED) {
+         emit(OP_PUSH_COVERED, static_cast<uint8_t>(p.col), p.covered ? 0 : 1, p.pos);
+      } else {
+         emit(OP_PUSH_DATE, static_cast<uint8_t>(p.col), p.with_nulls ? 1 : 0, p.cmp, static_cast<uint32_t>(p.value));
+      }
+      push();
+      ++prog.n_leaves;
+   }
+
+   // Emits a conditional jump whose target is patched once the node is complete.
+   size_t jump(uint8_t op) {
+      emit(op);
+      return prog.code.size() - 1;
+   }
+   void patch(const std::vector<size_t>& jumps) {
+      for (size_t j : jumps) prog.code[j].a = static_cast<uint32_t>(prog.code.size());
+   }
+
+   void node(const Op& op) {
+      switch (op.t) {
+         case OpT::EMPTY:
+            emit(OP_PUSH_EMPTY);
+            push();
+            return;
+         case OpT::FULL:
+            emit(OP_PUSH_FULL);
+            push();
+            return;
+         case OpT::INDEX_SCAN:
+            if (op.leaf.kind == Leaf::SEQ) {
+               emit(OP_PUSH_SCAN, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.pos, op.leaf.symmask);
+            } else if (op.leaf.kind == Leaf::NULLS) {
+               emit(OP_PUSH_NULLS, static_cast<uint8_t>(op.leaf.col));
+            } else {
+               emit(OP_PUSH_DICT, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.value);
+            }
+            push();
+            ++prog.n_leaves;
+            return;
+         case OpT::COMPLEMENT:
+            node(*op.children[0]);
+            emit(OP_NOT);
+            return;
+         case OpT::INTERSECTION: {
+            auto pos = order(op.children, true);
+            auto neg = order(op.negated, false);
+            std::vector<size_t> jumps;
+            node(*pos[0]);
+            for (size_t i = 1; i < pos.size(); ++i) {
+               if (opt.early_exit) jumps.push_back(jump(OP_JZ));
+               node(*pos[i]);
+               emit(OP_AND);
+               pop();
+            }
+            for (const Op* c : neg) {
+               if (opt.early_exit) jumps.push_back(jump(OP_JZ));
+               node(*c);
+               emit(OP_ANDNOT);
+               pop();
+            }
+            patch(jumps);
+            return;
+         }
+         case OpT::UNION: {
+            if (op.children.empty()) {
+               emit(OP_PUSH_EMPTY);
+               push();
+               return;
+            }
+            auto ch = order(op.children, false);
+            std::vector<size_t> jumps;
+            node(*ch[0]);
+            for (size_t i = 1; i < ch.size(); ++i) {
+               if (opt.early_exit) jumps.push_back(jump(OP_JFULL));
+               node(*ch[i]);
+               emit(OP_OR);
+               pop();
+            }
+            patch(jumps);
+            return;
+         }
+         case OpT::SELECTION: {
+            std::vector<size_t> jumps;
+            size_t first = 0;
+            if (!op.children.empty()) {
+               node(*op.children[0]);
+            } else {
+               pred(op.preds[0]);
+               first = 1;
+            }
+            for (size_t i = first; i < op.preds.size(); ++i) {
+               if (opt.early_exit) jumps.push_back(jump(OP_JZ));
+               pred(op.preds[i]);
+               emit(OP_AND);
+               pop();
+            }
+            patch(jumps);
+            return;
+         }
+         case OpT::THRESHOLD: {
+            uint32_t planes = 1;
+            while ((1u << planes) - 1 < static_cast<uint32_t>(op.n) + 1) ++planes;
+            if (planes > MAX_THR_PLANES) throw IllegalQuery("NOf threshold too large");
+            emit(OP_THR_BEGIN, 0, 0, planes);
+            for (uint32_t i = 0; i < planes; ++i) push();
+            for (const auto& c : op.children) {
+               node(*c);
+               emit(OP_THR_ADD, 0, 0, planes);
+               pop();
+            }
+            for (const auto& c : op.negated) {
+               node(*c);
+               emit(OP_THR_ADD, 0, 1, planes);
+               pop();
+            }
+            emit(OP_THR_END, 0, op.exact ? 1 : 0, planes, static_cast<uint32_t>(op.n));
+            pop(planes);
+            push();
+            return;
+         }
+      }
+   }
+};
+
+}  // namespace
+
+Program lower(const Op& op, const Estimator& est, const LowerOptions& opt) {
+   Lowerer l{est, opt, {}, 0};
+   l.node(op);
+   if (l.depth != 1) throw CompilationError("internal error: unbalanced filter program");
+   return std::move(l.prog);
+}
+
+Program plan_filter(const std::string& text, const TableImage& t, const Estimator* est, const LowerOptions& opt,
+                    std::string* operator_tree) {
+   ExprPtr e = parse_expression(text, t);
+   ExprPtr r = rewrite(*e, t, Ambiguity::NONE);
+   OpPtr op = compile(*r, t);
+   if (operator_tree) *operator_tree = op->to_string();
+   if (est) return lower(*op, *est, opt);
+   const Estimator rule = rule_estimator(t);
+   return lower(*op, rule, opt);
+}
+
+}  // namespace rhygpu

@@ -1,0 +1,125 @@
+// Filter expressions, their rewrite and compile to operator trees, and the lowering of operator
+// trees to device programs.
+//
+// Expression -> Operator mirrors the reference:
+//   ScalarExpression::rewrite(table, AmbiguityMode) and ::compile(table)
+//     (src/rhydb/query_engine/scalar_expressions/scalar_expression.h:81-90),
+//   Operator::negate (src/rhydb/query_engine/filter/operators/operator.cpp:23-66).
+// The operator tree keeps the reference's node kinds (Empty, Full, IndexScan, Intersection, Union,
+// Complement, Threshold, Selection with IsInCoveredRegion / date predicates) and the same shapes,
+// so the row set it denotes is the reference's. Only its evaluation differs: instead of merging
+// roaring containers on the CPU, the tree is lowered to a postorder program (program.h) that the
+// GPU evaluates tile by tile.
+//
+// Textual expression syntax (positions are 1-based as in the reference's query language):
+//   And(e, ...)  Or(e, ...)  Not(e)  NOf(n, exactly|atleast, e, ...)  Maybe(e)  Exact(e)
+//   SymEq(column, pos, c)  with c a symbol character or '.' for the reference symbol
+//   HasMut(column, pos)    StrEq(column, value)    DateBetween(column, from|*, to|*)
+//   True  False
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "program.h"
+#include "table.h"
+#include "util.h"
+
+namespace rhygpu {
+
+enum class Ambiguity : uint8_t { UPPER_BOUND, LOWER_BOUND, NONE };
+
+enum class EK : uint8_t { AND, OR, NOT, NOF, MAYBE, EXACT, SYM_EQ, HAS_MUT, SYM_IN_SET, STR_EQ, DATE_BETWEEN, BOOL };
+
+struct Expr;
+using ExprPtr = std::unique_ptr<Expr>;
+
+struct Expr {
+   EK kind;
+   std::vector<ExprPtr> children;
+   std::string column;
+   uint32_t pos = 0;        // 0-based position
+   int sym = -1;            // SYM_EQ: symbol, -1 = '.' (reference symbol)
+   uint32_t symmask = 0;    // SYM_IN_SET
+   int n = 0;               // NOF
+   bool exact = false;      // NOF
+   std::string value;       // STR_EQ
+   bool has_from = false, has_to = false;
+   int32_t from = 0, to = 0;  // DATE_BETWEEN
+   bool truth = false;      // BOOL
+   SymKind sym_kind = SymKind::NUC;
+
+   ExprPtr clone() const;
+   std::string to_string() const;
+};
+
+ExprPtr parse_expression(const std::string& text, const TableImage& table);
+
+// ---------------------------------------------------------------------------------------------
+// Operator trees
+
+enum class OpT : uint8_t { EMPTY, FULL, INDEX_SCAN, INTERSECTION, UNION, COMPLEMENT, THRESHOLD, SELECTION };
+
+struct Pred {
+   enum Kind : uint8_t { COVERED, DATE } kind = COVERED;
+   int col = 0;
+   uint32_t pos = 0;
+   bool covered = true;         // COVERED: IS_COVERED vs IS_NOT_COVERED
+   uint32_t cmp = CMP_EQ;       // DATE
+   int32_t value = 0;
+   bool with_nulls = false;
+   Pred negated() const;
+};
+
+struct Leaf {
+   enum Kind : uint8_t { SEQ, NULLS, DICT } kind = SEQ;
+   int col = 0;
+   uint32_t pos = 0;
+   uint32_t symmask = 0;
+   uint32_t value = 0;
+};
+
+struct Op;
+using OpPtr = std::unique_ptr<Op>;
+
+struct Op {
+   OpT t = OpT::EMPTY;
+   std::vector<OpPtr> children;  // INTERSECTION/UNION/THRESHOLD non-negated; COMPLEMENT/SELECTION child
+   std::vector<OpPtr> negated;   // INTERSECTION/THRESHOLD negated children
+   std::vector<Pred> preds;      // SELECTION
+   Leaf leaf;                    // INDEX_SCAN
+   int n = 0;                    // THRESHOLD
+   bool exact = false;           // THRESHOLD
+   std::string to_string() const;
+};
+
+ExprPtr rewrite(const Expr& e, const TableImage& t, Ambiguity mode);
+OpPtr compile(const Expr& e, const TableImage& t);
+OpPtr negate(OpPtr op);
+
+// Estimated number of rows of an operator's result; drives child ordering and early exits only,
+// never the result.
+using Estimator = std::function<double(const Op&)>;
+Estimator rule_estimator(const TableImage& t);
+
+struct Program {
+   std::vector<Instr> code;
+   uint32_t max_depth = 0;   // tiles of stack needed
+   uint32_t n_leaves = 0;
+};
+
+struct LowerOptions {
+   bool early_exit = true;   // emit JZ/JFULL after partial intersections/unions
+   bool reorder = true;      // order children by the estimator
+};
+
+Program lower(const Op& op, const Estimator& est, const LowerOptions& opt);
+
+// rewrite(NONE) -> compile -> lower (reference: src/rhydb/query_engine/operators/compute_filter.cpp:14-21).
+Program plan_filter(const std::string& text, const TableImage& t, const Estimator* est, const LowerOptions& opt,
+                    std::string* operator_tree = nullptr);
+
+}  // namespace rhygpu

@@ -1,0 +1,429 @@
+// Ingestion of a raw table into the storage image (see table.h for the layout).
+#include "table.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#include "util.h"
+
+namespace rhygpu {
+
+uint64_t ContainerSet::payload_bytes() const {
+   uint64_t b = 0;
+   for (const auto& c : ctrs) {
+      if (c.type == CT_BITSET) {
+         b += 8192;
+      } else if (c.type == CT_RUN) {
+         b += 4ull * c.nruns;
+      } else {
+         b += 2ull * (c.card_m1 + 1u);
+      }
+   }
+   return b;
+}
+
+int TableImage::find_seq(const std::string& name) const {
+   for (size_t i = 0; i < seq.size(); ++i)
+      if (seq[i].name == name) return static_cast<int>(i);
+   return -1;
+}
+int TableImage::find_dict(const std::string& name) const {
+   for (size_t i = 0; i < dict.size(); ++i)
+      if (dict[i].name == name) return static_cast<int>(i);
+   return -1;
+}
+int TableImage::find_date(const std::string& name) const {
+   for (size_t i = 0; i < date.size(); ++i)
+      if (date[i].name == name) return static_cast<int>(i);
+   return -1;
+}
+
+namespace {
+
+// key layout: key << 21 | sym << 16 | row_in_chunk
+inline uint64_t pack(uint64_t key, uint32_t sym, uint32_t row) { return (key << 21) | (uint64_t(sym) << 16) | row; }
+inline uint32_t key_of(uint64_t k) { return static_cast<uint32_t>(k >> 21); }
+inline uint32_t sym_of(uint64_t k) { return static_cast<uint32_t>((k >> 16) & 31); }
+inline uint32_t row_of(uint64_t k) { return static_cast<uint32_t>(k & 0xFFFF); }
+
+struct ChunkContainers {
+   std::vector<CtrDesc> ctrs;
+   std::vector<uint16_t> payload;
+};
+
+// Encodes sorted (key, sym, row) entries of one chunk as containers.
+void encode_chunk(const std::vector<uint64_t>& keys, uint16_t v, ChunkContainers& out) {
+   out.ctrs.clear();
+   out.payload.clear();
+   size_t i = 0;
+   std::vector<uint16_t> rows;
+   while (i < keys.size()) {
+      const uint64_t group = keys[i] >> 16;
+      rows.clear();
+      size_t j = i;
+      while (j < keys.size() && (keys[j] >> 16) == group) rows.push_back(static_cast<uint16_t>(row_of(keys[j++])));
+      rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+      const uint32_t card = static_cast<uint32_t>(rows.size());
+      uint32_t nruns = 1;
+      for (size_t k = 1; k < rows.size(); ++k) nruns += (rows[k] != rows[k - 1] + 1);
+      const uint32_t base_bytes = card <= 4096 ? 2 + 2 * card : 8192;
+      const uint32_t run_bytes = 2 + 4 * nruns;
+      CtrDesc d{};
+      d.key = key_of(keys[i]);
+      d.v = v;
+      d.sym = static_cast<uint8_t>(sym_of(keys[i]));
+      d.card_m1 = static_cast<uint16_t>(card - 1);
+      if (run_bytes < base_bytes) {
+         d.type = CT_RUN;
+         d.nruns = static_cast<uint16_t>(nruns);
+         d.payload = static_cast<uint32_t>(out.payload.size());
+         size_t k = 0;
+         while (k < rows.size()) {
+            size_t e = k;
+            while (e + 1 < rows.size() && rows[e + 1] == rows[e] + 1) ++e;
+            out.payload.push_back(rows[k]);
+            out.payload.push_back(static_cast<uint16_t>(e - k));
+            k = e + 1;
+         }
+      } else if (card <= 4096) {
+         d.type = CT_ARRAY;
+         d.payload = static_cast<uint32_t>(out.payload.size());
+         out.payload.insert(out.payload.end(), rows.begin(), rows.end());
+      } else {
+         d.type = CT_BITSET;
+         while (out.payload.size() % 8) out.payload.push_back(0);
+         d.payload = static_cast<uint32_t>(out.payload.size());
+         out.payload.resize(out.payload.size() + 4096, 0);
+         uint16_t* bits = out.payload.data() + d.payload;
+         for (uint16_t r : rows) bits[r >> 4] |= static_cast<uint16_t>(1u << (r & 15));
+      }
+      out.ctrs.push_back(d);
+      i = j;
+   }
+}
+
+// Concatenates per-chunk containers (chunk order) and builds the (v, key) offset table.
+void assemble(std::vector<ChunkContainers>& chunks, uint32_t nkeys, ContainerSet& cs) {
+   size_t nctr = 0, npay = 0;
+   for (const auto& c : chunks) {
+      nctr += c.ctrs.size();
+      npay += c.payload.size() + 8;
+   }
+   cs.ctrs.reserve(nctr);
+   cs.payload.reserve(npay);
+   cs.nkeys = nkeys;
+   for (auto& c : chunks) {
+      while (cs.payload.size() % 8) cs.payload.push_back(0);
+      const uint32_t base = static_cast<uint32_t>(cs.payload.size());
+      if (cs.payload.size() + c.payload.size() > 0xFFFFFFFFull) throw std::runtime_error("payload arena exceeds 2^32 entries");
+      cs.payload.insert(cs.payload.end(), c.payload.begin(), c.payload.end());
+      for (auto d : c.ctrs) {
+         d.payload += base;
+         cs.ctrs.push_back(d);
+      }
+      c = ChunkContainers{};
+   }
+   const uint64_t nslots = static_cast<uint64_t>(chunks.size()) * nkeys;
+   cs.off.assign(nslots + 1, 0);
+   for (const auto& d : cs.ctrs) cs.off[static_cast<uint64_t>(d.v) * nkeys + d.key + 1]++;
+   for (uint64_t i = 0; i < nslots; ++i) cs.off[i + 1] += cs.off[i];
+}
+
+struct ChunkRows {
+   std::vector<uint64_t> keys;
+   std::vector<CovExc> exc;
+   std::vector<uint32_t> nr_off;  // chunk_size + 1
+   std::vector<uint32_t> nr_s, nr_e;
+   std::vector<uint32_t> nulls;
+};
+
+void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<uint8_t>& ref_sym, uint32_t L,
+                  uint32_t v, uint32_t size, ChunkRows& out) {
+   out.nr_off.assign(1, 0);
+   const uint32_t missing = A.missing;
+   for (uint32_t r = 0; r < size; ++r) {
+      const uint32_t row = v * CHUNK_ROWS + r;
+      if (raw.is_null[row]) {
+         out.nulls.push_back(row);
+         out.exc.push_back({r, 0, 0, 0});
+         out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));
+         continue;
+      }
+      const uint64_t b = raw.row_off[row], e = raw.row_off[row + 1];
+      auto sym_at = [&](uint64_t k) {
+         const int s = A.sym(raw.run_char[k]);
+         if (s < 0) throw std::invalid_argument(std::string("illegal character '") + raw.run_char[k] + "' in column " + raw.name);
+         return static_cast<uint32_t>(s);
+      };
+      // Leading and trailing missing symbols are trimmed into the covered region
+      // (reference: src/rhydb/common/aligned_sequence.cpp:89-120).
+      uint32_t start = 0;
+      uint64_t k = b;
+      while (k < e && raw.run_pos[k] == start && sym_at(k) == missing) {
+         start = raw.run_pos[k] + raw.run_len[k];
+         ++k;
+      }
+      uint32_t end = L;
+      uint64_t kb = e;
+      while (kb > k && raw.run_pos[kb - 1] + raw.run_len[kb - 1] == end && sym_at(kb - 1) == missing) {
+         end = raw.run_pos[kb - 1];
+         --kb;
+      }
+      if (start >= end) {
+         // Fully missing sequence: empty covered region, nothing recorded.
+         out.exc.push_back({r, 0, 0, 0});
+         out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));
+         continue;
+      }
+      if (start != 0 || end != L) out.exc.push_back({r, start, end, 0});
+      for (uint64_t q = k; q < kb; ++q) {
+         const uint32_t s = sym_at(q);
+         const uint32_t p0 = raw.run_pos[q], len = raw.run_len[q];
+         if (p0 + len > L || len == 0) throw std::invalid_argument("run outside the genome in column " + raw.name);
+         if (s == missing) {
+            out.nr_s.push_back(p0);
+            out.nr_e.push_back(p0 + len);
+            continue;
+         }
+         for (uint32_t p = p0; p < p0 + len; ++p) {
+            if (s != ref_sym[p]) out.keys.push_back(pack(p, s, r));
+         }
+      }
+      out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));
+   }
+   std::sort(out.keys.begin(), out.keys.end());
+}
+
+SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
+   SeqColumnImage col;
+   col.name = raw.name;
+   col.kind = raw.kind;
+   const Alphabet& A = alphabet(raw.kind);
+   const uint32_t L = static_cast<uint32_t>(raw.reference.size());
+   if (L == 0) throw std::invalid_argument("empty reference for column " + raw.name);
+   col.L = L;
+   col.reference = raw.reference;
+   col.global_ref.resize(L);
+   for (uint32_t p = 0; p < L; ++p) {
+      const int s = A.sym(raw.reference[p]);
+      if (s < 0) throw std::invalid_argument("illegal reference character in column " + raw.name);
+      col.global_ref[p] = static_cast<uint8_t>(s);
+   }
+   col.local_ref = col.global_ref;
+   const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
+   const uint32_t nsym = A.count;
+
+   std::vector<ChunkRows> chunks(nchunks);
+   parallel_for(nchunks, threads, [&](uint32_t v) { ingest_chunk(raw, A, col.global_ref, L, v, chunk_sizes[v], chunks[v]); });
+
+   // ---- local reference adaptation (reference: sequence_column.cpp:158-195) ----
+   std::vector<int64_t> diff(L + 1, 0);
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const ChunkRows& c = chunks[v];
+      int64_t full_rows = chunk_sizes[v];
+      for (const auto& x : c.exc) {
+         --full_rows;
+         if (x.start < x.end) {
+            diff[x.start] += 1;
+            diff[x.end] -= 1;
+         }
+      }
+      diff[0] += full_rows;
+      diff[L] -= full_rows;
+      for (size_t i = 0; i < c.nr_s.size(); ++i) {
+         diff[c.nr_s[i]] -= 1;
+         diff[c.nr_e[i]] += 1;
+      }
+   }
+   std::vector<uint64_t> coverage(L);
+   int64_t run = 0;
+   for (uint32_t p = 0; p < L; ++p) {
+      run += diff[p];
+      coverage[p] = static_cast<uint64_t>(run);
+   }
+   std::vector<uint32_t> counts(static_cast<size_t>(L) * nsym, 0);
+   for (const auto& c : chunks) {
+      for (uint64_t k : c.keys) counts[static_cast<size_t>(key_of(k)) * nsym + sym_of(k)]++;
+   }
+   struct Flip {
+      uint32_t pos;
+      uint8_t old_sym, new_sym;
+   };
+   std::vector<Flip> flips;
+   for (uint32_t p = 0; p < L; ++p) {
+      const uint32_t ref = col.local_ref[p];
+      uint32_t ref_count = static_cast<uint32_t>(coverage[p]);
+      for (uint32_t s = 0; s < nsym; ++s) ref_count -= counts[static_cast<size_t>(p) * nsym + s];
+      uint32_t best = ref, best_count = ref_count;
+      for (uint32_t s = 0; s < nsym; ++s) {
+         if (s == ref) continue;
+         const uint32_t c = counts[static_cast<size_t>(p) * nsym + s];
+         if (c > best_count) {
+            best = s;
+            best_count = c;
+         }
+      }
+      if (best != ref) flips.push_back({p, static_cast<uint8_t>(ref), static_cast<uint8_t>(best)});
+   }
+   counts.clear();
+   counts.shrink_to_fit();
+   col.flipped_positions = static_cast<uint32_t>(flips.size());
+   if (!flips.empty()) {
+      parallel_for(nchunks, threads, [&](uint32_t v) {
+         ChunkRows& c = chunks[v];
+         const uint32_t size = chunk_sizes[v];
+         std::vector<uint8_t> covered(size);
+         std::vector<uint64_t> added;
+         std::vector<uint8_t> is_flip_pos_new;  // per key: drop?
+         for (const Flip& f : flips) {
+            // rows covered at f.pos
+            std::fill(covered.begin(), covered.end(), 1);
+            for (const auto& x : c.exc) covered[x.row] = (x.start <= f.pos && f.pos < x.end) ? 1 : 0;
+            for (uint32_t r = 0; r < size; ++r) {
+               if (!covered[r]) continue;
+               for (uint32_t q = c.nr_off[r]; q < c.nr_off[r + 1]; ++q) {
+                  if (c.nr_s[q] <= f.pos && f.pos < c.nr_e[q]) {
+                     covered[r] = 0;
+                     break;
+                  }
+               }
+            }
+            auto lo = std::lower_bound(c.keys.begin(), c.keys.end(), pack(f.pos, 0, 0));
+            auto hi = std::lower_bound(c.keys.begin(), c.keys.end(), pack(f.pos + 1, 0, 0));
+            for (auto it = lo; it != hi; ++it) covered[row_of(*it)] = 0;
+            for (uint32_t r = 0; r < size; ++r)
+               if (covered[r]) added.push_back(pack(f.pos, f.old_sym, r));
+         }
+         // drop the new reference symbol's entries at flipped positions
+         std::vector<uint64_t> kept;
+         kept.reserve(c.keys.size() + added.size());
+         size_t fi = 0;
+         for (uint64_t k : c.keys) {
+            const uint32_t p = key_of(k);
+            while (fi < flips.size() && flips[fi].pos < p) ++fi;
+            if (fi < flips.size() && flips[fi].pos == p && sym_of(k) == flips[fi].new_sym) continue;
+            kept.push_back(k);
+         }
+         kept.insert(kept.end(), added.begin(), added.end());
+         std::sort(kept.begin(), kept.end());
+         c.keys.swap(kept);
+      });
+      for (const Flip& f : flips) col.local_ref[f.pos] = f.new_sym;
+   }
+
+   // ---- containers ----
+   std::vector<ChunkContainers> enc(nchunks);
+   parallel_for(nchunks, threads, [&](uint32_t v) {
+      encode_chunk(chunks[v].keys, static_cast<uint16_t>(v), enc[v]);
+      std::vector<uint64_t>().swap(chunks[v].keys);
+   });
+   assemble(enc, L, col.vertical);
+
+   // ---- coverage, nulls, missing intervals ----
+   col.cov_exc_off.assign(1, 0);
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const ChunkRows& c = chunks[v];
+      col.cov_exc.insert(col.cov_exc.end(), c.exc.begin(), c.exc.end());
+      col.cov_exc_off.push_back(static_cast<uint32_t>(col.cov_exc.size()));
+      col.null_rows.insert(col.null_rows.end(), c.nulls.begin(), c.nulls.end());
+   }
+   col.nrow_off.assign(static_cast<size_t>(nchunks) * CHUNK_ROWS + 1, 0);
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const ChunkRows& c = chunks[v];
+      const uint32_t base = static_cast<uint32_t>(col.nrow_start.size());
+      for (uint32_t r = 0; r < CHUNK_ROWS; ++r) {
+         const uint32_t n = r < chunk_sizes[v] ? c.nr_off[r + 1] : c.nr_off[chunk_sizes[v]];
+         col.nrow_off[static_cast<size_t>(v) * CHUNK_ROWS + r + 1] = base + n;
+      }
+      col.nrow_start.insert(col.nrow_start.end(), c.nr_s.begin(), c.nr_s.end());
+      col.nrow_end.insert(col.nrow_end.end(), c.nr_e.begin(), c.nr_e.end());
+   }
+   col.nblocks = (L + NBLOCK - 1) / NBLOCK;
+   const size_t nbuckets = static_cast<size_t>(col.nblocks) * nchunks;
+   col.nblk_off.assign(nbuckets + 1, 0);
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const ChunkRows& c = chunks[v];
+      for (size_t i = 0; i < c.nr_s.size(); ++i) {
+         for (uint32_t b = c.nr_s[i] / NBLOCK; b <= (c.nr_e[i] - 1) / NBLOCK; ++b)
+            col.nblk_off[static_cast<size_t>(b) * nchunks + v + 1]++;
+      }
+   }
+   for (size_t i = 0; i < nbuckets; ++i) col.nblk_off[i + 1] += col.nblk_off[i];
+   col.nblk.resize(col.nblk_off[nbuckets]);
+   std::vector<uint32_t> fill(col.nblk_off.begin(), col.nblk_off.end() - 1);
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const ChunkRows& c = chunks[v];
+      for (uint32_t r = 0; r < chunk_sizes[v]; ++r) {
+         for (uint32_t q = c.nr_off[r]; q < c.nr_off[r + 1]; ++q) {
+            const uint32_t s = c.nr_s[q], e = c.nr_e[q];
+            for (uint32_t b = s / NBLOCK; b <= (e - 1) / NBLOCK; ++b) {
+               const uint32_t bs = b * NBLOCK;
+               NRunEntry en;
+               en.row = r;
+               en.lo = static_cast<uint16_t>(std::max(s, bs) - bs);
+               en.hi = static_cast<uint16_t>(std::min(e, bs + NBLOCK) - bs);
+               col.nblk[fill[static_cast<size_t>(b) * nchunks + v]++] = en;
+            }
+         }
+      }
+   }
+   return col;
+}
+
+DictColumnImage build_dict_column(const RawDictColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
+   DictColumnImage col;
+   col.name = raw.name;
+   col.values = raw.values;
+   for (uint32_t i = 0; i < raw.values.size(); ++i) col.index.emplace(raw.values[i], i);
+   const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
+   const uint32_t nvalues = static_cast<uint32_t>(raw.values.size());
+   std::vector<ChunkContainers> enc(nchunks);
+   parallel_for(nchunks, threads, [&](uint32_t v) {
+      std::vector<uint64_t> keys;
+      for (uint32_t r = 0; r < chunk_sizes[v]; ++r) {
+         const uint32_t id = raw.ids[v * CHUNK_ROWS + r];
+         if (id == UINT32_MAX) continue;
+         if (id >= nvalues) throw std::invalid_argument("dictionary id out of range in column " + raw.name);
+         keys.push_back(pack(id, 0, r));
+      }
+      std::sort(keys.begin(), keys.end());
+      encode_chunk(keys, static_cast<uint16_t>(v), enc[v]);
+   });
+   assemble(enc, std::max(1u, nvalues), col.inverted);
+   return col;
+}
+
+}  // namespace
+
+TableImage build_table(const RawTable& raw, uint32_t threads) {
+   TableImage t;
+   t.n_rows = raw.n_rows;
+   if (raw.n_rows == 0) throw std::invalid_argument("a partition needs at least one row");
+   for (uint32_t left = raw.n_rows; left > 0;) {
+      const uint32_t s = std::min(left, CHUNK_ROWS);
+      t.chunk_sizes.push_back(s);
+      left -= s;
+   }
+   if (t.chunk_sizes.size() >= 65535) throw std::invalid_argument("too many chunks");
+   for (const auto& c : raw.seq) {
+      if (c.is_null.size() != raw.n_rows || c.row_off.size() != raw.n_rows + 1ull)
+         throw std::invalid_argument("row count mismatch in column " + c.name);
+      t.seq.push_back(build_seq_column(c, t.chunk_sizes, threads));
+   }
+   for (const auto& c : raw.dict) {
+      if (c.ids.size() != raw.n_rows) throw std::invalid_argument("row count mismatch in column " + c.name);
+      t.dict.push_back(build_dict_column(c, t.chunk_sizes, threads));
+   }
+   for (const auto& c : raw.date) {
+      if (c.days.size() != raw.n_rows) throw std::invalid_argument("row count mismatch in column " + c.name);
+      DateColumnImage d;
+      d.name = c.name;
+      d.days.assign(static_cast<size_t>(t.nchunks()) * CHUNK_ROWS, INT32_MIN);
+      for (uint32_t i = 0; i < raw.n_rows; ++i) d.days[i] = c.days[i];  // full chunks: global id == row index
+      t.date.push_back(std::move(d));
+   }
+   return t;
+}
+
+}  // namespace rhygpu

@@ -1,0 +1,119 @@
+// Host storage image of one table partition: what ingestion produces and what is uploaded to HBM.
+//
+// Sequence columns keep the reference's storage semantics:
+//  * vertical index: one roaring-style container per (position, 2^16-row chunk, symbol) holding
+//    the rows whose symbol differs from the local reference (reference:
+//    src/rhydb/storage/column/vertical_sequence_index.h:20-113), with the missing symbol (N / X)
+//    never stored there;
+//  * coverage: per row the covered [start, end) and the missing positions inside it (reference:
+//    src/rhydb/storage/column/horizontal_coverage_index.h:21-114);
+//  * local reference: a position whose majority symbol differs from the reference is flipped at
+//    finalize (reference: src/rhydb/storage/column/sequence_column.cpp:158-212,
+//    vertical_sequence_index.cpp:217-283).
+// Containers keep their roaring encodings (array <= 4096 sorted u16, 8 KiB bitset, or runs),
+// chosen by the smallest serialized size (reference: src/rhydb/roaring_util/roaring_container.cpp:7-62).
+//
+// The coverage layout is redesigned for the GPU: rows whose covered region is not the whole genome
+// are kept as a short per-chunk exception list, and the missing positions inside coverage are kept
+// as intervals bucketed by 128-position blocks, so a coverage tile at one position reads only the
+// exceptions and the intervals of one block instead of every row.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "alphabet.h"
+#include "dataset.h"
+
+namespace rhygpu {
+
+constexpr uint32_t CHUNK_ROWS = 1u << 16;  // rows per chunk, reference: src/rhydb/storage/column/column.h:18
+constexpr uint32_t CHUNK_WORDS = CHUNK_ROWS / 32;
+constexpr uint32_t NBLOCK = 128;           // positions per N-interval bucket
+
+enum CtrType : uint8_t { CT_ARRAY = 0, CT_BITSET = 1, CT_RUN = 2 };
+
+// 16-byte container descriptor, identical on host and device.
+struct CtrDesc {
+   uint32_t payload;   // offset into the u16 payload arena
+   uint32_t key;       // position (sequence column) or value id (dictionary column)
+   uint16_t v;         // chunk id (v_index)
+   uint8_t sym;        // symbol (sequence column), 0 for dictionary columns
+   uint8_t type;       // CtrType
+   uint16_t nruns;     // run containers: number of (start, length-1) pairs
+   uint16_t card_m1;   // cardinality - 1
+};
+static_assert(sizeof(CtrDesc) == 16, "descriptor layout");
+
+struct CovExc {  // a row whose covered region is not [0, L)
+   uint32_t row;   // row within chunk
+   uint32_t start;
+   uint32_t end;
+   uint32_t pad;
+};
+
+struct NRunEntry {  // missing interval of one row clipped to one position block
+   uint32_t row;    // row within chunk
+   uint16_t lo;     // [lo, hi) relative to the block start
+   uint16_t hi;
+};
+
+struct ContainerSet {
+   std::vector<CtrDesc> ctrs;       // sorted by (v, key, sym)
+   std::vector<uint16_t> payload;   // bitset payloads start on 16-byte boundaries
+   std::vector<uint32_t> off;       // [nchunks * nkeys + 1]: ctrs of (v, key) are [off[v*nkeys+key], off[...+1])
+   uint32_t nkeys = 0;
+   uint64_t payload_bytes() const;
+};
+
+struct SeqColumnImage {
+   std::string name;
+   SymKind kind = SymKind::NUC;
+   uint32_t L = 0;
+   std::string reference;              // global reference chars
+   std::vector<uint8_t> global_ref;    // symbols
+   std::vector<uint8_t> local_ref;     // symbols after adaptation
+   ContainerSet vertical;              // keys = positions
+   std::vector<uint32_t> null_rows;    // global row ids (chunk << 16 | row)
+   std::vector<CovExc> cov_exc;        // sorted by (chunk, row)
+   std::vector<uint32_t> cov_exc_off;  // nchunks + 1
+   // Missing positions inside coverage, as intervals: per row CSR over global ids (chunk stride).
+   std::vector<uint32_t> nrow_off;     // nchunks * CHUNK_ROWS + 1
+   std::vector<uint32_t> nrow_start, nrow_end;
+   std::vector<NRunEntry> nblk;        // bucketed by (block, chunk), sorted by row
+   std::vector<uint32_t> nblk_off;     // nblocks * nchunks + 1
+   uint32_t nblocks = 0;
+   uint32_t flipped_positions = 0;
+};
+
+struct DictColumnImage {
+   std::string name;
+   std::vector<std::string> values;
+   std::map<std::string, uint32_t> index;
+   ContainerSet inverted;              // keys = value ids
+};
+
+struct DateColumnImage {
+   std::string name;
+   std::vector<int32_t> days;          // global-id (chunk stride) layout, INT32_MIN = null
+};
+
+struct TableImage {
+   uint32_t n_rows = 0;
+   std::vector<uint32_t> chunk_sizes;
+   std::vector<SeqColumnImage> seq;
+   std::vector<DictColumnImage> dict;
+   std::vector<DateColumnImage> date;
+   uint32_t nchunks() const { return static_cast<uint32_t>(chunk_sizes.size()); }
+   int find_seq(const std::string& name) const;
+   int find_dict(const std::string& name) const;
+   int find_date(const std::string& name) const;
+};
+
+// Ingestion: diff every row against the reference, split rows into 2^16-row chunks, build the
+// vertical containers, adapt the local reference, choose container encodings.
+TableImage build_table(const RawTable& raw, uint32_t threads = 0);
+
+}  // namespace rhygpu

@@ -1,0 +1,313 @@
+"""Python mirror of the filter / count / mutations path over the C-ABI of librhygpu.so.
+
+The names follow the reference's query engine: a filter expression is rewritten and compiled to
+an operator tree (``Table.plan``), evaluated to a row set (``Device.compute_filter``,
+reference: src/rhydb/query_engine/operators/compute_filter.cpp:14-21), counted
+(``Device.count``, reference: count_filter_node.cpp:35-71), or turned into per-position symbol
+counts and mutation rows (``Device.mutations``, reference: mutations_node.cpp:269-366).
+
+There is no CPU fallback: if the compiled library is missing, importing works but every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "librhygpu.so"
+
+CHUNK_ROWS = 1 << 16
+CHUNK_WORDS = CHUNK_ROWS // 32
+NUC_SYMBOLS = "-ACGTRYSWKMBDHVN"
+AA_SYMBOLS = "-ACDEFGHIKLMNOPQRSTUVWYBJZ*X"
+
+
+class RhyError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class IllegalQuery(RhyError):
+    pass
+
+
+class QueryCompilationError(RhyError):
+    pass
+
+
+class RawSeqColumn(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("kind", C.c_int), ("reference", C.c_char_p), ("L", C.c_uint32),
+                ("is_null", C.POINTER(C.c_uint8)), ("row_off", C.POINTER(C.c_uint64)),
+                ("run_pos", C.POINTER(C.c_uint32)), ("run_len", C.POINTER(C.c_uint32)),
+                ("run_char", C.POINTER(C.c_char))]
+
+
+class RawDictColumn(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("n_values", C.c_uint32), ("values", C.POINTER(C.c_char_p)),
+                ("ids", C.POINTER(C.c_uint32))]
+
+
+class RawDateColumn(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("days", C.POINTER(C.c_int32))]
+
+
+class RawTable(C.Structure):
+    _fields_ = [("n_rows", C.c_uint32), ("n_seq", C.c_uint32), ("n_dict", C.c_uint32), ("n_date", C.c_uint32),
+                ("seq", C.POINTER(RawSeqColumn)), ("dict", C.POINTER(RawDictColumn)),
+                ("date", C.POINTER(RawDateColumn))]
+
+
+class GenConfig(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_rows", C.c_uint32), ("genome_len", C.c_uint32),
+                ("pool_sites", C.c_uint32), ("n_aa_genes", C.c_uint32), ("null_fraction", C.c_double),
+                ("threads", C.c_uint32)]
+
+
+class TableInfo(C.Structure):
+    _fields_ = [("n_rows", C.c_uint32), ("n_chunks", C.c_uint32), ("n_seq", C.c_uint32), ("n_dict", C.c_uint32),
+                ("n_date", C.c_uint32)]
+
+
+class SeqColumnInfo(C.Structure):
+    _fields_ = [("L", C.c_uint32), ("n_symbols", C.c_uint32), ("kind", C.c_uint32), ("flipped_positions", C.c_uint32),
+                ("n_containers", C.c_uint64), ("payload_bytes", C.c_uint64), ("n_array", C.c_uint64),
+                ("n_bitset", C.c_uint64), ("n_run", C.c_uint64), ("n_missing_intervals", C.c_uint64),
+                ("n_coverage_exceptions", C.c_uint64), ("n_null_rows", C.c_uint64)]
+
+
+class MutationRow(C.Structure):
+    _fields_ = [("position", C.c_uint32), ("from_", C.c_char), ("to", C.c_char), ("count", C.c_uint32),
+                ("coverage", C.c_uint32), ("proportion", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads librhygpu.so; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() or lapis-silo_gb300/build.py")
+    L = C.CDLL(str(LIB_PATH))
+    P, U32, U64, I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    sig = {
+        "rhy_last_error": (C.c_char_p, []),
+        "rhy_generate": (I, [C.POINTER(GenConfig), C.POINTER(P)]),
+        "rhy_table_from_raw": (I, [C.POINTER(RawTable), U32, C.POINTER(P)]),
+        "rhy_table_info": (I, [P, C.POINTER(TableInfo)]),
+        "rhy_seq_column_info": (I, [P, U32, C.POINTER(SeqColumnInfo)]),
+        "rhy_seq_column_name": (I, [P, U32, C.c_char_p, C.c_size_t]),
+        "rhy_table_raw": (I, [P, C.POINTER(RawTable)]),
+        "rhy_local_reference": (I, [P, U32, C.c_char_p, C.c_size_t]),
+        "rhy_seq_containers": (I, [P, U32, P, P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_generate_queries": (I, [P, U64, U32, U32, U32, I, I, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_table_free": (None, [P]),
+        "rhy_plan": (I, [P, C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(U32), C.POINTER(U32)]),
+        "rhy_open": (I, [P, I, C.POINTER(P)]),
+        "rhy_set_tile_bits": (I, [P, U32]),
+        "rhy_device_bytes": (I, [P, C.POINTER(U64)]),
+        "rhy_count": (I, [P, C.c_char_p, P, C.POINTER(U64)]),
+        "rhy_eval": (I, [P, C.c_char_p, P, P, C.POINTER(U64)]),
+        "rhy_mutations": (I, [P, C.c_char_p, U32, P, P, C.POINTER(U64)]),
+        "rhy_mutation_rows": (I, [P, U32, P, C.c_double, C.POINTER(MutationRow), C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_close": (None, [P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc == 0:
+        return
+    msg = lib().rhy_last_error().decode(errors="replace")
+    if rc == 1:
+        raise IllegalQuery(rc, msg)
+    if rc == 2:
+        raise QueryCompilationError(rc, msg)
+    raise RhyError(rc, msg)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class SeqColumnStats:
+    name: str
+    L: int
+    n_symbols: int
+    kind: int
+    flipped_positions: int
+    n_containers: int
+    payload_bytes: int
+    n_array: int
+    n_bitset: int
+    n_run: int
+    n_missing_intervals: int
+    n_coverage_exceptions: int
+    n_null_rows: int
+
+    @property
+    def symbols(self) -> str:
+        return NUC_SYMBOLS if self.kind == 0 else AA_SYMBOLS
+
+
+class Table:
+    """Host storage image of one partition (ingested and finalized)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        info = TableInfo()
+        _check(lib().rhy_table_info(self._h, C.byref(info)))
+        self.n_rows = info.n_rows
+        self.n_chunks = info.n_chunks
+        self.n_seq, self.n_dict, self.n_date = info.n_seq, info.n_dict, info.n_date
+        self.columns = [self.column_stats(i) for i in range(self.n_seq)]
+
+    @classmethod
+    def generate(cls, n_rows: int, seed: int = 42, genome_len: int = 29903, pool_sites: int = 5000,
+                 n_aa_genes: int = 0, null_fraction: float = 0.0, threads: int = 0) -> "Table":
+        cfg = GenConfig(seed, n_rows, genome_len, pool_sites, n_aa_genes, null_fraction, threads)
+        h = C.c_void_p()
+        _check(lib().rhy_generate(C.byref(cfg), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_raw(cls, raw: RawTable, threads: int = 0) -> "Table":
+        h = C.c_void_p()
+        _check(lib().rhy_table_from_raw(C.byref(raw), threads, C.byref(h)))
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rhy_table_free(self._h)
+            self._h = None
+
+    def column_stats(self, i: int) -> SeqColumnStats:
+        info = SeqColumnInfo()
+        _check(lib().rhy_seq_column_info(self._h, i, C.byref(info)))
+        buf = C.create_string_buffer(256)
+        _check(lib().rhy_seq_column_name(self._h, i, buf, 256))
+        return SeqColumnStats(buf.value.decode(), info.L, info.n_symbols, info.kind, info.flipped_positions,
+                              info.n_containers, info.payload_bytes, info.n_array, info.n_bitset, info.n_run,
+                              info.n_missing_intervals, info.n_coverage_exceptions, info.n_null_rows)
+
+    def column_index(self, name: str) -> int:
+        for i, c in enumerate(self.columns):
+            if c.name == name:
+                return i
+        raise KeyError(name)
+
+    def raw(self) -> RawTable:
+        r = RawTable()
+        _check(lib().rhy_table_raw(self._h, C.byref(r)))
+        return r
+
+    def local_reference(self, column: int) -> str:
+        L = self.columns[column].L
+        buf = C.create_string_buffer(L + 1)
+        _check(lib().rhy_local_reference(self._h, column, buf, L + 1))
+        return buf.raw[:L].decode()
+
+    def containers(self, column: int):
+        """(position, chunk, symbol, cardinality, encoding) of every vertical container."""
+        n = C.c_size_t()
+        _check(lib().rhy_seq_containers(self._h, column, None, None, None, None, None, 0, C.byref(n)))
+        m = n.value
+        pos, chunk = np.zeros(m, np.uint32), np.zeros(m, np.uint16)
+        sym, card, typ = np.zeros(m, np.uint8), np.zeros(m, np.uint32), np.zeros(m, np.uint8)
+        if m:
+            _check(lib().rhy_seq_containers(self._h, column, _ptr(pos), _ptr(chunk), _ptr(sym), _ptr(card), _ptr(typ),
+                                            m, C.byref(n)))
+        return pos, chunk, sym, card, typ
+
+    def queries(self, n: int, seed: int = 43, max_depth: int = 4, max_nof_children: int = 8, use_aa: bool = False,
+                use_metadata: bool = False) -> list[str]:
+        need = C.c_size_t()
+        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, int(use_aa),
+                                          int(use_metadata), None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, int(use_aa),
+                                          int(use_metadata), buf, need.value, None))
+        return [q for q in buf.value.decode().split("\n") if q]
+
+    def plan(self, expr: str) -> tuple[str, int, int]:
+        """Operator tree of rewrite(NONE) + compile, program length and stack depth."""
+        buf = C.create_string_buffer(1 << 20)
+        n, d = C.c_uint32(), C.c_uint32()
+        _check(lib().rhy_plan(self._h, expr.encode(), buf, 1 << 20, C.byref(n), C.byref(d)))
+        return buf.value.decode(), n.value, d.value
+
+    def mutation_rows(self, column: int, counts: np.ndarray, min_proportion: float):
+        """Rows of the Mutations action (reference: mutations_node.cpp:292-366) from symbol counts."""
+        counts = np.ascontiguousarray(counts, dtype=np.uint32)
+        n = C.c_size_t()
+        _check(lib().rhy_mutation_rows(self._h, column, _ptr(counts), min_proportion, None, 0, C.byref(n)))
+        rows = (MutationRow * max(1, n.value))()
+        _check(lib().rhy_mutation_rows(self._h, column, _ptr(counts), min_proportion, rows, n.value, C.byref(n)))
+        return [(r.position, r.from_.decode(), r.to.decode(), r.count, r.coverage, r.proportion)
+                for r in rows[: n.value]]
+
+
+class Device:
+    """A partition resident in the HBM of one GPU."""
+
+    def __init__(self, table: Table, device: int = 0):
+        self.table = table
+        self._h = C.c_void_p()
+        _check(lib().rhy_open(table._h, device, C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rhy_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+    def set_tile_bits(self, bits: int):
+        _check(lib().rhy_set_tile_bits(self._h, bits))
+
+    def device_bytes(self) -> int:
+        v = C.c_uint64()
+        _check(lib().rhy_device_bytes(self._h, C.byref(v)))
+        return v.value
+
+    def count(self, expr: str, stream=None) -> int:
+        v = C.c_uint64()
+        _check(lib().rhy_count(self._h, expr.encode(), stream, C.byref(v)))
+        return v.value
+
+    def compute_filter(self, expr: str, stream=None) -> tuple[np.ndarray, int]:
+        """Dense row-set bitmap (n_chunks * 2048 uint32 words) and its cardinality."""
+        bits = np.zeros(self.table.n_chunks * CHUNK_WORDS, dtype=np.uint32)
+        v = C.c_uint64()
+        _check(lib().rhy_eval(self._h, expr.encode(), stream, _ptr(bits), C.byref(v)))
+        return bits, v.value
+
+    def mutations(self, expr: str, column: int = 0, stream=None) -> tuple[np.ndarray, int]:
+        """counts[symbol, position] of the filtered rows and the filter cardinality."""
+        col = self.table.columns[column]
+        counts = np.zeros((col.n_symbols, col.L), dtype=np.uint32)
+        v = C.c_uint64()
+        _check(lib().rhy_mutations(self._h, expr.encode(), column, stream, _ptr(counts), C.byref(v)))
+        return counts, v.value
+
+
+def bits_to_rows(bits: np.ndarray) -> np.ndarray:
+    """Global row ids (chunk << 16 | row) of a dense row-set bitmap."""
+    b = np.unpackbits(bits.view(np.uint8), bitorder="little")
+    return np.flatnonzero(b).astype(np.uint32)
