@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Benchmark of the filter / count / mutations hot path on one GB300.
+
+Workload: a seeded synthetic table of 2,000,000 sequences (29,903-nt genome, 12 amino-acid genes
+totalling 9,700 aa, country / lineage / date metadata) and seeded random filter expressions over
+nucleotide, amino-acid and metadata leaves. A step is one batch of 2,048 queries: 75% Aggregated
+count, 25% Mutations of the nucleotide column.
+
+value      queries/s of the batched path (persistent filter kernel + batched mutations kernels,
+           replayed from a captured CUDA graph) with programs and table resident in HBM.
+e2e        the same through the C-ABI call rhy_batch with host buffers: planning, host->device
+           copies, kernels and the device->host copy of every count and mutation table.
+plain      the plain single-query path over the same queries, one query at a time.
+roofline   the plain container pass of the Mutations action (mut_ctr_kernel), the kernel that
+           streams the whole vertical index: algorithmic bytes = container payloads + descriptors
+           + the filter tiles it stages, divided by its CUDA-event duration.
+cpu_baseline  the CPU oracle (a restatement of the reference's operators) on a bounded sample of
+           the same queries, one query per host thread as the reference serves them.
+
+`python bench.py --impl reference` times that CPU implementation alone on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "lapis-silo_gb300"))
+
+METRIC = "queries/s and p99 ms, batched+learned planner vs plain GPU path, bit-exact"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+MIN_PROPORTION = 0.05
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rows", type=int, default=2_000_000)
+    ap.add_argument("--batch", type=int, default=2048)
+    ap.add_argument("--mut-every", type=int, default=4, help="every n-th query is a Mutations query")
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--qseed", type=int, default=43)
+    ap.add_argument("--plain-queries", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--tile-bits", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(R, args):
+    table = R.Table.generate(args.rows, seed=args.seed, n_aa_genes=12)
+    queries = table.queries(args.batch, seed=args.qseed, use_aa=True, use_metadata=True)
+    actions = np.array([1 if (i % args.mut_every) == args.mut_every - 1 else 0 for i in range(len(queries))], np.int32)
+    columns = np.zeros(len(queries), np.uint32)
+    return table, queries, actions, columns
+
+
+def cpu_leg(table, queries, actions, columns, n_sample: int, threads: int):
+    """Times the CPU oracle on a sample of the workload; returns (queries/s, sample description, p50, p99)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as oracle_mod
+
+    t0 = time.perf_counter()
+    orc = oracle_mod.Oracle(table.raw(), table.n_chunks, [(c.name, c.n_symbols, c.L) for c in table.columns])
+    build_s = time.perf_counter() - t0
+    idx = list(range(min(n_sample, len(queries))))
+    secs, ms, _ = orc.run_batch([queries[i] for i in idx], [int(actions[i]) for i in idx],
+                                [int(columns[i]) for i in idx], threads)
+    qps = len(idx) / secs
+    desc = (f"first {len(idx)} queries of the batch ({int(sum(actions[i] for i in idx))} Mutations), "
+            f"{threads} worker threads, one query per thread; oracle ingestion {build_s:.1f} s not timed")
+    return qps, desc, float(np.percentile(ms, 50)), float(np.percentile(ms, 99)), secs
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "lapis-silo_gb300"))
+    import rhydb_gpu as R
+
+    table, queries, actions, columns = build_workload(R, args)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as oracle_mod
+
+    orc = oracle_mod.Oracle(table.raw(), table.n_chunks, [(c.name, c.n_symbols, c.L) for c in table.columns])
+    n = min(args.cpu_sample, len(queries))
+    step_s = []
+    all_ms = []
+    for step in range(args.warmup + args.steps):
+        lo = (step * n) % len(queries)
+        idx = [(lo + i) % len(queries) for i in range(n)]
+        secs, ms, _ = orc.run_batch([queries[i] for i in idx], [int(actions[i]) for i in idx],
+                                    [int(columns[i]) for i in idx], threads)
+        if step >= args.warmup:
+            step_s.append(secs)
+            all_ms.extend(ms.tolist())
+    total = sum(step_s)
+    qps = n * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": f"{args.rows} sequences, 12 aa genes; {n}-query samples of the {args.batch}-query "
+                               f"batch (1 in {args.mut_every} Mutations)", "rows": args.rows},
+        "p50_ms": float(np.percentile(all_ms, 50)), "p99_ms": float(np.percentile(all_ms, 99)),
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} queries per step, one query per worker thread ({threads} threads)"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, ws, rank)
+        return
+    import torch
+
+    import rhydb_gpu as R
+
+    R.lib()
+    torch.cuda.set_device(local)
+    dev_index = local
+    table, queries, actions, columns = build_workload(R, args)
+    dev = R.Device(table, dev_index)
+    n = len(queries)
+    n_mut = int(actions.sum())
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev_index}")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # ---------------- batched path: device-resident ----------------
+    dev.batch_prepare(queries, actions, columns, tile_bits=args.tile_bits)
+    info = dev.batch_info()
+    dev.batch_launch(sp, True, False)
+    dev.batch_capture_ex(sp, copy_in=False, copy_out=False)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        flush_l2()
+        dev.batch_replay(sp)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = ClockSampler(dev_index)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    step_ms = []
+    for _ in range(args.steps):
+        flush_l2()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        dev.batch_replay(sp)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    barrier(ws)
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, ws)
+    value = n * args.steps * ws / total_s
+    launches_per_step = 1 + (5 if n_mut else 0)
+
+    # results of the batched path for the parity self-check against the plain path
+    dev.batch_launch(sp, True, True)
+    torch.cuda.synchronize()
+    b_counts, b_muts = dev.batch_results()
+
+    # per-kernel times of the batched path
+    kernels_ms = {}
+    for name, parts in (("filter_batch", 1), ("transpose", 2), ("mut_ctr_batch", 4), ("mut_cov_batch", 8),
+                        ("mut_final_batch", 16)):
+        ts = []
+        for _ in range(2):
+            dev.batch_launch_parts(1, sp) if parts != 1 else None
+            flush_l2()
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            dev.batch_launch_parts(parts, sp)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        kernels_ms[name] = min(ts)
+
+    # ---------------- plain path: one query at a time ----------------
+    dev.plain_prepare(queries, actions, columns)
+    m = min(args.plain_queries, n)
+    for i in range(min(8, m)):
+        dev.plain_launch(i, sp)
+    torch.cuda.synchronize()
+    flush_l2()
+    torch.cuda.synchronize()
+    plain_ms = []
+    for i in range(m):
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        dev.plain_launch(i, sp)
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain_qps = m / (sum(plain_ms) / 1000.0)
+    # parity self-check: plain vs batched on the same queries (bit-exact)
+    mismatches = 0
+    for i in range(min(64, m)):
+        if actions[i] == 1:
+            cnt, fc = dev.mutations(queries[i], 0)
+            if fc != b_counts[i] or not np.array_equal(cnt, b_muts[i]):
+                mismatches += 1
+        else:
+            if dev.count(queries[i]) != b_counts[i]:
+                mismatches += 1
+
+    # plain e2e (C-ABI calls with host buffers)
+    t0 = time.perf_counter()
+    e2e_plain_ms = []
+    for i in range(m):
+        q0 = time.perf_counter()
+        if actions[i] == 1:
+            dev.mutations(queries[i], 0)
+        else:
+            dev.count(queries[i])
+        e2e_plain_ms.append(1000 * (time.perf_counter() - q0))
+    plain_e2e_qps = m / (time.perf_counter() - t0)
+
+    # ---------------- batched e2e through the C-ABI ----------------
+    e2e_s = []
+    for step in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        counts, muts = dev.batch(queries, actions, columns, tile_bits=args.tile_bits, stream=sp)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_qps = n * ws / max_over_ranks(statistics.median(e2e_s), ws)
+    col0 = table.columns[0]
+    prog_bytes = info.n_instr * 16 + n * 16 + info.n_items * 8 + n_mut * 4
+    d2h = n * 8 + n_mut * col0.n_symbols * col0.L * 4
+
+    # ---------------- roofline: plain container pass ----------------
+    payload_b, desc_b = dev.mutation_bytes(0)
+    mut_idx = [i for i in range(n) if actions[i] == 1][:16]
+    ctr_ms = []
+    for i in mut_idx:
+        dev.plain_launch(i, sp, parts=1)  # filter tile and count
+        flush_l2()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        dev.plain_launch(i, sp, parts=2)  # container pass only
+        e1.record(stream)
+        e1.synchronize()
+        ctr_ms.append(e0.elapsed_time(e1))
+    ctr_avg_ms = statistics.mean(ctr_ms)
+    alg_bytes = payload_b + desc_b + table.n_chunks * 8192
+    peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (ctr_avg_ms / 1000.0) / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "mut_ctr_kernel_2M.traffic.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+
+    # ---------------- CPU baseline ----------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cqps, cdesc, cp50, cp99, csecs = cpu_leg(table, queries, actions, columns, args.cpu_sample, threads)
+        cpu = {"value": cqps, "unit": "queries/s", "cores": threads, "kind": "port", "sample": cdesc,
+               "p50_ms": cp50, "p99_ms": cp99, "seconds": csecs}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded generator: 2M sequences, Zipf(1.1) substitutions, N-runs, gaps, 12 aa genes)",
+            "config": {"workload": f"{args.rows} sequences x {args.batch}-query batches "
+                                   f"({n - n_mut} Aggregated count + {n_mut} nucleotide Mutations)",
+                       "rows": args.rows, "batch": n, "mutations_per_batch": n_mut, "aa_genes": 12,
+                       "tile_bits": info.tile_bits, "grid": info.grid, "planner": "rule-based ordering",
+                       "l2": "flushed before every timed step (256 MiB write, outside the events)",
+                       "parallelism": f"replicas x{ws}"},
+            "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+            "latency_note": "batched: every query of a batch completes with its batch",
+            "plain": {"qps": plain_qps, "p50_ms": float(np.percentile(plain_ms, 50)),
+                      "p99_ms": float(np.percentile(plain_ms, 99)), "queries": m, "e2e_qps": plain_e2e_qps,
+                      "e2e_p99_ms": float(np.percentile(e2e_plain_ms, 99))},
+            "speedup_vs_plain": value / plain_qps,
+            "parity_plain_vs_batched_mismatches": mismatches,
+            "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": launches_per_step * args.steps,
+            "kernels_ms": kernels_ms,
+            "roofline": {"kernel": "mut_ctr_kernel (plain Mutations container pass, nucleotide column)",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": ctr_avg_ms,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    dev.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -153,6 +153,46 @@ int rhy_count(RhyDevice* d, const char* expr, void* stream, uint64_t* out);
 int rhy_eval(RhyDevice* d, const char* expr, void* stream, uint32_t* out_bits, uint64_t* out_count);
 /* counts: n_symbols * L words, counts[symbol * L + position]; filter_count may be NULL. */
 int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream, uint32_t* counts, uint64_t* filter_count);
+/* ---- batched path (no reference counterpart: the reference runs one query per worker thread,
+ * app/src/api.cpp:39-51) ----
+ * n queries; actions[i] 0 = count, 1 = mutations of columns[i]. counts[i] receives the filter
+ * cardinality; for a mutations query mut_counts[i] (n_symbols * L words) receives the symbol
+ * counts (mut_counts may be NULL, entries of count queries are ignored). tile_bits 0 = default.
+ * Synchronous on `stream`. */
+int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+              uint32_t tile_bits, void* stream, uint64_t* counts, uint32_t* const* mut_counts);
+
+typedef struct {
+   uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
+   uint64_t device_bytes;
+} RhyBatchInfo;
+
+/* Split form of rhy_batch for callers that reuse one batch shape: prepare plans and stages the
+ * batch (allocates on first use or growth), launch enqueues it without synchronising,
+ * capture/replay record it once into a CUDA graph and replay it, results copies the outputs of the
+ * last completed launch (the caller synchronises the stream first). */
+int rhy_batch_prepare(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+                      uint32_t tile_bits, uint32_t plan_threads);
+int rhy_batch_launch(RhyDevice* d, void* stream, int copy_in, int copy_out);
+int rhy_batch_capture(RhyDevice* d, void* stream);
+int rhy_batch_replay(RhyDevice* d, void* stream);
+int rhy_batch_results(RhyDevice* d, uint64_t* counts, uint32_t* const* mut_counts);
+int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out);
+/* Variants for timing: capture without the host copies; launch a subset of the kernels
+ * (bit 0 filter, bits 1..4 transpose / container / coverage / final mutations kernels). */
+int rhy_batch_capture_ex(RhyDevice* d, void* stream, int copy_in, int copy_out);
+int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts);
+
+/* Plain single-query path split for timing with device-resident inputs: prepare plans the queries
+ * and keeps their programs in HBM; launch enqueues query i (filter, and the mutations kernels for
+ * a mutations query) into the handle's scratch without synchronising. */
+int rhy_plain_prepare(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n);
+int rhy_plain_launch(RhyDevice* d, uint32_t i, void* stream);
+/* parts: bit 0 zeroing + filter kernel, bits 1..3 container / coverage / final mutations kernels. */
+int rhy_plain_launch_parts(RhyDevice* d, uint32_t i, void* stream, uint32_t parts);
+/* Bytes a mutations pass over `column` must read: container payloads plus descriptors. */
+int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_bytes, uint64_t* descriptor_bytes);
+
 /* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */
 int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,
                       RhyMutationRow* rows, size_t cap, size_t* n_rows);

@@ -30,7 +30,7 @@ def _sources():
 
 
 def _headers():
-    return sorted(CSRC.glob("*.h")) + [HERE.parent / "include" / "rhydb_gpu.h"]
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "rhydb_gpu.h"]
 
 
 def _compile(src: Path, verbose: bool) -> Path:

@@ -24,6 +24,18 @@ struct RhyTable {
 struct RhyDevice {
    const RhyTable* table;
    std::unique_ptr<rhygpu::Engine> engine;
+   // plain path with device-resident programs
+   struct PlainQuery {
+      rhygpu::Program prog;
+      size_t code_off;
+      int action;
+      uint32_t column;
+   };
+   std::vector<PlainQuery> plain;
+   rhygpu::Instr* d_plain_code = nullptr;
+   ~RhyDevice() {
+      if (d_plain_code) cudaFree(d_plain_code);
+   }
 };
 
 namespace {
@@ -385,6 +397,193 @@ int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream,
       if (column >= d->table->image.seq.size()) throw std::invalid_argument("no such sequence column");
       const rhygpu::Program p = d->engine->plan(expr);
       d->engine->mutations(p, static_cast<int>(column), counts, filter_count, static_cast<cudaStream_t>(stream));
+   });
+}
+
+namespace {
+
+std::vector<rhygpu::BatchQuery> make_batch(RhyDevice* d, const char* const* exprs, const int* actions,
+                                           const uint32_t* columns, uint32_t n, uint32_t plan_threads) {
+   need(exprs, "exprs");
+   std::vector<std::string> texts(n);
+   for (uint32_t i = 0; i < n; ++i) {
+      need(exprs[i], "expression");
+      texts[i] = exprs[i];
+   }
+   std::vector<rhygpu::Program> progs = rhygpu::plan_many(d->table->image, texts, plan_threads);
+   std::vector<rhygpu::BatchQuery> qs(n);
+   for (uint32_t i = 0; i < n; ++i) {
+      qs[i].prog = std::move(progs[i]);
+      qs[i].action = actions ? actions[i] : 0;
+      qs[i].column = columns ? static_cast<int>(columns[i]) : 0;
+      if (qs[i].action != 0 && qs[i].action != 1) throw std::invalid_argument("action must be 0 (count) or 1 (mutations)");
+   }
+   return qs;
+}
+
+void copy_batch_results(RhyDevice* d, uint32_t n, uint64_t* counts, uint32_t* const* mut_counts) {
+   rhygpu::Engine& e = *d->engine;
+   const auto& b = e.batch();
+   if (n != b.n_queries) throw std::invalid_argument("result arrays do not match the prepared batch");
+   e.check_error_flag();
+   for (uint32_t i = 0; i < n; ++i) {
+      if (counts) counts[i] = e.batch_count(i);
+      if (mut_counts && mut_counts[i]) {
+         const uint32_t* src = e.batch_mutation_counts(i);
+         if (!src) continue;
+         uint32_t col = 0;
+         for (const auto& g : b.groups) {
+            const uint32_t slot = b.slot_of_query[i];
+            if (slot >= g.slot_begin && slot < g.slot_begin + g.n) col = static_cast<uint32_t>(g.column);
+         }
+         const auto& dc = e.host_view().seq[col];
+         std::memcpy(mut_counts[i], src, static_cast<size_t>(dc.nsym) * dc.L * 4);
+      }
+   }
+}
+
+}  // namespace
+
+int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+              uint32_t tile_bits, void* stream, uint64_t* counts, uint32_t* const* mut_counts) {
+   return guarded([&] {
+      need(d, "device");
+      if (n == 0) return;
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_prepare(make_batch(d, exprs, actions, columns, n, 0), tile_bits);
+      cudaStream_t s = d->engine->stream_for(static_cast<cudaStream_t>(stream));
+      d->engine->batch_enqueue(s, true, true);
+      rhygpu::cuda_check(cudaStreamSynchronize(s), "batch");
+      copy_batch_results(d, n, counts, mut_counts);
+   });
+}
+
+int rhy_batch_prepare(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+                      uint32_t tile_bits, uint32_t plan_threads) {
+   return guarded([&] {
+      need(d, "device");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      d->engine->batch_prepare(make_batch(d, exprs, actions, columns, n, plan_threads), tile_bits);
+   });
+}
+
+int rhy_batch_launch(RhyDevice* d, void* stream, int copy_in, int copy_out) {
+   return guarded([&] {
+      need(d, "device");
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_enqueue(static_cast<cudaStream_t>(stream), copy_in != 0, copy_out != 0);
+   });
+}
+
+int rhy_batch_capture(RhyDevice* d, void* stream) {
+   return guarded([&] {
+      need(d, "device");
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_capture(static_cast<cudaStream_t>(stream));
+   });
+}
+
+int rhy_batch_replay(RhyDevice* d, void* stream) {
+   return guarded([&] {
+      need(d, "device");
+      d->engine->batch_replay(static_cast<cudaStream_t>(stream));
+   });
+}
+
+int rhy_batch_results(RhyDevice* d, uint64_t* counts, uint32_t* const* mut_counts) {
+   return guarded([&] {
+      need(d, "device");
+      copy_batch_results(d, d->engine->batch().n_queries, counts, mut_counts);
+   });
+}
+
+int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out) {
+   return guarded([&] {
+      need(d, "device");
+      need(out, "out");
+      const auto& b = d->engine->batch();
+      out->n_queries = b.n_queries;
+      out->n_mutation_slots = b.n_slots;
+      out->n_items = b.n_items;
+      out->n_instr = b.n_code;
+      out->max_depth = b.max_depth;
+      out->tile_bits = b.tile_bits;
+      out->grid = b.grid;
+      out->device_bytes = d->engine->device_bytes();
+   });
+}
+
+int rhy_plain_prepare(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n) {
+   return guarded([&] {
+      need(d, "device");
+      auto qs = make_batch(d, exprs, actions, columns, n, 0);
+      d->plain.clear();
+      size_t off = 0;
+      std::vector<rhygpu::Instr> code;
+      for (auto& q : qs) {
+         d->plain.push_back({std::move(q.prog), off, q.action, static_cast<uint32_t>(q.column)});
+         const auto& p = d->plain.back().prog;
+         code.insert(code.end(), p.code.begin(), p.code.end());
+         off += p.code.size();
+      }
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      if (d->d_plain_code) cudaFree(d->d_plain_code);
+      d->d_plain_code = nullptr;
+      rhygpu::cuda_check(cudaMalloc(&d->d_plain_code, std::max<size_t>(code.size(), 1) * sizeof(rhygpu::Instr)), "cudaMalloc");
+      rhygpu::cuda_check(cudaMemcpy(d->d_plain_code, code.data(), code.size() * sizeof(rhygpu::Instr), cudaMemcpyHostToDevice),
+                         "upload programs");
+   });
+}
+
+int rhy_plain_launch_parts(RhyDevice* d, uint32_t i, void* stream, uint32_t parts) {
+   return guarded([&] {
+      need(d, "device");
+      if (i >= d->plain.size()) throw std::invalid_argument("no such prepared query");
+      rhygpu::Engine& e = *d->engine;
+      const auto& q = d->plain[i];
+      cudaStream_t s = e.stream_for(static_cast<cudaStream_t>(stream));
+      if (parts & 1) rhygpu::cuda_check(cudaMemsetAsync(e.d_count, 0, sizeof(unsigned long long), s), "memset");
+      if (q.action == 1) {
+         const auto& dc = e.host_view().seq[q.column];
+         if (parts & 1) {
+            rhygpu::cuda_check(cudaMemsetAsync(e.d_counts, 0, static_cast<size_t>(dc.nsym) * dc.L * 4, s), "memset");
+            rhygpu::cuda_check(cudaMemsetAsync(e.d_scratch, 0, rhygpu::mut_scratch_words(dc.L) * 4, s), "memset");
+            e.launch_count(d->d_plain_code + q.code_off, q.prog, e.d_count, e.d_filter, s);
+         }
+         if (parts >> 1)
+            e.launch_mutations(static_cast<int>(q.column), e.d_filter, e.d_count, e.d_counts, e.d_scratch, s,
+                               (parts >> 1) & rhygpu::MUT_PART_ALL);
+      } else if (parts & 1) {
+         e.launch_count(d->d_plain_code + q.code_off, q.prog, e.d_count, nullptr, s);
+      }
+   });
+}
+
+int rhy_plain_launch(RhyDevice* d, uint32_t i, void* stream) { return rhy_plain_launch_parts(d, i, stream, 15); }
+
+int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_bytes, uint64_t* descriptor_bytes) {
+   return guarded([&] {
+      need(d, "device");
+      const auto& c = d->table->image.seq.at(column);
+      if (payload_bytes) *payload_bytes = c.vertical.payload_bytes();
+      if (descriptor_bytes) *descriptor_bytes = c.vertical.ctrs.size() * sizeof(rhygpu::CtrDesc);
+   });
+}
+
+int rhy_batch_capture_ex(RhyDevice* d, void* stream, int copy_in, int copy_out) {
+   return guarded([&] {
+      need(d, "device");
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_capture(static_cast<cudaStream_t>(stream), copy_in != 0, copy_out != 0);
+   });
+}
+
+int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts) {
+   return guarded([&] {
+      need(d, "device");
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_enqueue(static_cast<cudaStream_t>(stream), false, false, parts);
    });
 }
 

@@ -66,6 +66,14 @@ struct MutPart {
    uint32_t pad;
 };
 
+// Per-query scratch of the mutations pass, in u32 words:
+//   start_hist[L+1] | end_hist[L+1] | missing_diff[L+1] | seg_start[nseg] | seg_end[nseg] | seg_missing[nseg]
+// The histograms are difference arrays over positions; the segment totals (MUT_SEG positions each)
+// let every CTA of the final pass start its prefix sums without scanning the whole genome.
+constexpr uint32_t MUT_SEG = 1024;
+__host__ __device__ inline uint32_t mut_nseg(uint32_t L) { return (L + 1 + MUT_SEG - 1) / MUT_SEG; }
+__host__ __device__ inline size_t mut_scratch_words(uint32_t L) { return 3ull * (L + 1) + 3ull * mut_nseg(L); }
+
 // One unit of the batched filter kernel: tile `tile` of query `query`.
 struct WorkItem {
    uint32_t query;
@@ -90,17 +98,26 @@ void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr*
                          uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
                          uint32_t* d_next, uint32_t grid, int* d_err, void* stream);
 
-// Mutations. counts: nsym * L u32 (zeroed by the caller). scratch: 3 * (L + 1) u32 (zeroed by the caller).
+// Kernel selection masks (all bits set = the whole pass); used to time the kernels one by one.
+enum : uint32_t { MUT_PART_CTR = 1, MUT_PART_COV = 2, MUT_PART_FINAL = 4, MUT_PART_ALL = 7 };
+enum : uint32_t { BMUT_PART_TRANSPOSE = 1, BMUT_PART_CTR = 2, BMUT_PART_COV = 4, BMUT_PART_FINAL = 8, BMUT_PART_ALL = 15 };
+
+// Mutations. counts: nsym * L u32 and scratch: mut_scratch_words(L) u32, both zeroed by the caller.
 // The filter count decides on the device between the full path (|F| == rows: stored cardinalities),
 // the empty path and the mixed path, so no host round trip sits between filter and mutations.
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filter,
-                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream);
+                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
+                      uint32_t parts = MUT_PART_ALL);
 
-// Batched mutations over nq filters (query-major dense tiles), counts[q][nsym][L].
+// Batched mutations over nq filters (slot-major dense tiles, nchunks * CHUNK_WORDS each):
+// counts[slot][nsym][L] and scratch[slot][mut_scratch_words(L)] zeroed by the caller;
+// d_fcounts[d_slot_query[slot]] is the cardinality of the slot's filter; d_masks holds
+// mutations_batch_mask_bytes(nq, nchunks).
+size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks);
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
-                            const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filters, uint32_t nq,
-                            const unsigned long long* d_filter_counts, uint32_t* d_counts, uint32_t* d_scratch,
-                            void* stream);
+                            const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
+                            const uint32_t* d_slot_query, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
+                            int* d_err, void* stream, uint32_t parts = BMUT_PART_ALL);
 
 }  // namespace rhygpu

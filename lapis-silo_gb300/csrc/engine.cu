@@ -91,7 +91,7 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
       d_filter = static_cast<uint32_t*>(alloc(static_cast<size_t>(nchunks) * CHUNK_WORDS * 4));
       d_count = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
       counts_words = max_words;
-      scratch_words = 3ull * (max_L + 1);
+      scratch_words = mut_scratch_words(max_L);
       d_counts = static_cast<uint32_t*>(alloc(counts_words * 4));
       d_scratch = static_cast<uint32_t*>(alloc(scratch_words * 4));
       d_code = static_cast<Instr*>(alloc(MAX_PROGRAM * sizeof(Instr)));
@@ -114,6 +114,8 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
 Engine::~Engine() {
    cudaSetDevice(device_);
    if (stream_) cudaStreamSynchronize(stream_);
+   cudaDeviceSynchronize();
+   batch_free();
    for (void* p : allocs_) cudaFree(p);
    if (h_code_) cudaFreeHost(h_code_);
    if (h_count_) cudaFreeHost(h_count_);
@@ -145,10 +147,10 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
 }
 
 void Engine::launch_mutations(int column, const uint32_t* filter, const unsigned long long* count, uint32_t* counts,
-                              uint32_t* scratch, cudaStream_t stream) {
+                              uint32_t* scratch, cudaStream_t stream, uint32_t parts) {
    const DevSeqCol& c = view_.seq[column];
    rhygpu::launch_mutations(d_table_, c, static_cast<uint32_t>(column), nchunks(), d_parts_[column], nparts_[column],
-                            filter, count, counts, scratch, stream);
+                            filter, count, counts, scratch, stream, parts);
    cuda_check(cudaGetLastError(), "mutations kernel launch");
 }
 
@@ -203,7 +205,7 @@ void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint
    upload_program(p, d_code, stream);
    cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream), "memset");
    cuda_check(cudaMemsetAsync(d_counts, 0, words * 4, stream), "memset");
-   cuda_check(cudaMemsetAsync(d_scratch, 0, 3ull * (c.L + 1) * 4, stream), "memset");
+   cuda_check(cudaMemsetAsync(d_scratch, 0, mut_scratch_words(c.L) * 4, stream), "memset");
    launch_count(d_code, p, d_count, d_filter, stream);
    launch_mutations(column, d_filter, d_count, d_counts, d_scratch, stream);
    cuda_check(cudaMemcpyAsync(h_count_, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "copy count");
@@ -212,6 +214,233 @@ void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint
    cuda_check(cudaStreamSynchronize(stream), "mutations");
    check_error_flag();
    if (filter_count) *filter_count = *h_count_;
+}
+
+}  // namespace rhygpu
+
+// =================================================================================================
+// Batched path
+
+namespace rhygpu {
+
+std::vector<Program> plan_many(const TableImage& t, const std::vector<std::string>& exprs, uint32_t threads,
+                               const LowerOptions& opt) {
+   std::vector<Program> out(exprs.size());
+   const Estimator est = rule_estimator(t);
+   parallel_for(static_cast<uint32_t>(exprs.size()), threads,
+                [&](uint32_t i) { out[i] = plan_filter(exprs[i], t, &est, opt, nullptr); });
+   return out;
+}
+
+uint32_t Engine::fit_tile_bits(uint32_t requested, uint32_t depth) const {
+   uint32_t W = requested ? requested : tile_bits;
+   while (W > 4096 && static_cast<size_t>(depth) * (W / 8) > 200 * 1024) W >>= 1;
+   if (static_cast<size_t>(depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
+   return W;
+}
+
+namespace {
+template <typename T>
+void grow_device(T*& p, size_t& cap, size_t n) {
+   if (n <= cap && p) return;
+   if (p) cudaFree(p);
+   p = nullptr;
+   const size_t want = std::max<size_t>(n + n / 4, 16);
+   cuda_check(cudaMalloc(&p, want * sizeof(T)), "cudaMalloc (batch)");
+   cap = want;
+}
+template <typename T>
+void grow_host(T*& p, size_t n, size_t& cap) {
+   if (n <= cap && p) return;
+   if (p) cudaFreeHost(p);
+   p = nullptr;
+   const size_t want = std::max<size_t>(n + n / 4, 16);
+   cuda_check(cudaMallocHost(&p, want * sizeof(T)), "cudaMallocHost (batch)");
+   cap = want;
+}
+}  // namespace
+
+void Engine::batch_free() {
+   BatchState& b = batch_;
+   if (b.graph) cudaGraphExecDestroy(b.graph);
+   for (void* p : {static_cast<void*>(b.h_code), static_cast<void*>(b.h_q), static_cast<void*>(b.h_items),
+                   static_cast<void*>(b.h_slot_query), static_cast<void*>(b.h_counts), static_cast<void*>(b.h_mcounts)})
+      if (p) cudaFreeHost(p);
+   for (void* p : {static_cast<void*>(b.d_code), static_cast<void*>(b.d_q), static_cast<void*>(b.d_items),
+                   static_cast<void*>(b.d_slot_query), static_cast<void*>(b.d_counts), static_cast<void*>(b.d_next),
+                   static_cast<void*>(b.d_tiles), static_cast<void*>(b.d_mcounts), static_cast<void*>(b.d_mscratch),
+                   static_cast<void*>(b.d_masks)})
+      if (p) cudaFree(p);
+   b = BatchState{};
+}
+
+void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested_tile_bits) {
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   BatchState& b = batch_;
+   if (b.graph) {
+      cudaGraphExecDestroy(b.graph);
+      b.graph = nullptr;
+   }
+   const uint32_t n = static_cast<uint32_t>(qs.size());
+   uint32_t depth = 1;
+   size_t ncode = 0;
+   for (const auto& q : qs) {
+      depth = std::max(depth, q.prog.max_depth);
+      ncode += q.prog.code.size();
+      if (q.action == 1 && (q.column < 0 || static_cast<size_t>(q.column) >= table_.seq.size()))
+         throw std::invalid_argument("no such sequence column");
+   }
+   const uint32_t W = fit_tile_bits(requested_tile_bits, depth);
+   const uint32_t tiles_per_query = nchunks() * (CHUNK_ROWS / W);
+   // mutation slots grouped by column
+   std::vector<std::vector<uint32_t>> by_col(table_.seq.size());
+   for (uint32_t i = 0; i < n; ++i)
+      if (qs[i].action == 1) by_col[qs[i].column].push_back(i);
+   b.groups.clear();
+   b.slot_of_query.assign(n, UINT32_MAX);
+   std::vector<uint32_t> slot_query;
+   size_t counts_words = 0, scratch_words = 0, mask_bytes = 0;
+   for (size_t c = 0; c < by_col.size(); ++c) {
+      if (by_col[c].empty()) continue;
+      BatchState::ColGroup g{static_cast<int>(c), static_cast<uint32_t>(slot_query.size()),
+                             static_cast<uint32_t>(by_col[c].size()), counts_words, scratch_words};
+      for (uint32_t qi : by_col[c]) {
+         b.slot_of_query[qi] = static_cast<uint32_t>(slot_query.size());
+         slot_query.push_back(qi);
+      }
+      const DevSeqCol& dc = view_.seq[c];
+      counts_words += static_cast<size_t>(g.n) * dc.nsym * dc.L;
+      scratch_words += static_cast<size_t>(g.n) * mut_scratch_words(dc.L);
+      mask_bytes = std::max(mask_bytes, mutations_batch_mask_bytes(g.n, nchunks()));
+      b.groups.push_back(g);
+   }
+   const uint32_t nslots = static_cast<uint32_t>(slot_query.size());
+   const size_t nitems = static_cast<size_t>(n) * tiles_per_query;
+   if (nitems > 0xFFFFFFFFull) throw std::invalid_argument("batch too large");
+   grow_host(b.h_code, ncode, b.hc_code);
+   grow_device(b.d_code, b.dc_code, ncode);
+   grow_host(b.h_q, n, b.hc_q);
+   grow_device(b.d_q, b.dc_q, n);
+   grow_host(b.h_items, nitems, b.hc_items);
+   grow_device(b.d_items, b.dc_items, nitems);
+   grow_host(b.h_slot_query, nslots, b.hc_slot_query);
+   grow_device(b.d_slot_query, b.dc_slot_query, nslots);
+   grow_host(b.h_counts, n, b.hc_counts);
+   grow_device(b.d_counts, b.dc_counts, n);
+   grow_device(b.d_next, b.dc_next, 1);
+   grow_device(b.d_tiles, b.dc_tiles, static_cast<size_t>(nslots) * nchunks() * CHUNK_WORDS);
+   grow_host(b.h_mcounts, counts_words, b.hc_mcounts);
+   grow_device(b.d_mcounts, b.dc_mcounts, counts_words);
+   grow_device(b.d_mscratch, b.dc_mscratch, scratch_words);
+   grow_device(b.d_masks, b.dc_masks, mask_bytes / 2 + 8);
+   // programs, query descriptors, work items
+   size_t off = 0;
+   for (uint32_t i = 0; i < n; ++i) {
+      const Program& p = qs[i].prog;
+      std::memcpy(b.h_code + off, p.code.data(), p.code.size() * sizeof(Instr));
+      b.h_q[i] = QueryDesc{static_cast<uint32_t>(off), static_cast<uint32_t>(p.code.size()),
+                           b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1, 0};
+      off += p.code.size();
+   }
+   // items: tile-major interleaving spreads the expensive queries over the whole launch
+   size_t k = 0;
+   for (uint32_t t = 0; t < tiles_per_query; ++t)
+      for (uint32_t i = 0; i < n; ++i) b.h_items[k++] = WorkItem{i, t};
+   std::memcpy(b.h_slot_query, slot_query.data(), slot_query.size() * sizeof(uint32_t));
+   b.n_queries = n;
+   b.n_slots = nslots;
+   b.n_items = static_cast<uint32_t>(nitems);
+   b.n_code = static_cast<uint32_t>(ncode);
+   b.max_depth = depth;
+   b.tile_bits = W;
+   b.counts_words = counts_words;
+   b.scratch_words = scratch_words;
+   b.mask_bytes = mask_bytes;
+   int props = 0;
+   cuda_check(cudaDeviceGetAttribute(&props, cudaDevAttrMultiProcessorCount, device_), "attribute");
+   const size_t smem = static_cast<size_t>(depth) * (W / 8);
+   b.grid = static_cast<uint32_t>(props) * static_cast<uint32_t>(filter_batch_blocks_per_sm(smem));
+}
+
+void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t parts) {
+   s = stream_for(s);
+   BatchState& b = batch_;
+   if (b.n_queries == 0) return;
+   if (copy_in) {
+      cuda_check(cudaMemcpyAsync(b.d_code, b.h_code, b.n_code * sizeof(Instr), cudaMemcpyHostToDevice, s), "H2D");
+      cuda_check(cudaMemcpyAsync(b.d_q, b.h_q, b.n_queries * sizeof(QueryDesc), cudaMemcpyHostToDevice, s), "H2D");
+      cuda_check(cudaMemcpyAsync(b.d_items, b.h_items, static_cast<size_t>(b.n_items) * sizeof(WorkItem),
+                                 cudaMemcpyHostToDevice, s),
+                 "H2D");
+      if (b.n_slots)
+         cuda_check(cudaMemcpyAsync(b.d_slot_query, b.h_slot_query, b.n_slots * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
+                    "H2D");
+   }
+   if (parts & 1) {
+      cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
+      cuda_check(cudaMemsetAsync(b.d_next, 0, sizeof(uint32_t), s), "memset");
+      if (b.counts_words) cuda_check(cudaMemsetAsync(b.d_mcounts, 0, b.counts_words * 4, s), "memset");
+      if (b.scratch_words) cuda_check(cudaMemsetAsync(b.d_mscratch, 0, b.scratch_words * 4, s), "memset");
+      launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.tile_bits, b.max_depth, b.d_tiles,
+                          b.d_counts, b.d_next, b.grid, d_err, s);
+      cuda_check(cudaGetLastError(), "filter batch launch");
+   }
+   const size_t words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
+   for (const auto& g : b.groups) {
+      launch_mutations_batch(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), nchunks(),
+                             b.d_tiles + static_cast<size_t>(g.slot_begin) * words, g.n, b.d_counts,
+                             b.d_slot_query + g.slot_begin, b.d_masks, b.d_mcounts + g.counts_off,
+                             b.d_mscratch + g.scratch_off, d_err, s, (parts >> 1) & BMUT_PART_ALL);
+      cuda_check(cudaGetLastError(), "mutations batch launch");
+   }
+   if (copy_out) {
+      cuda_check(cudaMemcpyAsync(b.h_counts, b.d_counts, b.n_queries * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+                 "D2H");
+      if (b.counts_words)
+         cuda_check(cudaMemcpyAsync(b.h_mcounts, b.d_mcounts, b.counts_words * 4, cudaMemcpyDeviceToHost, s), "D2H");
+      cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+   }
+}
+
+void Engine::batch_capture(cudaStream_t s, bool copy_in, bool copy_out) {
+   s = stream_for(s);
+   BatchState& b = batch_;
+   if (b.graph) {
+      cudaGraphExecDestroy(b.graph);
+      b.graph = nullptr;
+   }
+   cudaGraph_t g = nullptr;
+   cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+   try {
+      batch_enqueue(s, copy_in, copy_out);
+   } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+   }
+   cuda_check(cudaStreamEndCapture(s, &g), "end capture");
+   cudaError_t e = cudaGraphInstantiate(&b.graph, g, 0);
+   cudaGraphDestroy(g);
+   cuda_check(e, "graph instantiate");
+}
+
+void Engine::batch_replay(cudaStream_t s) {
+   s = stream_for(s);
+   if (!batch_.graph) throw std::logic_error("no captured batch");
+   cuda_check(cudaGraphLaunch(batch_.graph, s), "graph launch");
+}
+
+const uint32_t* Engine::batch_mutation_counts(uint32_t query) const {
+   const BatchState& b = batch_;
+   const uint32_t slot = b.slot_of_query.at(query);
+   if (slot == UINT32_MAX) return nullptr;
+   for (const auto& g : b.groups) {
+      if (slot >= g.slot_begin && slot < g.slot_begin + g.n) {
+         const DevSeqCol& dc = view_.seq[g.column];
+         return b.h_mcounts + g.counts_off + static_cast<size_t>(slot - g.slot_begin) * dc.nsym * dc.L;
+      }
+   }
+   return nullptr;
 }
 
 }  // namespace rhygpu

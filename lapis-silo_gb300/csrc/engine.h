@@ -21,6 +21,50 @@ struct CudaError : std::runtime_error {
 
 void cuda_check(cudaError_t e, const char* what);
 
+// One query of a batch.
+struct BatchQuery {
+   Program prog;
+   int action = 0;  // 0 = count, 1 = mutations of `column`
+   int column = 0;
+};
+
+// Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
+struct BatchState {
+   struct ColGroup {
+      int column;
+      uint32_t slot_begin, n;
+      size_t counts_off, scratch_off;  // u32 offsets into the arenas
+   };
+   uint32_t n_queries = 0, n_slots = 0, n_items = 0, n_code = 0, max_depth = 1, tile_bits = 16384, grid = 0;
+   std::vector<ColGroup> groups;
+   std::vector<uint32_t> slot_of_query;  // UINT32_MAX for count-only queries
+   size_t counts_words = 0, scratch_words = 0, mask_bytes = 0;
+   // pinned host staging
+   Instr* h_code = nullptr;
+   QueryDesc* h_q = nullptr;
+   WorkItem* h_items = nullptr;
+   uint32_t* h_slot_query = nullptr;
+   unsigned long long* h_counts = nullptr;
+   uint32_t* h_mcounts = nullptr;
+   // device
+   Instr* d_code = nullptr;
+   QueryDesc* d_q = nullptr;
+   WorkItem* d_items = nullptr;
+   uint32_t* d_slot_query = nullptr;
+   unsigned long long* d_counts = nullptr;
+   uint32_t* d_next = nullptr;
+   uint32_t* d_tiles = nullptr;
+   uint32_t* d_mcounts = nullptr;
+   uint32_t* d_mscratch = nullptr;
+   uint16_t* d_masks = nullptr;
+   // capacities
+   // capacities (elements), one per buffer
+   size_t hc_code = 0, hc_q = 0, hc_items = 0, hc_slot_query = 0, hc_counts = 0, hc_mcounts = 0;
+   size_t dc_code = 0, dc_q = 0, dc_items = 0, dc_slot_query = 0, dc_counts = 0, dc_next = 0, dc_tiles = 0,
+          dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0;
+   cudaGraphExec_t graph = nullptr;
+};
+
 class Engine {
   public:
    Engine(const TableImage& table, int device);
@@ -34,6 +78,8 @@ class Engine {
    const DevTable* d_table() const { return d_table_; }
    const DevTable& host_view() const { return view_; }
    uint64_t device_bytes() const { return device_bytes_; }
+   // The stream a call runs on: the caller's, or the engine's own when the caller passed none.
+   cudaStream_t stream_for(cudaStream_t s) const { return s ? s : stream_; }
 
    // Tile width of the filter kernel (rows per CTA). 4096 .. 65536, power of two.
    uint32_t tile_bits = 16384;
@@ -51,8 +97,26 @@ class Engine {
    void launch_count(const Instr* d_code, const Program& p, unsigned long long* d_count, uint32_t* d_tiles,
                      cudaStream_t stream);
    void launch_mutations(int column, const uint32_t* d_filter, const unsigned long long* d_count, uint32_t* d_counts,
-                         uint32_t* d_scratch, cudaStream_t stream);
+                         uint32_t* d_scratch, cudaStream_t stream, uint32_t parts = MUT_PART_ALL);
    void check_error_flag();
+
+   // ---- batched path ----
+   // Plans every expression (host threads), lays the programs and (query, tile) work items out and
+   // sizes the device buffers (may allocate; call outside timed regions).
+   void batch_prepare(const std::vector<BatchQuery>& qs, uint32_t tile_bits = 0);
+   // Stream-ordered: optional H2D of the staged programs, the persistent filter kernel, the batched
+   // mutations kernels per column, optional D2H of the results into the pinned host buffers.
+   // parts: bit 0 = zeroing + filter kernel, bits 1..4 = transpose, container, coverage and final
+   // mutations kernels (all set = the whole batch); used to time kernels one by one.
+   void batch_enqueue(cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31);
+   // Captures batch_enqueue(copy_in, copy_out) into a CUDA graph for the prepared shape.
+   void batch_capture(cudaStream_t stream, bool copy_in = true, bool copy_out = true);
+   void batch_replay(cudaStream_t stream);
+   const BatchState& batch() const { return batch_; }
+   const uint32_t* batch_mutation_counts(uint32_t query) const;  // pinned host, after the stream synced
+   uint64_t batch_count(uint32_t query) const { return batch_.h_counts[query]; }
+   // Tile width that fits the batch's deepest program in the shared-memory budget.
+   uint32_t fit_tile_bits(uint32_t requested, uint32_t depth) const;
 
    const MutPart* d_parts(int column) const { return d_parts_[column]; }
    uint32_t nparts(int column) const { return nparts_[column]; }
@@ -85,6 +149,15 @@ class Engine {
    unsigned long long* h_count_ = nullptr; // pinned
    int* h_err_ = nullptr;                  // pinned
    uint64_t device_bytes_ = 0;
+   BatchState batch_;
+   void batch_free();
 };
+
+// Plans many expressions on host threads (rewrite -> compile -> lower per expression).
+std::vector<Program> plan_many(const TableImage& t, const std::vector<std::string>& exprs, uint32_t threads,
+                               const LowerOptions& opt = {});
+
+// Occupancy of the persistent filter kernel for a given shared-memory stack size.
+int filter_batch_blocks_per_sm(size_t smem_bytes);
 
 }  // namespace rhygpu

@@ -113,7 +113,7 @@ __device__ void push_covered(uint32_t* t, const TileCtx& c, const DevSeqCol* __r
    const uint32_t nb = __ldg(boff), ne = __ldg(boff + 1);
    for (uint32_t i = nb + threadIdx.x; i < ne; i += blockDim.x) {
       const uint2 raw = __ldg(reinterpret_cast<const uint2*>(col->nblk) + i);
-      const uint32_t r = raw.x - c.row0;
+      const uint32_t r = (raw.x & 0xFFFFu) - c.row0;
       const uint32_t lo = raw.y & 0xFFFFu, hi = raw.y >> 16;
       if (r < c.W && lo <= q && q < hi) atomicAnd(&t[r >> 5], ~(1u << (r & 31)));
    }
@@ -418,244 +418,6 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
       __syncthreads();
    }
 }
-
-// ------------------------------------------------------------------------------------------------
-// Mutations
-
-constexpr uint32_t MT = 256;       // threads per mutations CTA
-constexpr uint32_t SMALL_ARRAY = 32;
-
-__device__ __forceinline__ uint32_t test_bit(const uint32_t* F, uint32_t r) { return (F[r >> 5] >> (r & 31)) & 1u; }
-
-__device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, uint32_t b) {  // popcount of F in [a, b)
-   if (a >= b) return 0;
-   const uint32_t wa = a >> 5, wb = (b - 1) >> 5;
-   uint32_t s = 0;
-   for (uint32_t w = wa; w <= wb; ++w) {
-      uint32_t m = 0xFFFFFFFFu;
-      if (w == wa) m &= 0xFFFFFFFFu << (a & 31);
-      if (w == wb) m &= 0xFFFFFFFFu >> (31 - ((b - 1) & 31));
-      s += __popc(F[w] & m);
-   }
-   return s;
-}
-
-// Warp-cooperative |F ∩ container|.
-__device__ uint32_t warp_count(const CtrDesc& d, const uint32_t* F, const uint16_t* __restrict__ payload) {
-   const uint32_t lane = threadIdx.x & 31;
-   const uint16_t* p = payload + d.payload;
-   uint32_t c = 0;
-   if (d.type == CT_ARRAY) {
-      const uint32_t card = d.card_m1 + 1u;
-      for (uint32_t k = lane; k < card; k += 32) c += test_bit(F, __ldg(p + k));
-   } else if (d.type == CT_BITSET) {
-      const uint4* b = reinterpret_cast<const uint4*>(p);
-      const uint4* f = reinterpret_cast<const uint4*>(F);
-      for (uint32_t k = lane; k < CHUNK_WORDS / 4; k += 32) {
-         const uint4 x = __ldg(b + k);
-         const uint4 y = f[k];
-         c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
-      }
-   } else {
-      for (uint32_t k = lane; k < d.nruns; k += 32) {
-         const uint32_t s = __ldg(p + 2 * k);
-         c += count_range(F, s, s + __ldg(p + 2 * k + 1) + 1u);
-      }
-   }
-   return __reduce_add_sync(0xFFFFFFFFu, c);
-}
-
-__global__ void __launch_bounds__(MT) mut_ctr_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                     const MutPart* __restrict__ parts, uint32_t nparts,
-                                                     const uint32_t* __restrict__ filter,
-                                                     const unsigned long long* __restrict__ fcount, uint32_t* counts) {
-   __shared__ __align__(16) uint32_t F[CHUNK_WORDS];
-   // |F| == all rows: counts are the stored cardinalities (reference: mutations_node.cpp:240-266);
-   // |F| == 0: nothing to count (reference: mutations_node.cpp:279-286).
-   const unsigned long long fc = *fcount;
-   if (fc == 0) return;
-   const bool full = fc == tab->n_rows;
-   const DevSeqCol* cs = &tab->seq[col];
-   const CtrDesc* __restrict__ ctrs = cs->ctrs;
-   const uint16_t* __restrict__ payload = cs->payload;
-   const uint32_t L = cs->L;
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-   for (uint32_t pi = blockIdx.x; pi < nparts; pi += gridDim.x) {
-      const MutPart P = parts[pi];
-      if (!full) {
-         const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(P.v) * CHUNK_WORDS);
-         uint4* dst = reinterpret_cast<uint4*>(F);
-         for (uint32_t k = threadIdx.x; k < CHUNK_WORDS / 4; k += blockDim.x) dst[k] = __ldg(src + k);
-      }
-      __syncthreads();
-      for (uint32_t base = P.begin + warp * 32; base < P.end; base += nw * 32) {
-         const uint32_t idx = base + lane;
-         const bool valid = idx < P.end;
-         uint4 raw = make_uint4(0, 0, 0, 0);
-         if (valid) raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + idx);
-         const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
-         uint32_t cnt = 0;
-         bool big = false;
-         if (valid) {
-            if (full) {
-               cnt = d.card_m1 + 1u;
-            } else if (d.type == CT_ARRAY && d.card_m1 < SMALL_ARRAY) {
-               const uint16_t* p = payload + d.payload;
-               for (uint32_t k = 0; k <= d.card_m1; ++k) cnt += test_bit(F, __ldg(p + k));
-            } else {
-               big = true;
-            }
-         }
-         if (valid && !big && cnt) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], cnt);
-         uint32_t bigmask = __ballot_sync(0xFFFFFFFFu, big);
-         while (bigmask) {
-            const int j = __ffs(bigmask) - 1;
-            bigmask &= bigmask - 1;
-            uint4 rj;
-            rj.x = __shfl_sync(0xFFFFFFFFu, raw.x, j);
-            rj.y = __shfl_sync(0xFFFFFFFFu, raw.y, j);
-            rj.z = __shfl_sync(0xFFFFFFFFu, raw.z, j);
-            rj.w = __shfl_sync(0xFFFFFFFFu, raw.w, j);
-            const CtrDesc dj = *reinterpret_cast<const CtrDesc*>(&rj);
-            const uint32_t c = warp_count(dj, F, payload);
-            if (lane == 0 && c) atomicAdd(&counts[static_cast<size_t>(dj.sym) * L + dj.key], c);
-         }
-      }
-      __syncthreads();
-   }
-}
-
-// Blocks [0, nblocks): missing intervals of one position block; blocks [nblocks, nblocks + nchunks):
-// coverage exceptions of one chunk. scratch = start_hist[L+1] | end_hist[L+1] | missing[L+1].
-__global__ void __launch_bounds__(MT) mut_cov_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                     const uint32_t* __restrict__ filter,
-                                                     const unsigned long long* __restrict__ fcount, uint32_t* scratch) {
-   const DevSeqCol* cs = &tab->seq[col];
-   const unsigned long long fc = *fcount;
-   if (fc == 0) return;
-   const bool full = fc == tab->n_rows;
-   const uint32_t L = cs->L;
-   const uint32_t nchunks = tab->nchunks;
-   uint32_t* start_hist = scratch;
-   uint32_t* end_hist = scratch + (L + 1);
-   uint32_t* missing = scratch + 2 * (L + 1);
-   if (blockIdx.x < cs->nblocks) {
-      __shared__ int diff[NBLOCK + 1];
-      const uint32_t b = blockIdx.x;
-      for (uint32_t i = threadIdx.x; i <= NBLOCK; i += blockDim.x) diff[i] = 0;
-      __syncthreads();
-      for (uint32_t v = 0; v < nchunks; ++v) {
-         const uint32_t* boff = cs->nblk_off + static_cast<size_t>(b) * nchunks + v;
-         const uint32_t nb = __ldg(boff), ne = __ldg(boff + 1);
-         const uint32_t* Fv = filter + static_cast<size_t>(v) * CHUNK_WORDS;
-         for (uint32_t i = nb + threadIdx.x; i < ne; i += blockDim.x) {
-            const uint2 raw = __ldg(reinterpret_cast<const uint2*>(cs->nblk) + i);
-            if (full || ((__ldg(Fv + (raw.x >> 5)) >> (raw.x & 31)) & 1u)) {
-               atomicAdd(&diff[raw.y & 0xFFFFu], 1);
-               atomicSub(&diff[raw.y >> 16], 1);
-            }
-         }
-      }
-      __syncthreads();
-      if (threadIdx.x < 32) {
-         // inclusive scan of diff[0..NBLOCK) by one warp, 4 entries per lane
-         const uint32_t lane = threadIdx.x;
-         int v[NBLOCK / 32];
-         int s = 0;
-         for (uint32_t k = 0; k < NBLOCK / 32; ++k) {
-            s += diff[lane * (NBLOCK / 32) + k];
-            v[k] = s;
-         }
-         int incl = s;
-         for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (static_cast<int>(lane) >= o) incl += y;
-         }
-         const int excl = incl - s;
-         for (uint32_t k = 0; k < NBLOCK / 32; ++k) {
-            const uint32_t p = b * NBLOCK + lane * (NBLOCK / 32) + k;
-            if (p < L) missing[p] = static_cast<uint32_t>(excl + v[k]);
-         }
-      }
-   } else {
-      const uint32_t v = blockIdx.x - cs->nblocks;
-      if (v >= nchunks) return;
-      const uint32_t xb = __ldg(cs->exc_off + v), xe = __ldg(cs->exc_off + v + 1);
-      const uint32_t* Fv = filter + static_cast<size_t>(v) * CHUNK_WORDS;
-      for (uint32_t i = xb + threadIdx.x; i < xe; i += blockDim.x) {
-         const uint4 raw = __ldg(reinterpret_cast<const uint4*>(cs->exc) + i);
-         if (full || ((__ldg(Fv + (raw.x >> 5)) >> (raw.x & 31)) & 1u)) {
-            atomicAdd(&start_hist[raw.y], 1u);
-            atomicAdd(&end_hist[raw.z], 1u);
-         }
-      }
-   }
-}
-
-constexpr uint32_t FIN_T = 1024;
-
-__device__ __forceinline__ uint32_t block_reduce_all(uint32_t v, uint32_t* red) {
-   v = __reduce_add_sync(0xFFFFFFFFu, v);
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   __syncthreads();
-   if (lane == 0) red[warp] = v;
-   __syncthreads();
-   uint32_t s = 0;
-   for (uint32_t i = 0; i < (blockDim.x >> 5); ++i) s += red[i];
-   __syncthreads();
-   return s;
-}
-
-__device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t* red) {
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   uint32_t x = v;
-   for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-      if (static_cast<int>(lane) >= o) x += y;
-   }
-   __syncthreads();
-   if (lane == 31) red[warp] = x;
-   __syncthreads();
-   uint32_t add = 0;
-   for (uint32_t i = 0; i < warp; ++i) add += red[i];
-   __syncthreads();
-   return x + add;
-}
-
-// reference counts per position: |F| - outside coverage - missing - sum over stored symbols.
-__global__ void __launch_bounds__(FIN_T) mut_final_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                          const unsigned long long* __restrict__ fcount,
-                                                          uint32_t* counts, const uint32_t* __restrict__ scratch) {
-   __shared__ uint32_t red[FIN_T / 32];
-   const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t L = cs->L, nsym = cs->nsym;
-   const uint32_t* start_hist = scratch;
-   const uint32_t* end_hist = scratch + (L + 1);
-   const uint32_t* missing = scratch + 2 * (L + 1);
-   const uint32_t base = blockIdx.x * FIN_T;
-   uint32_t pre_s = 0, pre_e = 0, tot_s = 0;
-   for (uint32_t i = threadIdx.x; i <= L; i += blockDim.x) {
-      const uint32_t s = start_hist[i];
-      tot_s += s;
-      if (i < base) {
-         pre_s += s;
-         pre_e += end_hist[i];
-      }
-   }
-   pre_s = block_reduce_all(pre_s, red);
-   pre_e = block_reduce_all(pre_e, red);
-   tot_s = block_reduce_all(tot_s, red);
-   const uint32_t p = base + threadIdx.x;
-   const bool in = p < L;
-   const uint32_t sl = block_incl_scan(in ? start_hist[p] : 0u, red) + pre_s;
-   const uint32_t el = block_incl_scan(in ? end_hist[p] : 0u, red) + pre_e;
-   if (!in) return;
-   const uint32_t total = static_cast<uint32_t>(*fcount);
-   uint32_t ref = total - (tot_s - sl) - el - missing[p];
-   for (uint32_t s = 0; s < nsym; ++s) ref -= counts[static_cast<size_t>(s) * L + p];
-   counts[static_cast<size_t>(cs->local_ref[p]) * L + p] += ref;
-}
-
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------
@@ -670,6 +432,14 @@ void launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_cod
                                                                                 stack_tiles, d_out_tiles, d_count, d_err);
 }
 
+int filter_batch_blocks_per_sm(size_t smem_bytes) {
+   if (smem_bytes > 48 * 1024)
+      cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_bytes));
+   int n = 0;
+   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, filter_batch_kernel, FT, smem_bytes) != cudaSuccess) return 1;
+   return n > 0 ? n : 1;
+}
+
 void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
                          const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
                          uint32_t* d_out_tiles, unsigned long long* d_counts, uint32_t* d_next, uint32_t grid, int* d_err,
@@ -681,20 +451,5 @@ void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr*
    filter_batch_kernel<<<grid, FT, smem, static_cast<cudaStream_t>(stream)>>>(
       d_table, d_code, d_queries, d_items, n_items, tile_bits, stack_tiles, d_out_tiles, d_counts, d_next, d_err);
 }
-
-void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
-                      const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filter,
-                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream) {
-   cudaStream_t s = static_cast<cudaStream_t>(stream);
-   if (nparts > 0) {
-      const uint32_t grid = nparts < 152u * 8u ? nparts : 152u * 8u;
-      mut_ctr_kernel<<<grid, MT, 0, s>>>(d_table, col, d_parts, nparts, d_filter, d_filter_count, d_counts);
-   }
-   mut_cov_kernel<<<col_host.nblocks + nchunks, MT, 0, s>>>(d_table, col, d_filter, d_filter_count, d_scratch);
-   mut_final_kernel<<<(col_host.L + FIN_T - 1) / FIN_T, FIN_T, 0, s>>>(d_table, col, d_filter_count, d_counts, d_scratch);
-}
-
-void launch_mutations_batch(const DevTable*, const DevSeqCol&, uint32_t, uint32_t, const MutPart*, uint32_t,
-                            const uint32_t*, uint32_t, const unsigned long long*, uint32_t*, uint32_t*, void*) {}
 
 }  // namespace rhygpu

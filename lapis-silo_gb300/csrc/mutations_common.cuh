@@ -1,0 +1,135 @@
+// Device helpers shared by the single-query and batched Mutations kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace rhygpu {
+
+constexpr uint32_t SMALL_ARRAY = 32;  // array containers up to this size are counted by one lane
+
+__device__ __forceinline__ uint32_t test_bit(const uint32_t* F, uint32_t r) { return (F[r >> 5] >> (r & 31)) & 1u; }
+
+// popcount of F in [a, b)
+__device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, uint32_t b) {
+   if (a >= b) return 0;
+   const uint32_t wa = a >> 5, wb = (b - 1) >> 5;
+   uint32_t s = 0;
+   for (uint32_t w = wa; w <= wb; ++w) {
+      uint32_t m = 0xFFFFFFFFu;
+      if (w == wa) m &= 0xFFFFFFFFu << (a & 31);
+      if (w == wb) m &= 0xFFFFFFFFu >> (31 - ((b - 1) & 31));
+      s += __popc(F[w] & m);
+   }
+   return s;
+}
+
+// element t (0..7) of eight packed u16 values
+__device__ __forceinline__ uint32_t u16_of(const uint4& w, uint32_t t) {
+   const uint32_t x = t < 2 ? w.x : t < 4 ? w.y : t < 6 ? w.z : w.w;
+   return (t & 1u) ? (x >> 16) : (x & 0xFFFFu);
+}
+
+__device__ __forceinline__ CtrDesc shfl_desc(const uint4& raw, int lane) {
+   uint4 r;
+   r.x = __shfl_sync(0xFFFFFFFFu, raw.x, lane);
+   r.y = __shfl_sync(0xFFFFFFFFu, raw.y, lane);
+   r.z = __shfl_sync(0xFFFFFFFFu, raw.z, lane);
+   r.w = __shfl_sync(0xFFFFFFFFu, raw.w, lane);
+   return *reinterpret_cast<const CtrDesc*>(&r);
+}
+
+// Calls f(row) for every element of a small array container (card <= SMALL_ARRAY) with at most five
+// independent 16-byte loads. The payload arena is padded so the covering words stay in bounds.
+template <typename Fn>
+__device__ __forceinline__ void small_array_for_each(const CtrDesc& d, const uint16_t* __restrict__ payload, Fn&& f) {
+   const uint32_t s = d.payload, e = s + d.card_m1 + 1u;
+   const uint4* pw = reinterpret_cast<const uint4*>(payload);
+   const uint32_t w0 = s >> 3, w1 = (e - 1) >> 3;
+   uint4 buf[5];
+#pragma unroll
+   for (uint32_t k = 0; k < 5; ++k) buf[k] = (w0 + k <= w1) ? __ldg(pw + w0 + k) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+   for (uint32_t k = 0; k < 5; ++k) {
+#pragma unroll
+      for (uint32_t t = 0; t < 8; ++t) {
+         const uint32_t j = 8 * (w0 + k) + t;
+         if (j >= s && j < e) f(u16_of(buf[k], t));
+      }
+   }
+}
+
+__device__ __forceinline__ uint32_t small_array_count(const CtrDesc& d, const uint16_t* __restrict__ payload,
+                                                      const uint32_t* F) {
+   uint32_t c = 0;
+   small_array_for_each(d, payload, [&](uint32_t r) { c += test_bit(F, r); });
+   return c;
+}
+
+__device__ __forceinline__ uint32_t block_incl_scan_u32(uint32_t v, uint32_t* red) {
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   uint32_t x = v;
+#pragma unroll
+   for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (static_cast<int>(lane) >= o) x += y;
+   }
+   __syncthreads();
+   if (lane == 31) red[warp] = x;
+   __syncthreads();
+   uint32_t add = 0;
+   for (uint32_t i = 0; i < warp; ++i) add += red[i];
+   __syncthreads();
+   return x + add;
+}
+
+// Final pass for positions [blockIdx.x * MUT_SEG, +MUT_SEG) of one query (blockDim.x == MUT_SEG):
+//   ref(p) = |F| - #(start > p) - #(end <= p) - missing(p) - sum_s counts[s][p]
+//   counts[local_ref[p]][p] += ref(p)
+// All arithmetic is modulo 2^32 like the reference's uint32 vectors; the result is exact.
+__device__ __forceinline__ void final_position_counts(const DevSeqCol* cs, uint32_t total, uint32_t* counts,
+                                                      const uint32_t* __restrict__ scratch, uint32_t* red) {
+   __shared__ uint32_t pre[4];
+   const uint32_t L = cs->L, nsym = cs->nsym, nseg = mut_nseg(L);
+   const uint32_t* start_hist = scratch;
+   const uint32_t* end_hist = scratch + (L + 1);
+   const uint32_t* ndiff = scratch + 2 * (L + 1);
+   const uint32_t* seg_s = scratch + 3 * (L + 1);
+   const uint32_t* seg_e = seg_s + nseg;
+   const uint32_t* seg_n = seg_e + nseg;
+   if (threadIdx.x < 32) {
+      uint32_t ps = 0, pe = 0, pn = 0, ts = 0;
+      for (uint32_t k = threadIdx.x; k < nseg; k += 32) {
+         const uint32_t s = seg_s[k];
+         ts += s;
+         if (k < blockIdx.x) {
+            ps += s;
+            pe += seg_e[k];
+            pn += seg_n[k];
+         }
+      }
+      ps = __reduce_add_sync(0xFFFFFFFFu, ps);
+      pe = __reduce_add_sync(0xFFFFFFFFu, pe);
+      pn = __reduce_add_sync(0xFFFFFFFFu, pn);
+      ts = __reduce_add_sync(0xFFFFFFFFu, ts);
+      if (threadIdx.x == 0) {
+         pre[0] = ps;
+         pre[1] = pe;
+         pre[2] = pn;
+         pre[3] = ts;
+      }
+   }
+   __syncthreads();
+   const uint32_t p = blockIdx.x * MUT_SEG + threadIdx.x;
+   const bool in = p < L;
+   const uint32_t sl = block_incl_scan_u32(in ? start_hist[p] : 0u, red) + pre[0];
+   const uint32_t el = block_incl_scan_u32(in ? end_hist[p] : 0u, red) + pre[1];
+   const uint32_t nl = block_incl_scan_u32(in ? ndiff[p] : 0u, red) + pre[2];
+   if (!in) return;
+   uint32_t ref = total - (pre[3] - sl) - el - nl;
+   for (uint32_t s = 0; s < nsym; ++s) ref -= counts[static_cast<size_t>(s) * L + p];
+   counts[static_cast<size_t>(cs->local_ref[p]) * L + p] += ref;
+}
+
+}  // namespace rhygpu

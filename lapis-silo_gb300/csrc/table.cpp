@@ -124,6 +124,10 @@ void assemble(std::vector<ChunkContainers>& chunks, uint32_t nkeys, ContainerSet
       }
       c = ChunkContainers{};
    }
+   // pad to whole 16-byte words plus one spare word: kernels read array payloads with aligned
+   // 16-byte loads that may cover up to seven u16 past a container's last element
+   while (cs.payload.size() % 8) cs.payload.push_back(0);
+   cs.payload.insert(cs.payload.end(), 8, 0);
    const uint64_t nslots = static_cast<uint64_t>(chunks.size()) * nkeys;
    cs.off.assign(nslots + 1, 0);
    for (const auto& d : cs.ctrs) cs.off[static_cast<uint64_t>(d.v) * nkeys + d.key + 1]++;
@@ -360,7 +364,7 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
             for (uint32_t b = s / NBLOCK; b <= (e - 1) / NBLOCK; ++b) {
                const uint32_t bs = b * NBLOCK;
                NRunEntry en;
-               en.row = r;
+               en.row = (v << 16) | r;
                en.lo = static_cast<uint16_t>(std::max(s, bs) - bs);
                en.hi = static_cast<uint16_t>(std::min(e, bs + NBLOCK) - bs);
                col.nblk[fill[static_cast<size_t>(b) * nchunks + v]++] = en;

@@ -55,7 +55,7 @@ struct CovExc {  // a row whose covered region is not [0, L)
 };
 
 struct NRunEntry {  // missing interval of one row clipped to one position block
-   uint32_t row;    // row within chunk
+   uint32_t row;    // global row id (chunk << 16 | row within chunk)
    uint16_t lo;     // [lo, hi) relative to the block start
    uint16_t hi;
 };

@@ -81,6 +81,12 @@ class SeqColumnInfo(C.Structure):
                 ("n_coverage_exceptions", C.c_uint64), ("n_null_rows", C.c_uint64)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("n_queries", C.c_uint32), ("n_mutation_slots", C.c_uint32), ("n_items", C.c_uint32),
+                ("n_instr", C.c_uint32), ("max_depth", C.c_uint32), ("tile_bits", C.c_uint32), ("grid", C.c_uint32),
+                ("device_bytes", C.c_uint64)]
+
+
 class MutationRow(C.Structure):
     _fields_ = [("position", C.c_uint32), ("from_", C.c_char), ("to", C.c_char), ("count", C.c_uint32),
                 ("coverage", C.c_uint32), ("proportion", C.c_double)]
@@ -118,6 +124,19 @@ def lib():
         "rhy_eval": (I, [P, C.c_char_p, P, P, C.POINTER(U64)]),
         "rhy_mutations": (I, [P, C.c_char_p, U32, P, P, C.POINTER(U64)]),
         "rhy_mutation_rows": (I, [P, U32, P, C.c_double, C.POINTER(MutationRow), C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_batch": (I, [P, P, P, P, U32, U32, P, P, P]),
+        "rhy_batch_prepare": (I, [P, P, P, P, U32, U32, U32]),
+        "rhy_batch_launch": (I, [P, P, I, I]),
+        "rhy_batch_capture": (I, [P, P]),
+        "rhy_batch_replay": (I, [P, P]),
+        "rhy_batch_results": (I, [P, P, P]),
+        "rhy_batch_info": (I, [P, C.POINTER(BatchInfo)]),
+        "rhy_plain_prepare": (I, [P, P, P, P, U32]),
+        "rhy_plain_launch": (I, [P, U32, P]),
+        "rhy_plain_launch_parts": (I, [P, U32, P, U32]),
+        "rhy_mutation_bytes": (I, [P, U32, C.POINTER(U64), C.POINTER(U64)]),
+        "rhy_batch_capture_ex": (I, [P, P, I, I]),
+        "rhy_batch_launch_parts": (I, [P, P, U32]),
         "rhy_close": (None, [P]),
     }
     for name, (res, args) in sig.items():
@@ -305,6 +324,84 @@ class Device:
         v = C.c_uint64()
         _check(lib().rhy_mutations(self._h, expr.encode(), column, stream, _ptr(counts), C.byref(v)))
         return counts, v.value
+
+
+    # ---- batched path ----
+    @staticmethod
+    def _query_arrays(exprs, actions, columns):
+        n = len(exprs)
+        arr = (C.c_char_p * max(n, 1))(*[e.encode() for e in exprs])
+        act = np.asarray(actions if actions is not None else [0] * n, dtype=np.int32)
+        col = np.asarray(columns if columns is not None else [0] * n, dtype=np.uint32)
+        return n, arr, act, col
+
+    def batch(self, exprs, actions=None, columns=None, tile_bits: int = 0, stream=None):
+        """Evaluates many queries in one launch sequence. Returns (filter counts, {i: counts[symbol, position]})."""
+        n, arr, act, col = self._query_arrays(exprs, actions, columns)
+        counts = np.zeros(max(n, 1), np.uint64)
+        outs = {}
+        ptrs = (C.c_void_p * max(n, 1))()
+        for i in range(n):
+            if act[i] == 1:
+                c = self.table.columns[int(col[i])]
+                outs[i] = np.zeros((c.n_symbols, c.L), np.uint32)
+                ptrs[i] = outs[i].ctypes.data
+        _check(lib().rhy_batch(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), n, tile_bits, stream,
+                               _ptr(counts), C.cast(ptrs, C.c_void_p)))
+        return counts[:n], outs
+
+    def batch_prepare(self, exprs, actions=None, columns=None, tile_bits: int = 0, plan_threads: int = 0):
+        n, arr, act, col = self._query_arrays(exprs, actions, columns)
+        self._batch_n = n
+        self._batch_act, self._batch_col = act, col
+        _check(lib().rhy_batch_prepare(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), n, tile_bits,
+                                       plan_threads))
+
+    def batch_launch(self, stream=None, copy_in: bool = True, copy_out: bool = True):
+        _check(lib().rhy_batch_launch(self._h, stream, int(copy_in), int(copy_out)))
+
+    def batch_capture(self, stream=None):
+        _check(lib().rhy_batch_capture(self._h, stream))
+
+    def batch_replay(self, stream=None):
+        _check(lib().rhy_batch_replay(self._h, stream))
+
+    def batch_results(self, with_mutations: bool = True):
+        n = self._batch_n
+        counts = np.zeros(max(n, 1), np.uint64)
+        outs = {}
+        ptrs = (C.c_void_p * max(n, 1))()
+        if with_mutations:
+            for i in range(n):
+                if self._batch_act[i] == 1:
+                    c = self.table.columns[int(self._batch_col[i])]
+                    outs[i] = np.zeros((c.n_symbols, c.L), np.uint32)
+                    ptrs[i] = outs[i].ctypes.data
+        _check(lib().rhy_batch_results(self._h, _ptr(counts), C.cast(ptrs, C.c_void_p)))
+        return counts[:n], outs
+
+    def batch_info(self) -> BatchInfo:
+        info = BatchInfo()
+        _check(lib().rhy_batch_info(self._h, C.byref(info)))
+        return info
+
+    def plain_prepare(self, exprs, actions=None, columns=None):
+        n, arr, act, col = self._query_arrays(exprs, actions, columns)
+        _check(lib().rhy_plain_prepare(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), n))
+
+    def plain_launch(self, i: int, stream=None, parts: int = 15):
+        _check(lib().rhy_plain_launch_parts(self._h, i, stream, parts))
+
+    def batch_capture_ex(self, stream=None, copy_in: bool = False, copy_out: bool = False):
+        _check(lib().rhy_batch_capture_ex(self._h, stream, int(copy_in), int(copy_out)))
+
+    def batch_launch_parts(self, parts: int, stream=None):
+        _check(lib().rhy_batch_launch_parts(self._h, stream, parts))
+
+    def mutation_bytes(self, column: int = 0) -> tuple[int, int]:
+        p, d = C.c_uint64(), C.c_uint64()
+        _check(lib().rhy_mutation_bytes(self._h, column, C.byref(p), C.byref(d)))
+        return p.value, d.value
 
 
 def bits_to_rows(bits: np.ndarray) -> np.ndarray:

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <iterator>
 #include <map>
 #include <memory>
 #include <optional>
@@ -459,10 +460,20 @@ struct SeqColumn {
             if (s <= pos && pos < e) rows.push_back(static_cast<uint32_t>(k << 16 | r));
          }
       }
+      // remove the rows whose missing positions contain pos, walking every per-row bitmap like the
+      // reference does (horizontal_coverage_index.h:89-96)
+      std::vector<uint32_t> drop;
+      for (const auto& [row, ivs] : horizontal) {
+         for (const auto& iv : ivs) {
+            if (iv.s <= pos && pos < iv.e) {
+               drop.push_back(row);
+               break;
+            }
+         }
+      }
       std::vector<uint32_t> keep;
       keep.reserve(rows.size());
-      for (uint32_t r : rows)
-         if (!horizontal_contains(r, pos)) keep.push_back(r);
+      std::set_difference(rows.begin(), rows.end(), drop.begin(), drop.end(), std::back_inserter(keep));
       return rs_from_sorted_rows(keep);
    }
    // getMatchingContainersAsBitmap / fromContainerViews (vertical_sequence_index.cpp:206-227,297-322)
