@@ -10,6 +10,8 @@
 // Row sets are dense bitmaps of 2^16 bits (8 KiB) per chunk.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "program.h"
@@ -89,11 +91,12 @@ struct QueryDesc {
 
 // ---- launchers (kernels.cu) ----
 // tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth.
-void launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode, uint32_t tile_bits,
-                   uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count, int* d_err, void* stream);
+cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
+                          uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
+                          int* d_err, void* stream);
 
 // Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.
-void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
+cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
                          const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
                          uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
                          uint32_t* d_next, uint32_t grid, int* d_err, void* stream);

@@ -141,9 +141,12 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
    // shared memory: keep the stack under 200 KiB
    while (W > 4096 && static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) W >>= 1;
    if (static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
-   rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()), W, p.max_depth, tiles, count,
-                         d_err, stream);
-   cuda_check(cudaGetLastError(), "filter kernel launch");
+   cudaGetLastError();  // an error left by an unrelated earlier call must not be reported here
+   const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()), W,
+                                               p.max_depth, tiles, count, d_err, stream);
+   if (e != cudaSuccess)
+      throw CudaError("filter kernel launch (tile " + std::to_string(W) + " rows, stack " + std::to_string(p.max_depth) +
+                      " tiles): " + cudaGetErrorString(e));
 }
 
 void Engine::launch_mutations(int column, const uint32_t* filter, const unsigned long long* count, uint32_t* counts,
@@ -381,9 +384,9 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
       cuda_check(cudaMemsetAsync(b.d_next, 0, sizeof(uint32_t), s), "memset");
       if (b.counts_words) cuda_check(cudaMemsetAsync(b.d_mcounts, 0, b.counts_words * 4, s), "memset");
       if (b.scratch_words) cuda_check(cudaMemsetAsync(b.d_mscratch, 0, b.scratch_words * 4, s), "memset");
-      launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.tile_bits, b.max_depth, b.d_tiles,
-                          b.d_counts, b.d_next, b.grid, d_err, s);
-      cuda_check(cudaGetLastError(), "filter batch launch");
+      cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.tile_bits, b.max_depth,
+                                     b.d_tiles, b.d_counts, b.d_next, b.grid, d_err, s),
+                 "filter batch launch");
    }
    const size_t words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
    for (const auto& g : b.groups) {

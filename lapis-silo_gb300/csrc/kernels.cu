@@ -423,33 +423,45 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
 // ------------------------------------------------------------------------------------------------
 // launchers
 
-void launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode, uint32_t tile_bits,
-                   uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count, int* d_err, void* stream) {
+cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
+                          uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
+                          int* d_err, void* stream) {
    const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
-   if (smem > 48 * 1024) cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+   cudaError_t e = cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
+   if (e != cudaSuccess) return e;
    filter_kernel<<<nchunks * T, FT, smem, static_cast<cudaStream_t>(stream)>>>(d_table, d_code, ncode, tile_bits,
                                                                                 stack_tiles, d_out_tiles, d_count, d_err);
+   return cudaGetLastError();
 }
 
 int filter_batch_blocks_per_sm(size_t smem_bytes) {
-   if (smem_bytes > 48 * 1024)
-      cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_bytes));
+   if (cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            static_cast<int>(smem_bytes > 48 * 1024 ? smem_bytes : 48 * 1024)) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+   }
    int n = 0;
-   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, filter_batch_kernel, FT, smem_bytes) != cudaSuccess) return 1;
+   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, filter_batch_kernel, FT, smem_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+   }
    return n > 0 ? n : 1;
 }
 
-void launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
+cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
                          const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
                          uint32_t* d_out_tiles, unsigned long long* d_counts, uint32_t* d_next, uint32_t grid, int* d_err,
                          void* stream) {
    (void)nchunks;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
-   if (smem > 48 * 1024)
-      cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+   cudaError_t e = cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
+   if (e != cudaSuccess) return e;
    filter_batch_kernel<<<grid, FT, smem, static_cast<cudaStream_t>(stream)>>>(
       d_table, d_code, d_queries, d_items, n_items, tile_bits, stack_tiles, d_out_tiles, d_counts, d_next, d_err);
+   return cudaGetLastError();
 }
 
 }  // namespace rhygpu

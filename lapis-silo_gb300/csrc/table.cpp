@@ -146,6 +146,17 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
                   uint32_t v, uint32_t size, ChunkRows& out) {
    out.nr_off.assign(1, 0);
    const uint32_t missing = A.missing;
+   struct Run {
+      uint32_t pos, len, sym;
+   };
+   std::vector<Run> runs;
+   // intervals where the reference holds the missing symbol (empty for ordinary references)
+   std::vector<std::pair<uint32_t, uint32_t>> ref_missing;
+   for (uint32_t p = 0; p < L; ++p) {
+      if (ref_sym[p] != missing) continue;
+      if (!ref_missing.empty() && ref_missing.back().second == p) ref_missing.back().second = p + 1;
+      else ref_missing.emplace_back(p, p + 1);
+   }
    for (uint32_t r = 0; r < size; ++r) {
       const uint32_t row = v * CHUNK_ROWS + r;
       if (raw.is_null[row]) {
@@ -154,24 +165,42 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
          out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));
          continue;
       }
+      // The row's runs as (pos, len, symbol); positions where the reference itself holds the
+      // missing symbol are missing in the row too unless a run overrides them.
+      runs.clear();
       const uint64_t b = raw.row_off[row], e = raw.row_off[row + 1];
-      auto sym_at = [&](uint64_t k) {
+      size_t j = 0;
+      // adds the reference-missing positions inside the gap [a, z) between runs
+      auto fill_gap = [&](uint32_t a, uint32_t z) {
+         while (j < ref_missing.size() && ref_missing[j].second <= a) ++j;
+         for (size_t t = j; t < ref_missing.size() && ref_missing[t].first < z; ++t) {
+            const uint32_t lo = std::max(a, ref_missing[t].first), hi = std::min(z, ref_missing[t].second);
+            if (lo < hi) runs.push_back({lo, hi - lo, missing});
+         }
+      };
+      uint32_t cursor = 0;
+      for (uint64_t k = b; k < e; ++k) {
          const int s = A.sym(raw.run_char[k]);
          if (s < 0) throw std::invalid_argument(std::string("illegal character '") + raw.run_char[k] + "' in column " + raw.name);
-         return static_cast<uint32_t>(s);
-      };
+         const uint32_t p0 = raw.run_pos[k], len = raw.run_len[k];
+         if (len == 0 || p0 < cursor || static_cast<uint64_t>(p0) + len > L)
+            throw std::invalid_argument("runs must be sorted, non-overlapping and inside the genome in column " + raw.name);
+         if (!ref_missing.empty()) fill_gap(cursor, p0);
+         runs.push_back({p0, len, static_cast<uint32_t>(s)});
+         cursor = p0 + len;
+      }
+      if (!ref_missing.empty()) fill_gap(cursor, L);
       // Leading and trailing missing symbols are trimmed into the covered region
       // (reference: src/rhydb/common/aligned_sequence.cpp:89-120).
       uint32_t start = 0;
-      uint64_t k = b;
-      while (k < e && raw.run_pos[k] == start && sym_at(k) == missing) {
-         start = raw.run_pos[k] + raw.run_len[k];
+      size_t k = 0, kb = runs.size();
+      while (k < kb && runs[k].pos == start && runs[k].sym == missing) {
+         start = runs[k].pos + runs[k].len;
          ++k;
       }
       uint32_t end = L;
-      uint64_t kb = e;
-      while (kb > k && raw.run_pos[kb - 1] + raw.run_len[kb - 1] == end && sym_at(kb - 1) == missing) {
-         end = raw.run_pos[kb - 1];
+      while (kb > k && runs[kb - 1].pos + runs[kb - 1].len == end && runs[kb - 1].sym == missing) {
+         end = runs[kb - 1].pos;
          --kb;
       }
       if (start >= end) {
@@ -181,17 +210,19 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
          continue;
       }
       if (start != 0 || end != L) out.exc.push_back({r, start, end, 0});
-      for (uint64_t q = k; q < kb; ++q) {
-         const uint32_t s = sym_at(q);
-         const uint32_t p0 = raw.run_pos[q], len = raw.run_len[q];
-         if (p0 + len > L || len == 0) throw std::invalid_argument("run outside the genome in column " + raw.name);
-         if (s == missing) {
-            out.nr_s.push_back(p0);
-            out.nr_e.push_back(p0 + len);
+      for (size_t q = k; q < kb; ++q) {
+         const Run& run = runs[q];
+         if (run.sym == missing) {
+            if (!out.nr_s.empty() && out.nr_off.back() < out.nr_s.size() && out.nr_e.back() == run.pos) {
+               out.nr_e.back() = run.pos + run.len;  // adjacent missing runs form one interval
+            } else {
+               out.nr_s.push_back(run.pos);
+               out.nr_e.push_back(run.pos + run.len);
+            }
             continue;
          }
-         for (uint32_t p = p0; p < p0 + len; ++p) {
-            if (s != ref_sym[p]) out.keys.push_back(pack(p, s, r));
+         for (uint32_t p = run.pos; p < run.pos + run.len; ++p) {
+            if (run.sym != ref_sym[p]) out.keys.push_back(pack(p, run.sym, r));
          }
       }
       out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));

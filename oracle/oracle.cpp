@@ -532,17 +532,28 @@ struct Diff {
    std::vector<std::pair<uint32_t, int>> mutations;
 };
 
-Diff diff_runs(const ORawSeqColumn& raw, const Alpha& A, const std::vector<int>& ref, uint32_t row) {
+Diff diff_runs(const ORawSeqColumn& raw, const Alpha& A, const std::vector<int>& ref, uint32_t row, bool ref_has_missing) {
    Diff d;
    const uint32_t L = raw.L;
+   uint32_t cursor = 0;
+   // Positions outside the runs hold the reference character; where that character is the
+   // missing symbol the sequence is missing there (aligned_sequence.cpp:43-44 with
+   // reference_is_missing_somewhere).
+   auto reference_gap = [&](uint32_t a, uint32_t z) {
+      for (uint32_t p = a; p < z; ++p)
+         if (ref[p] == A.missing) d.missing.push_back(p);
+   };
    for (uint64_t k = raw.row_off[row]; k < raw.row_off[row + 1]; ++k) {
       const int s = A.sym(raw.run_char[k]);
       if (s < 0) throw std::invalid_argument("illegal character");
+      if (ref_has_missing) reference_gap(cursor, raw.run_pos[k]);
       for (uint32_t p = raw.run_pos[k]; p < raw.run_pos[k] + raw.run_len[k]; ++p) {
          if (s == A.missing) d.missing.push_back(p);
          else if (s != ref[p]) d.mutations.emplace_back(p, s);
       }
+      cursor = raw.run_pos[k] + raw.run_len[k];
    }
+   if (ref_has_missing) reference_gap(cursor, L);
    // leading / trailing missing positions (aligned_sequence.cpp:89-120)
    size_t lead = 0;
    while (lead < d.missing.size() && d.missing[lead] == lead) ++lead;
@@ -623,6 +634,7 @@ SeqColumn build_seq(const ORawSeqColumn& raw, const Layout& layout) {
       if (col.reference[p] < 0) throw std::invalid_argument("illegal reference character");
    }
    col.local_reference = col.reference;
+   const bool ref_has_missing = std::find(col.reference.begin(), col.reference.end(), A.missing) != col.reference.end();
    // appendChunk per 2^16-row chunk; each chunk flushes the per-position mutation buffer
    std::vector<std::vector<std::vector<uint32_t>>> buffer(raw.L, std::vector<std::vector<uint32_t>>(A.count));
    uint32_t row = 0;
@@ -636,7 +648,7 @@ SeqColumn build_seq(const ORawSeqColumn& raw, const Layout& layout) {
          if (raw.is_null[row]) {
             col.null_bitmap = rs_or(col.null_bitmap, rs_from_sorted_rows({g}));
          } else {
-            d = diff_runs(raw, A, col.reference, row);
+            d = diff_runs(raw, A, col.reference, row, ref_has_missing);
          }
          // insertCoverage (horizontal_coverage_index.cpp:17-46)
          col.start_end[k].emplace_back(d.start, d.end);

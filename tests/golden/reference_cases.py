@@ -1,0 +1,120 @@
+"""Known-answer scenarios of the reference's own test suite, restated in this project's expression
+syntax. Each dataset and expected result is taken from the cited reference test file; the test
+that consumes them (tests/test_golden_reference.py) runs them through the CPU oracle, the host
+planner and the GPU path.
+
+Reference test data: sequences as NDJSON rows, reference genomes per sequence column, metadata.
+Here a dataset is a dict with per-column literal aligned sequences (None = the row has no sequence)
+and metadata lists.
+"""
+
+# src/rhydb/query_engine/scalar_expressions/symbol_equals.test.cpp:42-66 (nucleotide TEST_DATA)
+SYMBOL_EQUALS_NUC = {
+    "name": "symbol_equals.test.cpp:42-66",
+    "n_rows": 5,
+    "seq": [
+        ("segment1", 0, "ATGCN", ["ATGCN", "ATGCN", "NNNNN", "CATTT", None]),
+        ("gene1", 1, "M*", [None, None, None, None, None]),
+    ],
+    "cases": [
+        # symbol_equals.test.cpp:86-226: nucleotideEquals(position, symbol) -> count
+        ("SymEq(segment1,1,C)", 1), ("SymEq(segment1,1,.)", 2),
+        ("SymEq(segment1,2,C)", 0), ("SymEq(segment1,3,C)", 0), ("SymEq(segment1,4,C)", 2), ("SymEq(segment1,5,C)", 0),
+        ("SymEq(segment1,1,A)", 2), ("SymEq(segment1,2,A)", 1), ("SymEq(segment1,3,A)", 0), ("SymEq(segment1,4,A)", 0),
+        ("SymEq(segment1,5,A)", 0),
+        ("SymEq(segment1,1,G)", 0), ("SymEq(segment1,2,G)", 0), ("SymEq(segment1,3,G)", 2), ("SymEq(segment1,4,G)", 0),
+        ("SymEq(segment1,5,G)", 0),
+        ("SymEq(segment1,1,T)", 0), ("SymEq(segment1,2,T)", 2), ("SymEq(segment1,3,T)", 1), ("SymEq(segment1,4,T)", 1),
+        ("SymEq(segment1,5,T)", 1),
+        ("SymEq(segment1,1,N)", 1), ("SymEq(segment1,5,N)", 3),
+        # symbol_equals.test.cpp:228-236: every amino-acid sequence is null, nothing matches X
+        ("SymEq(gene1,1,X)", 0),
+    ],
+    # symbol_equals.test.cpp:238-249: out of range -> user error
+    "errors": ["SymEq(segment1,1000,C)", "SymEq(segment1,0,.)"],
+}
+
+# src/rhydb/query_engine/scalar_expressions/has_mutation.test.cpp:22-44
+HAS_MUTATION = {
+    "name": "has_mutation.test.cpp:22-44",
+    "n_rows": 4,
+    "seq": [
+        ("segment1", 0, "ATGCN", ["ATGCN", "ATGCN", "NNNNN", "CATTT"]),
+        ("gene1", 1, "M*", ["M*", "C*", "M*", "X*"]),
+    ],
+    "cases": [
+        ("HasMut(segment1,1)", 1),   # has_mutation.test.cpp:46-52
+        ("HasMut(gene1,1)", 1),      # :54-59
+        ("HasMut(segment1,5)", 1),   # :85-91
+    ],
+    # :61-83, :93-99: positions out of bounds
+    "errors": ["HasMut(segment1,2000)", "HasMut(segment1,6)", "HasMut(gene1,1000)", "HasMut(segment1,0)"],
+}
+
+# src/rhydb/query_engine/scalar_expressions/symbol_equals.test.cpp:262-316 (amino-acid TEST_DATA)
+SYMBOL_EQUALS_AA = {
+    "name": "symbol_equals.test.cpp:262-316",
+    "n_rows": 4,
+    "seq": [
+        ("segment1", 0, "A", [None, None, None, None]),
+        ("gene1", 1, "M*", ["D*", "M*", "M*", "B*"]),
+    ],
+    "cases": [
+        ("SymEq(gene1,1,D)", 1),  # :301-307
+        ("SymEq(gene1,1,.)", 2),  # :309-315
+    ],
+    "errors": [],
+}
+
+# src/rhydb/query_engine/scalar_expressions/nof.test.cpp:56-120: five rows with country, region, date
+_NOF_ROWS = [("Switzerland", "Europe", "2020-01-01"), ("Germany", "Europe", "2021-06-15"),
+             ("USA", "Americas", "2019-03-20"), ("Switzerland", "Europe", "2018-11-01"),
+             ("France", "Europe", "2022-07-10")]
+NOF = {
+    "name": "nof.test.cpp:56-120",
+    "n_rows": 5,
+    "seq": [("segment1", 0, "ATGCN", ["ACGTN"] * 5)],
+    "dict": [("country", [r[0] for r in _NOF_ROWS]), ("region", [r[1] for r in _NOF_ROWS])],
+    "date": [("date", [r[2] for r in _NOF_ROWS])],
+    # expected row ids (the reference's expected primary keys id_<row>)
+    "row_cases": [
+        ("NOf(2,atleast,StrEq(country,Switzerland),StrEq(country,Germany),StrEq(region,Europe))", [0, 1, 3]),
+        ("NOf(3,atleast,StrEq(country,Switzerland),DateBetween(date,18262,18262),StrEq(region,Europe))", [0]),
+        ("NOf(3,atleast,StrEq(country,Switzerland),StrEq(country,Germany),StrEq(region,Europe))", []),
+        ("NOf(1,atleast,StrEq(country,Switzerland),StrEq(country,USA))", [0, 2, 3]),
+        ("NOf(1,exactly,StrEq(country,Switzerland),StrEq(region,Europe))", [1, 4]),
+        ("NOf(2,exactly,StrEq(country,Switzerland),StrEq(region,Europe))", [0, 3]),
+        ("NOf(0,atleast,StrEq(country,Switzerland),StrEq(country,Germany))", [0, 1, 2, 3, 4]),
+        ("NOf(0,exactly,StrEq(country,Switzerland),StrEq(region,Europe))", [2]),
+        ("NOf(2,atleast,StrEq(country,Switzerland),Not(StrEq(country,USA)))", [0, 3]),
+        ("NOf(1,atleast,StrEq(country,Switzerland),Not(StrEq(country,Germany)))", [0, 2, 3, 4]),
+        ("NOf(0,exactly,StrEq(country,Switzerland))", [1, 2, 4]),
+        ("NOf(0,exactly,Not(StrEq(country,Switzerland)))", [0, 3]),
+        ("NOf(2,atleast,Not(StrEq(country,Switzerland)),Not(StrEq(country,USA)))", [1, 4]),
+        ("NOf(0,exactly,StrEq(country,Switzerland),Not(StrEq(country,USA)))", [2]),
+        ("NOf(5,exactly,StrEq(country,Switzerland),StrEq(country,USA))", []),
+    ],
+    "cases": [],
+    "errors": [],
+}
+
+DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF]
+
+# Operator-level known answers: src/rhydb/query_engine/filter/operators/threshold.test.cpp:28-313.
+# (kind 0 = Threshold; non-negated row sets, negated row sets, n, exactly, expected)
+THRESHOLD_CASES = [
+    # :39-55 evaluatesCorrectOnlyNegated (RowLayout::of(4))
+    ([], [[1, 2, 3], [1, 3]], 1, True, [2]),
+    ([], [[1, 2, 3], [1, 3]], 1, False, [0, 2]),
+    # :57-83 evaluateShouldReturnCorrectValuesNoNegated
+    ([[1, 2], [1, 3], [1, 2, 3]], [], 1, True, []),
+    ([[1, 2], [1, 3], [1, 2, 3]], [], 2, True, [2, 3]),
+    ([[1, 2], [1, 3], [1, 2, 3]], [], 1, False, [1, 2, 3]),
+    ([[1, 2], [1, 3], [1, 2, 3]], [], 2, False, [1, 2, 3]),
+    # :85-150 evaluateShouldReturnCorrectValues
+    ([[1, 2, 3], [1, 3], [1, 2, 3]], [[], [3]], 1, True, []),
+    ([[1, 2, 3], [1, 3], [1, 2, 3]], [[], [3]], 2, True, [0]),
+    ([[1, 2, 3], [1, 3], [1, 2, 3]], [[], [3]], 3, True, []),
+    ([[1, 2, 3], [1, 3], [1, 2, 3]], [[], [3]], 4, True, [2, 3]),
+    ([[1, 2, 3], [1, 3], [1, 2, 3]], [[], [3]], 1, False, [0, 1, 2, 3]),
+]

@@ -1,0 +1,177 @@
+"""Bit-exact parity of the CUDA path (through the C-ABI) with the CPU oracle."""
+import numpy as np
+import pytest
+
+import rhydb_gpu as R
+from rawtable import RawBuilder, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def config1():
+    """100,000 sequences over a 29,903-nt genome, nucleotide leaves only, 1,000 trees of depth <= 4
+    with NOf(n <= 8) (the small configuration of the plain method)."""
+    t = R.Table.generate(100000, seed=42)
+    orc = oracle_for(t)
+    dev = R.Device(t, 0)
+    yield t, orc, dev, t.queries(1000, seed=43, max_depth=4, max_nof_children=8)
+    dev.close()
+
+
+@pytest.fixture(scope="module")
+def config2_small():
+    """The at-scale generator (12 amino-acid genes, metadata, null rows) at 100,000 rows."""
+    t = R.Table.generate(100000, seed=7, n_aa_genes=12, null_fraction=0.003)
+    orc = oracle_for(t)
+    dev = R.Device(t, 0)
+    yield t, orc, dev, t.queries(300, seed=8, use_aa=True, use_metadata=True)
+    dev.close()
+
+
+def check_filter(dev, orc, q):
+    bits, n = dev.compute_filter(q)
+    obits, on = orc.compute_filter(q)
+    assert n == on, q
+    assert np.array_equal(bits, obits), q
+
+
+def test_config1_filters_and_counts(config1):
+    t, orc, dev, qs = config1
+    for q in qs:
+        check_filter(dev, orc, q)
+        assert dev.count(q) == orc.count(q)
+
+
+def test_config1_mutations(config1):
+    t, orc, dev, qs = config1
+    for q in qs[:200]:
+        m, n = dev.mutations(q, 0)
+        om, on = orc.mutations(q, 0)
+        assert n == on and np.array_equal(m, om), q
+        assert t.mutation_rows(0, m, 0.05) == orc.mutation_rows(0, om, 0.05)
+
+
+def test_config1_batched(config1):
+    t, orc, dev, qs = config1
+    act = np.array([1 if i % 5 == 0 else 0 for i in range(len(qs))], np.int32)
+    counts, muts = dev.batch(qs, act)
+    for i, q in enumerate(qs):
+        assert counts[i] == orc.count(q), q
+    for i in np.flatnonzero(act)[:120]:
+        om, _ = orc.mutations(qs[i], 0)
+        assert np.array_equal(muts[int(i)], om), qs[i]
+
+
+def test_config2_all_columns(config2_small):
+    t, orc, dev, qs = config2_small
+    for q in qs:
+        check_filter(dev, orc, q)
+    rng = np.random.default_rng(3)
+    for q in qs[:60]:
+        col = int(rng.integers(0, t.n_seq))
+        m, n = dev.mutations(q, col)
+        om, on = orc.mutations(q, col)
+        assert n == on and np.array_equal(m, om), (q, col)
+
+
+def test_config2_batched_mixed_columns(config2_small):
+    t, orc, dev, qs = config2_small
+    rng = np.random.default_rng(4)
+    act = (rng.random(len(qs)) < 0.35).astype(np.int32)
+    col = rng.integers(0, t.n_seq, len(qs)).astype(np.uint32)
+    for tb in (4096, 16384, 65536):
+        counts, muts = dev.batch(qs, act, col, tile_bits=tb)
+        for i, q in enumerate(qs):
+            assert counts[i] == orc.count(q), (tb, q)
+        for i in np.flatnonzero(act)[:40]:
+            om, _ = orc.mutations(qs[i], int(col[i]))
+            assert np.array_equal(muts[int(i)], om), (tb, qs[i], col[i])
+
+
+def test_tile_widths(config2_small):
+    t, orc, dev, qs = config2_small
+    for tb in (4096, 8192, 32768, 65536):
+        dev.set_tile_bits(tb)
+        for q in qs[:80]:
+            check_filter(dev, orc, q)
+    dev.set_tile_bits(16384)
+
+
+def test_graph_replay_matches_direct(config2_small):
+    t, orc, dev, qs = config2_small
+    act = np.array([i % 3 == 0 for i in range(len(qs))], np.int32)
+    direct_c, direct_m = dev.batch(qs, act)
+    dev.batch_prepare(qs, act)
+    dev.batch_capture()
+    for _ in range(2):
+        dev.batch_replay()
+    c, m = dev.batch_results()
+    assert np.array_equal(c, direct_c)
+    assert all(np.array_equal(m[k], direct_m[k]) for k in direct_m)
+
+
+@pytest.mark.parametrize("rows", [1, 31, 65536, 65537, 131072])
+def test_chunk_boundaries(rows):
+    t = R.Table.generate(rows, seed=rows, genome_len=2000, pool_sites=200, n_aa_genes=1, null_fraction=0.05)
+    orc = oracle_for(t)
+    dev = R.Device(t, 0)
+    qs = t.queries(60, seed=1, use_aa=True, use_metadata=True) + ["True", "False", "Not(True)", "NOf(0,exactly)"]
+    for q in qs:
+        check_filter(dev, orc, q)
+    for q in qs[:15]:
+        for col in range(t.n_seq):
+            m, n = dev.mutations(q, col)
+            om, on = orc.mutations(q, col)
+            assert n == on and np.array_equal(m, om), (q, col)
+    assert dev.count("True") == rows
+    dev.close()
+
+
+def test_wide_and_deep_trees(config1):
+    t, orc, dev, qs = config1
+    leaves = [q for q in qs if q.startswith("SymEq") or q.startswith("HasMut")][:64]
+    assert len(leaves) >= 40
+    k = len(leaves)
+    exprs = [
+        "And(" + ",".join(leaves) + ")",
+        "Or(" + ",".join(leaves) + ")",
+        f"NOf({k // 2},atleast," + ",".join(leaves) + ")",
+        f"NOf(3,exactly," + ",".join(leaves) + ")",
+        f"NOf({k - 1},atleast," + ",".join("Not(" + x + ")" for x in leaves) + ")",
+        f"Maybe(NOf(2,exactly," + ",".join(leaves[:10]) + "))",
+    ]
+    nested = leaves[0]
+    for x in leaves[1:24]:
+        nested = f"Or(Not(And({nested},{x})),NOf(1,exactly,{x},{nested}))" if len(nested) < 3000 else nested
+    exprs.append(nested)
+    for q in exprs:
+        check_filter(dev, orc, q)
+    counts, _ = dev.batch(exprs)
+    assert counts.tolist() == [orc.count(q) for q in exprs]
+
+
+def test_complement_identity_at_scale():
+    """At 2,000,000 rows: Count(X) + Count(Not X) == rows, batched == plain, and a few queries
+    against the oracle."""
+    t = R.Table.generate(2000000, seed=42, n_aa_genes=12)
+    dev = R.Device(t, 0)
+    qs = t.queries(64, seed=43, use_aa=True, use_metadata=True)
+    plain = [dev.count(q) for q in qs]
+    neg = [dev.count(f"Not({q})") for q in qs]
+    assert all(a + b == t.n_rows for a, b in zip(plain, neg))
+    act = np.array([i % 4 == 3 for i in range(len(qs))], np.int32)
+    counts, muts = dev.batch(qs, act)
+    assert counts.tolist() == plain
+    for i in np.flatnonzero(act)[:6]:
+        m, _ = dev.mutations(qs[i], 0)
+        assert np.array_equal(m, muts[int(i)])
+        # every covered, filtered row holds exactly one symbol per position
+        assert int(m.sum(axis=0).max()) <= plain[int(i)]
+    orc = oracle_for(t)
+    for q in qs[:3]:
+        check_filter(dev, orc, q)
+    m, _ = dev.mutations(qs[3], 0)
+    om, _ = orc.mutations(qs[3], 0)
+    assert np.array_equal(m, om)
+    dev.close()
