@@ -193,6 +193,21 @@ int rhy_plain_launch_parts(RhyDevice* d, uint32_t i, void* stream, uint32_t part
 /* Bytes a mutations pass over `column` must read: container payloads plus descriptors. */
 int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_bytes, uint64_t* descriptor_bytes);
 
+/* Mutations pass that allocates no device memory (no counterpart in the reference, which runs on
+ * host memory). For callers that may not allocate during a query: a process whose device memory
+ * is owned by its own pool allocator, or a latency-critical thread that must avoid the implicit
+ * synchronisation of cudaMalloc / cudaFree. The caller passes device buffers it owns: the filter
+ * row set (n_chunks * 2048 words, as written by the filter kernels), its cardinality, and the
+ * output counts (n_symbols * L words, counts[symbol * L + position], overwritten). Working memory
+ * is one fixed array in the library's device image (1.5 MiB, held on every GPU that loads the
+ * library until the process exits), which limits the column to 131,072 positions; longer columns
+ * fail with RHY_INVALID_ARGUMENT. The first call on a device looks up the array's address; make
+ * that first call before any stream capture. All calls on a device share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. The work is enqueued on `stream`
+ * (NULL = the handle's stream); results are valid once that stream has been synchronised. */
+int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filter, const uint64_t* d_filter_count,
+                          uint32_t* d_counts, void* stream);
+
 /* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */
 int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,
                       RhyMutationRow* rows, size_t cap, size_t* n_rows);

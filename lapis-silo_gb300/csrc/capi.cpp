@@ -10,6 +10,7 @@
 #include "dataset.h"
 #include "engine.h"
 #include "expr.h"
+#include "noalloc.h"
 #include "table.h"
 
 struct RhyTable {
@@ -584,6 +585,16 @@ int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts) {
       need(d, "device");
       rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
       d->engine->batch_enqueue(static_cast<cudaStream_t>(stream), false, false, parts);
+   });
+}
+
+int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filter, const uint64_t* d_filter_count,
+                          uint32_t* d_counts, void* stream) {
+   return guarded([&] {
+      need(d, "device");
+      rhygpu::mutations_noalloc(*d->engine, column, d_filter,
+                                reinterpret_cast<const unsigned long long*>(d_filter_count), d_counts,
+                                static_cast<cudaStream_t>(stream));
    });
 }
 

@@ -137,6 +137,7 @@ def lib():
         "rhy_mutation_bytes": (I, [P, U32, C.POINTER(U64), C.POINTER(U64)]),
         "rhy_batch_capture_ex": (I, [P, P, I, I]),
         "rhy_batch_launch_parts": (I, [P, P, U32]),
+        "rhy_mutations_noalloc": (I, [P, U32, P, P, P, P]),
         "rhy_close": (None, [P]),
     }
     for name, (res, args) in sig.items():
@@ -397,6 +398,12 @@ class Device:
 
     def batch_launch_parts(self, parts: int, stream=None):
         _check(lib().rhy_batch_launch_parts(self._h, stream, parts))
+
+    def mutations_noalloc(self, column: int, d_filter: int, d_filter_count: int, d_counts: int, stream=None):
+        """Mutations pass over caller-owned device buffers (addresses as ints); allocates nothing.
+        Enqueued on `stream`; synchronise it before reading d_counts."""
+        _check(lib().rhy_mutations_noalloc(self._h, column, C.c_void_p(d_filter), C.c_void_p(d_filter_count),
+                                           C.c_void_p(d_counts), stream))
 
     def mutation_bytes(self, column: int = 0) -> tuple[int, int]:
         p, d = C.c_uint64(), C.c_uint64()
