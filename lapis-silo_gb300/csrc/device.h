@@ -33,10 +33,23 @@ struct DevSeqCol {
    const uint32_t* nblk_off;   // nblocks * nchunks + 1
    const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
    const uint8_t* local_ref;   // L
+   const uint32_t* mstart;     // missing-interval start events (row << 8 | position in block)
+   const uint32_t* mend;       // missing-interval end events
+   const CovEvent* cstart;     // coverage starts > 0
+   const CovEvent* cend;       // coverage ends < L
    uint32_t L;
    uint32_t nblocks;
    uint32_t nsym;
    uint32_t nctrs;
+};
+
+// A range of events of one list for the mutations coverage pass.
+enum : uint32_t { EV_MSTART = 0, EV_MEND = 1, EV_CSTART = 2, EV_CEND = 3 };
+struct EvItem {
+   uint32_t list;   // EV_*
+   uint32_t block;  // position block (missing lists)
+   uint32_t begin;
+   uint32_t end;
 };
 
 struct DevDictCol {
@@ -58,14 +71,6 @@ struct DevTable {
    DevSeqCol seq[MAX_SEQ_COLS];
    DevDictCol dict[MAX_DICT_COLS];
    DevDateCol date[MAX_DATE_COLS];
-};
-
-// A slice of one column's containers for the mutations pass: containers [begin, end) of chunk v.
-struct MutPart {
-   uint32_t v;
-   uint32_t begin;
-   uint32_t end;
-   uint32_t pad;
 };
 
 // Per-query scratch of the mutations pass, in u32 words:
@@ -109,7 +114,7 @@ enum : uint32_t { BMUT_PART_TRANSPOSE = 1, BMUT_PART_CTR = 2, BMUT_PART_COV = 4,
 // The filter count decides on the device between the full path (|F| == rows: stored cardinalities),
 // the empty path and the mixed path, so no host round trip sits between filter and mutations.
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
-                      const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filter,
+                      const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
                       uint32_t parts = MUT_PART_ALL);
 
@@ -120,7 +125,11 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
 size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks);
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                             const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
-                            const uint32_t* d_slot_query, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
-                            int* d_err, void* stream, uint32_t parts = BMUT_PART_ALL);
+                            const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, uint16_t* d_masks,
+                            uint32_t* d_counts, uint32_t* d_scratch, int* d_err, void* stream,
+                            uint32_t parts = BMUT_PART_ALL);
+
+// Events per CTA of the coverage pass.
+constexpr uint32_t EV_PER_CTA = 8192;
 
 }  // namespace rhygpu

@@ -58,23 +58,23 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
          d.nctrs = static_cast<uint32_t>(s.vertical.ctrs.size());
          max_words = std::max(max_words, d.nsym * s.L);
          max_L = std::max(max_L, s.L);
-         // mutation partitions: containers of one chunk, ~64 KiB of work each
-         std::vector<MutPart> parts;
-         const auto& ctrs = s.vertical.ctrs;
-         size_t i = 0;
-         while (i < ctrs.size()) {
-            MutPart p{ctrs[i].v, static_cast<uint32_t>(i), 0, 0};
-            uint64_t cost = 0;
-            while (i < ctrs.size() && ctrs[i].v == p.v && cost < 65536) {
-               const CtrDesc& x = ctrs[i];
-               cost += 48 + (x.type == CT_BITSET ? 8192u : x.type == CT_RUN ? 4u * x.nruns : 2u * (x.card_m1 + 1u));
-               ++i;
-            }
-            p.end = static_cast<uint32_t>(i);
-            parts.push_back(p);
+         d.mstart = upload(s.mstart);
+         d.mend = upload(s.mend);
+         d.cstart = upload(s.cstart);
+         d.cend = upload(s.cend);
+         // coverage-pass work items: event ranges of at most EV_PER_CTA, never spanning two blocks
+         std::vector<EvItem> items;
+         auto split = [&](uint32_t list, uint32_t block, uint32_t b, uint32_t e) {
+            for (uint32_t x = b; x < e; x += EV_PER_CTA) items.push_back({list, block, x, std::min(e, x + EV_PER_CTA)});
+         };
+         for (uint32_t b = 0; b < s.nblocks; ++b) {
+            split(EV_MSTART, b, s.mstart_off[b], s.mstart_off[b + 1]);
+            split(EV_MEND, b, s.mend_off[b], s.mend_off[b + 1]);
          }
-         nparts_.push_back(static_cast<uint32_t>(parts.size()));
-         d_parts_.push_back(upload(parts));
+         split(EV_CSTART, 0, 0, static_cast<uint32_t>(s.cstart.size()));
+         split(EV_CEND, 0, 0, static_cast<uint32_t>(s.cend.size()));
+         n_ev_.push_back(static_cast<uint32_t>(items.size()));
+         d_ev_.push_back(upload(items));
       }
       for (size_t c = 0; c < t.dict.size(); ++c) {
          const DictColumnImage& s = t.dict[c];
@@ -152,7 +152,7 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
 void Engine::launch_mutations(int column, const uint32_t* filter, const unsigned long long* count, uint32_t* counts,
                               uint32_t* scratch, cudaStream_t stream, uint32_t parts) {
    const DevSeqCol& c = view_.seq[column];
-   rhygpu::launch_mutations(d_table_, c, static_cast<uint32_t>(column), nchunks(), d_parts_[column], nparts_[column],
+   rhygpu::launch_mutations(d_table_, c, static_cast<uint32_t>(column), nchunks(), d_ev_[column], n_ev_[column],
                             filter, count, counts, scratch, stream, parts);
    cuda_check(cudaGetLastError(), "mutations kernel launch");
 }
@@ -392,7 +392,8 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
    for (const auto& g : b.groups) {
       launch_mutations_batch(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), nchunks(),
                              b.d_tiles + static_cast<size_t>(g.slot_begin) * words, g.n, b.d_counts,
-                             b.d_slot_query + g.slot_begin, b.d_masks, b.d_mcounts + g.counts_off,
+                             b.d_slot_query + g.slot_begin, d_ev_[g.column], n_ev_[g.column], b.d_masks,
+                             b.d_mcounts + g.counts_off,
                              b.d_mscratch + g.scratch_off, d_err, s, (parts >> 1) & BMUT_PART_ALL);
       cuda_check(cudaGetLastError(), "mutations batch launch");
    }

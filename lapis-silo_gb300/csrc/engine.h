@@ -118,8 +118,8 @@ class Engine {
    // Tile width that fits the batch's deepest program in the shared-memory budget.
    uint32_t fit_tile_bits(uint32_t requested, uint32_t depth) const;
 
-   const MutPart* d_parts(int column) const { return d_parts_[column]; }
-   uint32_t nparts(int column) const { return nparts_[column]; }
+   const EvItem* d_ev(int column) const { return d_ev_[column]; }
+   uint32_t n_ev(int column) const { return n_ev_[column]; }
    uint64_t mutation_payload_bytes(int column) const;
 
    // scratch of the single-query path
@@ -143,8 +143,8 @@ class Engine {
    DevTable view_{};
    DevTable* d_table_ = nullptr;
    std::vector<void*> allocs_;
-   std::vector<MutPart*> d_parts_;
-   std::vector<uint32_t> nparts_;
+   std::vector<EvItem*> d_ev_;
+   std::vector<uint32_t> n_ev_;
    Instr* h_code_ = nullptr;               // pinned staging
    unsigned long long* h_count_ = nullptr; // pinned
    int* h_err_ = nullptr;                  // pinned

@@ -880,12 +880,45 @@ struct Lowerer {
       return out;
    }
 
-   void pred(const Pred& p) {
-      if (p.kind == Pred::COVERED) {
-         emit(OP_PUSH_COVERED, static_cast<uint8_t>(p.col), p.covered ? 0 : 1, p.pos);
-      } else {
-         emit(OP_PUSH_DATE, static_cast<uint8_t>(p.col), p.with_nulls ? 1 : 0, p.cmp, static_cast<uint32_t>(p.value));
+   // A date comparison as "inside [lo, hi]" (or outside it) plus whether null dates match.
+   struct DateLeaf {
+      int col;
+      int32_t lo, hi;
+      bool invert, with_nulls;
+   };
+   static DateLeaf date_leaf(const Pred& p) {
+      DateLeaf d{p.col, p.value, p.value, false, p.with_nulls};
+      switch (p.cmp) {
+         case CMP_EQ: break;
+         case CMP_NE: d.invert = true; break;
+         case CMP_LT:
+            d.lo = INT32_MIN;
+            if (p.value == INT32_MIN) d.lo = 1, d.hi = 0;  // empty
+            else d.hi = p.value - 1;
+            break;
+         case CMP_LE: d.lo = INT32_MIN; break;
+         case CMP_GT:
+            d.hi = INT32_MAX;
+            if (p.value == INT32_MAX) d.lo = 1, d.hi = 0;
+            else d.lo = p.value + 1;
+            break;
+         default: d.hi = INT32_MAX; break;  // CMP_GE
       }
+      return d;
+   }
+   void date(const DateLeaf& d) {
+      emit(OP_PUSH_DATE, static_cast<uint8_t>(d.col), static_cast<uint16_t>((d.with_nulls ? 1 : 0) | (d.invert ? 2 : 0)),
+           static_cast<uint32_t>(d.lo), static_cast<uint32_t>(d.hi));
+      push();
+      ++prog.n_leaves;
+   }
+
+   void pred(const Pred& p) {
+      if (p.kind == Pred::DATE) {
+         date(date_leaf(p));
+         return;
+      }
+      emit(OP_PUSH_COVERED, static_cast<uint8_t>(p.col), p.covered ? 0 : 1, p.pos);
       push();
       ++prog.n_leaves;
    }
@@ -963,17 +996,38 @@ struct Lowerer {
             return;
          }
          case OpT::SELECTION: {
+            // The predicates are ANDed; date comparisons on one column that drop null dates merge
+            // into a single range leaf (DateBetween's two comparisons become one pass).
+            std::vector<DateLeaf> leaves;
+            for (const Pred& p : op.preds) {
+               if (p.kind != Pred::DATE) continue;
+               DateLeaf d = date_leaf(p);
+               bool merged = false;
+               for (DateLeaf& x : leaves) {
+                  if (!d.invert && !d.with_nulls && !x.invert && !x.with_nulls && x.col == d.col) {
+                     x.lo = std::max(x.lo, d.lo);
+                     x.hi = std::min(x.hi, d.hi);
+                     merged = true;
+                     break;
+                  }
+               }
+               if (!merged) leaves.push_back(d);
+            }
+            std::vector<std::function<void()>> parts;
+            for (const Pred& p : op.preds)
+               if (p.kind == Pred::COVERED) parts.push_back([this, p] { pred(p); });
+            for (const DateLeaf& d : leaves) parts.push_back([this, d] { date(d); });
             std::vector<size_t> jumps;
             size_t first = 0;
             if (!op.children.empty()) {
                node(*op.children[0]);
             } else {
-               pred(op.preds[0]);
+               parts[0]();
                first = 1;
             }
-            for (size_t i = first; i < op.preds.size(); ++i) {
+            for (size_t i = first; i < parts.size(); ++i) {
                if (opt.early_exit) jumps.push_back(jump(OP_JZ));
-               pred(op.preds[i]);
+               parts[i]();
                emit(OP_AND);
                pop();
             }

@@ -123,29 +123,29 @@ __device__ void push_covered(uint32_t* t, const TileCtx& c, const DevSeqCol* __r
    }
 }
 
-__device__ __forceinline__ bool date_match(int32_t d, uint32_t cmp, int32_t value, bool with_nulls) {
-   if (d == INT32_MIN) return with_nulls;
-   switch (cmp) {
-      case CMP_EQ: return d == value;
-      case CMP_NE: return d != value;
-      case CMP_LT: return d < value;
-      case CMP_LE: return d <= value;
-      case CMP_GT: return d > value;
-      default: return d >= value;
-   }
-}
-
-__device__ void push_date(uint32_t* t, const TileCtx& c, const DevDateCol* __restrict__ col, uint32_t cmp, int32_t value,
-                          bool with_nulls) {
+// Rows whose date lies in [lo, hi] (outside it when `invert`); null dates match when `with_nulls`.
+// Every comparison of the date predicates and the two-sided DateBetween reduce to this form.
+__device__ void push_date(uint32_t* t, const TileCtx& c, const DevDateCol* __restrict__ col, int32_t lo, int32_t hi,
+                          bool invert, bool with_nulls) {
    const uint32_t WW = c.W >> 5;
    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
    const int32_t* days = col->days + static_cast<size_t>(c.v) * CHUNK_ROWS + c.row0;
-   for (uint32_t w = warp; w < WW; w += nw) {
-      const uint32_t r = 32 * w + lane;
-      bool m = false;
-      if (r < c.nvalid) m = date_match(__ldg(days + r), cmp, value, with_nulls);
-      const uint32_t bits = __ballot_sync(0xFFFFFFFFu, m);
-      if (lane == 0) t[w] = bits;
+   constexpr uint32_t U = 4;  // words per warp in flight
+   for (uint32_t w0 = warp * U; w0 < WW; w0 += nw * U) {
+      int32_t d[U];
+#pragma unroll
+      for (uint32_t k = 0; k < U; ++k) {
+         const uint32_t r = 32 * (w0 + k) + lane;
+         d[k] = (w0 + k < WW && r < c.nvalid) ? __ldg(days + r) : INT32_MIN;
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < U; ++k) {
+         const uint32_t r = 32 * (w0 + k) + lane;
+         const bool inside = d[k] >= lo && d[k] <= hi;
+         const bool m = r < c.nvalid && (d[k] == INT32_MIN ? with_nulls : (inside != invert));
+         const uint32_t bits = __ballot_sync(0xFFFFFFFFu, m);
+         if (lane == 0 && w0 + k < WW) t[w0 + k] = bits;
+      }
    }
 }
 
@@ -187,7 +187,8 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             } else if (in.op == OP_PUSH_COVERED) {
                push_covered(t, c, &c.tab->seq[in.col], in.a, in.flags & 1);
             } else if (in.op == OP_PUSH_DATE) {
-               push_date(t, c, &c.tab->date[in.col], in.a, static_cast<int32_t>(in.b), in.flags & 1);
+               push_date(t, c, &c.tab->date[in.col], static_cast<int32_t>(in.a), static_cast<int32_t>(in.b), in.flags & 2,
+                         in.flags & 1);
             } else if (in.op == OP_PUSH_NULLS) {
                const uint32_t* src = c.tab->seq[in.col].null_tiles + static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5);
                for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = __ldg(src + w);

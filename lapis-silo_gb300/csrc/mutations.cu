@@ -2,9 +2,11 @@
 //
 //  mut_ctr_kernel    every vertical container once: |F ∩ container| against the filter tile of its
 //                    chunk staged in shared memory; integer counts per (symbol, position)
-//                    (reference: mutations_node.cpp:139-189). Payloads are read with 16-byte loads.
-//  mut_cov_kernel    rows of F outside their covered region (per-chunk exception lists) and inside
-//                    missing intervals (per 128-position block) as difference arrays
+//                    (reference: mutations_node.cpp:139-189). CTAs stay on one chunk; a warp takes
+//                    32 consecutive containers and streams their array payloads as one contiguous
+//                    range with 16-byte loads, attributing elements to containers by offset.
+//  mut_cov_kernel    rows of F outside their covered region and inside missing intervals, from
+//                    position-sorted start / end events aggregated per position with warp ballots
 //                    (reference: mutations_node.cpp:51-136).
 //  mut_final_kernel  prefix sums and the local-reference count per position
 //                    (reference: mutations_node.cpp:192-203).
@@ -20,26 +22,14 @@ namespace rhygpu {
 namespace {
 
 constexpr uint32_t MT = 256;
-constexpr uint32_t NSPLIT = 4;  // CTAs per missing-interval block
+constexpr uint32_t NW = MT / 32;
+constexpr uint32_t CTAS_PER_CHUNK_TARGET = 1216;  // 152 SMs x 8 CTAs, divided among the chunks
 
-// Warp-cooperative |F ∩ container| (all lanes return the total).
-__device__ uint32_t warp_count(const CtrDesc& d, const uint32_t* F, const uint16_t* __restrict__ payload) {
+// Warp-cooperative |F ∩ container| for bitset and run containers (all lanes return the total).
+__device__ uint32_t warp_count_other(const CtrDesc& d, const uint32_t* F, const uint16_t* __restrict__ payload) {
    const uint32_t lane = threadIdx.x & 31;
    uint32_t c = 0;
-   if (d.type == CT_ARRAY) {
-      const uint32_t s = d.payload, e = s + d.card_m1 + 1u;
-      const uint4* pw = reinterpret_cast<const uint4*>(payload);
-      const uint32_t w0 = s >> 3, w1 = (e - 1) >> 3;
-#pragma unroll 2
-      for (uint32_t w = w0 + lane; w <= w1; w += 32) {
-         const uint4 x = __ldg(pw + w);
-#pragma unroll
-         for (uint32_t t = 0; t < 8; ++t) {
-            const uint32_t j = 8 * w + t;
-            if (j >= s && j < e) c += test_bit(F, u16_of(x, t));
-         }
-      }
-   } else if (d.type == CT_BITSET) {
+   if (d.type == CT_BITSET) {
       const uint4* b = reinterpret_cast<const uint4*>(payload + d.payload);
       const uint4* f = reinterpret_cast<const uint4*>(F);
 #pragma unroll 4
@@ -58,8 +48,7 @@ __device__ uint32_t warp_count(const CtrDesc& d, const uint32_t* F, const uint16
    return __reduce_add_sync(0xFFFFFFFFu, c);
 }
 
-__global__ void __launch_bounds__(MT) mut_ctr_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                     const MutPart* __restrict__ parts, uint32_t nparts,
+__global__ void __launch_bounds__(MT) mut_ctr_kernel(const DevTable* __restrict__ tab, uint32_t col, uint32_t K,
                                                      const uint32_t* __restrict__ filter,
                                                      const unsigned long long* __restrict__ fcount, uint32_t* counts) {
    __shared__ __align__(16) uint32_t F[CHUNK_WORDS];
@@ -69,120 +58,153 @@ __global__ void __launch_bounds__(MT) mut_ctr_kernel(const DevTable* __restrict_
    const DevSeqCol* cs = &tab->seq[col];
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint16_t* __restrict__ payload = cs->payload;
+   const uint4* __restrict__ pw = reinterpret_cast<const uint4*>(payload);
    const uint32_t L = cs->L;
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-   for (uint32_t pi = blockIdx.x; pi < nparts; pi += gridDim.x) {
-      const MutPart P = parts[pi];
-      if (!full) {
-         const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(P.v) * CHUNK_WORDS);
-         uint4* dst = reinterpret_cast<uint4*>(F);
-         for (uint32_t k = threadIdx.x; k < CHUNK_WORDS / 4; k += blockDim.x) dst[k] = __ldg(src + k);
+   const uint32_t v = blockIdx.x / K, k = blockIdx.x % K;
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   if (!full) {
+      const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(v) * CHUNK_WORDS);
+      uint4* dst = reinterpret_cast<uint4*>(F);
+      for (uint32_t i = threadIdx.x; i < CHUNK_WORDS / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+   }
+   __syncthreads();
+   const uint32_t cb = __ldg(cs->off + static_cast<size_t>(v) * L), ce = __ldg(cs->off + static_cast<size_t>(v + 1) * L);
+   const uint32_t nslices = (ce - cb + 31) / 32;
+   for (uint32_t sl = k * NW + warp; sl < nslices; sl += K * NW) {
+      const uint32_t idx = cb + sl * 32 + lane;
+      const bool valid = idx < ce;
+      uint4 raw = make_uint4(0, 0, 0, 0);
+      if (valid) raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + idx);
+      const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+      if (full) {
+         if (valid) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], d.card_m1 + 1u);
+         continue;
       }
-      __syncthreads();
-      for (uint32_t base = P.begin + warp * 32; base < P.end; base += nw * 32) {
-         const uint32_t idx = base + lane;
-         const bool valid = idx < P.end;
-         uint4 raw = make_uint4(0, 0, 0, 0);
-         if (valid) raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + idx);
-         const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
-         uint32_t cnt = 0;
-         bool big = false;
-         if (valid) {
-            if (full) {
-               cnt = d.card_m1 + 1u;
-            } else if (d.type == CT_ARRAY && d.card_m1 < SMALL_ARRAY) {
-               cnt = small_array_count(d, payload, F);
-            } else {
-               big = true;
+      const bool is_arr = valid && d.type == CT_ARRAY;
+      const uint32_t amask = __ballot_sync(0xFFFFFFFFu, is_arr);
+      const uint32_t nA = __popc(amask);
+      if (nA) {
+         // Lane c takes the c-th array of the slice; the arrays are back to back in the payload
+         // arena, so the slice's elements are one range [P0, P1) streamed in windows of 32 words.
+         const uint32_t src = lane < nA ? __fns(amask, 0, lane + 1) : 0;
+         const uint32_t my_s = __shfl_sync(0xFFFFFFFFu, d.payload, src);
+         const uint32_t my_e = my_s + __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(d.card_m1), src) + 1u;
+         const uint32_t P0 = __shfl_sync(0xFFFFFFFFu, my_s, 0);
+         const uint32_t P1 = __shfl_sync(0xFFFFFFFFu, my_e, nA - 1);
+         uint32_t acc = 0;
+         for (uint32_t w0 = P0 >> 3; w0 <= (P1 - 1) >> 3; w0 += 32) {
+            const uint32_t w = w0 + lane;
+            uint32_t bits = 0;  // bit t: element 8w + t is in F
+            if (w <= (P1 - 1) >> 3) {
+               const uint4 x = __ldg(pw + w);
+#pragma unroll
+               for (uint32_t t = 0; t < 8; ++t) bits |= test_bit(F, u16_of(x, t)) << t;
             }
+            // exclusive prefix of set bits over the window's words
+            const uint32_t cnt = __popc(bits);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+               const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+               if (static_cast<int>(lane) >= o) incl += y;
+            }
+            const uint32_t excl = incl - cnt;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            // set bits of [8 w0, x) for x inside or at the end of the window
+            const uint32_t lo8 = 8 * w0, hi8 = 8 * (w0 + 32);
+            const uint32_t a = min(max(my_s, lo8), hi8), z = min(max(my_e, lo8), hi8);
+            const uint32_t wa = (a - lo8) >> 3, wz = (z - lo8) >> 3;
+            const uint32_t ea = __shfl_sync(0xFFFFFFFFu, excl, wa & 31), ba = __shfl_sync(0xFFFFFFFFu, bits, wa & 31);
+            const uint32_t ez = __shfl_sync(0xFFFFFFFFu, excl, wz & 31), bz = __shfl_sync(0xFFFFFFFFu, bits, wz & 31);
+            const uint32_t pa = wa >= 32 ? total : ea + __popc(ba & ((1u << ((a - lo8) & 7)) - 1u));
+            const uint32_t pz = wz >= 32 ? total : ez + __popc(bz & ((1u << ((z - lo8) & 7)) - 1u));
+            acc += pz - pa;
          }
-         if (valid && !big && cnt) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], cnt);
-         uint32_t bigmask = __ballot_sync(0xFFFFFFFFu, big);
-         while (bigmask) {
-            const int j = __ffs(bigmask) - 1;
-            bigmask &= bigmask - 1;
-            const CtrDesc dj = shfl_desc(raw, j);
-            const uint32_t c = warp_count(dj, F, payload);
-            if (lane == 0 && c) atomicAdd(&counts[static_cast<size_t>(dj.sym) * L + dj.key], c);
-         }
+         const uint32_t key = __shfl_sync(0xFFFFFFFFu, d.key, src);
+         const uint32_t sym = __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(d.sym), src);
+         if (lane < nA && acc) atomicAdd(&counts[static_cast<size_t>(sym) * L + key], acc);
       }
-      __syncthreads();
+      uint32_t other = __ballot_sync(0xFFFFFFFFu, valid && !is_arr);
+      while (other) {
+         const int j = __ffs(other) - 1;
+         other &= other - 1;
+         const CtrDesc dj = shfl_desc(raw, j);
+         const uint32_t c = warp_count_other(dj, F, payload);
+         if (lane == 0 && c) atomicAdd(&counts[static_cast<size_t>(dj.sym) * L + dj.key], c);
+      }
    }
 }
 
+// One CTA per event item. Missing events add +1 (start) / -1 (end) at their position; coverage
+// events count rows whose covered region starts (ends) there.
 __global__ void __launch_bounds__(MT) mut_cov_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                     const EvItem* __restrict__ items,
                                                      const uint32_t* __restrict__ filter,
                                                      const unsigned long long* __restrict__ fcount, uint32_t* scratch) {
+   __shared__ int cnt[NBLOCK + 1];
    const unsigned long long fc = *fcount;
    if (fc == 0) return;
    const bool full = fc == tab->n_rows;
    const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t L = cs->L, nchunks = tab->nchunks, nseg = mut_nseg(L);
+   const uint32_t L = cs->L, nseg = mut_nseg(L);
    uint32_t* start_hist = scratch;
    uint32_t* end_hist = scratch + (L + 1);
    uint32_t* ndiff = scratch + 2 * (L + 1);
    uint32_t* seg_s = scratch + 3 * (L + 1);
    uint32_t* seg_e = seg_s + nseg;
    uint32_t* seg_n = seg_e + nseg;
-   if (blockIdx.x < cs->nblocks * NSPLIT) {
-      __shared__ int diff[NBLOCK + 1];
-      __shared__ int red[2][MT / 32];
-      const uint32_t b = blockIdx.x / NSPLIT, part = blockIdx.x % NSPLIT;
-      for (uint32_t i = threadIdx.x; i <= NBLOCK; i += blockDim.x) diff[i] = 0;
+   const EvItem it = items[blockIdx.x];
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   if (it.list <= EV_MEND) {
+      for (uint32_t i = threadIdx.x; i <= NBLOCK; i += blockDim.x) cnt[i] = 0;
       __syncthreads();
-      // the buckets of every chunk of block b are contiguous; entries carry global row ids
-      const uint32_t nb = __ldg(cs->nblk_off + static_cast<size_t>(b) * nchunks);
-      const uint32_t ne = __ldg(cs->nblk_off + static_cast<size_t>(b + 1) * nchunks);
-      const uint32_t per = (ne - nb + NSPLIT - 1) / NSPLIT;
-      const uint32_t lo_i = nb + part * per, hi_i = min(ne, lo_i + per);
-      int at_start = 0, at_end = 0;  // intervals starting at the block start / ending at the block end
-      for (uint32_t i = lo_i + threadIdx.x; i < hi_i; i += blockDim.x) {
-         const uint2 raw = __ldg(reinterpret_cast<const uint2*>(cs->nblk) + i);
-         if (full || ((__ldg(filter + (raw.x >> 5)) >> (raw.x & 31)) & 1u)) {
-            const uint32_t lo = raw.y & 0xFFFFu, hi = raw.y >> 16;
-            if (lo == 0) ++at_start;
-            else atomicAdd(&diff[lo], 1);
-            if (hi == NBLOCK) ++at_end;
-            else atomicSub(&diff[hi], 1);
+      const uint32_t* ev = it.list == EV_MSTART ? cs->mstart : cs->mend;
+      constexpr uint32_t U = 4;  // events per lane in flight
+      for (uint32_t base = it.begin + warp * 32 * U; base < it.end; base += blockDim.x * U) {
+         uint32_t e[U], bit[U];
+#pragma unroll
+         for (uint32_t k = 0; k < U; ++k) {
+            const uint32_t i = base + 32 * k + lane;
+            e[k] = i < it.end ? __ldg(ev + i) : 0xFFFFFFFFu;
+         }
+#pragma unroll
+         for (uint32_t k = 0; k < U; ++k) {
+            const uint32_t row = e[k] >> 8;
+            bit[k] = (e[k] != 0xFFFFFFFFu && (full || ((__ldg(filter + (row >> 5)) >> (row & 31)) & 1u))) ? 1u : 0u;
+         }
+#pragma unroll
+         for (uint32_t k = 0; k < U; ++k) {
+            const bool active = e[k] != 0xFFFFFFFFu;
+            const uint32_t pos = e[k] & 0xFFu;
+            const uint32_t amask = __ballot_sync(0xFFFFFFFFu, active);
+            const uint32_t bits = __ballot_sync(0xFFFFFFFFu, bit[k]);
+            // lanes with equal positions form one group (events are sorted by position)
+            const uint32_t grp = __match_any_sync(0xFFFFFFFFu, active ? pos : 0xFFFFu) & amask;
+            if (active && lane == static_cast<uint32_t>(__ffs(grp) - 1)) {
+               const uint32_t n = __popc(bits & grp);
+               if (n) atomicAdd(&cnt[pos], static_cast<int>(n));
+            }
          }
       }
-      at_start = __reduce_add_sync(0xFFFFFFFFu, at_start);
-      at_end = __reduce_add_sync(0xFFFFFFFFu, at_end);
-      if ((threadIdx.x & 31) == 0) {
-         red[0][threadIdx.x >> 5] = at_start;
-         red[1][threadIdx.x >> 5] = at_end;
-      }
       __syncthreads();
-      if (threadIdx.x == 0) {
-         int a = 0, e = 0;
-         for (uint32_t w = 0; w < MT / 32; ++w) {
-            a += red[0][w];
-            e += red[1][w];
-         }
-         diff[0] += a;
-         diff[NBLOCK] -= e;
-      }
-      __syncthreads();
+      const int sign = it.list == EV_MSTART ? 1 : -1;
       for (uint32_t q = threadIdx.x; q <= NBLOCK; q += blockDim.x) {
-         const int x = diff[q];
-         const uint32_t p = b * NBLOCK + q;
+         const int x = cnt[q];
+         const uint32_t p = it.block * NBLOCK + q;
          if (x != 0 && p <= L) {
-            atomicAdd(&ndiff[p], static_cast<uint32_t>(x));
-            atomicAdd(&seg_n[p / MUT_SEG], static_cast<uint32_t>(x));
+            atomicAdd(&ndiff[p], static_cast<uint32_t>(sign * x));
+            atomicAdd(&seg_n[p / MUT_SEG], static_cast<uint32_t>(sign * x));
          }
       }
    } else {
-      const uint32_t v = blockIdx.x - cs->nblocks * NSPLIT;
-      if (v >= nchunks) return;
-      const uint32_t xb = __ldg(cs->exc_off + v), xe = __ldg(cs->exc_off + v + 1);
-      const uint32_t* Fv = filter + static_cast<size_t>(v) * CHUNK_WORDS;
-      for (uint32_t i = xb + threadIdx.x; i < xe; i += blockDim.x) {
-         const uint4 raw = __ldg(reinterpret_cast<const uint4*>(cs->exc) + i);
-         if (full || ((__ldg(Fv + (raw.x >> 5)) >> (raw.x & 31)) & 1u)) {
-            atomicAdd(&start_hist[raw.y], 1u);
-            atomicAdd(&seg_s[raw.y / MUT_SEG], 1u);
-            atomicAdd(&end_hist[raw.z], 1u);
-            atomicAdd(&seg_e[raw.z / MUT_SEG], 1u);
+      const CovEvent* ev = it.list == EV_CSTART ? cs->cstart : cs->cend;
+      uint32_t* hist = it.list == EV_CSTART ? start_hist : end_hist;
+      uint32_t* seg = it.list == EV_CSTART ? seg_s : seg_e;
+      for (uint32_t i = it.begin + threadIdx.x; i < it.end; i += blockDim.x) {
+         const uint2 e = __ldg(reinterpret_cast<const uint2*>(ev) + i);
+         if (full || ((__ldg(filter + (e.x >> 5)) >> (e.x & 31)) & 1u)) {
+            atomicAdd(&hist[e.y], 1u);
+            atomicAdd(&seg[e.y / MUT_SEG], 1u);
          }
       }
    }
@@ -199,16 +221,16 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __re
 }  // namespace
 
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
-                      const MutPart* d_parts, uint32_t nparts, const uint32_t* d_filter,
+                      const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
                       uint32_t parts) {
    cudaStream_t s = static_cast<cudaStream_t>(stream);
-   if (nparts > 0 && (parts & MUT_PART_CTR)) {
-      const uint32_t grid = nparts < 152u * 8u ? nparts : 152u * 8u;
-      mut_ctr_kernel<<<grid, MT, 0, s>>>(d_table, col, d_parts, nparts, d_filter, d_filter_count, d_counts);
+   if (parts & MUT_PART_CTR) {
+      const uint32_t K = (CTAS_PER_CHUNK_TARGET + nchunks - 1) / nchunks;
+      mut_ctr_kernel<<<nchunks * K, MT, 0, s>>>(d_table, col, K, d_filter, d_filter_count, d_counts);
    }
-   if (parts & MUT_PART_COV)
-      mut_cov_kernel<<<col_host.nblocks * NSPLIT + nchunks, MT, 0, s>>>(d_table, col, d_filter, d_filter_count, d_scratch);
+   if ((parts & MUT_PART_COV) && n_ev > 0)
+      mut_cov_kernel<<<n_ev, MT, 0, s>>>(d_table, col, d_ev, d_filter, d_filter_count, d_scratch);
    if (parts & MUT_PART_FINAL)
       mut_final_kernel<<<(col_host.L + MUT_SEG - 1) / MUT_SEG, MUT_SEG, 0, s>>>(d_table, col, d_filter_count, d_counts,
                                                                                d_scratch);

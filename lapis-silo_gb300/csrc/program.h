@@ -18,7 +18,8 @@ enum OpCode : uint8_t {
    OP_PUSH_NULLS = 3,    // col = sequence column: rows whose sequence is null
    OP_PUSH_DICT = 4,     // col = dictionary column, a = value id: inverted-index rows
    OP_PUSH_COVERED = 5,  // col = sequence column, a = position, flags&1: not covered instead of covered
-   OP_PUSH_DATE = 6,     // col = date column, a = comparator, b = value, flags&1 = nulls match
+   OP_PUSH_DATE = 6,     // col = date column; rows with lo <= date <= hi (a = lo, b = hi as int32),
+                         // flags&2 = inverted (outside the range), flags&1 = null dates match
    OP_AND = 7,           // pop y, pop x, push x & y
    OP_ANDNOT = 8,        // pop y, pop x, push x & ~y
    OP_OR = 9,            // pop y, pop x, push x | y

@@ -52,10 +52,14 @@ struct ChunkContainers {
    std::vector<uint16_t> payload;
 };
 
-// Encodes sorted (key, sym, row) entries of one chunk as containers.
+// Encodes sorted (key, sym, row) entries of one chunk as containers. Array payloads come first and
+// back to back in descriptor order (a warp can stream the arrays of consecutive descriptors as one
+// contiguous range); bitsets (16-byte aligned) and runs follow them.
 void encode_chunk(const std::vector<uint64_t>& keys, uint16_t v, ChunkContainers& out) {
    out.ctrs.clear();
    out.payload.clear();
+   std::vector<uint16_t> other;            // bitset and run payloads
+   std::vector<size_t> other_ctrs;         // descriptors whose payload offset is into `other`
    size_t i = 0;
    std::vector<uint16_t> rows;
    while (i < keys.size()) {
@@ -77,30 +81,36 @@ void encode_chunk(const std::vector<uint64_t>& keys, uint16_t v, ChunkContainers
       if (run_bytes < base_bytes) {
          d.type = CT_RUN;
          d.nruns = static_cast<uint16_t>(nruns);
-         d.payload = static_cast<uint32_t>(out.payload.size());
+         d.payload = static_cast<uint32_t>(other.size());
          size_t k = 0;
          while (k < rows.size()) {
             size_t e = k;
             while (e + 1 < rows.size() && rows[e + 1] == rows[e] + 1) ++e;
-            out.payload.push_back(rows[k]);
-            out.payload.push_back(static_cast<uint16_t>(e - k));
+            other.push_back(rows[k]);
+            other.push_back(static_cast<uint16_t>(e - k));
             k = e + 1;
          }
+         other_ctrs.push_back(out.ctrs.size());
       } else if (card <= 4096) {
          d.type = CT_ARRAY;
          d.payload = static_cast<uint32_t>(out.payload.size());
          out.payload.insert(out.payload.end(), rows.begin(), rows.end());
       } else {
          d.type = CT_BITSET;
-         while (out.payload.size() % 8) out.payload.push_back(0);
-         d.payload = static_cast<uint32_t>(out.payload.size());
-         out.payload.resize(out.payload.size() + 4096, 0);
-         uint16_t* bits = out.payload.data() + d.payload;
+         while (other.size() % 8) other.push_back(0);
+         d.payload = static_cast<uint32_t>(other.size());
+         other.resize(other.size() + 4096, 0);
+         uint16_t* bits = other.data() + d.payload;
          for (uint16_t r : rows) bits[r >> 4] |= static_cast<uint16_t>(1u << (r & 15));
+         other_ctrs.push_back(out.ctrs.size());
       }
       out.ctrs.push_back(d);
       i = j;
    }
+   while (out.payload.size() % 8) out.payload.push_back(0);
+   const uint32_t base = static_cast<uint32_t>(out.payload.size());
+   out.payload.insert(out.payload.end(), other.begin(), other.end());
+   for (size_t k : other_ctrs) out.ctrs[k].payload += base;
 }
 
 // Concatenates per-chunk containers (chunk order) and builds the (v, key) offset table.
@@ -228,6 +238,64 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
       out.nr_off.push_back(static_cast<uint32_t>(out.nr_s.size()));
    }
    std::sort(out.keys.begin(), out.keys.end());
+}
+
+// Start / end events of the missing intervals, counting-sorted by (block, position) with rows in
+// increasing order inside each bucket, and the coverage boundary events.
+void build_mutation_events(SeqColumnImage& col, const std::vector<ChunkRows>& chunks,
+                           const std::vector<uint32_t>& chunk_sizes) {
+   const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
+   if (nchunks > MAX_EVENT_CHUNKS)
+      throw std::invalid_argument("a partition holds at most " + std::to_string(MAX_EVENT_CHUNKS) + " chunks (" +
+                                  std::to_string(MAX_EVENT_CHUNKS * CHUNK_ROWS) + " rows)");
+   const uint32_t W = NBLOCK + 1;  // positions 0..NBLOCK inside a block
+   const size_t nbuckets = static_cast<size_t>(col.nblocks) * W;
+   std::vector<uint32_t> cs(nbuckets + 1, 0), ce(nbuckets + 1, 0);
+   auto each = [&](auto&& fn) {
+      for (uint32_t v = 0; v < nchunks; ++v) {
+         const ChunkRows& c = chunks[v];
+         for (uint32_t r = 0; r < chunk_sizes[v]; ++r) {
+            for (uint32_t q = c.nr_off[r]; q < c.nr_off[r + 1]; ++q) {
+               const uint32_t s = c.nr_s[q], e = c.nr_e[q];
+               for (uint32_t b = s / NBLOCK; b <= (e - 1) / NBLOCK; ++b) {
+                  const uint32_t bs = b * NBLOCK;
+                  fn((v << 16) | r, b, std::max(s, bs) - bs, std::min(e, bs + NBLOCK) - bs);
+               }
+            }
+         }
+      }
+   };
+   each([&](uint32_t, uint32_t b, uint32_t lo, uint32_t hi) {
+      cs[static_cast<size_t>(b) * W + lo + 1]++;
+      ce[static_cast<size_t>(b) * W + hi + 1]++;
+   });
+   for (size_t i = 0; i < nbuckets; ++i) {
+      cs[i + 1] += cs[i];
+      ce[i + 1] += ce[i];
+   }
+   col.mstart.resize(cs[nbuckets]);
+   col.mend.resize(ce[nbuckets]);
+   col.mstart_off.resize(col.nblocks + 1);
+   col.mend_off.resize(col.nblocks + 1);
+   for (uint32_t b = 0; b <= col.nblocks; ++b) {
+      col.mstart_off[b] = cs[static_cast<size_t>(b) * W];
+      col.mend_off[b] = ce[static_cast<size_t>(b) * W];
+   }
+   each([&](uint32_t g, uint32_t b, uint32_t lo, uint32_t hi) {
+      col.mstart[cs[static_cast<size_t>(b) * W + lo]++] = (g << 8) | lo;
+      col.mend[ce[static_cast<size_t>(b) * W + hi]++] = (g << 8) | hi;
+   });
+   // coverage boundaries
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      for (const CovExc& x : chunks[v].exc) {
+         const uint32_t g = (v << 16) | x.row;
+         if (x.start > 0) col.cstart.push_back({g, x.start});
+         if (x.end < col.L) col.cend.push_back({g, x.end});
+      }
+   }
+   auto by_pos = [](const CovEvent& a, const CovEvent& b) { return a.pos != b.pos ? a.pos < b.pos : a.row < b.row; };
+   std::sort(col.cstart.begin(), col.cstart.end(), by_pos);
+   std::sort(col.cend.begin(), col.cend.end(), by_pos);
 }
 
 SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
@@ -403,6 +471,7 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
          }
       }
    }
+   build_mutation_events(col, chunks, chunk_sizes);
    return col;
 }
 

@@ -54,6 +54,13 @@ struct CovExc {  // a row whose covered region is not [0, L)
    uint32_t pad;
 };
 
+struct CovEvent {  // coverage boundary of one row
+   uint32_t row;   // global row id
+   uint32_t pos;
+};
+
+constexpr uint32_t MAX_EVENT_CHUNKS = 256;  // packed mutations events hold 24-bit row ids
+
 struct NRunEntry {  // missing interval of one row clipped to one position block
    uint32_t row;    // global row id (chunk << 16 | row within chunk)
    uint16_t lo;     // [lo, hi) relative to the block start
@@ -85,6 +92,14 @@ struct SeqColumnImage {
    std::vector<NRunEntry> nblk;        // bucketed by (block, chunk), sorted by row
    std::vector<uint32_t> nblk_off;     // nblocks * nchunks + 1
    uint32_t nblocks = 0;
+   // Mutations pass: the same missing intervals as start and end events, packed as
+   // (global row << 8 | position within the block, 0..128) and sorted by (block, position, row),
+   // so counts per position aggregate over runs of equal positions; per-block offsets.
+   std::vector<uint32_t> mstart, mend;
+   std::vector<uint32_t> mstart_off, mend_off;  // nblocks + 1
+   // Coverage boundaries of rows whose covered region is not the whole genome, sorted by
+   // position: starts above 0 and ends below L (a row without coverage has end 0).
+   std::vector<CovEvent> cstart, cend;
    uint32_t flipped_positions = 0;
 };
 
