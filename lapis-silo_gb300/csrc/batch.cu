@@ -4,8 +4,10 @@
 // one pass: their row sets are transposed into one 16-bit query mask per row (transpose_kernel,
 // warp ballots over 32 x 16 bit blocks), a CTA stages the masks of one chunk (128 KiB) into shared
 // memory with a TMA bulk copy, and every container element yields the membership of all 16 queries
-// with a single shared-memory load. Coverage exceptions and missing intervals are counted per
-// query group the same way. Results are bit-identical to the single-query kernels.
+// with a single shared-memory load. The coverage pass reads every missing-interval and coverage
+// boundary event once for all queries: the transpose also writes a row-major copy of the masks,
+// and one lane per 16-query group gathers its mask of the event's row. Results are bit-identical
+// to the single-query kernels.
 #include <cuda_runtime.h>
 
 #include "device.h"
@@ -21,25 +23,51 @@ constexpr uint32_t BT = 256;
 constexpr uint32_t CT = 1024;   // container kernel: one 128 KiB-mask CTA per SM, so make it wide
 
 
-// T[g][v * CHUNK_ROWS + row] = bit q set iff row is in filter (16 g + q).
+// Query masks in two layouts, both with bit q of a 16-bit mask set iff the row is in filter 16 g + q:
+//   group-major T[g][v * CHUNK_ROWS + row]   one 128 KiB slab per (group, chunk), staged by the
+//                                            container kernel;
+//   row-major   R[row][c] (u32, c < nqc)     the masks of all groups of one row side by side, 4 nqc
+//                                            bytes, gathered by the coverage kernel.
+// A CTA covers TR_WORDS filter words (32 TR_WORDS rows); warp w turns word w of 32 filters at a
+// time into 32 row masks with ballots and stages them in shared memory for coalesced row stores.
+constexpr uint32_t TR_WORDS = BT / 32;
+constexpr uint32_t TR_CHUNKS = 32;  // query chunks of 32 staged per round
+
 __global__ void __launch_bounds__(BT) transpose_kernel(const uint32_t* __restrict__ tiles, uint32_t nq, uint32_t nchunks,
-                                                       uint16_t* __restrict__ T) {
-   const uint32_t lane = threadIdx.x & 31;
-   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // global warp id
+                                                       uint16_t* __restrict__ T, uint32_t* __restrict__ R) {
+   __shared__ uint32_t stage[TR_WORDS * 32 * (TR_CHUNKS + 1)];
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
    const uint32_t words = nchunks * CHUNK_WORDS;
    const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;
-   if (gw >= words * ngroups) return;
-   const uint32_t g = gw / words, w = gw % words;
-   const uint32_t q = g * MUT_GROUP + lane;
-   uint32_t x = 0;
-   if (lane < MUT_GROUP && q < nq) x = __ldg(tiles + static_cast<size_t>(q) * words + w);
-   uint32_t mine = 0;
+   const uint32_t nqc = (nq + 31) / 32;
+   const uint32_t w = blockIdx.x * TR_WORDS + warp;  // words is a multiple of TR_WORDS
+   const size_t rows = static_cast<size_t>(words) * 32;
+   for (uint32_t c0 = 0; c0 < nqc; c0 += TR_CHUNKS) {
+      const uint32_t nc = nqc - c0 < TR_CHUNKS ? nqc - c0 : TR_CHUNKS;
+      const uint32_t P = nc | 1u;  // odd stride: the 32 lanes of a warp hit 32 banks
+      for (uint32_t c = 0; c < nc; ++c) {
+         const uint32_t q = 32 * (c0 + c) + lane;
+         const uint32_t x = q < nq ? __ldg(tiles + static_cast<size_t>(q) * words + w) : 0u;
+         uint32_t mine = 0;
 #pragma unroll
-   for (uint32_t b = 0; b < 32; ++b) {
-      const uint32_t m = __ballot_sync(0xFFFFFFFFu, (x >> b) & 1u);
-      if (lane == b) mine = m;
+         for (uint32_t b = 0; b < 32; ++b) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, (x >> b) & 1u);
+            if (lane == b) mine = m;
+         }
+         const uint32_t g0 = 2 * (c0 + c);
+         const size_t row = static_cast<size_t>(w) * 32 + lane;
+         T[static_cast<size_t>(g0) * rows + row] = static_cast<uint16_t>(mine);
+         if (g0 + 1 < ngroups) T[static_cast<size_t>(g0 + 1) * rows + row] = static_cast<uint16_t>(mine >> 16);
+         stage[(warp * 32 + lane) * P + c] = mine;
+      }
+      __syncthreads();
+      const size_t row0 = static_cast<size_t>(blockIdx.x) * TR_WORDS * 32;
+      for (uint32_t k = threadIdx.x; k < TR_WORDS * 32 * nc; k += blockDim.x) {
+         const uint32_t r = k / nc, c = k % nc;
+         R[(row0 + r) * nqc + c0 + c] = stage[r * P + c];
+      }
+      __syncthreads();
    }
-   T[static_cast<size_t>(g) * words * 32 + static_cast<size_t>(w) * 32 + lane] = static_cast<uint16_t>(mine);
 }
 
 __device__ __forceinline__ void bulk_load_smem(void* smem, const void* gmem, uint32_t bytes, uint64_t* bar) {
@@ -233,89 +261,148 @@ __global__ void __launch_bounds__(CT) mut_ctr_batch_kernel(const DevTable* __res
    }
 }
 
-// One CTA per (event item, query group). Missing events: per position, the queries whose filter
-// holds the event's row add +1 (start) / -1 (end); coverage events count per query.
-__global__ void __launch_bounds__(BT) mut_cov_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                           const EvItem* __restrict__ items, uint32_t n_items,
-                                                           const uint16_t* __restrict__ T, uint32_t nq,
+// Per-lane counters of the 16 queries of one group at the current position. Masks are added two
+// events at a time as one 32-bit word w = m1 | m2 << 16 into four words of nibble counters:
+// nibble k of nib[j] counts query j + 4 (k % 4). After at most 15 additions the nibbles are
+// drained into 32-bit counters.
+struct GroupCounter {
+   uint32_t nib[4];
+   uint32_t nadd;
+   uint32_t c[MUT_GROUP];    // counts at the current position
+   uint32_t seg[MUT_GROUP];  // counts in the current MUT_SEG segment
+
+   __device__ __forceinline__ void drain() {
+#pragma unroll
+      for (uint32_t q = 0; q < MUT_GROUP; ++q) {
+         const uint32_t a = nib[q & 3u], sh = 4u * (q >> 2);
+         c[q] += ((a >> sh) & 0xFu) + ((a >> (sh + 16u)) & 0xFu);
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) nib[j] = 0;
+      nadd = 0;
+   }
+   __device__ __forceinline__ void add(uint32_t w) {
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) nib[j] += (w >> j) & 0x11111111u;
+      if (++nadd == 15) drain();
+   }
+};
+
+// One CTA per event item and pass of up to 32 query groups (blockIdx.y). A sub-warp of gsz lanes,
+// one lane per query group, streams a contiguous slice of the item's position-sorted events: each
+// lane gathers its group's mask of the event's row from the row-major matrix R and counts its 16
+// queries; when the position changes it adds the nonzero counts to the query's difference array
+// (missing events: +1 start, -1 end) or boundary histogram (coverage events), and once per segment
+// to the segment totals. Events are read once for all groups of the pass.
+__global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                           const EvItem* __restrict__ items,
+                                                           const uint16_t* __restrict__ R, uint32_t nq,
                                                            uint32_t* __restrict__ scratch) {
-   __shared__ int cnt[MUT_GROUP][NBLOCK + 1];
-   __shared__ PackedLut lut;
    const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t L = cs->L, nchunks = tab->nchunks, nseg = mut_nseg(L);
-   const uint32_t item = blockIdx.x % n_items, g = blockIdx.x / n_items;
-   const uint32_t qbase = g * MUT_GROUP;
-   const uint32_t nqg = nq - qbase < MUT_GROUP ? nq - qbase : MUT_GROUP;
+   const uint32_t L = cs->L, nseg = mut_nseg(L);
    const size_t per_query = mut_scratch_words(L);
-   const uint16_t* Tg = T + static_cast<size_t>(g) * nchunks * CHUNK_ROWS;
-   const EvItem it = items[item];
+   const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;
+   const uint32_t S = 2u * ((nq + 31) / 32);  // u16 masks per row of R
+   const uint32_t gpass = blockIdx.y * 32;
+   const uint32_t gleft = ngroups - gpass;
+   uint32_t gsz = 1;
+   while (gsz < gleft && gsz < 32) gsz <<= 1;
    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   if (it.list <= EV_MEND) {
-      build_lut(lut);
-      for (uint32_t i = threadIdx.x; i < MUT_GROUP * (NBLOCK + 1); i += blockDim.x) (&cnt[0][0])[i] = 0;
-      __syncthreads();
-      const uint32_t* ev = it.list == EV_MSTART ? cs->mstart : cs->mend;
-      constexpr uint32_t U = 4;  // events per lane in flight
-      for (uint32_t base = it.begin + warp * 32 * U; base < it.end; base += blockDim.x * U) {
-         uint32_t e[U], mk[U];
+   const uint32_t g = gpass + (lane & (gsz - 1));
+   const bool gvalid = g < ngroups;
+   const uint32_t spw = 32 / gsz;
+   const uint32_t nsub = (blockDim.x >> 5) * spw, sub = warp * spw + lane / gsz;
+   const EvItem it = items[blockIdx.x];
+   const uint32_t n = it.end - it.begin;
+   const uint32_t s0 = it.begin + static_cast<uint32_t>(static_cast<uint64_t>(n) * sub / nsub);
+   const uint32_t s1 = it.begin + static_cast<uint32_t>(static_cast<uint64_t>(n) * (sub + 1) / nsub);
+
+   const bool missing = it.list <= EV_MEND;
+   const uint32_t* mev = it.list == EV_MSTART ? cs->mstart : cs->mend;
+   const uint2* cev = reinterpret_cast<const uint2*>(it.list == EV_CSTART ? cs->cstart : cs->cend);
+   const uint32_t pbase = missing ? it.block * NBLOCK : 0u;
+   const uint32_t hist = missing ? 2 * (L + 1) : (it.list == EV_CSTART ? 0u : L + 1);
+   const uint32_t segb = 3 * (L + 1) + (missing ? 2 * nseg : (it.list == EV_CSTART ? 0u : nseg));
+   const uint32_t sign = it.list == EV_MEND ? 0xFFFFFFFFu : 1u;  // multiplier modulo 2^32
+   uint32_t* sc = scratch + static_cast<size_t>(g) * MUT_GROUP * per_query;
+
+   GroupCounter k;
 #pragma unroll
-         for (uint32_t k = 0; k < U; ++k) {
-            const uint32_t i = base + 32 * k + lane;
-            e[k] = i < it.end ? __ldg(ev + i) : 0xFFFFFFFFu;
+   for (uint32_t q = 0; q < MUT_GROUP; ++q) k.c[q] = k.seg[q] = 0;
+#pragma unroll
+   for (uint32_t j = 0; j < 4; ++j) k.nib[j] = 0;
+   k.nadd = 0;
+   constexpr uint32_t NONE = 0xFFFFFFFEu, INVALID = 0xFFFFFFFFu;
+   uint32_t cur = NONE, curseg = NONE;
+
+   auto flush_seg = [&]() {
+      if (curseg == NONE) return;
+#pragma unroll
+      for (uint32_t q = 0; q < MUT_GROUP; ++q) {
+         if (k.seg[q] && MUT_GROUP * g + q < nq)
+            atomicAdd(sc + q * per_query + segb + curseg, k.seg[q] * sign);
+         k.seg[q] = 0;
+      }
+   };
+   auto flush_pos = [&]() {
+      k.drain();
+      if (cur != NONE && cur <= L) {
+#pragma unroll
+         for (uint32_t q = 0; q < MUT_GROUP; ++q) {
+            if (k.c[q] && MUT_GROUP * g + q < nq) atomicAdd(sc + q * per_query + hist + cur, k.c[q] * sign);
+            k.seg[q] += k.c[q];
          }
+      }
 #pragma unroll
-         for (uint32_t k = 0; k < U; ++k) mk[k] = e[k] != 0xFFFFFFFFu ? __ldg(Tg + (e[k] >> 8)) : 0u;
+      for (uint32_t q = 0; q < MUT_GROUP; ++q) k.c[q] = 0;
+   };
+   auto move_to = [&](uint32_t p) {
+      flush_pos();
+      cur = p;
+      if (p / MUT_SEG != curseg) {
+         flush_seg();
+         curseg = p / MUT_SEG;
+      }
+   };
+
+   constexpr uint32_t U = 4;  // events in flight per lane
+   for (uint32_t i = s0; i < s1; i += U) {
+      uint32_t row[U], pos[U], m[U];
 #pragma unroll
-         for (uint32_t k = 0; k < U; ++k) {
-            const bool active = e[k] != 0xFFFFFFFFu;
-            const uint32_t pos = e[k] & 0xFFu;
-            const uint32_t amask = __ballot_sync(0xFFFFFFFFu, active);
-            const uint32_t grp = __match_any_sync(0xFFFFFFFFu, active ? pos : 0xFFFFu);
-            if (active) {
-               uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-               add_packed(acc, lut, mk[k]);
-               const uint32_t members = grp & amask;
-#pragma unroll
-               for (uint32_t j = 0; j < 8; ++j) acc[j] = __reduce_add_sync(members, acc[j]);
-               // the lanes of the group share the per-query additions
-               const uint32_t gsize = __popc(members);
-               const uint32_t grank = __popc(members & ((1u << lane) - 1u));
-               for (uint32_t q = grank; q < nqg; q += gsize) {
-                  const uint32_t c = unpack(acc, q);
-                  if (c) atomicAdd(&cnt[q][pos], static_cast<int>(c));
-               }
+      for (uint32_t u = 0; u < U; ++u) {
+         row[u] = 0;
+         pos[u] = INVALID;
+         if (i + u < s1) {
+            if (missing) {
+               const uint32_t e = __ldg(mev + i + u);
+               row[u] = e >> 8;
+               pos[u] = pbase + (e & 0xFFu);
+            } else {
+               const uint2 e = __ldg(cev + i + u);
+               row[u] = e.x;
+               pos[u] = e.y;
             }
          }
       }
-      __syncthreads();
-      const int sign = it.list == EV_MSTART ? 1 : -1;
-      for (uint32_t k = threadIdx.x; k < MUT_GROUP * (NBLOCK + 1); k += blockDim.x) {
-         const uint32_t q = k / (NBLOCK + 1), o = k % (NBLOCK + 1);
-         const int x = cnt[q][o];
-         const uint32_t p = it.block * NBLOCK + o;
-         if (q < nqg && x != 0 && p <= L) {
-            uint32_t* sc = scratch + static_cast<size_t>(qbase + q) * per_query;
-            atomicAdd(&sc[2 * (L + 1) + p], static_cast<uint32_t>(sign * x));
-            atomicAdd(&sc[3 * (L + 1) + 2 * nseg + p / MUT_SEG], static_cast<uint32_t>(sign * x));
-         }
-      }
-   } else {
-      const CovEvent* ev = it.list == EV_CSTART ? cs->cstart : cs->cend;
-      const uint32_t hist_off = it.list == EV_CSTART ? 0 : (L + 1);
-      const uint32_t seg_off = 3 * (L + 1) + (it.list == EV_CSTART ? 0 : nseg);
-      for (uint32_t i = it.begin + threadIdx.x; i < it.end; i += blockDim.x) {
-         const uint2 e = __ldg(reinterpret_cast<const uint2*>(ev) + i);
-         uint32_t m = __ldg(Tg + e.x);
-         while (m) {
-            const uint32_t q = __ffs(m) - 1;
-            m &= m - 1;
-            if (q >= nqg) break;
-            uint32_t* sc = scratch + static_cast<size_t>(qbase + q) * per_query;
-            atomicAdd(&sc[hist_off + e.y], 1u);
-            atomicAdd(&sc[seg_off + e.y / MUT_SEG], 1u);
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u)
+         m[u] = (pos[u] != INVALID && gvalid) ? __ldg(R + static_cast<size_t>(row[u]) * S + g) : 0u;
+#pragma unroll
+      for (uint32_t u = 0; u < U; u += 2) {
+         if (pos[u] == cur && pos[u + 1] == cur) {
+            k.add(__byte_perm(m[u], m[u + 1], 0x5410));
+         } else {
+#pragma unroll
+            for (uint32_t x = u; x < u + 2; ++x) {
+               if (pos[x] == INVALID) continue;
+               if (pos[x] != cur) move_to(pos[x]);
+               k.add(m[x]);
+            }
          }
       }
    }
+   flush_pos();
+   flush_seg();
 }
 
 // grid (ceil(L / MUT_SEG), nq): reference counts of slot blockIdx.y.
@@ -336,7 +423,8 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_batch_kernel(const DevTable
 
 size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks) {
    const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;
-   return static_cast<size_t>(ngroups) * nchunks * CHUNK_ROWS * 2;
+   const uint32_t nqc = (nq + 31) / 32;
+   return static_cast<size_t>(ngroups) * nchunks * CHUNK_ROWS * 2 + static_cast<size_t>(nqc) * nchunks * CHUNK_ROWS * 4;
 }
 
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
@@ -346,16 +434,17 @@ void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, 
    if (nq == 0) return;
    cudaStream_t s = static_cast<cudaStream_t>(stream);
    const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;
-   const uint64_t warps = static_cast<uint64_t>(nchunks) * CHUNK_WORDS * ngroups;
+   uint16_t* d_rows = d_masks + static_cast<size_t>(ngroups) * nchunks * CHUNK_ROWS;  // row-major masks
    if (parts & BMUT_PART_TRANSPOSE)
-      transpose_kernel<<<static_cast<uint32_t>((warps * 32 + BT - 1) / BT), BT, 0, s>>>(d_filters, nq, nchunks, d_masks);
+      transpose_kernel<<<nchunks * CHUNK_WORDS / TR_WORDS, BT, 0, s>>>(d_filters, nq, nchunks, d_masks,
+                                                                       reinterpret_cast<uint32_t*>(d_rows));
    if (parts & BMUT_PART_CTR) {
       const int smem = CHUNK_ROWS * 2;
       cudaFuncSetAttribute(mut_ctr_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       mut_ctr_batch_kernel<<<nchunks * ngroups, CT, smem, s>>>(d_table, col, d_masks, nq, d_counts, d_err);
    }
    if ((parts & BMUT_PART_COV) && n_ev > 0)
-      mut_cov_batch_kernel<<<n_ev * ngroups, BT, 0, s>>>(d_table, col, d_ev, n_ev, d_masks, nq, d_scratch);
+      mut_cov_batch_kernel<<<dim3(n_ev, (ngroups + 31) / 32), BT, 0, s>>>(d_table, col, d_ev, d_rows, nq, d_scratch);
    if (parts & BMUT_PART_FINAL) {
       dim3 fin((col_host.L + MUT_SEG - 1) / MUT_SEG, nq);
       mut_final_batch_kernel<<<fin, MUT_SEG, 0, s>>>(d_table, col, d_fcounts, d_slot_query, d_counts, d_scratch);

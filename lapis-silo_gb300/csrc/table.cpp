@@ -241,7 +241,9 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
 }
 
 // Start / end events of the missing intervals, counting-sorted by (block, position) with rows in
-// increasing order inside each bucket, and the coverage boundary events.
+// increasing order inside each bucket, and the coverage boundary events. An interval [s, e)
+// contributes +1 at s and -1 at e to the per-position difference array: its start event lives in
+// block s / NBLOCK at offset s % NBLOCK, its end event in block (e - 1) / NBLOCK at offset 1..NBLOCK.
 void build_mutation_events(SeqColumnImage& col, const std::vector<ChunkRows>& chunks,
                            const std::vector<uint32_t>& chunk_sizes) {
    const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
@@ -257,17 +259,15 @@ void build_mutation_events(SeqColumnImage& col, const std::vector<ChunkRows>& ch
          for (uint32_t r = 0; r < chunk_sizes[v]; ++r) {
             for (uint32_t q = c.nr_off[r]; q < c.nr_off[r + 1]; ++q) {
                const uint32_t s = c.nr_s[q], e = c.nr_e[q];
-               for (uint32_t b = s / NBLOCK; b <= (e - 1) / NBLOCK; ++b) {
-                  const uint32_t bs = b * NBLOCK;
-                  fn((v << 16) | r, b, std::max(s, bs) - bs, std::min(e, bs + NBLOCK) - bs);
-               }
+               const uint32_t sb = s / NBLOCK, eb = (e - 1) / NBLOCK;
+               fn((v << 16) | r, sb, s - sb * NBLOCK, eb, e - eb * NBLOCK);
             }
          }
       }
    };
-   each([&](uint32_t, uint32_t b, uint32_t lo, uint32_t hi) {
-      cs[static_cast<size_t>(b) * W + lo + 1]++;
-      ce[static_cast<size_t>(b) * W + hi + 1]++;
+   each([&](uint32_t, uint32_t sb, uint32_t lo, uint32_t eb, uint32_t hi) {
+      cs[static_cast<size_t>(sb) * W + lo + 1]++;
+      ce[static_cast<size_t>(eb) * W + hi + 1]++;
    });
    for (size_t i = 0; i < nbuckets; ++i) {
       cs[i + 1] += cs[i];
@@ -281,9 +281,9 @@ void build_mutation_events(SeqColumnImage& col, const std::vector<ChunkRows>& ch
       col.mstart_off[b] = cs[static_cast<size_t>(b) * W];
       col.mend_off[b] = ce[static_cast<size_t>(b) * W];
    }
-   each([&](uint32_t g, uint32_t b, uint32_t lo, uint32_t hi) {
-      col.mstart[cs[static_cast<size_t>(b) * W + lo]++] = (g << 8) | lo;
-      col.mend[ce[static_cast<size_t>(b) * W + hi]++] = (g << 8) | hi;
+   each([&](uint32_t g, uint32_t sb, uint32_t lo, uint32_t eb, uint32_t hi) {
+      col.mstart[cs[static_cast<size_t>(sb) * W + lo]++] = (g << 8) | lo;
+      col.mend[ce[static_cast<size_t>(eb) * W + hi]++] = (g << 8) | hi;
    });
    // coverage boundaries
    for (uint32_t v = 0; v < nchunks; ++v) {
