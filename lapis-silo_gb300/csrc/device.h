@@ -118,15 +118,24 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
                       uint32_t parts = MUT_PART_ALL);
 
+// One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),
+// at most CTR_UNIT_CHUNKS chunks and, unless a single chunk exceeds it, CTR_UNIT_ELEMENTS elements.
+struct CtrUnit {
+   uint32_t pos;
+   uint16_t v0, v1;
+};
+constexpr uint32_t CTR_UNIT_CHUNKS = 32;
+constexpr uint32_t CTR_UNIT_ELEMENTS = 4096;
+
 // Batched mutations over nq filters (slot-major dense tiles, nchunks * CHUNK_WORDS each):
 // counts[slot][nsym][L] and scratch[slot][mut_scratch_words(L)] zeroed by the caller;
 // d_fcounts[d_slot_query[slot]] is the cardinality of the slot's filter; d_masks holds
-// mutations_batch_mask_bytes(nq, nchunks).
+// mutations_batch_mask_bytes(nq, nchunks); d_units lists the column's container units, heaviest first.
 size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks);
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                             const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
-                            const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, uint16_t* d_masks,
-                            uint32_t* d_counts, uint32_t* d_scratch, int* d_err, void* stream,
+                            const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
+                            uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
                             uint32_t parts = BMUT_PART_ALL);
 
 // Events per CTA of the coverage pass.

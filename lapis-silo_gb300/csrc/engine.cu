@@ -19,6 +19,34 @@ void* Engine::alloc(size_t bytes) {
    return p;
 }
 
+// Work units of the batched container pass: per position, runs of consecutive chunks holding at
+// most CTR_UNIT_ELEMENTS container elements (a heavier chunk forms a unit of its own) and at most
+// CTR_UNIT_CHUNKS chunks; positions without containers have none. Sorted by element count,
+// heaviest first, so the long units start in the first wave.
+std::vector<CtrUnit> container_units(const SeqColumnImage& s, uint32_t nchunks) {
+   const ContainerSet& cs = s.vertical;
+   std::vector<std::pair<uint32_t, CtrUnit>> units;
+   for (uint32_t p = 0; p < s.L; ++p) {
+      uint32_t v0 = 0, acc = 0;
+      for (uint32_t v = 0; v < nchunks; ++v) {
+         uint32_t w = 0;
+         for (uint32_t i = cs.off[static_cast<size_t>(v) * s.L + p]; i < cs.off[static_cast<size_t>(v) * s.L + p + 1]; ++i)
+            w += cs.ctrs[i].card_m1 + 1u;
+         if (v > v0 && (acc + w > CTR_UNIT_ELEMENTS || v - v0 == CTR_UNIT_CHUNKS)) {
+            if (acc) units.push_back({acc, CtrUnit{p, static_cast<uint16_t>(v0), static_cast<uint16_t>(v)}});
+            v0 = v;
+            acc = 0;
+         }
+         acc += w;
+      }
+      if (acc) units.push_back({acc, CtrUnit{p, static_cast<uint16_t>(v0), static_cast<uint16_t>(nchunks)}});
+   }
+   std::stable_sort(units.begin(), units.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+   std::vector<CtrUnit> out(units.size());
+   for (size_t i = 0; i < units.size(); ++i) out[i] = units[i].second;
+   return out;
+}
+
 template <typename T>
 T* Engine::upload(const std::vector<T>& v, size_t min_elems) {
    const size_t n = std::max(v.size(), min_elems);
@@ -75,6 +103,9 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
          split(EV_CEND, 0, 0, static_cast<uint32_t>(s.cend.size()));
          n_ev_.push_back(static_cast<uint32_t>(items.size()));
          d_ev_.push_back(upload(items));
+         const std::vector<CtrUnit> units = container_units(s, nchunks);
+         n_cu_.push_back(static_cast<uint32_t>(units.size()));
+         d_cu_.push_back(upload(units));
       }
       for (size_t c = 0; c < t.dict.size(); ++c) {
          const DictColumnImage& s = t.dict[c];
@@ -392,9 +423,9 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
    for (const auto& g : b.groups) {
       launch_mutations_batch(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), nchunks(),
                              b.d_tiles + static_cast<size_t>(g.slot_begin) * words, g.n, b.d_counts,
-                             b.d_slot_query + g.slot_begin, d_ev_[g.column], n_ev_[g.column], b.d_masks,
-                             b.d_mcounts + g.counts_off,
-                             b.d_mscratch + g.scratch_off, d_err, s, (parts >> 1) & BMUT_PART_ALL);
+                             b.d_slot_query + g.slot_begin, d_ev_[g.column], n_ev_[g.column], d_cu_[g.column],
+                             n_cu_[g.column], b.d_masks, b.d_mcounts + g.counts_off, b.d_mscratch + g.scratch_off, s,
+                             (parts >> 1) & BMUT_PART_ALL);
       cuda_check(cudaGetLastError(), "mutations batch launch");
    }
    if (copy_out) {

@@ -145,6 +145,8 @@ class Engine {
    std::vector<void*> allocs_;
    std::vector<EvItem*> d_ev_;
    std::vector<uint32_t> n_ev_;
+   std::vector<CtrUnit*> d_cu_;  // container units of the batched Mutations pass, heaviest first
+   std::vector<uint32_t> n_cu_;
    Instr* h_code_ = nullptr;               // pinned staging
    unsigned long long* h_count_ = nullptr; // pinned
    int* h_err_ = nullptr;                  // pinned
