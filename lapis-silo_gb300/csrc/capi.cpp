@@ -360,6 +360,7 @@ int rhy_set_tile_bits(RhyDevice* d, uint32_t tile_bits) {
       if (tile_bits < 4096 || tile_bits > 65536 || (tile_bits & (tile_bits - 1)))
          throw std::invalid_argument("tile_bits must be a power of two in [4096, 65536]");
       d->engine->tile_bits = tile_bits;
+      d->engine->batch_tile_bits = tile_bits;
    });
 }
 

@@ -6,7 +6,7 @@
 //   offset table, per-chunk coverage exceptions, missing-interval buckets per 128-position block,
 //   a dense null-row bitmap (8 KiB per chunk) and the local reference;
 //   dictionary column: the inverted index in the same container format, keyed by value id;
-//   date column: one int32 per row (chunk stride 2^16).
+//   date column: bit-sliced index (one dense bitmap per bit of date - min date) and a null bitmap.
 // Row sets are dense bitmaps of 2^16 bits (8 KiB) per chunk.
 #pragma once
 
@@ -31,6 +31,8 @@ struct DevSeqCol {
    const uint32_t* exc_off;    // nchunks + 1
    const NRunEntry* nblk;
    const uint32_t* nblk_off;   // nblocks * nchunks + 1
+   const uint32_t* exc_toff;   // nchunks * TOFF_N: tile row-range offsets into exc
+   const uint32_t* nblk_toff;  // nblocks * nchunks * TOFF_N: the same into each nblk bucket
    const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
    const uint8_t* local_ref;   // L
    const uint32_t* mstart;     // missing-interval start events (row << 8 | position in block)
@@ -60,8 +62,16 @@ struct DevDictCol {
    uint32_t pad;
 };
 
+// Date column as a bit-sliced index: plane i holds bit i of (date - base) for every row (dense,
+// nchunks * CHUNK_WORDS words per plane), `nulls` the rows without a date. A range predicate then
+// reads nbits + 1 bits per row instead of a 32-bit value.
+constexpr uint32_t MAX_DATE_BITS = 32;
 struct DevDateCol {
-   const int32_t* days;        // nchunks * CHUNK_ROWS
+   const uint32_t* planes;     // nbits * nchunks * CHUNK_WORDS
+   const uint32_t* nulls;      // nchunks * CHUNK_WORDS
+   int64_t base;               // smallest date
+   uint32_t nbits;             // 1..32
+   uint32_t pad;
 };
 
 struct DevTable {
@@ -91,13 +101,14 @@ struct QueryDesc {
    uint32_t code_off;     // offset of the program in the shared instruction buffer
    uint32_t code_len;
    uint32_t out_tiles;    // 1 = write the row set to the query's output tiles
-   uint32_t pad;
+   uint32_t n_leaves;     // container leaves | coverage leaves << 16 (numbered 1.. in their c field)
 };
 
 // ---- launchers (kernels.cu) ----
-// tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth.
+// tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth. n_leaves: container
+// leaves of the program (Program::n_ctr_leaves).
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
-                          uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
+                          uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
                           int* d_err, void* stream);
 
 // Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.

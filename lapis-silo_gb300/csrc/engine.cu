@@ -55,6 +55,34 @@ T* Engine::upload(const std::vector<T>& v, size_t min_elems) {
    return p;
 }
 
+// Bit-sliced date index: base = smallest date, nbits = bits of (largest - smallest), at least 1.
+void Engine::upload_dates(const DateColumnImage& dc, uint32_t nchunks, DevDateCol& out) {
+   const size_t words = static_cast<size_t>(nchunks) * CHUNK_WORDS;
+   int64_t lo = INT64_MAX, hi = INT64_MIN;
+   for (int32_t d : dc.days)
+      if (d != INT32_MIN) lo = std::min<int64_t>(lo, d), hi = std::max<int64_t>(hi, d);
+   if (lo > hi) lo = hi = 0;
+   const uint64_t span = static_cast<uint64_t>(hi - lo);
+   uint32_t nbits = 1;
+   while (nbits < MAX_DATE_BITS && (span >> nbits) != 0) ++nbits;
+   std::vector<uint32_t> planes(static_cast<size_t>(nbits) * words, 0), nulls(words, 0);
+   for (size_t g = 0; g < dc.days.size() && g < words * 32; ++g) {
+      const int32_t d = dc.days[g];
+      if (d == INT32_MIN) {
+         nulls[g >> 5] |= 1u << (g & 31);
+         continue;
+      }
+      const uint64_t x = static_cast<uint64_t>(d - lo);
+      for (uint32_t i = 0; i < nbits; ++i)
+         if ((x >> i) & 1u) planes[i * words + (g >> 5)] |= 1u << (g & 31);
+   }
+   out.planes = upload(planes);
+   out.nulls = upload(nulls);
+   out.base = lo;
+   out.nbits = nbits;
+   out.pad = 0;
+}
+
 Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
    if (t.seq.size() > MAX_SEQ_COLS || t.dict.size() > MAX_DICT_COLS || t.date.size() > MAX_DATE_COLS)
       throw std::invalid_argument("too many columns for the device image");
@@ -76,6 +104,8 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
          d.exc_off = upload(s.cov_exc_off);
          d.nblk = upload(s.nblk);
          d.nblk_off = upload(s.nblk_off);
+         d.exc_toff = upload(s.exc_toff);
+         d.nblk_toff = upload(s.nblk_toff);
          std::vector<uint32_t> nulls(static_cast<size_t>(nchunks) * CHUNK_WORDS, 0);
          for (uint32_t g : s.null_rows) nulls[g >> 5] |= 1u << (g & 31);
          d.null_tiles = upload(nulls);
@@ -115,7 +145,7 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
          d.off = upload(s.inverted.off);
          d.nkeys = s.inverted.nkeys;
       }
-      for (size_t c = 0; c < t.date.size(); ++c) view_.date[c].days = upload(t.date[c].days);
+      for (size_t c = 0; c < t.date.size(); ++c) upload_dates(t.date[c], nchunks, view_.date[c]);
       d_table_ = static_cast<DevTable*>(alloc(sizeof(DevTable)));
       cuda_check(cudaMemcpy(d_table_, &view_, sizeof(DevTable), cudaMemcpyHostToDevice), "upload table view");
 
@@ -173,7 +203,8 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
    while (W > 4096 && static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) W >>= 1;
    if (static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
    cudaGetLastError();  // an error left by an unrelated earlier call must not be reported here
-   const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()), W,
+   const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()),
+                                               p.n_ctr_leaves | (p.n_cov_leaves << 16), W,
                                                p.max_depth, tiles, count, d_err, stream);
    if (e != cudaSuccess)
       throw CudaError("filter kernel launch (tile " + std::to_string(W) + " rows, stack " + std::to_string(p.max_depth) +
@@ -266,8 +297,8 @@ std::vector<Program> plan_many(const TableImage& t, const std::vector<std::strin
    return out;
 }
 
-uint32_t Engine::fit_tile_bits(uint32_t requested, uint32_t depth) const {
-   uint32_t W = requested ? requested : tile_bits;
+uint32_t Engine::fit_tile_bits(uint32_t requested, uint32_t depth, bool batch) const {
+   uint32_t W = requested ? requested : batch ? batch_tile_bits : tile_bits;
    while (W > 4096 && static_cast<size_t>(depth) * (W / 8) > 200 * 1024) W >>= 1;
    if (static_cast<size_t>(depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
    return W;
@@ -324,7 +355,7 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
       if (q.action == 1 && (q.column < 0 || static_cast<size_t>(q.column) >= table_.seq.size()))
          throw std::invalid_argument("no such sequence column");
    }
-   const uint32_t W = fit_tile_bits(requested_tile_bits, depth);
+   const uint32_t W = fit_tile_bits(requested_tile_bits, depth, true);
    const uint32_t tiles_per_query = nchunks() * (CHUNK_ROWS / W);
    // mutation slots grouped by column
    std::vector<std::vector<uint32_t>> by_col(table_.seq.size());
@@ -373,7 +404,8 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
       const Program& p = qs[i].prog;
       std::memcpy(b.h_code + off, p.code.data(), p.code.size() * sizeof(Instr));
       b.h_q[i] = QueryDesc{static_cast<uint32_t>(off), static_cast<uint32_t>(p.code.size()),
-                           b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1, 0};
+                           b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1,
+                           p.n_ctr_leaves | (p.n_cov_leaves << 16)};
       off += p.code.size();
    }
    // items: tile-major interleaving spreads the expensive queries over the whole launch

@@ -81,8 +81,11 @@ class Engine {
    // The stream a call runs on: the caller's, or the engine's own when the caller passed none.
    cudaStream_t stream_for(cudaStream_t s) const { return s ? s : stream_; }
 
-   // Tile width of the filter kernel (rows per CTA). 4096 .. 65536, power of two.
+   // Tile width of the filter kernel (rows per CTA). 4096 .. 65536, power of two. The single-query
+   // path wants many CTAs (one per tile); the persistent batched kernel amortises each leaf's
+   // latency over wider tiles. rhy_set_tile_bits sets both.
    uint32_t tile_bits = 16384;
+   uint32_t batch_tile_bits = 65536;
 
    Program plan(const std::string& expr, const LowerOptions& opt = {}, std::string* tree = nullptr) const;
 
@@ -116,7 +119,7 @@ class Engine {
    const uint32_t* batch_mutation_counts(uint32_t query) const;  // pinned host, after the stream synced
    uint64_t batch_count(uint32_t query) const { return batch_.h_counts[query]; }
    // Tile width that fits the batch's deepest program in the shared-memory budget.
-   uint32_t fit_tile_bits(uint32_t requested, uint32_t depth) const;
+   uint32_t fit_tile_bits(uint32_t requested, uint32_t depth, bool batch = false) const;
 
    const EvItem* d_ev(int column) const { return d_ev_[column]; }
    uint32_t n_ev(int column) const { return n_ev_[column]; }
@@ -136,6 +139,7 @@ class Engine {
    template <typename T>
    T* upload(const std::vector<T>& v, size_t min_elems = 1);
    void* alloc(size_t bytes);
+   void upload_dates(const DateColumnImage& dc, uint32_t nchunks, DevDateCol& out);
 
    const TableImage& table_;
    int device_;

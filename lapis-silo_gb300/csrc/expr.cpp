@@ -918,7 +918,7 @@ struct Lowerer {
          date(date_leaf(p));
          return;
       }
-      emit(OP_PUSH_COVERED, static_cast<uint8_t>(p.col), p.covered ? 0 : 1, p.pos);
+      emit(OP_PUSH_COVERED, static_cast<uint8_t>(p.col), p.covered ? 0 : 1, p.pos, 0, ++prog.n_cov_leaves);
       push();
       ++prog.n_leaves;
    }
@@ -944,11 +944,12 @@ struct Lowerer {
             return;
          case OpT::INDEX_SCAN:
             if (op.leaf.kind == Leaf::SEQ) {
-               emit(OP_PUSH_SCAN, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.pos, op.leaf.symmask);
+               emit(OP_PUSH_SCAN, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.pos, op.leaf.symmask,
+                    ++prog.n_ctr_leaves);
             } else if (op.leaf.kind == Leaf::NULLS) {
                emit(OP_PUSH_NULLS, static_cast<uint8_t>(op.leaf.col));
             } else {
-               emit(OP_PUSH_DICT, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.value);
+               emit(OP_PUSH_DICT, static_cast<uint8_t>(op.leaf.col), 0, op.leaf.value, 0, ++prog.n_ctr_leaves);
             }
             push();
             ++prog.n_leaves;

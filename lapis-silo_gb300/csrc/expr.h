@@ -109,6 +109,8 @@ struct Program {
    std::vector<Instr> code;
    uint32_t max_depth = 0;   // tiles of stack needed
    uint32_t n_leaves = 0;
+   uint32_t n_ctr_leaves = 0;  // PUSH_SCAN / PUSH_DICT leaves, numbered 1.. in their c field
+   uint32_t n_cov_leaves = 0;  // PUSH_COVERED leaves, numbered 1.. in their c field
 };
 
 struct LowerOptions {

@@ -78,85 +78,284 @@ struct TileCtx {
    uint32_t nvalid;
 };
 
-__device__ __forceinline__ void tile_zero(uint32_t* t, uint32_t WW) {
-   for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = 0u;
+// Per-item staging of the program's leaves for the chunk and row range of the current tile:
+//  - container leaves (PUSH_SCAN / PUSH_DICT, c = ordinal + 1): the slot offsets of all leaves are
+//    read in one round of loads and their descriptors in a second, so a leaf then costs one round
+//    trip (its payload) instead of three;
+//  - coverage leaves (PUSH_COVERED, c = ordinal + 1): the tile's ranges of coverage exceptions and
+//    missing intervals.
+// Every staged payload and range is also handed to the TMA engine as a bulk L2 prefetch, so the
+// leaves find their data in L2 when the program reaches them.
+constexpr uint32_t LC_LEAVES = 128;
+constexpr uint32_t LC_DESCS = 256;
+constexpr uint32_t LC_COV = 64;
+constexpr uint32_t LC_NONE = 0xFFFFFFFFu;
+
+struct LeafCache {
+   uint4 desc[LC_DESCS];
+   const uint4* src[LC_LEAVES];
+   const uint16_t* pay[LC_LEAVES];
+   uint32_t n[LC_LEAVES];
+   uint32_t beg[LC_LEAVES];  // LC_NONE: not staged (the leaf reads its descriptors from global memory)
+   uint4 cov[LC_COV];        // exception range (x, y) and missing-interval range (z, w) of the tile
+   uint32_t nl;              // container leaves 1..nl are described by the table
+   uint32_t ncov;            // coverage leaves 1..ncov
+};
+
+// Bulk prefetch of global bytes [a, b) into L2; a is rounded down and b up to 16 bytes, so the
+// caller guarantees the rounded range stays inside the allocation.
+__device__ __forceinline__ void prefetch_l2(const void* a, const void* b) {
+   const uintptr_t s = reinterpret_cast<uintptr_t>(a) & ~static_cast<uintptr_t>(15);
+   const uintptr_t e = (reinterpret_cast<uintptr_t>(b) + 15) & ~static_cast<uintptr_t>(15);
+   if (e <= s) return;
+   const uint32_t n = static_cast<uint32_t>(min(e - s, static_cast<uintptr_t>(32768)));
+   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"(n) : "memory");
 }
 
-// Scan of one (key) slot of a container set: OR of the containers whose symbol is in `mask`.
+// Clears the leaf tables for nl container and ncov coverage leaves; a barrier must follow.
+__device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_t ncov) {
+   if (threadIdx.x == 0) {
+      lc.nl = nl;
+      lc.ncov = ncov;
+   }
+   for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
+      lc.n[k] = 0;
+      lc.src[k] = nullptr;
+   }
+   for (uint32_t k = threadIdx.x; k < ncov; k += blockDim.x) lc.cov[k] = make_uint4(0, 0, 0, 0);
+}
+
+// The tile's ranges in the coverage exceptions of chunk v and in the missing-interval bucket of
+// position pos (both lists are sorted by row; TOFF_ROWS divides every tile boundary).
+__device__ __forceinline__ uint4 cover_ranges(const DevTable* __restrict__ tab, const DevSeqCol* __restrict__ col,
+                                              uint32_t v, uint32_t row0, uint32_t W, uint32_t pos) {
+   const uint32_t k0 = row0 / TOFF_ROWS, k1 = (row0 + W) / TOFF_ROWS;
+   const uint32_t* xo = col->exc_toff + static_cast<size_t>(v) * TOFF_N;
+   const uint32_t* no = col->nblk_toff + (static_cast<size_t>(pos / NBLOCK) * tab->nchunks + v) * TOFF_N;
+   return make_uint4(__ldg(xo + k0), __ldg(xo + k1), __ldg(no + k0), __ldg(no + k1));
+}
+
+__device__ void stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __restrict__ code, uint32_t ncode) {
+   const DevTable* __restrict__ tab = c.tab;
+   const uint32_t nl = lc.nl, ncov = lc.ncov;
+   for (uint32_t i = threadIdx.x; i < ncode; i += blockDim.x) {
+      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(code) + i);
+      const Instr in = *reinterpret_cast<const Instr*>(&raw);
+      if (in.op == OP_PUSH_COVERED) {
+         if (in.c == 0 || in.c > ncov) continue;
+         const DevSeqCol* col = &tab->seq[in.col];
+         const uint4 r = cover_ranges(tab, col, c.v, c.row0, c.W, in.a);
+         lc.cov[in.c - 1] = r;
+         prefetch_l2(col->exc + r.x, col->exc + r.y);
+         prefetch_l2(col->nblk + r.z, col->nblk + (r.w & ~1u));  // stays inside the 8-byte-entry array
+         continue;
+      }
+      if ((in.op != OP_PUSH_SCAN && in.op != OP_PUSH_DICT) || in.c == 0 || in.c > nl) continue;
+      const CtrDesc* ctrs;
+      const uint32_t* off;
+      const uint16_t* payload;
+      size_t slot;
+      if (in.op == OP_PUSH_SCAN) {
+         const DevSeqCol* col = &tab->seq[in.col];
+         ctrs = col->ctrs;
+         off = col->off;
+         payload = col->payload;
+         slot = static_cast<size_t>(c.v) * col->L + in.a;
+      } else {
+         const DevDictCol* col = &tab->dict[in.col];
+         ctrs = col->ctrs;
+         off = col->off;
+         payload = col->payload;
+         slot = static_cast<size_t>(c.v) * col->nkeys + in.a;
+      }
+      const uint32_t b = __ldg(off + slot), e = __ldg(off + slot + 1);
+      lc.src[in.c - 1] = reinterpret_cast<const uint4*>(ctrs) + b;
+      lc.pay[in.c - 1] = payload;
+      lc.n[in.c - 1] = e - b;
+   }
+   __syncthreads();
+   if (threadIdx.x < 32) {  // exclusive scan of the counts; leaves that do not fit stay unstaged
+      const uint32_t lane = threadIdx.x;
+      uint32_t carry = 0;
+      for (uint32_t k0 = 0; k0 < nl; k0 += 32) {
+         const uint32_t k = k0 + lane;
+         const uint32_t x = k < nl ? lc.n[k] : 0u;
+         uint32_t incl = x;
+#pragma unroll
+         for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+         }
+         const uint32_t ex = carry + incl - x;
+         if (k < nl) lc.beg[k] = (x > 0 && ex + x <= LC_DESCS) ? ex : LC_NONE;
+         carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+      }
+   }
+   __syncthreads();
+   for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
+      const uint32_t b = lc.beg[k];
+      if (b == LC_NONE) continue;
+      const uint4* s = lc.src[k];
+      const uint16_t* pay = lc.pay[k];
+      for (uint32_t i = 0; i < lc.n[k]; ++i) {
+         const uint4 raw = __ldg(s + i);
+         lc.desc[b + i] = raw;
+         const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+         // the arena ends with 16 spare bytes, so rounding the end up stays inside it
+         const uint16_t* p = pay + d.payload;
+         if (d.type == CT_ARRAY) prefetch_l2(p, p + d.card_m1 + 1u);
+         else if (d.type == CT_BITSET) prefetch_l2(p + (c.row0 >> 4), p + ((c.row0 + c.W) >> 4));
+         else prefetch_l2(p, p + 2u * d.nruns);
+      }
+   }
+   __syncthreads();
+}
+
+// OR of the containers of one slot whose symbol is in `mask` (all of them when !use_mask), from
+// the staged descriptors when the leaf was staged.
 __device__ void push_containers(uint32_t* t, const TileCtx& c, const CtrDesc* __restrict__ ctrs,
                                 const uint16_t* __restrict__ payload, const uint32_t* __restrict__ off, size_t slot,
-                                uint32_t mask, bool use_mask) {
-   const uint32_t b = __ldg(off + slot), e = __ldg(off + slot + 1);
-   for (uint32_t i = b; i < e; ++i) {
-      CtrDesc d;
-      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + i);
-      d = *reinterpret_cast<const CtrDesc*>(&raw);
+                                uint32_t mask, bool use_mask, const LeafCache& lc, uint32_t leaf) {
+   const uint4* src;
+   uint32_t n;
+   if (leaf >= 1 && leaf <= lc.nl && lc.beg[leaf - 1] != LC_NONE) {
+      src = lc.desc + lc.beg[leaf - 1];
+      n = lc.n[leaf - 1];
+   } else {
+      const uint32_t b = __ldg(off + slot), e = __ldg(off + slot + 1);
+      src = reinterpret_cast<const uint4*>(ctrs) + b;
+      n = e - b;
+   }
+   for (uint32_t i = 0; i < n; ++i) {
+      const uint4 raw = src[i];
+      const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
       if (use_mask && !((mask >> d.sym) & 1u)) continue;
       or_container(t, d, payload, c.row0, c.W);
    }
 }
 
-__device__ void push_covered(uint32_t* t, const TileCtx& c, const DevSeqCol* __restrict__ col, uint32_t pos, bool negate) {
-   const uint32_t WW = c.W >> 5;
-   for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = valid_word(w, c.nvalid);
+// Word-parallel tile operations use one fixed mapping: thread i owns the uint4 words i, i +
+// blockDim.x, ... of every tile. Consecutive word-parallel operations therefore need no barrier
+// between them; leaves that scatter with shared-memory atomics (or write per warp) are fenced by
+// barriers on both sides.
+__device__ __forceinline__ uint4 valid4(uint32_t w4, const TileCtx& c) {
+   if (c.nvalid == c.W) return make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+   return make_uint4(valid_word(4 * w4, c.nvalid), valid_word(4 * w4 + 1, c.nvalid), valid_word(4 * w4 + 2, c.nvalid),
+                     valid_word(4 * w4 + 3, c.nvalid));
+}
+__device__ __forceinline__ uint4 and4(uint4 a, uint4 b) { return make_uint4(a.x & b.x, a.y & b.y, a.z & b.z, a.w & b.w); }
+__device__ __forceinline__ uint4 andnot4(uint4 a, uint4 b) {
+   return make_uint4(a.x & ~b.x, a.y & ~b.y, a.z & ~b.z, a.w & ~b.w);
+}
+__device__ __forceinline__ uint4 or4(uint4 a, uint4 b) { return make_uint4(a.x | b.x, a.y | b.y, a.z | b.z, a.w | b.w); }
+__device__ __forceinline__ bool any4(uint4 a) { return (a.x | a.y | a.z | a.w) != 0u; }
+__device__ __forceinline__ bool ne4(uint4 a, uint4 b) {
+   return ((a.x ^ b.x) | (a.y ^ b.y) | (a.z ^ b.z) | (a.w ^ b.w)) != 0u;
+}
+__device__ __forceinline__ uint32_t get4(const uint4& a, uint32_t i) { return i == 0 ? a.x : i == 1 ? a.y : i == 2 ? a.z : a.w; }
+
+// Rows covered at pos (or not covered when `negate`): all valid rows minus the exceptions whose
+// covered region misses pos and the rows with a missing interval over pos, within the tile's
+// ranges r of both lists.
+__device__ void push_covered(uint32_t* t, const TileCtx& c, const DevSeqCol* __restrict__ col, uint32_t pos, bool negate,
+                             uint4 r) {
+   const uint32_t W4 = c.W >> 7;
+   uint4* t4 = reinterpret_cast<uint4*>(t);
+   for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = valid4(w4, c);
    __syncthreads();
-   // rows whose covered region does not contain pos
-   const uint32_t xb = __ldg(col->exc_off + c.v), xe = __ldg(col->exc_off + c.v + 1);
-   for (uint32_t i = xb + threadIdx.x; i < xe; i += blockDim.x) {
-      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(col->exc) + i);
-      const uint32_t r = raw.x - c.row0;
-      if (r < c.W && !(raw.y <= pos && pos < raw.z)) atomicAnd(&t[r >> 5], ~(1u << (r & 31)));
+   constexpr uint32_t U = 4;  // entries per thread in flight
+   const uint4* exc = reinterpret_cast<const uint4*>(col->exc);
+   for (uint32_t i0 = r.x + threadIdx.x; i0 < r.y; i0 += U * blockDim.x) {
+      uint4 e[U];
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u) {
+         const uint32_t i = i0 + u * blockDim.x;
+         e[u] = i < r.y ? __ldg(exc + i) : make_uint4(c.row0, 0, 0xFFFFFFFFu, 0);
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u) {
+         const uint32_t row = e[u].x - c.row0;
+         if (row < c.W && !(e[u].y <= pos && pos < e[u].z)) atomicAnd(&t[row >> 5], ~(1u << (row & 31)));
+      }
    }
-   // rows with a missing interval over pos
-   const uint32_t blk = pos / NBLOCK, q = pos % NBLOCK;
-   const uint32_t* boff = col->nblk_off + static_cast<size_t>(blk) * c.tab->nchunks + c.v;
-   const uint32_t nb = __ldg(boff), ne = __ldg(boff + 1);
-   for (uint32_t i = nb + threadIdx.x; i < ne; i += blockDim.x) {
-      const uint2 raw = __ldg(reinterpret_cast<const uint2*>(col->nblk) + i);
-      const uint32_t r = (raw.x & 0xFFFFu) - c.row0;
-      const uint32_t lo = raw.y & 0xFFFFu, hi = raw.y >> 16;
-      if (r < c.W && lo <= q && q < hi) atomicAnd(&t[r >> 5], ~(1u << (r & 31)));
+   const uint32_t q = pos % NBLOCK;
+   const uint2* nb = reinterpret_cast<const uint2*>(col->nblk);
+   for (uint32_t i0 = r.z + threadIdx.x; i0 < r.w; i0 += U * blockDim.x) {
+      uint2 e[U];
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u) {
+         const uint32_t i = i0 + u * blockDim.x;
+         e[u] = i < r.w ? __ldg(nb + i) : make_uint2(0, 0);
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u) {
+         const uint32_t row = (e[u].x & 0xFFFFu) - c.row0;
+         const uint32_t lo = e[u].y & 0xFFFFu, hi = e[u].y >> 16;
+         if (row < c.W && lo <= q && q < hi) atomicAnd(&t[row >> 5], ~(1u << (row & 31)));
+      }
    }
+   __syncthreads();
    if (negate) {
-      __syncthreads();
-      for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = valid_word(w, c.nvalid) & ~t[w];
+      for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = andnot4(valid4(w4, c), t4[w4]);
    }
 }
 
 // Rows whose date lies in [lo, hi] (outside it when `invert`); null dates match when `with_nulls`.
-// Every comparison of the date predicates and the two-sided DateBetween reduce to this form.
-__device__ void push_date(uint32_t* t, const TileCtx& c, const DevDateCol* __restrict__ col, int32_t lo, int32_t hi,
+// Every comparison of the date predicates and the two-sided DateBetween reduce to this form. The
+// bit-sliced index is compared against the clamped bounds from the top bit down (lo <= x keeps
+// "greater" and "equal" masks, x <= hi "less" and "equal"); word-parallel in the fixed mapping.
+__device__ void push_date(uint4* t4, const TileCtx& c, const DevDateCol* __restrict__ col, int32_t lo, int32_t hi,
                           bool invert, bool with_nulls) {
-   const uint32_t WW = c.W >> 5;
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-   const int32_t* days = col->days + static_cast<size_t>(c.v) * CHUNK_ROWS + c.row0;
-   constexpr uint32_t U = 4;  // words per warp in flight
-   for (uint32_t w0 = warp * U; w0 < WW; w0 += nw * U) {
-      int32_t d[U];
-#pragma unroll
-      for (uint32_t k = 0; k < U; ++k) {
-         const uint32_t r = 32 * (w0 + k) + lane;
-         d[k] = (w0 + k < WW && r < c.nvalid) ? __ldg(days + r) : INT32_MIN;
+   const uint32_t W4 = c.W >> 7, nbits = col->nbits;
+   const int64_t maxv = (int64_t{1} << nbits) - 1;
+   const int64_t l = static_cast<int64_t>(lo) - col->base, h = static_cast<int64_t>(hi) - col->base;
+   const bool empty = lo > hi || h < 0 || l > maxv;
+   const uint32_t L = static_cast<uint32_t>(l < 0 ? 0 : l), H = static_cast<uint32_t>(h > maxv ? maxv : h);
+   const size_t stride4 = static_cast<size_t>(c.tab->nchunks) * (CHUNK_WORDS / 4);
+   const size_t base4 = (static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5)) / 4;
+   const uint4* planes = reinterpret_cast<const uint4*>(col->planes) + base4;
+   const uint4* nulls = reinterpret_cast<const uint4*>(col->nulls) + base4;
+   const uint4 ones = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+   for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) {
+      uint4 inside = make_uint4(0, 0, 0, 0);
+      if (!empty) {
+         uint4 eqL = ones, gtL = inside, eqH = ones, ltH = inside;
+#pragma unroll 4
+         for (int i = static_cast<int>(nbits) - 1; i >= 0; --i) {
+            const uint4 x = __ldg(planes + static_cast<size_t>(i) * stride4 + w4);
+            if ((L >> i) & 1u) {
+               eqL = and4(eqL, x);
+            } else {
+               gtL = or4(gtL, and4(eqL, x));
+               eqL = andnot4(eqL, x);
+            }
+            if ((H >> i) & 1u) {
+               ltH = or4(ltH, andnot4(eqH, x));
+               eqH = and4(eqH, x);
+            } else {
+               eqH = andnot4(eqH, x);
+            }
+         }
+         inside = and4(or4(gtL, eqL), or4(ltH, eqH));
       }
-#pragma unroll
-      for (uint32_t k = 0; k < U; ++k) {
-         const uint32_t r = 32 * (w0 + k) + lane;
-         const bool inside = d[k] >= lo && d[k] <= hi;
-         const bool m = r < c.nvalid && (d[k] == INT32_MIN ? with_nulls : (inside != invert));
-         const uint32_t bits = __ballot_sync(0xFFFFFFFFu, m);
-         if (lane == 0 && w0 + k < WW) t[w0 + k] = bits;
-      }
+      const uint4 nul = __ldg(nulls + w4);
+      const uint4 m = invert ? andnot4(ones, inside) : inside;
+      const uint4 res = with_nulls ? or4(andnot4(m, nul), nul) : andnot4(m, nul);
+      t4[w4] = and4(res, valid4(w4, c));
    }
 }
 
-// Runs a filter program for one tile. The result is left in stack slot 0. Returns false on a
-// malformed program (the error flag is set).
+// Runs a filter program for one tile. The result is left in stack slot 0, complete for the thread
+// that owns each uint4 word (see valid4); a barrier is needed before other threads read it.
+// Returns false on a malformed program (the error flag is set).
 __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, uint32_t ncode, uint32_t* stk,
-                            uint32_t cap, int* err) {
-   const uint32_t WW = c.W >> 5;
+                            uint32_t cap, const LeafCache& lc, int* err) {
+   const uint32_t WW = c.W >> 5, W4 = c.W >> 7;
+   uint4* stk4 = reinterpret_cast<uint4*>(stk);
    uint32_t sp = 0;
    uint32_t pc = 0;
    uint32_t steps = 0;
+   bool synced = true;  // no word-parallel write since the last barrier
    while (pc < ncode) {
       if (++steps > 4u * MAX_PROGRAM) {  // jumps only go forward; this bounds a corrupted program
          if (threadIdx.x == 0) atomicExch(err, 3);
@@ -181,30 +380,43 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                return false;
             }
             uint32_t* t = stk + sp * WW;
+            uint4* t4 = stk4 + sp * W4;
             ++sp;
             if (in.op == OP_PUSH_FULL) {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = valid_word(w, c.nvalid);
-            } else if (in.op == OP_PUSH_COVERED) {
-               push_covered(t, c, &c.tab->seq[in.col], in.a, in.flags & 1);
-            } else if (in.op == OP_PUSH_DATE) {
-               push_date(t, c, &c.tab->date[in.col], static_cast<int32_t>(in.a), static_cast<int32_t>(in.b), in.flags & 2,
-                         in.flags & 1);
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = valid4(w4, c);
+               synced = false;
+            } else if (in.op == OP_PUSH_EMPTY) {
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = make_uint4(0, 0, 0, 0);
+               synced = false;
             } else if (in.op == OP_PUSH_NULLS) {
-               const uint32_t* src = c.tab->seq[in.col].null_tiles + static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5);
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) t[w] = __ldg(src + w);
+               const uint4* src = reinterpret_cast<const uint4*>(c.tab->seq[in.col].null_tiles +
+                                                                 static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5));
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = __ldg(src + w4);
+               synced = false;
+            } else if (in.op == OP_PUSH_COVERED) {
+               const DevSeqCol* col = &c.tab->seq[in.col];
+               const uint4 r = (in.c >= 1 && in.c <= lc.ncov) ? lc.cov[in.c - 1]
+                                                              : cover_ranges(c.tab, col, c.v, c.row0, c.W, in.a);
+               push_covered(t, c, col, in.a, in.flags & 1, r);
+               synced = !(in.flags & 1);
+            } else if (in.op == OP_PUSH_DATE) {
+               push_date(t4, c, &c.tab->date[in.col], static_cast<int32_t>(in.a), static_cast<int32_t>(in.b), in.flags & 2,
+                         in.flags & 1);
+               synced = false;
             } else {
-               tile_zero(t, WW);
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = make_uint4(0, 0, 0, 0);
+               __syncthreads();
                if (in.op == OP_PUSH_SCAN) {
-                  __syncthreads();
                   const DevSeqCol* col = &c.tab->seq[in.col];
                   push_containers(t, c, col->ctrs, col->payload, col->off, static_cast<size_t>(c.v) * col->L + in.a, in.b,
-                                  true);
-               } else if (in.op == OP_PUSH_DICT) {
-                  __syncthreads();
+                                  true, lc, in.c);
+               } else {
                   const DevDictCol* col = &c.tab->dict[in.col];
                   push_containers(t, c, col->ctrs, col->payload, col->off, static_cast<size_t>(c.v) * col->nkeys + in.a, 0,
-                                  false);
+                                  false, lc, in.c);
                }
+               __syncthreads();
+               synced = true;
             }
             break;
          }
@@ -215,16 +427,17 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 2);
                return false;
             }
-            uint32_t* x = stk + (sp - 2) * WW;
-            const uint32_t* y = stk + (sp - 1) * WW;
+            uint4* x = stk4 + (sp - 2) * W4;
+            const uint4* y = stk4 + (sp - 1) * W4;
             if (in.op == OP_AND) {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) x[w] &= y[w];
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) x[w4] = and4(x[w4], y[w4]);
             } else if (in.op == OP_ANDNOT) {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) x[w] &= ~y[w];
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) x[w4] = andnot4(x[w4], y[w4]);
             } else {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) x[w] |= y[w];
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) x[w4] = or4(x[w4], y[w4]);
             }
             --sp;
+            synced = false;
             break;
          }
          case OP_NOT: {
@@ -232,8 +445,9 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 2);
                return false;
             }
-            uint32_t* x = stk + (sp - 1) * WW;
-            for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) x[w] = valid_word(w, c.nvalid) & ~x[w];
+            uint4* x = stk4 + (sp - 1) * W4;
+            for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) x[w4] = andnot4(valid4(w4, c), x[w4]);
+            synced = false;
             break;
          }
          case OP_THR_BEGIN: {
@@ -241,8 +455,10 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 1);
                return false;
             }
-            for (uint32_t i = 0; i < in.a; ++i) tile_zero(stk + (sp + i) * WW, WW);
+            for (uint32_t i = 0; i < in.a; ++i)
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) stk4[(sp + i) * W4 + w4] = make_uint4(0, 0, 0, 0);
             sp += in.a;
+            synced = false;
             break;
          }
          case OP_THR_ADD: {
@@ -251,21 +467,27 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 2);
                return false;
             }
-            const uint32_t* x = stk + (sp - 1) * WW;
+            const uint4* x4 = stk4 + (sp - 1) * W4;
             uint32_t* planes = stk + (sp - 1 - P) * WW;
             const bool neg = in.flags & 1;
-            for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) {
-               uint32_t carry = neg ? (valid_word(w, c.nvalid) & ~x[w]) : x[w];
-               for (uint32_t i = 0; i < P && carry; ++i) {
-                  const uint32_t p = planes[i * WW + w];
-                  planes[i * WW + w] = p ^ carry;
-                  carry &= p;
-               }
-               if (carry) {  // saturate at 2^P - 1
-                  for (uint32_t i = 0; i < P; ++i) planes[i * WW + w] |= carry;
+            for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) {
+               const uint4 xv = neg ? andnot4(valid4(w4, c), x4[w4]) : x4[w4];
+#pragma unroll
+               for (uint32_t j = 0; j < 4; ++j) {
+                  const uint32_t w = 4 * w4 + j;
+                  uint32_t carry = get4(xv, j);
+                  for (uint32_t i = 0; i < P && carry; ++i) {
+                     const uint32_t p = planes[i * WW + w];
+                     planes[i * WW + w] = p ^ carry;
+                     carry &= p;
+                  }
+                  if (carry) {  // saturate at 2^P - 1
+                     for (uint32_t i = 0; i < P; ++i) planes[i * WW + w] |= carry;
+                  }
                }
             }
             --sp;
+            synced = false;
             break;
          }
          case OP_THR_END: {
@@ -276,18 +498,24 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             }
             uint32_t* planes = stk + (sp - P) * WW;
             const bool exact = in.flags & 1;
-            for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) {
-               uint32_t gt = 0, eq = 0xFFFFFFFFu;
-               for (int i = static_cast<int>(P) - 1; i >= 0; --i) {
-                  const uint32_t p = planes[i * WW + w];
-                  const uint32_t nb = ((n >> i) & 1u) ? 0xFFFFFFFFu : 0u;
-                  gt |= eq & p & ~nb;
-                  eq &= ~(p ^ nb);
+            for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) {
+               const uint4 vm = valid4(w4, c);
+#pragma unroll
+               for (uint32_t j = 0; j < 4; ++j) {
+                  const uint32_t w = 4 * w4 + j;
+                  uint32_t gt = 0, eq = 0xFFFFFFFFu;
+                  for (int i = static_cast<int>(P) - 1; i >= 0; --i) {
+                     const uint32_t p = planes[i * WW + w];
+                     const uint32_t nb = ((n >> i) & 1u) ? 0xFFFFFFFFu : 0u;
+                     gt |= eq & p & ~nb;
+                     eq &= ~(p ^ nb);
+                  }
+                  if (n >> P) eq = 0;  // n does not fit: the saturated count can only be below it
+                  planes[w] = (exact ? eq : (gt | eq)) & get4(vm, j);
                }
-               if (n >> P) eq = 0;  // n does not fit: the saturated count can only be below it
-               planes[w] = (exact ? eq : (gt | eq)) & valid_word(w, c.nvalid);
             }
             sp = sp - P + 1;
+            synced = false;
             break;
          }
          case OP_JZ:
@@ -296,14 +524,15 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 2);
                return false;
             }
-            const uint32_t* x = stk + (sp - 1) * WW;
+            const uint4* x = stk4 + (sp - 1) * W4;
             int differs = 0;
             if (in.op == OP_JZ) {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) differs |= (x[w] != 0u);
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) differs |= any4(x[w4]);
             } else {
-               for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) differs |= (x[w] != valid_word(w, c.nvalid));
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) differs |= ne4(x[w4], valid4(w4, c));
             }
             differs = __syncthreads_or(differs);
+            synced = true;
             if (!differs) {
                if (in.a <= pc || in.a > ncode) {
                   if (threadIdx.x == 0) atomicExch(err, 4);
@@ -317,7 +546,6 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             if (threadIdx.x == 0) atomicExch(err, 5);
             return false;
       }
-      __syncthreads();
       pc = next;
    }
    if (sp != 1) {
@@ -340,11 +568,25 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
    return s;  // valid in thread 0
 }
 
+// Popcount of the result tile (slot 0) by the owners of its words, optionally copied to dst.
+__device__ __forceinline__ uint32_t result_popc(const uint32_t* smem, uint32_t W, uint32_t* dst) {
+   const uint4* r4 = reinterpret_cast<const uint4*>(smem);
+   uint4* d4 = reinterpret_cast<uint4*>(dst);
+   uint32_t pc = 0;
+   for (uint32_t w4 = threadIdx.x; w4 < (W >> 7); w4 += blockDim.x) {
+      const uint4 x = r4[w4];
+      pc += __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w);
+      if (dst) d4[w4] = x;
+   }
+   return pc;
+}
+
 __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__ tab, const Instr* __restrict__ code,
-                                                    uint32_t ncode, uint32_t tile_bits, uint32_t cap,
+                                                    uint32_t ncode, uint32_t n_leaves, uint32_t tile_bits, uint32_t cap,
                                                     uint32_t* __restrict__ out_tiles, unsigned long long* count, int* err) {
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
+   __shared__ LeafCache lc;
    const uint32_t T = CHUNK_ROWS / tile_bits;
    TileCtx c;
    c.tab = tab;
@@ -353,20 +595,17 @@ __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__
    c.row0 = (blockIdx.x % T) * tile_bits;
    const uint32_t csize = __ldg(tab->chunk_sizes + c.v);
    c.nvalid = csize > c.row0 ? min(tile_bits, csize - c.row0) : 0u;
-   const uint32_t WW = tile_bits >> 5;
-   uint32_t* result = smem;
    if (c.nvalid == 0) {
-      tile_zero(result, WW);
+      for (uint32_t w4 = threadIdx.x; w4 < (tile_bits >> 7); w4 += blockDim.x)
+         reinterpret_cast<uint4*>(smem)[w4] = make_uint4(0, 0, 0, 0);
+   } else {
+      clear_leaves(lc, min(n_leaves & 0xFFFFu, LC_LEAVES), min(n_leaves >> 16, LC_COV));
       __syncthreads();
-   } else if (!run_program(c, code, ncode, smem, cap, err)) {
-      return;
+      stage_leaves(lc, c, code, ncode);
+      if (!run_program(c, code, ncode, smem, cap, lc, err)) return;
    }
-   uint32_t pc = 0;
-   for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) {
-      const uint32_t x = result[w];
-      pc += __popc(x);
-      if (out_tiles) out_tiles[static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5) + w] = x;
-   }
+   const uint32_t pc =
+      result_popc(smem, tile_bits, out_tiles ? out_tiles + static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5) : nullptr);
    if (count) {
       const uint32_t s = block_sum(pc, red);
       if (threadIdx.x == 0 && s) atomicAdd(count, static_cast<unsigned long long>(s));
@@ -381,17 +620,18 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
    __shared__ uint32_t item_idx;
+   __shared__ LeafCache lc;
    const uint32_t T = CHUNK_ROWS / tile_bits;
-   const uint32_t WW = tile_bits >> 5;
    const size_t per_query = static_cast<size_t>(tab->nchunks) * CHUNK_WORDS;
    for (;;) {
       if (threadIdx.x == 0) item_idx = atomicAdd(next_item, 1u);
       __syncthreads();
       const uint32_t it = item_idx;
-      __syncthreads();
       if (it >= n_items) return;
       const WorkItem wi = items[it];
       const QueryDesc q = queries[wi.query];
+      clear_leaves(lc, min(q.n_leaves & 0xFFFFu, LC_LEAVES), min(q.n_leaves >> 16, LC_COV));
+      __syncthreads();
       TileCtx c;
       c.tab = tab;
       c.v = wi.tile / T;
@@ -400,20 +640,16 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
       const uint32_t csize = __ldg(tab->chunk_sizes + c.v);
       c.nvalid = csize > c.row0 ? min(tile_bits, csize - c.row0) : 0u;
       if (c.nvalid == 0) {
-         tile_zero(smem, WW);
-         __syncthreads();
-      } else if (!run_program(c, code + q.code_off, q.code_len, smem, cap, err)) {
-         return;
+         for (uint32_t w4 = threadIdx.x; w4 < (tile_bits >> 7); w4 += blockDim.x)
+            reinterpret_cast<uint4*>(smem)[w4] = make_uint4(0, 0, 0, 0);
+      } else {
+         stage_leaves(lc, c, code + q.code_off, q.code_len);
+         if (!run_program(c, code + q.code_off, q.code_len, smem, cap, lc, err)) return;
       }
-      uint32_t pc = 0;
       uint32_t* dst = q.out_tiles ? out_tiles + static_cast<size_t>(q.out_tiles - 1) * per_query +
                                        static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5)
                                   : nullptr;
-      for (uint32_t w = threadIdx.x; w < WW; w += blockDim.x) {
-         const uint32_t x = smem[w];
-         pc += __popc(x);
-         if (dst) dst[w] = x;
-      }
+      const uint32_t pc = result_popc(smem, tile_bits, dst);
       const uint32_t s = block_sum(pc, red);
       if (threadIdx.x == 0 && s) atomicAdd(counts + wi.query, static_cast<unsigned long long>(s));
       __syncthreads();
@@ -425,15 +661,15 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
 // launchers
 
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
-                          uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
+                          uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
                           int* d_err, void* stream) {
    const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
    cudaError_t e = cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
    if (e != cudaSuccess) return e;
-   filter_kernel<<<nchunks * T, FT, smem, static_cast<cudaStream_t>(stream)>>>(d_table, d_code, ncode, tile_bits,
-                                                                                stack_tiles, d_out_tiles, d_count, d_err);
+   filter_kernel<<<nchunks * T, FT, smem, static_cast<cudaStream_t>(stream)>>>(
+      d_table, d_code, ncode, n_leaves, tile_bits, stack_tiles, d_out_tiles, d_count, d_err);
    return cudaGetLastError();
 }
 

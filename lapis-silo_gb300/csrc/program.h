@@ -15,9 +15,11 @@ enum OpCode : uint8_t {
    OP_PUSH_EMPTY = 0,
    OP_PUSH_FULL = 1,     // all rows of the tile that exist in the chunk
    OP_PUSH_SCAN = 2,     // col = sequence column, a = position, b = symbol mask: OR of the containers
+                         // (c = ordinal among the program's PUSH_SCAN / PUSH_DICT leaves, from 1)
    OP_PUSH_NULLS = 3,    // col = sequence column: rows whose sequence is null
-   OP_PUSH_DICT = 4,     // col = dictionary column, a = value id: inverted-index rows
+   OP_PUSH_DICT = 4,     // col = dictionary column, a = value id: inverted-index rows (c as for PUSH_SCAN)
    OP_PUSH_COVERED = 5,  // col = sequence column, a = position, flags&1: not covered instead of covered
+                         // (c = ordinal among the program's PUSH_COVERED leaves, from 1)
    OP_PUSH_DATE = 6,     // col = date column; rows with lo <= date <= hi (a = lo, b = hi as int32),
                          // flags&2 = inverted (outside the range), flags&1 = null dates match
    OP_AND = 7,           // pop y, pop x, push x & y

@@ -471,6 +471,22 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
          }
       }
    }
+   // tile row-range offsets into both sorted lists
+   auto toff = [](uint32_t* out, uint32_t b, uint32_t e, auto&& row_of) {
+      uint32_t i = b;
+      for (uint32_t k = 0; k < TOFF_N; ++k) {
+         while (i < e && row_of(i) < k * TOFF_ROWS) ++i;
+         out[k] = i;
+      }
+   };
+   col.exc_toff.resize(static_cast<size_t>(nchunks) * TOFF_N);
+   for (uint32_t v = 0; v < nchunks; ++v)
+      toff(&col.exc_toff[static_cast<size_t>(v) * TOFF_N], col.cov_exc_off[v], col.cov_exc_off[v + 1],
+           [&](uint32_t i) { return col.cov_exc[i].row; });
+   col.nblk_toff.resize(nbuckets * TOFF_N);
+   for (size_t bv = 0; bv < nbuckets; ++bv)
+      toff(&col.nblk_toff[bv * TOFF_N], col.nblk_off[bv], col.nblk_off[bv + 1],
+           [&](uint32_t i) { return col.nblk[i].row & 0xFFFFu; });
    build_mutation_events(col, chunks, chunk_sizes);
    return col;
 }

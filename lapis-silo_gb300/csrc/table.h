@@ -61,6 +61,9 @@ struct CovEvent {  // coverage boundary of one row
 
 constexpr uint32_t MAX_EVENT_CHUNKS = 256;  // packed mutations events hold 24-bit row ids
 
+constexpr uint32_t TOFF_ROWS = 4096;
+constexpr uint32_t TOFF_N = CHUNK_ROWS / TOFF_ROWS + 1;
+
 struct NRunEntry {  // missing interval of one row clipped to one position block
    uint32_t row;    // global row id (chunk << 16 | row within chunk)
    uint16_t lo;     // [lo, hi) relative to the block start
@@ -91,6 +94,11 @@ struct SeqColumnImage {
    std::vector<uint32_t> nrow_start, nrow_end;
    std::vector<NRunEntry> nblk;        // bucketed by (block, chunk), sorted by row
    std::vector<uint32_t> nblk_off;     // nblocks * nchunks + 1
+   // Row-range offsets for tiles: exc_toff[v * TOFF_N + k] is the index of the first coverage
+   // exception of chunk v with row >= k * TOFF_ROWS, nblk_toff[(b * nchunks + v) * TOFF_N + k] the
+   // same inside bucket (b, v) of nblk.
+   std::vector<uint32_t> exc_toff;
+   std::vector<uint32_t> nblk_toff;
    uint32_t nblocks = 0;
    // Mutations pass: the same missing intervals as start and end events, packed as
    // (global row << 8 | position within the block, 0..128) and sorted by (block, position, row),
