@@ -8,8 +8,9 @@ count, 25% Mutations of the nucleotide column.
 
 value      queries/s of the batched path (persistent filter kernel + batched mutations kernels,
            replayed from a captured CUDA graph) with programs and table resident in HBM.
-e2e        the same through the C-ABI call rhy_batch with host buffers: planning, host->device
-           copies, kernels and the device->host copy of every count and mutation table.
+e2e        the same through the C-ABI call rhy_batch_rows with host buffers: planning, host->device
+           copies, kernels, the Mutations output rows built on the device (minimum proportion
+           0.05) and the device->host copy of every count and row.
 plain      the plain single-query path over the same queries, one query at a time.
 roofline   the plain container pass of the Mutations action (mut_ctr_kernel), the kernel that
            streams the whole vertical index: algorithmic bytes = container payloads + descriptors
@@ -327,22 +328,43 @@ def main():
     plain_e2e_qps = m / (time.perf_counter() - t0)
 
     # ---------------- batched e2e through the C-ABI ----------------
+    # rows of the Mutations action built on the device; the dense-count variant is kept for context
     e2e_s = []
+    min_props = np.full(n, 0.05)
     for step in range(max(2, min(args.steps, 3))):
         t0 = time.perf_counter()
-        counts, muts = dev.batch(queries, actions, columns, tile_bits=args.tile_bits, stream=sp)
+        r_counts, rows, r_begin, r_cnt = dev.batch_rows(queries, actions, columns, min_props,
+                                                        tile_bits=args.tile_bits, stream=sp)
         e2e_s.append(time.perf_counter() - t0)
     e2e_qps = n * ws / max_over_ranks(statistics.median(e2e_s), ws)
+    dense_s = []
+    for step in range(2):
+        t0 = time.perf_counter()
+        dev.batch(queries, actions, columns, tile_bits=args.tile_bits, stream=sp)
+        dense_s.append(time.perf_counter() - t0)
+    dense_qps = n * ws / max_over_ranks(statistics.median(dense_s), ws)
+    # the device rows equal the host conversion of the dense counts
+    rows_mismatches = int(not np.array_equal(r_counts, b_counts))
+    for i in [j for j in range(n) if actions[j] == 1][:64]:
+        got = rows[int(r_begin[i]):int(r_begin[i]) + int(r_cnt[i])]
+        want = table.mutation_rows(0, b_muts[i], 0.05)
+        if [(int(r["position"]), r["from_"].decode(), r["to"].decode(), int(r["count"]), int(r["coverage"]),
+             float(r["proportion"])) for r in got] != want:
+            rows_mismatches += 1
     col0 = table.columns[0]
-    prog_bytes = info.n_instr * 16 + n * 16 + info.n_items * 8 + n_mut * 4
-    d2h = n * 8 + n_mut * col0.n_symbols * col0.L * 4
+    prog_bytes = info.n_instr * 16 + n * 16 + info.n_items * 8 + n_mut * 12
+    d2h = n * 8 + n * 12 + len(rows) * 24
 
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)
-    mut_idx = [i for i in range(n) if actions[i] == 1][:16]
+    # queries whose filter is neither empty nor every row: the pass reads the whole column
+    mut_idx = [i for i in range(n) if actions[i] == 1 and 0 < int(b_counts[i]) < table.n_rows][:16]
     ctr_ms = []
     for i in mut_idx:
         dev.plain_launch(i, sp, parts=1)  # filter tile and count
+        # two flushes keep the GPU busy while the host submits the timed launch, so the events
+        # bracket the kernel and not the submission
+        flush_l2()
         flush_l2()
         e0, e1 = ev(), ev()
         e0.record(stream)
@@ -388,7 +410,9 @@ def main():
             "speedup_vs_plain": value / plain_qps,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "output": "Mutations rows (min proportion 0.05) + counts",
+                    "rows_per_step": int(len(rows)), "rows_mismatches": rows_mismatches,
+                    "dense_counts_qps": dense_qps},
             "gpu_launches": launches_per_step * args.steps,
             "kernels_ms": kernels_ms,
             "roofline": {"kernel": "mut_ctr_kernel (plain Mutations container pass, nucleotide column)",

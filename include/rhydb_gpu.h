@@ -162,6 +162,19 @@ int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream,
 int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
               uint32_t tile_bits, void* stream, uint64_t* counts, uint32_t* const* mut_counts);
 
+/* Mutations action output of a batch computed on the device (replaces addMutationsToOutput,
+ * reference mutations_node.cpp:292-366, behind MutationsNode::addToExecPlan, :377): for every
+ * Mutations query the rows (position, from, to, count, coverage, proportion) whose count exceeds
+ * ceil(coverage * min_proportion) - 1 (any count > 0 when min_proportion is 0), packed in query-slot
+ * order. counts[i] receives every query's filter cardinality; *n_rows the total number of rows,
+ * which are copied when *n_rows <= rows_cap (otherwise rhy_batch_rows_fetch copies them without
+ * recomputing). Query i's rows are rows[row_begin[i] .. row_begin[i] + row_count[i]).
+ * min_proportions may be NULL (0.05 for every query); each must lie in [0, 1]. */
+int rhy_batch_rows(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns,
+                   const double* min_proportions, uint32_t n, uint32_t tile_bits, void* stream, uint64_t* counts,
+                   RhyMutationRow* rows, size_t rows_cap, uint64_t* row_begin, uint32_t* row_count, size_t* n_rows);
+int rhy_batch_rows_fetch(RhyDevice* d, void* stream, RhyMutationRow* rows, size_t rows_cap);
+
 typedef struct {
    uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
    uint64_t device_bytes;

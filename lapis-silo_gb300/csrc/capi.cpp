@@ -1,6 +1,7 @@
 // extern "C" boundary (include/rhydb_gpu.h). No exception crosses it: every entry point maps
 // exceptions to a status code and a thread-local message.
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -458,6 +459,41 @@ int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const 
       d->engine->batch_enqueue(s, true, true);
       rhygpu::cuda_check(cudaStreamSynchronize(s), "batch");
       copy_batch_results(d, n, counts, mut_counts);
+   });
+}
+
+int rhy_batch_rows(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns,
+                   const double* min_proportions, uint32_t n, uint32_t tile_bits, void* stream, uint64_t* counts,
+                   RhyMutationRow* rows, size_t rows_cap, uint64_t* row_begin, uint32_t* row_count, size_t* n_rows) {
+   static_assert(sizeof(RhyMutationRow) == sizeof(rhygpu::DevMutationRow), "row layout");
+   static_assert(offsetof(RhyMutationRow, proportion) == offsetof(rhygpu::DevMutationRow, proportion), "row layout");
+   return guarded([&] {
+      need(d, "device");
+      need(n_rows, "n_rows");
+      *n_rows = 0;
+      if (n == 0) return;
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      std::vector<rhygpu::BatchQuery> qs = make_batch(d, exprs, actions, columns, n, 0);
+      if (min_proportions)
+         for (uint32_t i = 0; i < n; ++i) qs[i].min_proportion = min_proportions[i];
+      d->engine->batch_prepare(qs, tile_bits);
+      cudaStream_t s = d->engine->stream_for(static_cast<cudaStream_t>(stream));
+      *n_rows = d->engine->batch_rows(s, reinterpret_cast<rhygpu::DevMutationRow*>(rows), rows ? rows_cap : 0, row_begin,
+                                      row_count);
+      if (counts)
+         for (uint32_t i = 0; i < n; ++i) counts[i] = d->engine->batch_count(i);
+   });
+}
+
+int rhy_batch_rows_fetch(RhyDevice* d, void* stream, RhyMutationRow* rows, size_t rows_cap) {
+   return guarded([&] {
+      need(d, "device");
+      need(rows, "rows");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      d->engine->batch_rows_fetch(static_cast<cudaStream_t>(stream), reinterpret_cast<rhygpu::DevMutationRow*>(rows),
+                                  rows_cap);
    });
 }
 

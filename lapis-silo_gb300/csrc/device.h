@@ -23,6 +23,19 @@ constexpr int MAX_SEQ_COLS = 32;
 constexpr int MAX_DICT_COLS = 8;
 constexpr int MAX_DATE_COLS = 8;
 
+// One unit of the Mutations container pass (see mut_stream_kernel). e0/e1: payload-arena element
+// range (SU_ARRAYS: up to SU elements of one chunk's array payloads; SU_BITSET: the bitset's 4096
+// u16); c0/c1: descriptor range (arrays: every descriptor overlapping [e0, e1); bitset / run: one).
+enum : uint32_t { SU_ARRAYS = 0, SU_BITSET = 1, SU_RUN = 2 };
+constexpr uint32_t SU = 8192;
+struct StreamUnit {
+   uint32_t kind;
+   uint32_t v;
+   uint32_t e0, e1;
+   uint32_t c0, c1;
+   uint32_t pad[2];
+};
+
 struct DevSeqCol {
    const CtrDesc* ctrs;
    const uint16_t* payload;
@@ -31,6 +44,7 @@ struct DevSeqCol {
    const uint32_t* exc_off;    // nchunks + 1
    const NRunEntry* nblk;
    const uint32_t* nblk_off;   // nblocks * nchunks + 1
+   const StreamUnit* su;       // units of the Mutations container pass, chunk-major
    const uint32_t* exc_toff;   // nchunks * TOFF_N: tile row-range offsets into exc
    const uint32_t* nblk_toff;  // nblocks * nchunks * TOFF_N: the same into each nblk bucket
    const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
@@ -43,6 +57,10 @@ struct DevSeqCol {
    uint32_t nblocks;
    uint32_t nsym;
    uint32_t nctrs;
+   uint32_t nsu;
+   uint32_t valid_mask;        // symbols counted in a position's coverage (valid mutation symbols)
+   const uint8_t* global_ref;  // L: the column's reference symbols (the "from" of a mutation)
+   char chars[32];             // symbol -> character
 };
 
 // A range of events of one list for the mutations coverage pass.
@@ -126,8 +144,8 @@ enum : uint32_t { BMUT_PART_TRANSPOSE = 1, BMUT_PART_CTR = 2, BMUT_PART_COV = 4,
 // the empty path and the mixed path, so no host round trip sits between filter and mutations.
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
-                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
-                      uint32_t parts = MUT_PART_ALL);
+                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
+                      void* stream, uint32_t parts = MUT_PART_ALL);
 
 // One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),
 // at most CTR_UNIT_CHUNKS chunks and, unless a single chunk exceeds it, CTR_UNIT_ELEMENTS elements.
@@ -148,6 +166,30 @@ void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, 
                             const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
                             uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
                             uint32_t parts = BMUT_PART_ALL);
+
+// Output rows of the Mutations action (same layout as RhyMutationRow in the C-ABI header).
+struct DevMutationRow {
+   uint32_t position;  // 1-based
+   char from, to;
+   uint16_t pad;
+   uint32_t count;
+   uint32_t coverage;
+   double proportion;
+};
+static_assert(sizeof(DevMutationRow) == 24, "row layout");
+
+// Rows of nq query slots whose dense counts lie at d_counts + slot * nsym * L, with per-slot minimum
+// proportions. Count pass: d_blk[slot * rows_blocks(L) + b] = rows of position block b; the scan
+// turns n entries into exclusive offsets with the total at d_blk[n]; the write pass emits the rows
+// at their offsets in (slot, position, symbol) order.
+constexpr uint32_t ROWS_BLOCK = 1024;
+uint32_t rows_blocks(uint32_t L);
+void launch_rows_count(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, const uint32_t* d_counts,
+                       uint32_t nq, const double* d_min_prop, uint32_t* d_blk, void* stream);
+void launch_rows_scan(uint32_t* d_blk, uint32_t n, void* stream);
+void launch_rows_write(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, const uint32_t* d_counts,
+                       uint32_t nq, const double* d_min_prop, const uint32_t* d_blk, DevMutationRow* d_rows,
+                       void* stream);
 
 // Events per CTA of the coverage pass.
 constexpr uint32_t EV_PER_CTA = 8192;

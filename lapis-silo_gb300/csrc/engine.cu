@@ -47,6 +47,39 @@ std::vector<CtrUnit> container_units(const SeqColumnImage& s, uint32_t nchunks) 
    return out;
 }
 
+// Units of the Mutations container pass, chunk by chunk: the chunk's array payloads (back to back in
+// descriptor order) cut into SU-element pieces, each with the descriptors that overlap it, then one
+// unit per bitset and per run container.
+std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks) {
+   const ContainerSet& cs = s.vertical;
+   std::vector<StreamUnit> out;
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const uint32_t cb = cs.off[static_cast<size_t>(v) * s.L], ce = cs.off[static_cast<size_t>(v + 1) * s.L];
+      std::vector<uint32_t> arr;
+      for (uint32_t i = cb; i < ce; ++i)
+         if (cs.ctrs[i].type == CT_ARRAY) arr.push_back(i);
+      if (!arr.empty()) {
+         const uint32_t A0 = cs.ctrs[arr.front()].payload;
+         const uint32_t A1 = cs.ctrs[arr.back()].payload + cs.ctrs[arr.back()].card_m1 + 1u;
+         size_t lo = 0;  // first array ending after e0
+         for (uint32_t e0 = A0; e0 < A1; e0 += SU) {
+            const uint32_t e1 = std::min(e0 + SU, A1);
+            auto end_of = [&](size_t k) { return cs.ctrs[arr[k]].payload + cs.ctrs[arr[k]].card_m1 + 1u; };
+            while (lo < arr.size() && end_of(lo) <= e0) ++lo;
+            size_t hi = lo;  // one past the last array starting before e1
+            while (hi < arr.size() && cs.ctrs[arr[hi]].payload < e1) ++hi;
+            out.push_back(StreamUnit{SU_ARRAYS, v, e0, e1, arr[lo], arr[hi - 1] + 1, {0, 0}});
+         }
+      }
+      for (uint32_t i = cb; i < ce; ++i) {
+         const CtrDesc& d = cs.ctrs[i];
+         if (d.type == CT_BITSET) out.push_back(StreamUnit{SU_BITSET, v, d.payload, d.payload + 4096, i, i + 1, {0, 0}});
+         else if (d.type == CT_RUN) out.push_back(StreamUnit{SU_RUN, v, 0, 0, i, i + 1, {0, 0}});
+      }
+   }
+   return out;
+}
+
 template <typename T>
 T* Engine::upload(const std::vector<T>& v, size_t min_elems) {
    const size_t n = std::max(v.size(), min_elems);
@@ -104,12 +137,23 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
          d.exc_off = upload(s.cov_exc_off);
          d.nblk = upload(s.nblk);
          d.nblk_off = upload(s.nblk_off);
+         {
+            const std::vector<StreamUnit> su = stream_units(s, nchunks);
+            d.su = upload(su);
+            d.nsu = static_cast<uint32_t>(su.size());
+         }
          d.exc_toff = upload(s.exc_toff);
          d.nblk_toff = upload(s.nblk_toff);
          std::vector<uint32_t> nulls(static_cast<size_t>(nchunks) * CHUNK_WORDS, 0);
          for (uint32_t g : s.null_rows) nulls[g >> 5] |= 1u << (g & 31);
          d.null_tiles = upload(nulls);
          d.local_ref = upload(s.local_ref);
+         d.global_ref = upload(s.global_ref);
+         {
+            const Alphabet& A = alphabet(s.kind);
+            d.valid_mask = A.valid_mask;
+            for (uint32_t k = 0; k < 32; ++k) d.chars[k] = k < A.count ? A.chars[k] : '?';
+         }
          d.L = s.L;
          d.nblocks = s.nblocks;
          d.nsym = alphabet(s.kind).count;
@@ -215,7 +259,7 @@ void Engine::launch_mutations(int column, const uint32_t* filter, const unsigned
                               uint32_t* scratch, cudaStream_t stream, uint32_t parts) {
    const DevSeqCol& c = view_.seq[column];
    rhygpu::launch_mutations(d_table_, c, static_cast<uint32_t>(column), nchunks(), d_ev_[column], n_ev_[column],
-                            filter, count, counts, scratch, stream, parts);
+                            filter, count, counts, scratch, d_err, stream, parts);
    cuda_check(cudaGetLastError(), "mutations kernel launch");
 }
 
@@ -329,12 +373,14 @@ void Engine::batch_free() {
    BatchState& b = batch_;
    if (b.graph) cudaGraphExecDestroy(b.graph);
    for (void* p : {static_cast<void*>(b.h_code), static_cast<void*>(b.h_q), static_cast<void*>(b.h_items),
-                   static_cast<void*>(b.h_slot_query), static_cast<void*>(b.h_counts), static_cast<void*>(b.h_mcounts)})
+                   static_cast<void*>(b.h_slot_query), static_cast<void*>(b.h_counts), static_cast<void*>(b.h_mcounts),
+                   static_cast<void*>(b.h_minprop), static_cast<void*>(b.h_rowblk)})
       if (p) cudaFreeHost(p);
    for (void* p : {static_cast<void*>(b.d_code), static_cast<void*>(b.d_q), static_cast<void*>(b.d_items),
                    static_cast<void*>(b.d_slot_query), static_cast<void*>(b.d_counts), static_cast<void*>(b.d_next),
                    static_cast<void*>(b.d_tiles), static_cast<void*>(b.d_mcounts), static_cast<void*>(b.d_mscratch),
-                   static_cast<void*>(b.d_masks)})
+                   static_cast<void*>(b.d_masks), static_cast<void*>(b.d_minprop), static_cast<void*>(b.d_rowblk),
+                   static_cast<void*>(b.d_rows)})
       if (p) cudaFree(p);
    b = BatchState{};
 }
@@ -365,10 +411,12 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
    b.slot_of_query.assign(n, UINT32_MAX);
    std::vector<uint32_t> slot_query;
    size_t counts_words = 0, scratch_words = 0, mask_bytes = 0;
+   uint32_t n_blk = 0;
    for (size_t c = 0; c < by_col.size(); ++c) {
       if (by_col[c].empty()) continue;
       BatchState::ColGroup g{static_cast<int>(c), static_cast<uint32_t>(slot_query.size()),
-                             static_cast<uint32_t>(by_col[c].size()), counts_words, scratch_words};
+                             static_cast<uint32_t>(by_col[c].size()), counts_words, scratch_words, n_blk};
+      n_blk += g.n * rows_blocks(view_.seq[c].L);
       for (uint32_t qi : by_col[c]) {
          b.slot_of_query[qi] = static_cast<uint32_t>(slot_query.size());
          slot_query.push_back(qi);
@@ -398,6 +446,17 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
    grow_device(b.d_mcounts, b.dc_mcounts, counts_words);
    grow_device(b.d_mscratch, b.dc_mscratch, scratch_words);
    grow_device(b.d_masks, b.dc_masks, mask_bytes / 2 + 8);
+   grow_host(b.h_minprop, nslots, b.hc_minprop);
+   grow_device(b.d_minprop, b.dc_minprop, nslots);
+   grow_host(b.h_rowblk, static_cast<size_t>(n_blk) + 1, b.hc_rowblk);
+   grow_device(b.d_rowblk, b.dc_rowblk, static_cast<size_t>(n_blk) + 1);
+   for (uint32_t k = 0; k < nslots; ++k) {
+      const double mp = qs[slot_query[k]].min_proportion;
+      if (!(mp >= 0.0 && mp <= 1.0)) throw std::invalid_argument("min_proportion must lie in [0, 1]");
+      b.h_minprop[k] = mp;
+   }
+   b.n_blk = n_blk;
+   b.n_rows = 0;
    // programs, query descriptors, work items
    size_t off = 0;
    for (uint32_t i = 0; i < n; ++i) {
@@ -438,9 +497,11 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
       cuda_check(cudaMemcpyAsync(b.d_items, b.h_items, static_cast<size_t>(b.n_items) * sizeof(WorkItem),
                                  cudaMemcpyHostToDevice, s),
                  "H2D");
-      if (b.n_slots)
+      if (b.n_slots) {
          cuda_check(cudaMemcpyAsync(b.d_slot_query, b.h_slot_query, b.n_slots * sizeof(uint32_t), cudaMemcpyHostToDevice, s),
                     "H2D");
+         cuda_check(cudaMemcpyAsync(b.d_minprop, b.h_minprop, b.n_slots * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+      }
    }
    if (parts & 1) {
       cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
@@ -467,6 +528,67 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
          cuda_check(cudaMemcpyAsync(b.h_mcounts, b.d_mcounts, b.counts_words * 4, cudaMemcpyDeviceToHost, s), "D2H");
       cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
    }
+}
+
+size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count) {
+   s = stream_for(s);
+   BatchState& b = batch_;
+   if (b.n_queries == 0) return 0;
+   batch_enqueue(s, true, false);
+   cuda_check(cudaMemcpyAsync(b.h_counts, b.d_counts, b.n_queries * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+              "D2H");
+   cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+   for (const auto& g : b.groups)
+      launch_rows_count(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), b.d_mcounts + g.counts_off, g.n,
+                        b.d_minprop + g.slot_begin, b.d_rowblk + g.blk_off, s);
+   if (b.n_slots) {
+      launch_rows_scan(b.d_rowblk, b.n_blk, s);
+      cuda_check(cudaMemcpyAsync(b.h_rowblk, b.d_rowblk, (static_cast<size_t>(b.n_blk) + 1) * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, s),
+                 "D2H");
+   }
+   cuda_check(cudaGetLastError(), "rows launch");
+   cuda_check(cudaStreamSynchronize(s), "batch rows");
+   check_error_flag();
+   const size_t total = b.n_slots ? b.h_rowblk[b.n_blk] : 0;
+   b.n_rows = total;
+   if (total) {
+      grow_device(b.d_rows, b.dc_rows, total);
+      for (const auto& g : b.groups)
+         launch_rows_write(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), b.d_mcounts + g.counts_off, g.n,
+                           b.d_minprop + g.slot_begin, b.d_rowblk + g.blk_off, b.d_rows, s);
+      cuda_check(cudaGetLastError(), "rows launch");
+      if (rows && total <= cap)
+         cuda_check(cudaMemcpyAsync(rows, b.d_rows, total * sizeof(DevMutationRow), cudaMemcpyDeviceToHost, s), "D2H");
+      cuda_check(cudaStreamSynchronize(s), "batch rows");
+   }
+   for (uint32_t i = 0; i < b.n_queries; ++i) {
+      const uint32_t slot = b.slot_of_query[i];
+      uint64_t begin = 0;
+      uint32_t count = 0;
+      if (slot != UINT32_MAX) {
+         for (const auto& g : b.groups) {
+            if (slot < g.slot_begin || slot >= g.slot_begin + g.n) continue;
+            const uint32_t nb = rows_blocks(view_.seq[g.column].L);
+            const size_t k = g.blk_off + static_cast<size_t>(slot - g.slot_begin) * nb;
+            begin = b.h_rowblk[k];
+            count = b.h_rowblk[k + nb] - b.h_rowblk[k];
+         }
+      }
+      if (row_begin) row_begin[i] = begin;
+      if (row_count) row_count[i] = count;
+   }
+   return total;
+}
+
+void Engine::batch_rows_fetch(cudaStream_t s, DevMutationRow* rows, size_t cap) {
+   s = stream_for(s);
+   const BatchState& b = batch_;
+   if (b.n_rows > cap) throw std::invalid_argument("rows buffer holds " + std::to_string(cap) + " rows, " +
+                                                   std::to_string(b.n_rows) + " needed");
+   if (b.n_rows == 0) return;
+   cuda_check(cudaMemcpyAsync(rows, b.d_rows, b.n_rows * sizeof(DevMutationRow), cudaMemcpyDeviceToHost, s), "D2H");
+   cuda_check(cudaStreamSynchronize(s), "rows fetch");
 }
 
 void Engine::batch_capture(cudaStream_t s, bool copy_in, bool copy_out) {

@@ -26,6 +26,7 @@ struct BatchQuery {
    Program prog;
    int action = 0;  // 0 = count, 1 = mutations of `column`
    int column = 0;
+   double min_proportion = 0.05;  // Mutations rows: minimum proportion of a reported mutation
 };
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
@@ -34,6 +35,7 @@ struct BatchState {
       int column;
       uint32_t slot_begin, n;
       size_t counts_off, scratch_off;  // u32 offsets into the arenas
+      uint32_t blk_off;                // first entry of the group's slots in the row-block table
    };
    uint32_t n_queries = 0, n_slots = 0, n_items = 0, n_code = 0, max_depth = 1, tile_bits = 16384, grid = 0;
    std::vector<ColGroup> groups;
@@ -46,6 +48,8 @@ struct BatchState {
    uint32_t* h_slot_query = nullptr;
    unsigned long long* h_counts = nullptr;
    uint32_t* h_mcounts = nullptr;
+   double* h_minprop = nullptr;       // per slot
+   uint32_t* h_rowblk = nullptr;      // row-block offsets of the last batch_rows, n_blk + 1
    // device
    Instr* d_code = nullptr;
    QueryDesc* d_q = nullptr;
@@ -57,11 +61,17 @@ struct BatchState {
    uint32_t* d_mcounts = nullptr;
    uint32_t* d_mscratch = nullptr;
    uint16_t* d_masks = nullptr;
+   double* d_minprop = nullptr;
+   uint32_t* d_rowblk = nullptr;
+   DevMutationRow* d_rows = nullptr;
+   uint32_t n_blk = 0;                // row-block table entries (all slots)
+   size_t n_rows = 0;                 // rows of the last batch_rows
    // capacities
    // capacities (elements), one per buffer
-   size_t hc_code = 0, hc_q = 0, hc_items = 0, hc_slot_query = 0, hc_counts = 0, hc_mcounts = 0;
+   size_t hc_code = 0, hc_q = 0, hc_items = 0, hc_slot_query = 0, hc_counts = 0, hc_mcounts = 0, hc_minprop = 0,
+          hc_rowblk = 0;
    size_t dc_code = 0, dc_q = 0, dc_items = 0, dc_slot_query = 0, dc_counts = 0, dc_next = 0, dc_tiles = 0,
-          dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0;
+          dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0, dc_minprop = 0, dc_rowblk = 0, dc_rows = 0;
    cudaGraphExec_t graph = nullptr;
 };
 
@@ -117,6 +127,13 @@ class Engine {
    void batch_replay(cudaStream_t stream);
    const BatchState& batch() const { return batch_; }
    const uint32_t* batch_mutation_counts(uint32_t query) const;  // pinned host, after the stream synced
+   // Mutations action output of the prepared batch: enqueues the batch and the row passes,
+   // synchronises once to size the packed rows, copies them to `rows` when they fit `cap` and
+   // returns their number. Query i's rows are rows[row_begin[i] .. row_begin[i] + row_count[i])
+   // (count queries: none). The filter counts are in batch_count afterwards.
+   size_t batch_rows(cudaStream_t stream, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count);
+   // Copies the rows of the last batch_rows again (for a caller whose buffer was too small).
+   void batch_rows_fetch(cudaStream_t stream, DevMutationRow* rows, size_t cap);
    uint64_t batch_count(uint32_t query) const { return batch_.h_counts[query]; }
    // Tile width that fits the batch's deepest program in the shared-memory budget.
    uint32_t fit_tile_bits(uint32_t requested, uint32_t depth, bool batch = false) const;

@@ -1,10 +1,9 @@
 // Mutations action kernels of the plain single-query path.
 //
-//  mut_ctr_kernel    every vertical container once: |F ∩ container| against the filter tile of its
+//  mut_stream_kernel every vertical container once: |F ∩ container| against the filter tile of its
 //                    chunk staged in shared memory; integer counts per (symbol, position)
-//                    (reference: mutations_node.cpp:139-189). CTAs stay on one chunk; a warp takes
-//                    32 consecutive containers and streams their array payloads as one contiguous
-//                    range with 16-byte loads, attributing elements to containers by offset.
+//                    (reference: mutations_node.cpp:139-189). The payload arena is streamed in
+//                    units of 16 KiB by TMA bulk copies into double-buffered shared memory.
 //  mut_cov_kernel    rows of F outside their covered region and inside missing intervals, from
 //                    position-sorted start / end events aggregated per position with warp ballots
 //                    (reference: mutations_node.cpp:51-136).
@@ -13,6 +12,9 @@
 // The filter count decides on the device between the full path (|F| == rows: stored
 // cardinalities, reference: mutations_node.cpp:240-266), the empty path and the mixed path.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
 
 #include "device.h"
 #include "mutations_common.cuh"
@@ -23,115 +25,190 @@ namespace {
 
 constexpr uint32_t MT = 256;
 constexpr uint32_t NW = MT / 32;
-constexpr uint32_t CTAS_PER_CHUNK_TARGET = 1216;  // 152 SMs x 8 CTAs, divided among the chunks
 
-// Warp-cooperative |F ∩ container| for bitset and run containers (all lanes return the total).
-__device__ uint32_t warp_count_other(const CtrDesc& d, const uint32_t* F, const uint16_t* __restrict__ payload) {
-   const uint32_t lane = threadIdx.x & 31;
-   uint32_t c = 0;
-   if (d.type == CT_BITSET) {
-      const uint4* b = reinterpret_cast<const uint4*>(payload + d.payload);
-      const uint4* f = reinterpret_cast<const uint4*>(F);
-#pragma unroll 4
-      for (uint32_t k = lane; k < CHUNK_WORDS / 4; k += 32) {
-         const uint4 x = __ldg(b + k);
-         const uint4 y = f[k];
-         c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
-      }
-   } else {
-      const uint16_t* p = payload + d.payload;
-      for (uint32_t k = lane; k < d.nruns; k += 32) {
-         const uint32_t s = __ldg(p + 2 * k);
-         c += count_range(F, s, s + __ldg(p + 2 * k + 1) + 1u);
-      }
+// Block-wide exclusive prefix sum of one value per thread; *total receives the sum. Contains
+// one barrier; the caller separates consecutive calls with another.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, uint32_t* total) {
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   uint32_t incl = x;
+#pragma unroll
+   for (uint32_t o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += y;
    }
-   return __reduce_add_sync(0xFFFFFFFFu, c);
+   if (lane == 31) wsum[warp] = incl;
+   __syncthreads();
+   uint32_t before = 0, all = 0;
+#pragma unroll
+   for (uint32_t w = 0; w < NW; ++w) {
+      const uint32_t v = wsum[w];
+      before += w < warp ? v : 0u;
+      all += v;
+   }
+   *total = all;
+   return before + incl - x;
 }
 
-__global__ void __launch_bounds__(MT) mut_ctr_kernel(const DevTable* __restrict__ tab, uint32_t col, uint32_t K,
-                                                     const uint32_t* __restrict__ filter,
-                                                     const unsigned long long* __restrict__ fcount, uint32_t* counts) {
-   __shared__ __align__(16) uint32_t F[CHUNK_WORDS];
+// Container pass of the Mutations action, streaming the payload arena. Persistent CTAs walk a
+// contiguous range of the column's stream units (chunk-major):
+//   SU_ARRAYS  up to SU consecutive elements of a chunk's array payloads (arrays are stored back to
+//              back in descriptor order), with the descriptor range [c0, c1) overlapping them;
+//   SU_BITSET  one bitset container; SU_RUN one run container.
+// Array and bitset payloads are double-buffered into shared memory by TMA bulk copies (the copy
+// of the next unit is in flight while the current one is counted). For array units thread t
+// tests elements 32t..32t+31 against the filter tile of the chunk (staged in shared memory), a
+// block prefix sum over the membership bits gives every container its |F ∩ c| as the difference
+// of two prefix values, added to counts[symbol][position] (containers cut by a unit boundary add
+// two partial counts). Full filters (|F| == rows) use the stored cardinalities
+// (reference: mutations_node.cpp:139-190, full path :240-266).
+__global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                        const uint32_t* __restrict__ filter,
+                                                        const unsigned long long* __restrict__ fcount,
+                                                        uint32_t* counts, int* err) {
+   extern __shared__ __align__(128) uint4 sm4[];  // two SU-element buffers, then the filter tile
+   __shared__ __align__(8) uint64_t bar[2];
+   __shared__ uint32_t wsum[NW], msk[MT], exq[MT];
    const unsigned long long fc = *fcount;
    if (fc == 0) return;
    const bool full = fc == tab->n_rows;
    const DevSeqCol* cs = &tab->seq[col];
+   const uint32_t n_units = cs->nsu;
+   const uint32_t u0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * n_units / gridDim.x);
+   const uint32_t u1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * n_units / gridDim.x);
+   if (u0 >= u1) return;
+   const StreamUnit* __restrict__ units = cs->su;
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint16_t* __restrict__ payload = cs->payload;
-   const uint4* __restrict__ pw = reinterpret_cast<const uint4*>(payload);
-   const uint32_t L = cs->L;
-   const uint32_t v = blockIdx.x / K, k = blockIdx.x % K;
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   if (!full) {
-      const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(v) * CHUNK_WORDS);
-      uint4* dst = reinterpret_cast<uint4*>(F);
-      for (uint32_t i = threadIdx.x; i < CHUNK_WORDS / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+   const uint32_t L = cs->L, tid = threadIdx.x;
+   uint32_t* F = reinterpret_cast<uint32_t*>(sm4 + 2 * (SU / 8));
+   if (tid == 0) {
+      mbar_init(&bar[0]);
+      mbar_init(&bar[1]);
    }
    __syncthreads();
-   const uint32_t cb = __ldg(cs->off + static_cast<size_t>(v) * L), ce = __ldg(cs->off + static_cast<size_t>(v + 1) * L);
-   const uint32_t nslices = (ce - cb + 31) / 32;
-   for (uint32_t sl = k * NW + warp; sl < nslices; sl += K * NW) {
-      const uint32_t idx = cb + sl * 32 + lane;
-      const bool valid = idx < ce;
-      uint4 raw = make_uint4(0, 0, 0, 0);
-      if (valid) raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + idx);
-      const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
-      if (full) {
-         if (valid) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], d.card_m1 + 1u);
-         continue;
+   auto copies = [&](const StreamUnit& U) { return !full && U.kind != SU_RUN; };
+   auto issue = [&](const StreamUnit& U, uint32_t b) {  // thread 0
+      const uint32_t bytes = U.kind == SU_BITSET ? CHUNK_ROWS / 8 : ((U.e1 - U.e0) * 2u + 15u) & ~15u;
+      bulk_copy_g2s(sm4 + b * (SU / 8), payload + U.e0, bytes, &bar[b]);
+   };
+   uint32_t issued0 = 0, issued1 = 0;  // copies issued into each buffer (the same in every thread)
+   {
+      const StreamUnit U = units[u0];
+      if (copies(U)) {
+         if (tid == 0) issue(U, 0);
+         ++issued0;
       }
-      const bool is_arr = valid && d.type == CT_ARRAY;
-      const uint32_t amask = __ballot_sync(0xFFFFFFFFu, is_arr);
-      const uint32_t nA = __popc(amask);
-      if (nA) {
-         // Lane c takes the c-th array of the slice; the arrays are back to back in the payload
-         // arena, so the slice's elements are one range [P0, P1) streamed in windows of 32 words.
-         const uint32_t src = lane < nA ? __fns(amask, 0, lane + 1) : 0;
-         const uint32_t my_s = __shfl_sync(0xFFFFFFFFu, d.payload, src);
-         const uint32_t my_e = my_s + __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(d.card_m1), src) + 1u;
-         const uint32_t P0 = __shfl_sync(0xFFFFFFFFu, my_s, 0);
-         const uint32_t P1 = __shfl_sync(0xFFFFFFFFu, my_e, nA - 1);
-         uint32_t acc = 0;
-         for (uint32_t w0 = P0 >> 3; w0 <= (P1 - 1) >> 3; w0 += 32) {
-            const uint32_t w = w0 + lane;
-            uint32_t bits = 0;  // bit t: element 8w + t is in F
-            if (w <= (P1 - 1) >> 3) {
-               const uint4 x = __ldg(pw + w);
-#pragma unroll
-               for (uint32_t t = 0; t < 8; ++t) bits |= test_bit(F, u16_of(x, t)) << t;
-            }
-            // exclusive prefix of set bits over the window's words
-            const uint32_t cnt = __popc(bits);
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-               const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-               if (static_cast<int>(lane) >= o) incl += y;
-            }
-            const uint32_t excl = incl - cnt;
-            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            // set bits of [8 w0, x) for x inside or at the end of the window
-            const uint32_t lo8 = 8 * w0, hi8 = 8 * (w0 + 32);
-            const uint32_t a = min(max(my_s, lo8), hi8), z = min(max(my_e, lo8), hi8);
-            const uint32_t wa = (a - lo8) >> 3, wz = (z - lo8) >> 3;
-            const uint32_t ea = __shfl_sync(0xFFFFFFFFu, excl, wa & 31), ba = __shfl_sync(0xFFFFFFFFu, bits, wa & 31);
-            const uint32_t ez = __shfl_sync(0xFFFFFFFFu, excl, wz & 31), bz = __shfl_sync(0xFFFFFFFFu, bits, wz & 31);
-            const uint32_t pa = wa >= 32 ? total : ea + __popc(ba & ((1u << ((a - lo8) & 7)) - 1u));
-            const uint32_t pz = wz >= 32 ? total : ez + __popc(bz & ((1u << ((z - lo8) & 7)) - 1u));
-            acc += pz - pa;
+   }
+   uint32_t cur_v = 0xFFFFFFFFu;
+   bool ok = true;
+   for (uint32_t u = u0; u < u1 && ok; ++u) {
+      const uint32_t b = (u - u0) & 1u;
+      const StreamUnit U = units[u];
+      if (!full && U.v != cur_v) {
+         const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(U.v) * CHUNK_WORDS);
+         for (uint32_t i = tid; i < CHUNK_WORDS / 4; i += MT) reinterpret_cast<uint4*>(F)[i] = __ldg(src + i);
+         cur_v = U.v;
+      }
+      if (u + 1 < u1) {
+         const StreamUnit N = units[u + 1];
+         if (copies(N)) {
+            if (tid == 0) issue(N, b ^ 1u);
+            if (b) ++issued0;
+            else ++issued1;
          }
-         const uint32_t key = __shfl_sync(0xFFFFFFFFu, d.key, src);
-         const uint32_t sym = __shfl_sync(0xFFFFFFFFu, static_cast<uint32_t>(d.sym), src);
-         if (lane < nA && acc) atomicAdd(&counts[static_cast<size_t>(sym) * L + key], acc);
       }
-      uint32_t other = __ballot_sync(0xFFFFFFFFu, valid && !is_arr);
-      while (other) {
-         const int j = __ffs(other) - 1;
-         other &= other - 1;
-         const CtrDesc dj = shfl_desc(raw, j);
-         const uint32_t c = warp_count_other(dj, F, payload);
-         if (lane == 0 && c) atomicAdd(&counts[static_cast<size_t>(dj.sym) * L + dj.key], c);
+      if (copies(U)) ok = mbar_wait(&bar[b], ((b ? issued1 : issued0) - 1u) & 1u);
+      if (!__syncthreads_and(ok)) {
+         ok = false;  // in every thread: the cleanup below has a barrier
+         if (tid == 0) atomicExch(err, 7);
+         break;
       }
+      if (U.kind == SU_ARRAYS) {
+         if (full) {
+            for (uint32_t c = U.c0 + tid; c < U.c1; c += MT) {
+               const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
+               const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+               if (d.type != CT_ARRAY) continue;
+               const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
+               if (s < e) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], e - s);
+            }
+         } else {
+            // this thread's first descriptor is loaded before the element tests hide its latency
+            const uint32_t c_first = U.c0 + tid;
+            uint4 raw0 = make_uint4(0, 0, 0, 0);
+            if (c_first < U.c1) raw0 = __ldg(reinterpret_cast<const uint4*>(ctrs) + c_first);
+            const uint32_t n = U.e1 - U.e0;
+            const uint4* q = sm4 + b * (SU / 8) + 4 * tid;
+            uint32_t m = 0;
+            if (n == SU) {
+#pragma unroll
+               for (uint32_t j = 0; j < 4; ++j) {
+                  const uint4 x = q[j];
+#pragma unroll
+                  for (uint32_t t = 0; t < 8; ++t) m |= test_bit(F, u16_of(x, t)) << (8 * j + t);
+               }
+            } else {
+#pragma unroll
+               for (uint32_t j = 0; j < 4; ++j) {
+                  const uint4 x = q[j];
+#pragma unroll
+                  for (uint32_t t = 0; t < 8; ++t) {
+                     const uint32_t i = 32 * tid + 8 * j + t;
+                     if (i < n) m |= test_bit(F, u16_of(x, t)) << (8 * j + t);
+                  }
+               }
+            }
+            uint32_t total;
+            const uint32_t ex = block_excl_scan(__popc(m), wsum, &total);
+            msk[tid] = m;
+            exq[tid] = ex;
+            __syncthreads();
+            auto prefix = [&](uint32_t i) -> uint32_t {  // members among elements [0, i)
+               if ((i >> 5) >= MT) return total;
+               return exq[i >> 5] + __popc(msk[i >> 5] & ((1u << (i & 31)) - 1u));
+            };
+            for (uint32_t c = c_first; c < U.c1; c += MT) {
+               const uint4 raw = c == c_first ? raw0 : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
+               const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+               if (d.type != CT_ARRAY) continue;
+               const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
+               if (s >= e) continue;
+               const uint32_t k = prefix(e - U.e0) - prefix(s - U.e0);
+               if (k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
+            }
+         }
+      } else {
+         const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + U.c0);
+         const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+         uint32_t k = 0;
+         if (full) {
+            k = tid == 0 ? d.card_m1 + 1u : 0u;
+         } else if (U.kind == SU_BITSET) {
+            const uint4* x = sm4 + b * (SU / 8);
+            const uint4* f = reinterpret_cast<const uint4*>(F);
+#pragma unroll
+            for (uint32_t j = 0; j < CHUNK_WORDS / 4 / MT; ++j) {
+               const uint4 a = x[tid + j * MT], y = f[tid + j * MT];
+               k += __popc(a.x & y.x) + __popc(a.y & y.y) + __popc(a.z & y.z) + __popc(a.w & y.w);
+            }
+         } else {
+            const uint16_t* r = payload + d.payload;
+            for (uint32_t i = tid; i < d.nruns; i += MT) {
+               const uint32_t s = __ldg(r + 2 * i);
+               k += count_range(F, s, s + __ldg(r + 2 * i + 1) + 1u);
+            }
+         }
+         k = __reduce_add_sync(0xFFFFFFFFu, k);
+         if ((tid & 31) == 0 && k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
+      }
+      __syncthreads();
+   }
+   if (!ok) {  // let the copies still in flight land before the CTA's shared memory is released
+      if (tid == 0) {
+         if (issued0) mbar_wait(&bar[0], (issued0 - 1u) & 1u);
+         if (issued1) mbar_wait(&bar[1], (issued1 - 1u) & 1u);
+      }
+      __syncthreads();
    }
 }
 
@@ -222,12 +299,27 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __re
 
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
-                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
-                      uint32_t parts) {
+                      const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
+                      void* stream, uint32_t parts) {
    cudaStream_t s = static_cast<cudaStream_t>(stream);
-   if (parts & MUT_PART_CTR) {
-      const uint32_t K = (CTAS_PER_CHUNK_TARGET + nchunks - 1) / nchunks;
-      mut_ctr_kernel<<<nchunks * K, MT, 0, s>>>(d_table, col, K, d_filter, d_filter_count, d_counts);
+   if ((parts & MUT_PART_CTR) && col_host.nsu > 0) {
+      const size_t smem = 2 * SU * 2 + CHUNK_WORDS * 4;
+      // resident CTAs per device, computed once per device
+      static std::atomic<uint32_t> resident[64];
+      int dev = 0;
+      cudaGetDevice(&dev);
+      uint32_t res = dev >= 0 && dev < 64 ? resident[dev].load(std::memory_order_relaxed) : 0u;
+      if (res == 0) {
+         int sms = 0, per_sm = 0;
+         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mut_stream_kernel, MT, smem) != cudaSuccess ||
+             per_sm < 1)
+            per_sm = 1;
+         res = static_cast<uint32_t>(std::max(sms, 1) * per_sm);
+         if (dev >= 0 && dev < 64) resident[dev].store(res, std::memory_order_relaxed);
+      }
+      const uint32_t grid = std::min<uint32_t>(col_host.nsu, res);
+      mut_stream_kernel<<<grid, MT, smem, s>>>(d_table, col, d_filter, d_filter_count, d_counts, d_err);
    }
    if ((parts & MUT_PART_COV) && n_ev > 0)
       mut_cov_kernel<<<n_ev, MT, 0, s>>>(d_table, col, d_ev, d_filter, d_filter_count, d_scratch);

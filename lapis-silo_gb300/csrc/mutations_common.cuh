@@ -9,6 +9,43 @@ namespace rhygpu {
 
 constexpr uint32_t SMALL_ARRAY = 32;  // array containers up to this size are counted by one lane
 
+// mbarrier + TMA bulk-copy helpers. A barrier is initialised with one arrival; the issuing thread
+// arrives with the expected byte count and starts the copy, whose completion flips the phase.
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Copies `bytes` (a multiple of 16, both addresses 16-byte aligned) from global to shared memory
+// and completes them on `bar`. Called by one thread.
+__device__ __forceinline__ void bulk_copy_g2s(void* smem, const void* gmem, uint32_t bytes, uint64_t* bar) {
+   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+   // order earlier generic-proxy accesses of the buffer before the asynchronous write
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(b), "r"(bytes)
+                : "memory");
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(s),
+                "l"(gmem), "r"(bytes), "r"(b)
+                : "memory");
+}
+
+// Waits (bounded) for the phase with the given parity to complete. Returns false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+   for (uint32_t i = 0; i < (1u << 22); ++i) {
+      uint32_t done;
+      asm volatile(
+         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         : "=r"(done)
+         : "r"(b), "r"(parity)
+         : "memory");
+      if (done) return true;
+   }
+   return false;
+}
+
 __device__ __forceinline__ uint32_t test_bit(const uint32_t* F, uint32_t r) { return (F[r >> 5] >> (r & 31)) & 1u; }
 
 // popcount of F in [a, b)

@@ -72,7 +72,7 @@ void mutations_noalloc(Engine& engine, uint32_t column, const uint32_t* d_filter
    cuda_check(cudaMemsetAsync(d_counts, 0, static_cast<size_t>(col.nsym) * col.L * sizeof(uint32_t), s), "clear counts");
    cudaGetLastError();
    launch_mutations(engine.d_table(), col, column, engine.nchunks(), engine.d_ev(static_cast<int>(column)),
-                    engine.n_ev(static_cast<int>(column)), d_filter, d_filter_count, d_counts, scratch, s);
+                    engine.n_ev(static_cast<int>(column)), d_filter, d_filter_count, d_counts, scratch, engine.d_err, s);
    cuda_check(cudaGetLastError(), "mutations (no allocation) launch");
 }
 

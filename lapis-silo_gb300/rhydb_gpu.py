@@ -125,6 +125,8 @@ def lib():
         "rhy_mutations": (I, [P, C.c_char_p, U32, P, P, C.POINTER(U64)]),
         "rhy_mutation_rows": (I, [P, U32, P, C.c_double, C.POINTER(MutationRow), C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_batch": (I, [P, P, P, P, U32, U32, P, P, P]),
+        "rhy_batch_rows": (I, [P, P, P, P, P, U32, U32, P, P, P, C.c_size_t, P, P, C.POINTER(C.c_size_t)]),
+        "rhy_batch_rows_fetch": (I, [P, P, P, C.c_size_t]),
         "rhy_batch_prepare": (I, [P, P, P, P, U32, U32, U32]),
         "rhy_batch_launch": (I, [P, P, I, I]),
         "rhy_batch_capture": (I, [P, P]),
@@ -350,6 +352,30 @@ class Device:
         _check(lib().rhy_batch(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), n, tile_bits, stream,
                                _ptr(counts), C.cast(ptrs, C.c_void_p)))
         return counts[:n], outs
+
+    ROW_DTYPE = np.dtype({"names": ["position", "from_", "to", "count", "coverage", "proportion"],
+                          "formats": [np.uint32, "S1", "S1", np.uint32, np.uint32, np.float64],
+                          "offsets": [0, 4, 5, 8, 12, 16], "itemsize": 24})
+
+    def batch_rows(self, exprs, actions=None, columns=None, min_proportions=None, tile_bits: int = 0, stream=None,
+                   rows_cap: int = 1 << 20):
+        """Batch with the Mutations output computed on the device. Returns (filter counts, rows,
+        row_begin, row_count): query i's rows are rows[row_begin[i]:row_begin[i] + row_count[i]], a
+        structured array with the fields of RhyMutationRow."""
+        n, arr, act, col = self._query_arrays(exprs, actions, columns)
+        counts = np.zeros(max(n, 1), np.uint64)
+        begin = np.zeros(max(n, 1), np.uint64)
+        cnt = np.zeros(max(n, 1), np.uint32)
+        mp = None if min_proportions is None else np.ascontiguousarray(min_proportions, dtype=np.float64)
+        rows = np.zeros(max(rows_cap, 1), self.ROW_DTYPE)
+        total = C.c_size_t()
+        _check(lib().rhy_batch_rows(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col),
+                                    None if mp is None else _ptr(mp), n, tile_bits, stream, _ptr(counts),
+                                    rows.ctypes.data, rows_cap, _ptr(begin), _ptr(cnt), C.byref(total)))
+        if total.value > rows_cap:
+            rows = np.zeros(total.value, self.ROW_DTYPE)
+            _check(lib().rhy_batch_rows_fetch(self._h, stream, rows.ctypes.data, total.value))
+        return counts[:n], rows[:total.value], begin[:n], cnt[:n]
 
     def batch_prepare(self, exprs, actions=None, columns=None, tile_bits: int = 0, plan_threads: int = 0):
         n, arr, act, col = self._query_arrays(exprs, actions, columns)

@@ -89,6 +89,35 @@ def test_config2_batched_mixed_columns(config2_small):
             assert np.array_equal(muts[int(i)], om), (tb, qs[i], col[i])
 
 
+def test_batched_mutation_rows(config2_small):
+    """The Mutations output computed on the device (rhy_batch_rows) equals the host conversion of
+    the dense counts, which equals the oracle's, row for row and bit for bit in the proportions."""
+    t, orc, dev, qs = config2_small
+    rng = np.random.default_rng(5)
+    act = (rng.random(len(qs)) < 0.5).astype(np.int32)
+    col = rng.integers(0, t.n_seq, len(qs)).astype(np.uint32)
+    props = rng.choice([0.0, 0.05, 0.3, 1.0], len(qs))
+    # a small buffer exercises the refetch of rows that did not fit
+    counts, rows, begin, cnt = dev.batch_rows(qs, act, col, props, rows_cap=1000)
+    dcounts, muts = dev.batch(qs, act, col)
+    assert np.array_equal(counts, dcounts)
+    assert len(rows) > 1000
+    for i in range(len(qs)):
+        if act[i] == 0:
+            assert cnt[i] == 0
+            continue
+        got = rows[int(begin[i]):int(begin[i]) + int(cnt[i])]
+        want = t.mutation_rows(int(col[i]), muts[i], float(props[i]))
+        assert [(int(r["position"]), r["from_"].decode(), r["to"].decode(), int(r["count"]), int(r["coverage"]),
+                 float(r["proportion"])) for r in got] == want, (qs[i], props[i])
+    for i in np.flatnonzero(act)[:12]:
+        om, _ = orc.mutations(qs[i], int(col[i]))
+        assert orc.mutation_rows(int(col[i]), om, float(props[i])) == t.mutation_rows(int(col[i]), muts[int(i)],
+                                                                                      float(props[i]))
+    with pytest.raises(R.RhyError):
+        dev.batch_rows(qs[:4], [1, 1, 0, 0], None, [0.05, 1.5, 0.05, 0.05])
+
+
 def test_tile_widths(config2_small):
     t, orc, dev, qs = config2_small
     for tb in (4096, 8192, 32768, 65536):
