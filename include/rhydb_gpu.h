@@ -224,6 +224,42 @@ int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filte
 /* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */
 int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,
                       RhyMutationRow* rows, size_t cap, size_t* n_rows);
+/* ---- learned planner (no counterpart in the reference, whose operators order children by
+ * cardinality only: intersection.cpp:59-106) ----
+ * The network (24 -> 64 -> 64 -> 2, BF16 weights, FP32 arithmetic) predicts per operator node the
+ * natural log of its result's fraction of the rows and of its cycles per tile. collect runs each
+ * expression through the single-query path in trace mode and appends one sample per operator node;
+ * train fits the network on the GPU (80/20 split, Adam) and judges it on the held-out part against
+ * the rule-based estimator; mode 1 plans batches with it (only once accepted), mode 0 (the
+ * default) with the rule-based ordering. Plans differ only in child order and item order; results
+ * are identical. */
+#define RHY_PLANNER_FEATURES 24
+#define RHY_MLP_NPARAM 5890 /* W1[64][24] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
+typedef struct {
+   uint32_t n_train, n_val, epochs;
+   float train_loss, val_loss;
+   float qerr_learned_median, qerr_rule_median, qerr_learned_p90, qerr_rule_p90;
+   float cost_err_median;
+   float train_ms;
+   int accepted;
+} RhyPlannerStats;
+/* Features of every operator node of the compiled expression, in preorder (host only). */
+int rhy_plan_features(const RhyTable* t, const char* expr, float* x /* [n][24] */, size_t cap, size_t* n);
+int rhy_planner_collect(RhyDevice* d, const char* const* exprs, uint32_t n, size_t* n_added);
+int rhy_planner_train(RhyDevice* d, uint32_t epochs, uint32_t batch, float lr, uint64_t seed, RhyPlannerStats* out);
+int rhy_planner_mode(RhyDevice* d, int mode);
+/* Samples: x[n][24] features; y[n][3] = ln selectivity, ln cycles per tile, ln rule selectivity. */
+int rhy_planner_samples(RhyDevice* d, float* x, float* y, size_t cap, size_t* n);
+int rhy_planner_weights(RhyDevice* d, float* w /* RHY_MLP_NPARAM FP32 master weights */);
+/* Network predictions (GPU inference) for feature rows: selectivity (fraction of rows) and cycles
+ * per tile. */
+int rhy_planner_predict(RhyDevice* d, const float* x, uint32_t n, double* sel, double* cost);
+/* One forward + backward of the network with the given FP32 master weights (used in BF16) on the
+ * device: gradient of mean_n sum_k (y_k - t_k)^2 with respect to the BF16 weights, the loss and the
+ * outputs y[n][2]. Leaves the planner untouched. */
+int rhy_mlp_gradient(RhyDevice* d, const float* w, const float* x, const float* t, uint32_t n, float* grad, float* loss,
+                     float* y);
+
 void rhy_close(RhyDevice* d);
 
 #ifdef __cplusplus

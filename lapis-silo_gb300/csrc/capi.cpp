@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -413,10 +414,8 @@ std::vector<rhygpu::BatchQuery> make_batch(RhyDevice* d, const char* const* expr
       need(exprs[i], "expression");
       texts[i] = exprs[i];
    }
-   std::vector<rhygpu::Program> progs = rhygpu::plan_many(d->table->image, texts, plan_threads);
-   std::vector<rhygpu::BatchQuery> qs(n);
+   std::vector<rhygpu::BatchQuery> qs = d->engine->plan_batch(texts, plan_threads);
    for (uint32_t i = 0; i < n; ++i) {
-      qs[i].prog = std::move(progs[i]);
       qs[i].action = actions ? actions[i] : 0;
       qs[i].column = columns ? static_cast<int>(columns[i]) : 0;
       if (qs[i].action != 0 && qs[i].action != 1) throw std::invalid_argument("action must be 0 (count) or 1 (mutations)");
@@ -669,6 +668,134 @@ int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts
          }
       }
       *n_rows = n;
+   });
+}
+
+// ---- learned planner ----
+
+static_assert(RHY_PLANNER_FEATURES == rhygpu::PLAN_FEATURES, "feature count");
+static_assert(RHY_MLP_NPARAM == rhygpu::MLP_NPARAM, "parameter count");
+
+int rhy_plan_features(const RhyTable* t, const char* expr, float* x, size_t cap, size_t* n) {
+   return guarded([&] {
+      need(t, "table");
+      need(expr, "expression");
+      need(n, "n");
+      const rhygpu::FeatureContext ctx = rhygpu::feature_context(t->image);
+      rhygpu::OpPtr op = rhygpu::compile_filter(expr, t->image);
+      std::vector<const rhygpu::Op*> nodes;
+      std::function<void(const rhygpu::Op&)> walk = [&](const rhygpu::Op& o) {
+         nodes.push_back(&o);
+         for (const auto& c : o.children) walk(*c);
+         for (const auto& c : o.negated) walk(*c);
+      };
+      walk(*op);
+      *n = nodes.size();
+      for (size_t i = 0; i < nodes.size() && i < cap && x; ++i) rhygpu::op_features(*nodes[i], ctx, x + i * RHY_PLANNER_FEATURES);
+   });
+}
+
+int rhy_planner_collect(RhyDevice* d, const char* const* exprs, uint32_t n, size_t* n_added) {
+   return guarded([&] {
+      need(d, "device");
+      if (n) need(exprs, "exprs");
+      std::vector<std::string> texts;
+      for (uint32_t i = 0; i < n; ++i) {
+         need(exprs[i], "expression");
+         texts.emplace_back(exprs[i]);
+      }
+      const size_t k = d->engine->planner_collect(texts);
+      if (n_added) *n_added = k;
+   });
+}
+
+int rhy_planner_train(RhyDevice* d, uint32_t epochs, uint32_t batch, float lr, uint64_t seed, RhyPlannerStats* out) {
+   return guarded([&] {
+      need(d, "device");
+      const rhygpu::PlannerStats st = d->engine->planner_train(epochs, batch, lr, seed);
+      if (out) {
+         out->n_train = st.n_train;
+         out->n_val = st.n_val;
+         out->epochs = st.epochs;
+         out->train_loss = st.train_loss;
+         out->val_loss = st.val_loss;
+         out->qerr_learned_median = st.qerr_learned_median;
+         out->qerr_rule_median = st.qerr_rule_median;
+         out->qerr_learned_p90 = st.qerr_learned_p90;
+         out->qerr_rule_p90 = st.qerr_rule_p90;
+         out->cost_err_median = st.cost_err_median;
+         out->train_ms = st.train_ms;
+         out->accepted = st.accepted;
+      }
+   });
+}
+
+int rhy_planner_mode(RhyDevice* d, int mode) {
+   return guarded([&] {
+      need(d, "device");
+      d->engine->set_planner_mode(mode);
+   });
+}
+
+int rhy_planner_samples(RhyDevice* d, float* x, float* y, size_t cap, size_t* n) {
+   return guarded([&] {
+      need(d, "device");
+      need(n, "n");
+      const auto& sm = d->engine->planner().samples;
+      *n = sm.size();
+      for (size_t i = 0; i < sm.size() && i < cap; ++i) {
+         if (x) std::copy(sm[i].x.begin(), sm[i].x.end(), x + i * RHY_PLANNER_FEATURES);
+         if (y) {
+            y[3 * i] = sm[i].log_sel;
+            y[3 * i + 1] = sm[i].log_cost;
+            y[3 * i + 2] = sm[i].rule_log_sel;
+         }
+      }
+   });
+}
+
+int rhy_planner_predict(RhyDevice* d, const float* x, uint32_t n, double* sel, double* cost) {
+   return guarded([&] {
+      need(d, "device");
+      if (n) need(x, "x");
+      std::vector<std::array<float, rhygpu::PLAN_FEATURES>> rows(n);
+      for (uint32_t i = 0; i < n; ++i) std::copy(x + static_cast<size_t>(i) * RHY_PLANNER_FEATURES,
+                                                 x + static_cast<size_t>(i + 1) * RHY_PLANNER_FEATURES, rows[i].begin());
+      std::vector<double> s, c;
+      {
+         std::lock_guard<std::mutex> lock(d->engine->mu);
+         rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+         if (!d->engine->planner().trained) throw std::invalid_argument("the planner network is not trained");
+         d->engine->planner().predict(rows, s, c);
+      }
+      for (uint32_t i = 0; i < n; ++i) {
+         if (sel) sel[i] = s[i];
+         if (cost) cost[i] = c[i];
+      }
+   });
+}
+
+int rhy_planner_weights(RhyDevice* d, float* w) {
+   return guarded([&] {
+      need(d, "device");
+      need(w, "w");
+      d->engine->planner().net.get_master(w);
+   });
+}
+
+int rhy_mlp_gradient(RhyDevice* d, const float* w, const float* x, const float* t, uint32_t n, float* grad, float* loss,
+                     float* y) {
+   return guarded([&] {
+      need(d, "device");
+      need(w, "w");
+      if (n) {
+         need(x, "x");
+         need(t, "t");
+      }
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      rhygpu::PlannerNet net(d->engine->device());
+      net.set_master(w);
+      net.gradient(x, t, n, grad, loss, y);
    });
 }
 

@@ -124,10 +124,11 @@ struct QueryDesc {
 
 // ---- launchers (kernels.cu) ----
 // tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth. n_leaves: container
-// leaves of the program (Program::n_ctr_leaves).
+// leaves | coverage leaves << 16. d_trace (trace mode, optional): nchunks * (CHUNK_ROWS / tile_bits)
+// tiles x ncode x 2 u32 (cycles, result popcount per executed instruction), zeroed by the caller.
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
-                          uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
-                          int* d_err, void* stream);
+                          uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles,
+                          unsigned long long* d_count, int* d_err, void* stream, uint32_t* d_trace = nullptr);
 
 // Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.
 cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,

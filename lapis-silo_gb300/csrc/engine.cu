@@ -2,7 +2,12 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <numeric>
+#include <unordered_map>
+
+#include "util.h"
 
 namespace rhygpu {
 
@@ -116,7 +121,7 @@ void Engine::upload_dates(const DateColumnImage& dc, uint32_t nchunks, DevDateCo
    out.pad = 0;
 }
 
-Engine::Engine(const TableImage& t, int device) : table_(t), device_(device) {
+Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), planner_(device) {
    if (t.seq.size() > MAX_SEQ_COLS || t.dict.size() > MAX_DICT_COLS || t.date.size() > MAX_DATE_COLS)
       throw std::invalid_argument("too many columns for the device image");
    cuda_check(cudaSetDevice(device), "cudaSetDevice");
@@ -467,10 +472,18 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
                            p.n_ctr_leaves | (p.n_cov_leaves << 16)};
       off += p.code.size();
    }
-   // items: tile-major interleaving spreads the expensive queries over the whole launch
+   // items: tile-major interleaving spreads the expensive queries over the whole launch; with
+   // predicted costs (learned planner) the queries go heaviest first so the long ones do not end
+   // the launch alone
+   std::vector<uint32_t> qorder(n);
+   std::iota(qorder.begin(), qorder.end(), 0u);
+   bool costed = false;
+   for (const auto& q : qs) costed |= q.cost > 0;
+   if (costed)
+      std::stable_sort(qorder.begin(), qorder.end(), [&](uint32_t x, uint32_t y) { return qs[x].cost > qs[y].cost; });
    size_t k = 0;
    for (uint32_t t = 0; t < tiles_per_query; ++t)
-      for (uint32_t i = 0; i < n; ++i) b.h_items[k++] = WorkItem{i, t};
+      for (uint32_t i = 0; i < n; ++i) b.h_items[k++] = WorkItem{qorder[i], t};
    std::memcpy(b.h_slot_query, slot_query.data(), slot_query.size() * sizeof(uint32_t));
    b.n_queries = n;
    b.n_slots = nslots;
@@ -630,6 +643,142 @@ const uint32_t* Engine::batch_mutation_counts(uint32_t query) const {
       }
    }
    return nullptr;
+}
+
+// =================================================================================================
+// Learned planner
+
+const FeatureContext& Engine::fctx() {
+   if (!fctx_) fctx_ = std::make_unique<FeatureContext>(feature_context(table_));
+   return *fctx_;
+}
+
+size_t Engine::planner_collect(const std::vector<std::string>& exprs) {
+   std::lock_guard<std::mutex> lock(mu);
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   const FeatureContext& ctx = fctx();
+   const uint32_t W = tile_bits;
+   const uint32_t ntiles = nchunks() * (CHUNK_ROWS / W);
+   const double rows = std::max(1u, table_.n_rows);
+   cudaStream_t s = stream_;
+   uint32_t* d_trace = nullptr;
+   size_t cap = 0;
+   std::vector<uint32_t> trace;
+   size_t added = 0;
+   try {
+      for (const std::string& text : exprs) {
+         OpPtr op = compile_filter(text, table_);
+         LowerOptions o;
+         o.early_exit = false;
+         o.record_spans = true;
+         const Program p = lower(*op, ctx.rule, o);
+         const uint32_t nc = static_cast<uint32_t>(p.code.size());
+         const size_t words = static_cast<size_t>(ntiles) * nc * 2;
+         if (words > cap) {
+            if (d_trace) cudaFree(d_trace);
+            d_trace = nullptr;
+            cuda_check(cudaMalloc(&d_trace, words * sizeof(uint32_t)), "cudaMalloc (trace)");
+            cap = words;
+         }
+         upload_program(p, d_code, s);
+         cuda_check(cudaMemsetAsync(d_trace, 0, words * sizeof(uint32_t), s), "memset");
+         cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), s), "memset");
+         const uint32_t Wf = fit_tile_bits(W, p.max_depth);
+         if (Wf != W) continue;  // too deep for the trace tile width: skip
+         cudaGetLastError();
+         cuda_check(launch_filter(d_table_, nchunks(), d_code, nc, p.n_ctr_leaves | (p.n_cov_leaves << 16), W, p.max_depth,
+                                  nullptr, d_count, d_err, s, d_trace),
+                    "trace launch");
+         trace.resize(words);
+         cuda_check(cudaMemcpyAsync(trace.data(), d_trace, words * sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "D2H");
+         cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+         cuda_check(cudaStreamSynchronize(s), "trace");
+         check_error_flag();
+         for (const NodeSpan& sp : p.spans) {
+            if (sp.op->t == OpT::EMPTY || sp.op->t == OpT::FULL) continue;
+            double popc = 0, cyc = 0;
+            uint32_t live = 0;
+            for (uint32_t tl = 0; tl < ntiles; ++tl) {
+               const uint32_t* tr = trace.data() + static_cast<size_t>(tl) * nc * 2;
+               if (tr[2 * sp.last] == 0) continue;  // tile without rows
+               ++live;
+               popc += tr[2 * sp.last + 1];
+               for (uint32_t pc = sp.first; pc <= sp.last; ++pc) cyc += tr[2 * pc];
+            }
+            if (!live) continue;
+            PlannerSample smp;
+            op_features(*sp.op, ctx, smp.x.data());
+            smp.log_sel = static_cast<float>(std::log(std::max(popc / rows, 1e-7)));
+            smp.log_cost = static_cast<float>(std::log(std::max(cyc / live, 1.0)));
+            smp.rule_log_sel = static_cast<float>(std::log(std::max(std::min(1.0, ctx.rule(*sp.op) / rows), 1e-7)));
+            planner_.samples.push_back(smp);
+            ++added;
+         }
+      }
+   } catch (...) {
+      if (d_trace) cudaFree(d_trace);
+      throw;
+   }
+   if (d_trace) cudaFree(d_trace);
+   return added;
+}
+
+PlannerStats Engine::planner_train(uint32_t epochs, uint32_t batch, float lr, uint64_t seed) {
+   std::lock_guard<std::mutex> lock(mu);
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   return planner_.train(epochs, batch, lr, seed);
+}
+
+void Engine::set_planner_mode(int mode) {
+   if (mode != 0 && mode != 1) throw std::invalid_argument("planner mode must be 0 (rule-based) or 1 (learned)");
+   if (mode == 1 && !(planner_.trained && planner_.accepted))
+      throw std::invalid_argument("the learned planner is not trained or was not accepted against the rule-based ordering");
+   use_learned_ = mode == 1;
+}
+
+std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs, uint32_t threads) {
+   const uint32_t n = static_cast<uint32_t>(exprs.size());
+   std::vector<BatchQuery> qs(n);
+   if (!use_learned_) {
+      std::vector<Program> progs = plan_many(table_, exprs, threads);
+      for (uint32_t i = 0; i < n; ++i) qs[i].prog = std::move(progs[i]);
+      return qs;
+   }
+   const FeatureContext& ctx = fctx();
+   std::vector<OpPtr> ops(n);
+   parallel_for(n, threads, [&](uint32_t i) { ops[i] = compile_filter(exprs[i], table_); });
+   // every operator node of every expression, features in one table
+   std::vector<const Op*> nodes;
+   std::vector<uint32_t> root_of(n);
+   std::function<void(const Op&)> walk = [&](const Op& op) {
+      nodes.push_back(&op);
+      for (const auto& c : op.children) walk(*c);
+      for (const auto& c : op.negated) walk(*c);
+   };
+   for (uint32_t i = 0; i < n; ++i) {
+      root_of[i] = static_cast<uint32_t>(nodes.size());
+      walk(*ops[i]);
+   }
+   std::vector<std::array<float, PLAN_FEATURES>> x(nodes.size());
+   parallel_for(static_cast<uint32_t>(nodes.size()), threads, [&](uint32_t k) { op_features(*nodes[k], ctx, x[k].data()); });
+   std::vector<double> sel, cost;
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   planner_.predict(x, sel, cost);
+   std::unordered_map<const Op*, double> est_rows;
+   est_rows.reserve(nodes.size());
+   const double rows = std::max(1u, table_.n_rows);
+   for (size_t k = 0; k < nodes.size(); ++k)
+      if (std::isfinite(sel[k])) est_rows.emplace(nodes[k], sel[k] * rows);
+   const Estimator learned = [&](const Op& op) -> double {
+      const auto it = est_rows.find(&op);
+      return it != est_rows.end() ? it->second : ctx.rule(op);  // the rule where the network has no answer
+   };
+   parallel_for(n, threads, [&](uint32_t i) {
+      qs[i].prog = lower(*ops[i], learned, LowerOptions{});
+      const double c = cost[root_of[i]];
+      qs[i].cost = std::isfinite(c) ? c : 0.0;
+   });
+   return qs;
 }
 
 }  // namespace rhygpu

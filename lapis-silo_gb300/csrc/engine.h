@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -11,6 +12,7 @@
 
 #include "device.h"
 #include "expr.h"
+#include "planner.h"
 #include "table.h"
 
 namespace rhygpu {
@@ -27,6 +29,7 @@ struct BatchQuery {
    int action = 0;  // 0 = count, 1 = mutations of `column`
    int column = 0;
    double min_proportion = 0.05;  // Mutations rows: minimum proportion of a reported mutation
+   double cost = 0;               // predicted cycles per tile (learned planner); 0 = unknown
 };
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
@@ -138,6 +141,19 @@ class Engine {
    // Tile width that fits the batch's deepest program in the shared-memory budget.
    uint32_t fit_tile_bits(uint32_t requested, uint32_t depth, bool batch = false) const;
 
+   // ---- learned planner ----
+   // Runs every expression through the single-query path in trace mode (program lowered without
+   // early exits) and appends one training sample per operator node. Returns the samples added.
+   size_t planner_collect(const std::vector<std::string>& exprs);
+   PlannerStats planner_train(uint32_t epochs, uint32_t batch, float lr, uint64_t seed);
+   // 0: rule-based ordering; 1: learned (only once a trained network was accepted by the judge).
+   void set_planner_mode(int mode);
+   int planner_mode() const { return use_learned_ ? 1 : 0; }
+   Planner& planner() { return planner_; }
+   // Plans a batch: rule-based, or with the learned planner's estimates (one GPU inference over
+   // all operator nodes of all expressions) and a predicted cost per query. The caller holds mu.
+   std::vector<BatchQuery> plan_batch(const std::vector<std::string>& exprs, uint32_t threads);
+
    const EvItem* d_ev(int column) const { return d_ev_[column]; }
    uint32_t n_ev(int column) const { return n_ev_[column]; }
    uint64_t mutation_payload_bytes(int column) const;
@@ -173,6 +189,10 @@ class Engine {
    int* h_err_ = nullptr;                  // pinned
    uint64_t device_bytes_ = 0;
    BatchState batch_;
+   Planner planner_;
+   bool use_learned_ = false;
+   std::unique_ptr<FeatureContext> fctx_;  // built on first use
+   const FeatureContext& fctx();
    void batch_free();
 };
 

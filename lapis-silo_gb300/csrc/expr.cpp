@@ -933,6 +933,13 @@ struct Lowerer {
    }
 
    void node(const Op& op) {
+      const uint32_t first = static_cast<uint32_t>(prog.code.size());
+      node_body(op);
+      if (opt.record_spans && prog.code.size() > first)
+         prog.spans.push_back(NodeSpan{&op, first, static_cast<uint32_t>(prog.code.size() - 1)});
+   }
+
+   void node_body(const Op& op) {
       switch (op.t) {
          case OpT::EMPTY:
             emit(OP_PUSH_EMPTY);
@@ -1067,6 +1074,12 @@ Program lower(const Op& op, const Estimator& est, const LowerOptions& opt) {
    l.node(op);
    if (l.depth != 1) throw CompilationError("internal error: unbalanced filter program");
    return std::move(l.prog);
+}
+
+OpPtr compile_filter(const std::string& text, const TableImage& t) {
+   ExprPtr e = parse_expression(text, t);
+   ExprPtr r = rewrite(*e, t, Ambiguity::NONE);
+   return compile(*r, t);
 }
 
 Program plan_filter(const std::string& text, const TableImage& t, const Estimator* est, const LowerOptions& opt,

@@ -105,8 +105,15 @@ OpPtr negate(OpPtr op);
 using Estimator = std::function<double(const Op&)>;
 Estimator rule_estimator(const TableImage& t);
 
+// Instructions [first, last] of one operator node: its result is on top of the stack after `last`.
+struct NodeSpan {
+   const Op* op;
+   uint32_t first, last;
+};
+
 struct Program {
    std::vector<Instr> code;
+   std::vector<NodeSpan> spans;  // with LowerOptions::record_spans; the ops belong to the caller's tree
    uint32_t max_depth = 0;   // tiles of stack needed
    uint32_t n_leaves = 0;
    uint32_t n_ctr_leaves = 0;  // PUSH_SCAN / PUSH_DICT leaves, numbered 1.. in their c field
@@ -116,7 +123,11 @@ struct Program {
 struct LowerOptions {
    bool early_exit = true;   // emit JZ/JFULL after partial intersections/unions
    bool reorder = true;      // order children by the estimator
+   bool record_spans = false;  // fill Program::spans
 };
+
+// parse -> rewrite(NONE) -> compile, without lowering.
+OpPtr compile_filter(const std::string& text, const TableImage& t);
 
 Program lower(const Op& op, const Estimator& est, const LowerOptions& opt);
 

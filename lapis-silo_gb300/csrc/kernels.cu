@@ -348,8 +348,12 @@ __device__ void push_date(uint4* t4, const TileCtx& c, const DevDateCol* __restr
 // Runs a filter program for one tile. The result is left in stack slot 0, complete for the thread
 // that owns each uint4 word (see valid4); a barrier is needed before other threads read it.
 // Returns false on a malformed program (the error flag is set).
+// With `trace` (trace mode of the single-query kernel, for planner training) every executed
+// instruction pc stores trace[2 pc] = its cycles (first thread, between barriers around the
+// instruction) and trace[2 pc + 1] = the population count of the top of the stack after it.
 __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, uint32_t ncode, uint32_t* stk,
-                            uint32_t cap, const LeafCache& lc, int* err) {
+                            uint32_t cap, const LeafCache& lc, int* err, uint32_t* trace = nullptr) {
+   __shared__ uint32_t tred[FT / 32];
    const uint32_t WW = c.W >> 5, W4 = c.W >> 7;
    uint4* stk4 = reinterpret_cast<uint4*>(stk);
    uint32_t sp = 0;
@@ -360,6 +364,11 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
       if (++steps > 4u * MAX_PROGRAM) {  // jumps only go forward; this bounds a corrupted program
          if (threadIdx.x == 0) atomicExch(err, 3);
          return false;
+      }
+      long long t_start = 0;
+      if (trace) {
+         __syncthreads();
+         t_start = clock64();
       }
       Instr in;
       {
@@ -546,6 +555,28 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             if (threadIdx.x == 0) atomicExch(err, 5);
             return false;
       }
+      if (trace) {
+         __syncthreads();
+         const long long t_end = clock64();
+         uint32_t n = 0;
+         if (sp >= 1) {
+            const uint4* x = stk4 + (sp - 1) * W4;
+            for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x)
+               n += __popc(x[w4].x) + __popc(x[w4].y) + __popc(x[w4].z) + __popc(x[w4].w);
+         }
+         n = __reduce_add_sync(0xFFFFFFFFu, n);
+         if ((threadIdx.x & 31) == 0) tred[threadIdx.x >> 5] = n;
+         __syncthreads();
+         if (threadIdx.x == 0) {
+            uint32_t s = 0;
+            for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) s += tred[w];
+            const long long dt = t_end - t_start;
+            trace[2 * pc] = static_cast<uint32_t>(dt < 1 ? 1 : (dt > 0xFFFFFFFFll ? 0xFFFFFFFFll : dt));
+            trace[2 * pc + 1] = s;
+         }
+         __syncthreads();
+         synced = true;
+      }
       pc = next;
    }
    if (sp != 1) {
@@ -583,7 +614,8 @@ __device__ __forceinline__ uint32_t result_popc(const uint32_t* smem, uint32_t W
 
 __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__ tab, const Instr* __restrict__ code,
                                                     uint32_t ncode, uint32_t n_leaves, uint32_t tile_bits, uint32_t cap,
-                                                    uint32_t* __restrict__ out_tiles, unsigned long long* count, int* err) {
+                                                    uint32_t* __restrict__ out_tiles, unsigned long long* count, int* err,
+                                                    uint32_t* trace) {
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
    __shared__ LeafCache lc;
@@ -602,7 +634,9 @@ __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__
       clear_leaves(lc, min(n_leaves & 0xFFFFu, LC_LEAVES), min(n_leaves >> 16, LC_COV));
       __syncthreads();
       stage_leaves(lc, c, code, ncode);
-      if (!run_program(c, code, ncode, smem, cap, lc, err)) return;
+      if (!run_program(c, code, ncode, smem, cap, lc, err,
+                       trace ? trace + static_cast<size_t>(blockIdx.x) * ncode * 2 : nullptr))
+         return;
    }
    const uint32_t pc =
       result_popc(smem, tile_bits, out_tiles ? out_tiles + static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5) : nullptr);
@@ -662,14 +696,14 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
 
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
                           uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
-                          int* d_err, void* stream) {
+                          int* d_err, void* stream, uint32_t* d_trace) {
    const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
    cudaError_t e = cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
    if (e != cudaSuccess) return e;
    filter_kernel<<<nchunks * T, FT, smem, static_cast<cudaStream_t>(stream)>>>(
-      d_table, d_code, ncode, n_leaves, tile_bits, stack_tiles, d_out_tiles, d_count, d_err);
+      d_table, d_code, ncode, n_leaves, tile_bits, stack_tiles, d_out_tiles, d_count, d_err, d_trace);
    return cudaGetLastError();
 }
 

@@ -87,6 +87,21 @@ class BatchInfo(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+class PlannerStats(C.Structure):
+    _fields_ = [("n_train", C.c_uint32), ("n_val", C.c_uint32), ("epochs", C.c_uint32),
+                ("train_loss", C.c_float), ("val_loss", C.c_float),
+                ("qerr_learned_median", C.c_float), ("qerr_rule_median", C.c_float),
+                ("qerr_learned_p90", C.c_float), ("qerr_rule_p90", C.c_float),
+                ("cost_err_median", C.c_float), ("train_ms", C.c_float), ("accepted", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+PLANNER_FEATURES = 24
+MLP_NPARAM = 5890
+
+
 class MutationRow(C.Structure):
     _fields_ = [("position", C.c_uint32), ("from_", C.c_char), ("to", C.c_char), ("count", C.c_uint32),
                 ("coverage", C.c_uint32), ("proportion", C.c_double)]
@@ -140,6 +155,14 @@ def lib():
         "rhy_batch_capture_ex": (I, [P, P, I, I]),
         "rhy_batch_launch_parts": (I, [P, P, U32]),
         "rhy_mutations_noalloc": (I, [P, U32, P, P, P, P]),
+        "rhy_plan_features": (I, [P, C.c_char_p, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_planner_collect": (I, [P, P, U32, C.POINTER(C.c_size_t)]),
+        "rhy_planner_train": (I, [P, U32, U32, C.c_float, U64, C.POINTER(PlannerStats)]),
+        "rhy_planner_mode": (I, [P, I]),
+        "rhy_planner_samples": (I, [P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_planner_weights": (I, [P, P]),
+        "rhy_planner_predict": (I, [P, P, U32, P, P]),
+        "rhy_mlp_gradient": (I, [P, P, P, P, U32, P, P, P]),
         "rhy_close": (None, [P]),
     }
     for name, (res, args) in sig.items():
@@ -271,6 +294,14 @@ class Table:
         n, d = C.c_uint32(), C.c_uint32()
         _check(lib().rhy_plan(self._h, expr.encode(), buf, 1 << 20, C.byref(n), C.byref(d)))
         return buf.value.decode(), n.value, d.value
+
+    def plan_features(self, expr: str) -> np.ndarray:
+        """Planner features of every operator node of the compiled expression (preorder)."""
+        n = C.c_size_t()
+        _check(lib().rhy_plan_features(self._h, expr.encode(), None, 0, C.byref(n)))
+        x = np.zeros((max(n.value, 1), PLANNER_FEATURES), np.float32)
+        _check(lib().rhy_plan_features(self._h, expr.encode(), _ptr(x), n.value, C.byref(n)))
+        return x[:n.value]
 
     def mutation_rows(self, column: int, counts: np.ndarray, min_proportion: float):
         """Rows of the Mutations action (reference: mutations_node.cpp:292-366) from symbol counts."""
@@ -430,6 +461,54 @@ class Device:
         Enqueued on `stream`; synchronise it before reading d_counts."""
         _check(lib().rhy_mutations_noalloc(self._h, column, C.c_void_p(d_filter), C.c_void_p(d_filter_count),
                                            C.c_void_p(d_counts), stream))
+
+    # ---- learned planner ----
+    def planner_collect(self, exprs) -> int:
+        arr = (C.c_char_p * max(len(exprs), 1))(*[e.encode() for e in exprs])
+        n = C.c_size_t()
+        _check(lib().rhy_planner_collect(self._h, C.cast(arr, C.c_void_p), len(exprs), C.byref(n)))
+        return n.value
+
+    def planner_train(self, epochs: int = 60, batch: int = 1024, lr: float = 2e-3, seed: int = 1) -> dict:
+        st = PlannerStats()
+        _check(lib().rhy_planner_train(self._h, epochs, batch, lr, seed, C.byref(st)))
+        return st.as_dict()
+
+    def planner_mode(self, mode: int):
+        _check(lib().rhy_planner_mode(self._h, mode))
+
+    def planner_samples(self):
+        n = C.c_size_t()
+        _check(lib().rhy_planner_samples(self._h, None, None, 0, C.byref(n)))
+        x = np.zeros((max(n.value, 1), PLANNER_FEATURES), np.float32)
+        y = np.zeros((max(n.value, 1), 3), np.float32)
+        _check(lib().rhy_planner_samples(self._h, _ptr(x), _ptr(y), n.value, C.byref(n)))
+        return x[:n.value], y[:n.value]
+
+    def planner_predict(self, x: np.ndarray):
+        x = np.ascontiguousarray(x, np.float32)
+        n = x.shape[0]
+        sel = np.zeros(max(n, 1), np.float64)
+        cost = np.zeros(max(n, 1), np.float64)
+        _check(lib().rhy_planner_predict(self._h, _ptr(x), n, _ptr(sel), _ptr(cost)))
+        return sel[:n], cost[:n]
+
+    def planner_weights(self) -> np.ndarray:
+        w = np.zeros(MLP_NPARAM, np.float32)
+        _check(lib().rhy_planner_weights(self._h, _ptr(w)))
+        return w
+
+    def mlp_gradient(self, w: np.ndarray, x: np.ndarray, t: np.ndarray):
+        """One forward + backward of the planner network on the device: (gradient, loss, outputs)."""
+        w = np.ascontiguousarray(w, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        n = x.shape[0]
+        grad = np.zeros(MLP_NPARAM, np.float32)
+        loss = np.zeros(1, np.float32)
+        y = np.zeros((max(n, 1), 2), np.float32)
+        _check(lib().rhy_mlp_gradient(self._h, _ptr(w), _ptr(x), _ptr(t), n, _ptr(grad), _ptr(loss), _ptr(y)))
+        return grad, float(loss[0]), y[:n]
 
     def mutation_bytes(self, column: int = 0) -> tuple[int, int]:
         p, d = C.c_uint64(), C.c_uint64()
