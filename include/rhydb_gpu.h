@@ -41,7 +41,8 @@ enum {
    RHY_COMPILATION = 2,     /* QueryCompilationException in the reference */
    RHY_CUDA = 3,
    RHY_INVALID_ARGUMENT = 4,
-   RHY_INTERNAL = 5
+   RHY_INTERNAL = 5,
+   RHY_TIMEOUT = 6          /* rhy_server_result: not done within the timeout */
 };
 
 typedef struct RhyTable RhyTable;
@@ -259,6 +260,43 @@ int rhy_planner_predict(RhyDevice* d, const float* x, uint32_t n, double* sel, d
  * outputs y[n][2]. Leaves the planner untouched. */
 int rhy_mlp_gradient(RhyDevice* d, const float* w, const float* x, const float* t, uint32_t n, float* grad, float* loss,
                      float* y);
+
+/* ---- serving (continuous batching; no counterpart in the reference, which runs one query per
+ * request thread, api.cpp:39-51) ----
+ * A loop thread admits submitted requests into micro-batches while the in-flight queries fit
+ * max_inflight and their device buffers fit memory_budget, and keeps `streams` micro-batches in
+ * flight, so requests that arrive while others run are admitted as slots and memory free up and
+ * overlap on the device. A partial micro-batch launches once its oldest request waited
+ * max_wait_ms (at once when the device is idle). Actions: 0 Aggregated count, 1 Mutations rows
+ * (min_proportion, column), 2 Details (the first k row ids, ascending). Results equal those of the
+ * same query alone. */
+typedef struct RhyServer RhyServer;
+typedef struct {
+   uint32_t max_batch;       /* queries per micro-batch (default 512) */
+   uint32_t streams;         /* micro-batches in flight (default 3) */
+   uint32_t max_inflight;    /* admitted, unfinished queries (default 4096) */
+   uint64_t memory_budget;   /* device bytes of in-flight work; 0 = a quarter of the free memory */
+   double max_wait_ms;       /* default 0.25 */
+} RhyServerConfig;
+typedef struct {
+   uint64_t submitted, completed, rejected, batches;
+   double p50_ms, p99_ms, mean_batch, qps;
+   uint64_t peak_bytes, budget_bytes;
+   uint32_t peak_inflight;
+} RhyServerStats;
+int rhy_server_start(RhyDevice* d, const RhyServerConfig* cfg /* NULL: defaults */, RhyServer** out);
+/* Validates and queues a request (user errors are returned here). */
+int rhy_server_submit(RhyServer* s, const char* expr, int action, uint32_t column, double min_proportion, uint32_t k,
+                      uint64_t* id);
+/* Waits for a request (timeout_ms < 0: no limit; RHY_TIMEOUT if not done) and copies its result:
+ * the filter count, Mutations rows, Details ids and the latency from submission. When rows or ids
+ * do not fit their caps only *n_rows / *n_ids are set, RHY_INVALID_ARGUMENT is returned and the
+ * result is kept for another call; otherwise it is released. */
+int rhy_server_result(RhyServer* s, uint64_t id, double timeout_ms, uint64_t* count, RhyMutationRow* rows,
+                      size_t rows_cap, size_t* n_rows, uint32_t* ids, size_t ids_cap, size_t* n_ids, double* latency_ms);
+int rhy_server_stats(RhyServer* s, RhyServerStats* out);
+/* Finishes every queued request, stops the loop and frees the server. */
+void rhy_server_stop(RhyServer* s);
 
 void rhy_close(RhyDevice* d);
 

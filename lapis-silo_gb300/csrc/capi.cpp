@@ -11,6 +11,7 @@
 #include "../../include/rhydb_gpu.h"
 #include "dataset.h"
 #include "engine.h"
+#include "server.h"
 #include "expr.h"
 #include "noalloc.h"
 #include "table.h"
@@ -418,7 +419,8 @@ std::vector<rhygpu::BatchQuery> make_batch(RhyDevice* d, const char* const* expr
    for (uint32_t i = 0; i < n; ++i) {
       qs[i].action = actions ? actions[i] : 0;
       qs[i].column = columns ? static_cast<int>(columns[i]) : 0;
-      if (qs[i].action != 0 && qs[i].action != 1) throw std::invalid_argument("action must be 0 (count) or 1 (mutations)");
+      if (qs[i].action < 0 || qs[i].action > 2)
+         throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
    }
    return qs;
 }
@@ -427,7 +429,7 @@ void copy_batch_results(RhyDevice* d, uint32_t n, uint64_t* counts, uint32_t* co
    rhygpu::Engine& e = *d->engine;
    const auto& b = e.batch();
    if (n != b.n_queries) throw std::invalid_argument("result arrays do not match the prepared batch");
-   e.check_error_flag();
+   e.check_batch_error(e.batch_state());
    for (uint32_t i = 0; i < n; ++i) {
       if (counts) counts[i] = e.batch_count(i);
       if (mut_counts && mut_counts[i]) {
@@ -797,6 +799,98 @@ int rhy_mlp_gradient(RhyDevice* d, const float* w, const float* x, const float* 
       net.set_master(w);
       net.gradient(x, t, n, grad, loss, y);
    });
+}
+
+// ---- serving ----
+
+struct RhyServer {
+   std::unique_ptr<rhygpu::Server> server;
+};
+
+int rhy_server_start(RhyDevice* d, const RhyServerConfig* cfg, RhyServer** out) {
+   return guarded([&] {
+      need(d, "device");
+      need(out, "out");
+      *out = nullptr;
+      rhygpu::ServerConfig c;
+      if (cfg) {
+         if (cfg->max_batch) c.max_batch = cfg->max_batch;
+         if (cfg->streams) c.streams = cfg->streams;
+         if (cfg->max_inflight) c.max_inflight = cfg->max_inflight;
+         c.memory_budget = cfg->memory_budget;
+         if (cfg->max_wait_ms >= 0) c.max_wait_ms = cfg->max_wait_ms;
+      }
+      auto s = std::make_unique<RhyServer>();
+      s->server = std::make_unique<rhygpu::Server>(*d->engine, c);
+      *out = s.release();
+   });
+}
+
+int rhy_server_submit(RhyServer* s, const char* expr, int action, uint32_t column, double min_proportion, uint32_t k,
+                      uint64_t* id) {
+   return guarded([&] {
+      need(s, "server");
+      need(expr, "expression");
+      need(id, "id");
+      *id = s->server->submit(expr, action, static_cast<int>(column), min_proportion, k);
+   });
+}
+
+int rhy_server_result(RhyServer* s, uint64_t id, double timeout_ms, uint64_t* count, RhyMutationRow* rows,
+                      size_t rows_cap, size_t* n_rows, uint32_t* ids, size_t ids_cap, size_t* n_ids, double* latency_ms) {
+   int code = RHY_OK;
+   const int rc = guarded([&] {
+      need(s, "server");
+      std::shared_ptr<rhygpu::ServeRequest> r = s->server->wait(id, timeout_ms);
+      if (!r) {
+         code = RHY_TIMEOUT;
+         throw std::runtime_error("request " + std::to_string(id) + " not done within the timeout");
+      }
+      if (!r->error.empty()) {
+         s->server->release(id);
+         code = r->error.find("device program error") != std::string::npos ? RHY_COMPILATION : RHY_CUDA;
+         throw std::runtime_error(r->error);
+      }
+      if (n_rows) *n_rows = r->rows.size();
+      if (n_ids) *n_ids = r->ids.size();
+      if (count) *count = r->count;
+      if (latency_ms) *latency_ms = 1000.0 * (r->t_done - r->t_submit);
+      if ((!r->rows.empty() && (!rows || rows_cap < r->rows.size())) || (!r->ids.empty() && (!ids || ids_cap < r->ids.size())))
+         throw std::invalid_argument("result buffers too small: " + std::to_string(r->rows.size()) + " rows, " +
+                                     std::to_string(r->ids.size()) + " ids");
+      if (!r->rows.empty()) std::memcpy(rows, r->rows.data(), r->rows.size() * sizeof(RhyMutationRow));
+      if (!r->ids.empty()) std::memcpy(ids, r->ids.data(), r->ids.size() * sizeof(uint32_t));
+      s->server->release(id);
+   });
+   return rc == RHY_INTERNAL && code != RHY_OK ? code : rc;
+}
+
+int rhy_server_stats(RhyServer* s, RhyServerStats* out) {
+   return guarded([&] {
+      need(s, "server");
+      need(out, "out");
+      const rhygpu::ServerStats st = s->server->stats();
+      out->submitted = st.submitted;
+      out->completed = st.completed;
+      out->rejected = st.rejected;
+      out->batches = st.batches;
+      out->p50_ms = st.p50_ms;
+      out->p99_ms = st.p99_ms;
+      out->mean_batch = st.mean_batch;
+      out->qps = st.qps;
+      out->peak_bytes = st.peak_bytes;
+      out->budget_bytes = st.budget_bytes;
+      out->peak_inflight = st.peak_inflight;
+   });
+}
+
+void rhy_server_stop(RhyServer* s) {
+   if (!s) return;
+   try {
+      s->server->stop();
+   } catch (...) {
+   }
+   delete s;
 }
 
 void rhy_close(RhyDevice* d) { delete d; }

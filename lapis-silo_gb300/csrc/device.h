@@ -192,6 +192,11 @@ void launch_rows_write(const DevTable* d_table, const DevSeqCol& col_host, uint3
                        uint32_t nq, const double* d_min_prop, const uint32_t* d_blk, DevMutationRow* d_rows,
                        void* stream);
 
+// Details: the first k_of[q] row ids (ascending) of each of nq dense row sets (nchunks * CHUNK_WORDS
+// words apart) to d_ids + out_off[q]; d_n[q] receives min(k, |row set|).
+void launch_first_k(const uint32_t* d_tiles, uint32_t nq, uint32_t nchunks, const uint32_t* d_k,
+                    const uint32_t* d_out_off, uint32_t* d_ids, uint32_t* d_n, void* stream);
+
 // Events per CTA of the coverage pass.
 constexpr uint32_t EV_PER_CTA = 8192;
 

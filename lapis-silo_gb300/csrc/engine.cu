@@ -225,7 +225,7 @@ Engine::~Engine() {
    cudaSetDevice(device_);
    if (stream_) cudaStreamSynchronize(stream_);
    cudaDeviceSynchronize();
-   batch_free();
+   batch_free(batch_);
    for (void* p : allocs_) cudaFree(p);
    if (h_code_) cudaFreeHost(h_code_);
    if (h_count_) cudaFreeHost(h_count_);
@@ -374,25 +374,47 @@ void grow_host(T*& p, size_t n, size_t& cap) {
 }
 }  // namespace
 
-void Engine::batch_free() {
-   BatchState& b = batch_;
+void Engine::batch_free(BatchState& b) {
    if (b.graph) cudaGraphExecDestroy(b.graph);
    for (void* p : {static_cast<void*>(b.h_code), static_cast<void*>(b.h_q), static_cast<void*>(b.h_items),
                    static_cast<void*>(b.h_slot_query), static_cast<void*>(b.h_counts), static_cast<void*>(b.h_mcounts),
-                   static_cast<void*>(b.h_minprop), static_cast<void*>(b.h_rowblk)})
+                   static_cast<void*>(b.h_minprop), static_cast<void*>(b.h_rowblk), static_cast<void*>(b.h_err),
+                   static_cast<void*>(b.h_k), static_cast<void*>(b.h_ids), static_cast<void*>(b.h_nids)})
       if (p) cudaFreeHost(p);
    for (void* p : {static_cast<void*>(b.d_code), static_cast<void*>(b.d_q), static_cast<void*>(b.d_items),
                    static_cast<void*>(b.d_slot_query), static_cast<void*>(b.d_counts), static_cast<void*>(b.d_next),
                    static_cast<void*>(b.d_tiles), static_cast<void*>(b.d_mcounts), static_cast<void*>(b.d_mscratch),
                    static_cast<void*>(b.d_masks), static_cast<void*>(b.d_minprop), static_cast<void*>(b.d_rowblk),
-                   static_cast<void*>(b.d_rows)})
+                   static_cast<void*>(b.d_rows), static_cast<void*>(b.d_err), static_cast<void*>(b.d_k),
+                   static_cast<void*>(b.d_ids), static_cast<void*>(b.d_nids)})
       if (p) cudaFree(p);
    b = BatchState{};
 }
 
-void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested_tile_bits) {
+size_t Engine::batch_device_bytes(const std::vector<BatchQuery>& qs, uint32_t tile_bits) const {
+   const uint32_t W = tile_bits ? tile_bits : batch_tile_bits;
+   const size_t tiles = static_cast<size_t>(nchunks()) * (CHUNK_ROWS / W);
+   const size_t tile_bytes = static_cast<size_t>(nchunks()) * CHUNK_WORDS * 4;
+   size_t bytes = 0;
+   std::vector<uint32_t> per_col(table_.seq.size(), 0);
+   for (const auto& q : qs) {
+      bytes += q.prog.code.size() * sizeof(Instr) + sizeof(QueryDesc) + tiles * sizeof(WorkItem) + 8;
+      if (q.action == 1 && q.column >= 0 && static_cast<size_t>(q.column) < per_col.size()) {
+         const DevSeqCol& dc = view_.seq[q.column];
+         bytes += tile_bytes + static_cast<size_t>(dc.nsym) * dc.L * 4 + mut_scratch_words(dc.L) * 4 + 16 +
+                  (rows_blocks(dc.L) + 1) * 4 + static_cast<size_t>(dc.L) * 2 * sizeof(DevMutationRow);
+         ++per_col[q.column];
+      } else if (q.action == 2) {
+         bytes += tile_bytes + static_cast<size_t>(q.k) * 4 + 16;
+      }
+   }
+   for (size_t c = 0; c < per_col.size(); ++c)
+      if (per_col[c]) bytes += mutations_batch_mask_bytes(per_col[c], nchunks());
+   return bytes;
+}
+
+void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uint32_t requested_tile_bits) {
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-   BatchState& b = batch_;
    if (b.graph) {
       cudaGraphExecDestroy(b.graph);
       b.graph = nullptr;
@@ -405,13 +427,17 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
       ncode += q.prog.code.size();
       if (q.action == 1 && (q.column < 0 || static_cast<size_t>(q.column) >= table_.seq.size()))
          throw std::invalid_argument("no such sequence column");
+      if (q.action < 0 || q.action > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
    }
    const uint32_t W = fit_tile_bits(requested_tile_bits, depth, true);
    const uint32_t tiles_per_query = nchunks() * (CHUNK_ROWS / W);
-   // mutation slots grouped by column
+   // slots (queries whose row set is kept): Mutations grouped by column, then Details
    std::vector<std::vector<uint32_t>> by_col(table_.seq.size());
-   for (uint32_t i = 0; i < n; ++i)
+   std::vector<uint32_t> details;
+   for (uint32_t i = 0; i < n; ++i) {
       if (qs[i].action == 1) by_col[qs[i].column].push_back(i);
+      if (qs[i].action == 2) details.push_back(i);
+   }
    b.groups.clear();
    b.slot_of_query.assign(n, UINT32_MAX);
    std::vector<uint32_t> slot_query;
@@ -432,9 +458,18 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
       mask_bytes = std::max(mask_bytes, mutations_batch_mask_bytes(g.n, nchunks()));
       b.groups.push_back(g);
    }
+   const uint32_t n_mut = static_cast<uint32_t>(slot_query.size());
+   for (uint32_t qi : details) {
+      b.slot_of_query[qi] = static_cast<uint32_t>(slot_query.size());
+      slot_query.push_back(qi);
+   }
    const uint32_t nslots = static_cast<uint32_t>(slot_query.size());
+   const uint32_t n_det = nslots - n_mut;
    const size_t nitems = static_cast<size_t>(n) * tiles_per_query;
    if (nitems > 0xFFFFFFFFull) throw std::invalid_argument("batch too large");
+   size_t n_ids = 0;
+   for (uint32_t qi : details) n_ids += qs[qi].k;
+   if (n_ids > 0xFFFFFFFFull) throw std::invalid_argument("details: too many row ids requested");
    grow_host(b.h_code, ncode, b.hc_code);
    grow_device(b.d_code, b.dc_code, ncode);
    grow_host(b.h_q, n, b.hc_q);
@@ -455,13 +490,31 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
    grow_device(b.d_minprop, b.dc_minprop, nslots);
    grow_host(b.h_rowblk, static_cast<size_t>(n_blk) + 1, b.hc_rowblk);
    grow_device(b.d_rowblk, b.dc_rowblk, static_cast<size_t>(n_blk) + 1);
+   grow_host(b.h_err, 1, b.hc_err);
+   grow_device(b.d_err, b.dc_err, 1);
+   grow_host(b.h_k, 2 * static_cast<size_t>(n_det), b.hc_k);
+   grow_device(b.d_k, b.dc_k, 2 * static_cast<size_t>(n_det));
+   grow_host(b.h_ids, n_ids, b.hc_ids);
+   grow_device(b.d_ids, b.dc_ids, n_ids);
+   grow_host(b.h_nids, n_det, b.hc_nids);
+   grow_device(b.d_nids, b.dc_nids, n_det);
    for (uint32_t k = 0; k < nslots; ++k) {
       const double mp = qs[slot_query[k]].min_proportion;
       if (!(mp >= 0.0 && mp <= 1.0)) throw std::invalid_argument("min_proportion must lie in [0, 1]");
       b.h_minprop[k] = mp;
    }
+   uint32_t koff = 0;
+   for (uint32_t j = 0; j < n_det; ++j) {  // k of each Details slot, then its offset into the ids
+      b.h_k[j] = qs[slot_query[n_mut + j]].k;
+      b.h_k[n_det + j] = koff;
+      koff += b.h_k[j];
+   }
+   *b.h_err = 0;
    b.n_blk = n_blk;
    b.n_rows = 0;
+   b.n_mut_slots = n_mut;
+   b.n_details = n_det;
+   b.n_ids = static_cast<uint32_t>(n_ids);
    // programs, query descriptors, work items
    size_t off = 0;
    for (uint32_t i = 0; i < n; ++i) {
@@ -500,9 +553,8 @@ void Engine::batch_prepare(const std::vector<BatchQuery>& qs, uint32_t requested
    b.grid = static_cast<uint32_t>(props) * static_cast<uint32_t>(filter_batch_blocks_per_sm(smem));
 }
 
-void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t parts) {
+void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool copy_out, uint32_t parts) {
    s = stream_for(s);
-   BatchState& b = batch_;
    if (b.n_queries == 0) return;
    if (copy_in) {
       cuda_check(cudaMemcpyAsync(b.d_code, b.h_code, b.n_code * sizeof(Instr), cudaMemcpyHostToDevice, s), "H2D");
@@ -515,6 +567,11 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
                     "H2D");
          cuda_check(cudaMemcpyAsync(b.d_minprop, b.h_minprop, b.n_slots * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
       }
+      if (b.n_details)
+         cuda_check(cudaMemcpyAsync(b.d_k, b.h_k, 2 * static_cast<size_t>(b.n_details) * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, s),
+                    "H2D");
+      cuda_check(cudaMemsetAsync(b.d_err, 0, sizeof(int), s), "memset");
    }
    if (parts & 1) {
       cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
@@ -522,7 +579,7 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
       if (b.counts_words) cuda_check(cudaMemsetAsync(b.d_mcounts, 0, b.counts_words * 4, s), "memset");
       if (b.scratch_words) cuda_check(cudaMemsetAsync(b.d_mscratch, 0, b.scratch_words * 4, s), "memset");
       cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.tile_bits, b.max_depth,
-                                     b.d_tiles, b.d_counts, b.d_next, b.grid, d_err, s),
+                                     b.d_tiles, b.d_counts, b.d_next, b.grid, b.d_err, s),
                  "filter batch launch");
    }
    const size_t words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
@@ -534,36 +591,59 @@ void Engine::batch_enqueue(cudaStream_t s, bool copy_in, bool copy_out, uint32_t
                              (parts >> 1) & BMUT_PART_ALL);
       cuda_check(cudaGetLastError(), "mutations batch launch");
    }
+   if (b.n_details && (parts & 1)) {
+      launch_first_k(b.d_tiles + static_cast<size_t>(b.n_mut_slots) * words, b.n_details, nchunks(), b.d_k,
+                     b.d_k + b.n_details, b.d_ids, b.d_nids, s);
+      cuda_check(cudaGetLastError(), "details launch");
+   }
    if (copy_out) {
       cuda_check(cudaMemcpyAsync(b.h_counts, b.d_counts, b.n_queries * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
                  "D2H");
       if (b.counts_words)
          cuda_check(cudaMemcpyAsync(b.h_mcounts, b.d_mcounts, b.counts_words * 4, cudaMemcpyDeviceToHost, s), "D2H");
-      cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+      copy_details(b, s);
+      cuda_check(cudaMemcpyAsync(b.h_err, b.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
    }
 }
 
-size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count) {
+void Engine::copy_details(BatchState& b, cudaStream_t s) {
+   if (!b.n_details) return;
+   cuda_check(cudaMemcpyAsync(b.h_nids, b.d_nids, b.n_details * sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "D2H");
+   if (b.n_ids) cuda_check(cudaMemcpyAsync(b.h_ids, b.d_ids, b.n_ids * sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "D2H");
+}
+
+void Engine::check_batch_error(BatchState& b) {
+   if (b.h_err && *b.h_err != 0) {
+      const int e = *b.h_err;
+      *b.h_err = 0;
+      throw CompilationError("device program error " + std::to_string(e));
+   }
+}
+
+void Engine::rows_phase1(BatchState& b, cudaStream_t s) {
    s = stream_for(s);
-   BatchState& b = batch_;
-   if (b.n_queries == 0) return 0;
-   batch_enqueue(s, true, false);
+   if (b.n_queries == 0) return;
+   batch_enqueue(b, s, true, false);
    cuda_check(cudaMemcpyAsync(b.h_counts, b.d_counts, b.n_queries * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
               "D2H");
-   cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+   copy_details(b, s);
+   cuda_check(cudaMemcpyAsync(b.h_err, b.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
    for (const auto& g : b.groups)
       launch_rows_count(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), b.d_mcounts + g.counts_off, g.n,
                         b.d_minprop + g.slot_begin, b.d_rowblk + g.blk_off, s);
-   if (b.n_slots) {
+   if (b.n_mut_slots) {
       launch_rows_scan(b.d_rowblk, b.n_blk, s);
       cuda_check(cudaMemcpyAsync(b.h_rowblk, b.d_rowblk, (static_cast<size_t>(b.n_blk) + 1) * sizeof(uint32_t),
                                  cudaMemcpyDeviceToHost, s),
                  "D2H");
    }
    cuda_check(cudaGetLastError(), "rows launch");
-   cuda_check(cudaStreamSynchronize(s), "batch rows");
-   check_error_flag();
-   const size_t total = b.n_slots ? b.h_rowblk[b.n_blk] : 0;
+}
+
+size_t Engine::rows_phase2(BatchState& b, cudaStream_t s, DevMutationRow* rows, size_t cap) {
+   s = stream_for(s);
+   check_batch_error(b);
+   const size_t total = b.n_mut_slots ? b.h_rowblk[b.n_blk] : 0;
    b.n_rows = total;
    if (total) {
       grow_device(b.d_rows, b.dc_rows, total);
@@ -573,21 +653,45 @@ size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint
       cuda_check(cudaGetLastError(), "rows launch");
       if (rows && total <= cap)
          cuda_check(cudaMemcpyAsync(rows, b.d_rows, total * sizeof(DevMutationRow), cudaMemcpyDeviceToHost, s), "D2H");
-      cuda_check(cudaStreamSynchronize(s), "batch rows");
    }
+   return total;
+}
+
+void Engine::row_range(const BatchState& b, uint32_t i, uint64_t* begin, uint32_t* count) const {
+   *begin = 0;
+   *count = 0;
+   const uint32_t slot = b.slot_of_query[i];
+   if (slot == UINT32_MAX) return;
+   for (const auto& g : b.groups) {
+      if (slot < g.slot_begin || slot >= g.slot_begin + g.n) continue;
+      const uint32_t nb = rows_blocks(view_.seq[g.column].L);
+      const size_t k = g.blk_off + static_cast<size_t>(slot - g.slot_begin) * nb;
+      *begin = b.h_rowblk[k];
+      *count = b.h_rowblk[k + nb] - b.h_rowblk[k];
+   }
+}
+
+const uint32_t* Engine::details_ids(const BatchState& b, uint32_t i, uint32_t* n) const {
+   *n = 0;
+   const uint32_t slot = b.slot_of_query[i];
+   if (slot == UINT32_MAX || slot < b.n_mut_slots) return nullptr;
+   const uint32_t j = slot - b.n_mut_slots;
+   *n = b.h_nids[j];
+   return b.h_ids + b.h_k[b.n_details + j];
+}
+
+size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count) {
+   s = stream_for(s);
+   BatchState& b = batch_;
+   if (b.n_queries == 0) return 0;
+   rows_phase1(b, s);
+   cuda_check(cudaStreamSynchronize(s), "batch rows");
+   const size_t total = rows_phase2(b, s, rows, cap);
+   cuda_check(cudaStreamSynchronize(s), "batch rows");
    for (uint32_t i = 0; i < b.n_queries; ++i) {
-      const uint32_t slot = b.slot_of_query[i];
-      uint64_t begin = 0;
-      uint32_t count = 0;
-      if (slot != UINT32_MAX) {
-         for (const auto& g : b.groups) {
-            if (slot < g.slot_begin || slot >= g.slot_begin + g.n) continue;
-            const uint32_t nb = rows_blocks(view_.seq[g.column].L);
-            const size_t k = g.blk_off + static_cast<size_t>(slot - g.slot_begin) * nb;
-            begin = b.h_rowblk[k];
-            count = b.h_rowblk[k + nb] - b.h_rowblk[k];
-         }
-      }
+      uint64_t begin;
+      uint32_t count;
+      row_range(b, i, &begin, &count);
       if (row_begin) row_begin[i] = begin;
       if (row_count) row_count[i] = count;
    }
@@ -614,7 +718,7 @@ void Engine::batch_capture(cudaStream_t s, bool copy_in, bool copy_out) {
    cudaGraph_t g = nullptr;
    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
    try {
-      batch_enqueue(s, copy_in, copy_out);
+      batch_enqueue(b, s, copy_in, copy_out);
    } catch (...) {
       cudaStreamEndCapture(s, &g);
       if (g) cudaGraphDestroy(g);
@@ -635,7 +739,7 @@ void Engine::batch_replay(cudaStream_t s) {
 const uint32_t* Engine::batch_mutation_counts(uint32_t query) const {
    const BatchState& b = batch_;
    const uint32_t slot = b.slot_of_query.at(query);
-   if (slot == UINT32_MAX) return nullptr;
+   if (slot == UINT32_MAX || slot >= b.n_mut_slots) return nullptr;
    for (const auto& g : b.groups) {
       if (slot >= g.slot_begin && slot < g.slot_begin + g.n) {
          const DevSeqCol& dc = view_.seq[g.column];

@@ -23,13 +23,15 @@ struct CudaError : std::runtime_error {
 
 void cuda_check(cudaError_t e, const char* what);
 
-// One query of a batch.
+// One query of a batch. Actions: 0 = Aggregated count, 1 = Mutations of `column`, 2 = Details
+// (the first k row ids of the filter, ascending).
 struct BatchQuery {
    Program prog;
    int action = 0;  // 0 = count, 1 = mutations of `column`
    int column = 0;
    double min_proportion = 0.05;  // Mutations rows: minimum proportion of a reported mutation
    double cost = 0;               // predicted cycles per tile (learned planner); 0 = unknown
+   uint32_t k = 1000;             // Details: number of row ids returned (the first ones)
 };
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
@@ -67,14 +69,24 @@ struct BatchState {
    double* d_minprop = nullptr;
    uint32_t* d_rowblk = nullptr;
    DevMutationRow* d_rows = nullptr;
-   uint32_t n_blk = 0;                // row-block table entries (all slots)
-   size_t n_rows = 0;                 // rows of the last batch_rows
+   int* d_err = nullptr;              // error flag of this batch's kernels
+   int* h_err = nullptr;              // pinned
+   uint32_t* d_k = nullptr;           // Details: k per slot, then offsets into the ids
+   uint32_t* h_k = nullptr;
+   uint32_t* d_ids = nullptr;         // Details: row ids
+   uint32_t* h_ids = nullptr;
+   uint32_t* d_nids = nullptr;        // Details: ids per slot
+   uint32_t* h_nids = nullptr;
+   uint32_t n_blk = 0;                // row-block table entries (Mutations slots)
+   size_t n_rows = 0;                 // rows of the last row pass
+   uint32_t n_mut_slots = 0, n_details = 0, n_ids = 0;
    // capacities
    // capacities (elements), one per buffer
    size_t hc_code = 0, hc_q = 0, hc_items = 0, hc_slot_query = 0, hc_counts = 0, hc_mcounts = 0, hc_minprop = 0,
-          hc_rowblk = 0;
+          hc_rowblk = 0, hc_err = 0, hc_k = 0, hc_ids = 0, hc_nids = 0;
    size_t dc_code = 0, dc_q = 0, dc_items = 0, dc_slot_query = 0, dc_counts = 0, dc_next = 0, dc_tiles = 0,
-          dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0, dc_minprop = 0, dc_rowblk = 0, dc_rows = 0;
+          dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0, dc_minprop = 0, dc_rowblk = 0, dc_rows = 0, dc_err = 0, dc_k = 0,
+          dc_ids = 0, dc_nids = 0;
    cudaGraphExec_t graph = nullptr;
 };
 
@@ -119,12 +131,29 @@ class Engine {
    // ---- batched path ----
    // Plans every expression (host threads), lays the programs and (query, tile) work items out and
    // sizes the device buffers (may allocate; call outside timed regions).
-   void batch_prepare(const std::vector<BatchQuery>& qs, uint32_t tile_bits = 0);
+   void batch_prepare(const std::vector<BatchQuery>& qs, uint32_t tile_bits = 0) { batch_prepare(batch_, qs, tile_bits); }
+   void batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uint32_t tile_bits = 0);
+   // Device bytes a batch of these queries holds (buffers of batch_prepare and the row pass).
+   size_t batch_device_bytes(const std::vector<BatchQuery>& qs, uint32_t tile_bits = 0) const;
+   void batch_free(BatchState& b);
    // Stream-ordered: optional H2D of the staged programs, the persistent filter kernel, the batched
    // mutations kernels per column, optional D2H of the results into the pinned host buffers.
    // parts: bit 0 = zeroing + filter kernel, bits 1..4 = transpose, container, coverage and final
    // mutations kernels (all set = the whole batch); used to time kernels one by one.
-   void batch_enqueue(cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31);
+   void batch_enqueue(cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31) {
+      batch_enqueue(batch_, stream, copy_in, copy_out, parts);
+   }
+   void batch_enqueue(BatchState& b, cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31);
+   // Row pass of a batch in two stream-ordered phases around one host step: phase 1 enqueues the
+   // batch, the D2H of the counts / Details ids and the count + scan of the rows; once the stream
+   // has passed it, phase 2 sizes the rows, enqueues their write and copies them to `rows`.
+   void rows_phase1(BatchState& b, cudaStream_t stream);
+   size_t rows_phase2(BatchState& b, cudaStream_t stream, DevMutationRow* rows, size_t cap);
+   void row_range(const BatchState& b, uint32_t query, uint64_t* begin, uint32_t* count) const;
+   const uint32_t* details_ids(const BatchState& b, uint32_t query, uint32_t* n) const;  // pinned host
+   void check_batch_error(BatchState& b);
+   BatchState& batch_state() { return batch_; }
+   uint64_t batch_state_count(const BatchState& b, uint32_t query) const { return b.h_counts[query]; }
    // Captures batch_enqueue(copy_in, copy_out) into a CUDA graph for the prepared shape.
    void batch_capture(cudaStream_t stream, bool copy_in = true, bool copy_out = true);
    void batch_replay(cudaStream_t stream);
@@ -189,11 +218,12 @@ class Engine {
    int* h_err_ = nullptr;                  // pinned
    uint64_t device_bytes_ = 0;
    BatchState batch_;
+   void copy_details(BatchState& b, cudaStream_t s);
    Planner planner_;
    bool use_learned_ = false;
    std::unique_ptr<FeatureContext> fctx_;  // built on first use
    const FeatureContext& fctx();
-   void batch_free();
+
 };
 
 // Plans many expressions on host threads (rewrite -> compile -> lower per expression).

@@ -1,0 +1,290 @@
+// Serving loop (see server.h).
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <stdexcept>
+
+namespace rhygpu {
+
+namespace {
+
+double now_s() {
+   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+Server::Server(Engine& engine, const ServerConfig& cfg) : engine_(engine), cfg_(cfg) {
+   if (cfg_.max_batch == 0 || cfg_.streams == 0 || cfg_.max_inflight == 0)
+      throw std::invalid_argument("server: max_batch, streams and max_inflight must be positive");
+   cuda_check(cudaSetDevice(engine_.device()), "cudaSetDevice");
+   if (cfg_.memory_budget == 0) {
+      size_t free_b = 0, total_b = 0;
+      cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+      cfg_.memory_budget = free_b / 4;
+   }
+   st_.budget_bytes = cfg_.memory_budget;
+   slots_.resize(cfg_.streams);
+   for (Slot& s : slots_) {
+      cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      cuda_check(cudaEventCreateWithFlags(&s.event, cudaEventDisableTiming), "cudaEventCreate");
+   }
+   thread_ = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+   stop();
+   cudaSetDevice(engine_.device());
+   for (Slot& s : slots_) {
+      if (s.stream) cudaStreamSynchronize(s.stream);
+      engine_.batch_free(s.b);
+      if (s.h_rows) cudaFreeHost(s.h_rows);
+      if (s.event) cudaEventDestroy(s.event);
+      if (s.stream) cudaStreamDestroy(s.stream);
+   }
+}
+
+size_t Server::request_bytes(const ServeRequest& r) const {
+   BatchQuery q;
+   q.action = r.action;
+   q.column = r.column;
+   q.k = r.k;
+   size_t b = engine_.batch_device_bytes({q});
+   if (r.action == 1) b += static_cast<size_t>(engine_.nchunks()) * CHUNK_ROWS / 8;  // share of the query masks
+   return b;
+}
+
+uint64_t Server::submit(const std::string& expr, int action, int column, double min_proportion, uint32_t k) {
+   if (action < 0 || action > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
+   if (action == 1 && (column < 0 || static_cast<size_t>(column) >= engine_.table().seq.size()))
+      throw std::invalid_argument("no such sequence column");
+   if (!(min_proportion >= 0.0 && min_proportion <= 1.0)) throw std::invalid_argument("min_proportion must lie in [0, 1]");
+   compile_filter(expr, engine_.table());  // user errors surface here, before anything is queued
+   auto r = std::make_shared<ServeRequest>();
+   r->expr = expr;
+   r->action = action;
+   r->column = column;
+   r->min_proportion = min_proportion;
+   r->k = k;
+   r->bytes = request_bytes(*r);
+   if (r->bytes > cfg_.memory_budget)
+      throw std::invalid_argument("request needs " + std::to_string(r->bytes) + " device bytes, the server's budget is " +
+                                  std::to_string(cfg_.memory_budget));
+   std::lock_guard<std::mutex> lock(mu_);
+   if (stop_) throw std::logic_error("server stopped");
+   r->id = next_id_++;
+   r->t_submit = now_s();
+   if (t_first_ < 0) t_first_ = r->t_submit;
+   all_[r->id] = r;
+   pending_.push_back(r);
+   ++st_.submitted;
+   cv_work_.notify_one();
+   return r->id;
+}
+
+std::shared_ptr<ServeRequest> Server::wait(uint64_t id, double timeout_ms) {
+   std::unique_lock<std::mutex> lock(mu_);
+   auto it = all_.find(id);
+   if (it == all_.end()) throw std::invalid_argument("no such request");
+   std::shared_ptr<ServeRequest> r = it->second;
+   auto ready = [&] { return r->done; };
+   if (timeout_ms < 0) {
+      cv_done_.wait(lock, ready);
+   } else if (!cv_done_.wait_for(lock, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+      return nullptr;
+   }
+   return r;
+}
+
+void Server::release(uint64_t id) {
+   std::lock_guard<std::mutex> lock(mu_);
+   all_.erase(id);
+}
+
+ServerStats Server::stats() {
+   std::lock_guard<std::mutex> lock(mu_);
+   ServerStats s = st_;
+   if (!latencies_ms_.empty()) {
+      std::vector<double> v = latencies_ms_;
+      std::sort(v.begin(), v.end());
+      s.p50_ms = v[(v.size() - 1) / 2];
+      s.p99_ms = v[static_cast<size_t>(0.99 * static_cast<double>(v.size() - 1))];
+   }
+   s.mean_batch = st_.batches ? static_cast<double>(batched_queries_) / static_cast<double>(st_.batches) : 0.0;
+   if (t_first_ >= 0 && t_last_ > t_first_) s.qps = static_cast<double>(st_.completed) / (t_last_ - t_first_);
+   return s;
+}
+
+void Server::stop() {
+   {
+      std::lock_guard<std::mutex> lock(mu_);
+      if (stop_ && !thread_.joinable()) return;
+      stop_ = true;
+   }
+   cv_work_.notify_all();
+   if (thread_.joinable()) thread_.join();
+}
+
+void Server::loop() {
+   cudaSetDevice(engine_.device());
+   for (;;) {
+      bool progressed = false;
+      for (Slot& s : slots_) {
+         if (s.phase == 0) continue;
+         const cudaError_t e = cudaEventQuery(s.event);
+         if (e == cudaErrorNotReady) continue;
+         if (e != cudaSuccess) {
+            fail(s, std::string("device error: ") + cudaGetErrorString(e));
+         } else {
+            advance(s);
+         }
+         progressed = true;
+      }
+      Slot* idle = nullptr;
+      bool busy = false;
+      for (Slot& s : slots_) {
+         if (s.phase == 0 && !idle) idle = &s;
+         busy |= s.phase != 0;
+      }
+      std::vector<std::shared_ptr<ServeRequest>> take;
+      {
+         std::unique_lock<std::mutex> lock(mu_);
+         if (stop_ && pending_.empty() && !busy) break;
+         if (idle && !pending_.empty()) {
+            const double waited_ms = 1000.0 * (now_s() - pending_.front()->t_submit);
+            if (!busy || stop_ || pending_.size() >= cfg_.max_batch || waited_ms >= cfg_.max_wait_ms) {
+               size_t bytes = 0;
+               while (!pending_.empty() && take.size() < cfg_.max_batch && inflight_ + take.size() < cfg_.max_inflight) {
+                  const auto& r = pending_.front();
+                  if (inflight_bytes_ + bytes + r->bytes > cfg_.memory_budget) break;  // admission by device memory
+                  bytes += r->bytes;
+                  take.push_back(r);
+                  pending_.pop_front();
+               }
+               if (!take.empty()) {
+                  inflight_ += static_cast<uint32_t>(take.size());
+                  inflight_bytes_ += bytes;
+                  idle->bytes = bytes;
+                  st_.peak_bytes = std::max<uint64_t>(st_.peak_bytes, inflight_bytes_);
+                  st_.peak_inflight = std::max(st_.peak_inflight, inflight_);
+                  ++st_.batches;
+                  batched_queries_ += take.size();
+               }
+            }
+         }
+         if (take.empty() && !progressed) {
+            // nothing to launch and nothing finished: sleep until a submit or a short poll period
+            cv_work_.wait_for(lock, std::chrono::microseconds(busy ? 20 : 2000));
+            continue;
+         }
+      }
+      if (!take.empty()) launch(*idle, std::move(take));
+   }
+}
+
+void Server::launch(Slot& slot, std::vector<std::shared_ptr<ServeRequest>>&& reqs) {
+   slot.reqs = std::move(reqs);
+   try {
+      std::lock_guard<std::mutex> lock(engine_.mu);
+      std::vector<std::string> texts;
+      texts.reserve(slot.reqs.size());
+      for (const auto& r : slot.reqs) texts.push_back(r->expr);
+      std::vector<BatchQuery> qs = engine_.plan_batch(texts, 0);
+      for (size_t i = 0; i < qs.size(); ++i) {
+         qs[i].action = slot.reqs[i]->action;
+         qs[i].column = slot.reqs[i]->column;
+         qs[i].min_proportion = slot.reqs[i]->min_proportion;
+         qs[i].k = slot.reqs[i]->k;
+      }
+      engine_.batch_prepare(slot.b, qs, 0);
+      engine_.rows_phase1(slot.b, slot.stream);
+      cuda_check(cudaEventRecord(slot.event, slot.stream), "event record");
+      slot.phase = 1;
+   } catch (const std::exception& e) {
+      fail(slot, e.what());
+   }
+}
+
+void Server::advance(Slot& slot) {
+   if (slot.phase == 1 && slot.b.n_mut_slots > 0) {
+      try {
+         std::lock_guard<std::mutex> lock(engine_.mu);
+         engine_.check_batch_error(slot.b);
+         const size_t total = slot.b.h_rowblk[slot.b.n_blk];
+         if (total > slot.h_rows_cap) {
+            if (slot.h_rows) cudaFreeHost(slot.h_rows);
+            slot.h_rows = nullptr;
+            slot.h_rows_cap = 0;
+            const size_t cap = total + total / 4 + 1024;
+            cuda_check(cudaMallocHost(&slot.h_rows, cap * sizeof(DevMutationRow)), "cudaMallocHost (rows)");
+            slot.h_rows_cap = cap;
+         }
+         engine_.rows_phase2(slot.b, slot.stream, slot.h_rows, slot.h_rows_cap);
+         cuda_check(cudaEventRecord(slot.event, slot.stream), "event record");
+         slot.phase = 2;
+      } catch (const std::exception& e) {
+         fail(slot, e.what());
+      }
+      return;
+   }
+   finish(slot);
+}
+
+void Server::finish(Slot& slot) {
+   try {
+      engine_.check_batch_error(slot.b);
+   } catch (const std::exception& e) {
+      fail(slot, e.what());
+      return;
+   }
+   const double t = now_s();
+   std::lock_guard<std::mutex> lock(mu_);
+   for (size_t i = 0; i < slot.reqs.size(); ++i) {
+      ServeRequest& r = *slot.reqs[i];
+      const uint32_t q = static_cast<uint32_t>(i);
+      r.count = engine_.batch_state_count(slot.b, q);
+      if (r.action == 1) {
+         uint64_t begin;
+         uint32_t n;
+         engine_.row_range(slot.b, q, &begin, &n);
+         r.rows.assign(slot.h_rows + begin, slot.h_rows + begin + n);
+      } else if (r.action == 2) {
+         uint32_t n;
+         const uint32_t* ids = engine_.details_ids(slot.b, q, &n);
+         if (ids) r.ids.assign(ids, ids + n);
+      }
+      r.t_done = t;
+      r.done = true;
+      latencies_ms_.push_back(1000.0 * (r.t_done - r.t_submit));
+      ++st_.completed;
+   }
+   t_last_ = t;
+   inflight_ -= static_cast<uint32_t>(slot.reqs.size());
+   inflight_bytes_ -= slot.bytes;
+   slot.reqs.clear();
+   slot.bytes = 0;
+   slot.phase = 0;
+   cv_done_.notify_all();
+}
+
+void Server::fail(Slot& slot, const std::string& what) {
+   if (slot.stream) cudaStreamSynchronize(slot.stream);
+   const double t = now_s();
+   std::lock_guard<std::mutex> lock(mu_);
+   for (auto& r : slot.reqs) {
+      r->error = what;
+      r->t_done = t;
+      r->done = true;
+      ++st_.rejected;
+   }
+   inflight_ -= static_cast<uint32_t>(slot.reqs.size());
+   inflight_bytes_ -= slot.bytes;
+   slot.reqs.clear();
+   slot.bytes = 0;
+   slot.phase = 0;
+   cv_done_.notify_all();
+}
+
+}  // namespace rhygpu

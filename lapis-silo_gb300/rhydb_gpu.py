@@ -98,6 +98,21 @@ class PlannerStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_batch", C.c_uint32), ("streams", C.c_uint32), ("max_inflight", C.c_uint32),
+                ("memory_budget", C.c_uint64), ("max_wait_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("batches", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_batch", C.c_double), ("qps", C.c_double), ("peak_bytes", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("peak_inflight", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 PLANNER_FEATURES = 24
 MLP_NPARAM = 5890
 
@@ -163,6 +178,12 @@ def lib():
         "rhy_planner_weights": (I, [P, P]),
         "rhy_planner_predict": (I, [P, P, U32, P, P]),
         "rhy_mlp_gradient": (I, [P, P, P, P, U32, P, P, P]),
+        "rhy_server_start": (I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+        "rhy_server_submit": (I, [P, C.c_char_p, I, U32, C.c_double, U32, C.POINTER(U64)]),
+        "rhy_server_result": (I, [P, U64, C.c_double, C.POINTER(U64), P, C.c_size_t, C.POINTER(C.c_size_t), P,
+                                  C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_double)]),
+        "rhy_server_stats": (I, [P, C.POINTER(ServerStats)]),
+        "rhy_server_stop": (None, [P]),
         "rhy_close": (None, [P]),
     }
     for name, (res, args) in sig.items():
@@ -514,6 +535,53 @@ class Device:
         p, d = C.c_uint64(), C.c_uint64()
         _check(lib().rhy_mutation_bytes(self._h, column, C.byref(p), C.byref(d)))
         return p.value, d.value
+
+
+class Server:
+    """Continuous-batching request loop over a Device (rhy_server_*)."""
+
+    def __init__(self, device: "Device", max_batch: int = 0, streams: int = 0, max_inflight: int = 0,
+                 memory_budget: int = 0, max_wait_ms: float = -1.0):
+        cfg = ServerConfig(max_batch, streams, max_inflight, memory_budget, max_wait_ms)
+        h = C.c_void_p()
+        _check(lib().rhy_server_start(device._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    def submit(self, expr: str, action: int = 0, column: int = 0, min_proportion: float = 0.05, k: int = 1000) -> int:
+        i = C.c_uint64()
+        _check(lib().rhy_server_submit(self._h, expr.encode(), action, column, min_proportion, k, C.byref(i)))
+        return i.value
+
+    def result(self, rid: int, timeout_ms: float = -1.0) -> dict:
+        rows_cap, ids_cap = 4096, 1024
+        while True:
+            rows = np.zeros(rows_cap, Device.ROW_DTYPE)
+            ids = np.zeros(ids_cap, np.uint32)
+            cnt, nr, ni, lat = C.c_uint64(), C.c_size_t(), C.c_size_t(), C.c_double()
+            rc = lib().rhy_server_result(self._h, rid, timeout_ms, C.byref(cnt), rows.ctypes.data, rows_cap,
+                                         C.byref(nr), ids.ctypes.data, ids_cap, C.byref(ni), C.byref(lat))
+            if rc == 4 and (nr.value > rows_cap or ni.value > ids_cap):
+                rows_cap, ids_cap = max(rows_cap, nr.value), max(ids_cap, ni.value)
+                continue
+            _check(rc)
+            return {"count": cnt.value, "rows": rows[:nr.value], "ids": ids[:ni.value], "latency_ms": lat.value}
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().rhy_server_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def stop(self):
+        if self._h:
+            lib().rhy_server_stop(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 def bits_to_rows(bits: np.ndarray) -> np.ndarray:

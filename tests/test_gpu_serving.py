@@ -1,0 +1,106 @@
+"""Serving loop: continuous batching gives every request the result it gets alone, admission
+respects the device-memory budget, and user errors surface at submission."""
+import threading
+
+import numpy as np
+import pytest
+
+import rhydb_gpu as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    t = R.Table.generate(300000, seed=21, n_aa_genes=12, null_fraction=0.002)
+    qs = t.queries(240, seed=22, use_aa=True, use_metadata=True)
+    dev = R.Device(t, 0)
+    rng = np.random.default_rng(23)
+    acts = rng.choice([0, 1, 2], len(qs), p=[0.6, 0.25, 0.15])
+    cols = rng.integers(0, t.n_seq, len(qs))
+    props = rng.choice([0.0, 0.05, 0.5], len(qs))
+    ks = rng.choice([1, 10, 1000, 5000], len(qs))
+    yield t, dev, qs, acts, cols, props, ks
+    dev.close()
+
+
+def canon(res):
+    return res["count"], tuple(map(tuple, res["rows"].tolist())), tuple(res["ids"].tolist())
+
+
+def submit(srv, setup, i):
+    _, _, qs, acts, cols, props, ks = setup
+    return srv.submit(qs[i], int(acts[i]), int(cols[i]), float(props[i]), int(ks[i]))
+
+
+def test_each_result_same_alone_and_in_the_mix(setup):
+    t, dev, qs, acts, cols, props, ks = setup
+    srv = R.Server(dev, max_batch=64, streams=3)
+    alone = [canon(srv.result(submit(srv, setup, i))) for i in range(len(qs))]
+    # the mix: four clients submit at once while earlier micro-batches are still on the device
+    rids = [None] * len(qs)
+
+    def client(part):
+        for i in part:
+            rids[i] = submit(srv, setup, i)
+
+    threads = [threading.Thread(target=client, args=(range(j, len(qs), 4),)) for j in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    mixed = [canon(srv.result(rids[i])) for i in range(len(qs))]
+    st = srv.stats()
+    srv.stop()
+    assert alone == mixed
+    assert st["completed"] == 2 * len(qs) and st["rejected"] == 0
+    assert st["batches"] < 2 * len(qs)  # requests were batched together
+    assert 0 < st["p50_ms"] <= st["p99_ms"]
+    # the results equal the batch path's and, for Details, the first ids of the row set
+    counts, rows, begin, cnt = dev.batch_rows(qs, acts, cols, props)
+    for i in range(len(qs)):
+        c, r, ids = alone[i]
+        assert c == counts[i], qs[i]
+        if acts[i] == 1:
+            want = rows[int(begin[i]):int(begin[i]) + int(cnt[i])]
+            assert r == tuple(map(tuple, want.tolist())), qs[i]
+        if acts[i] == 2:
+            bits, n = dev.compute_filter(qs[i])
+            assert n == c
+            assert ids == tuple(R.bits_to_rows(bits)[:int(ks[i])].tolist()), qs[i]
+
+
+def test_admission_by_device_memory(setup):
+    t, dev, qs, acts, cols, props, ks = setup
+    budget = 12 << 20  # a few Mutations queries at a time
+    srv = R.Server(dev, max_batch=256, streams=3, memory_budget=budget)
+    mut = [i for i in range(len(qs)) if acts[i] == 1][:40]
+    rids = [srv.submit(qs[i], 1, int(cols[i]), 0.05) for i in mut]
+    res = [srv.result(r) for r in rids]
+    st = srv.stats()
+    assert st["completed"] == len(mut)
+    assert st["budget_bytes"] == budget and 0 < st["peak_bytes"] <= budget
+    assert st["batches"] > 1  # the budget split the requests
+    counts, rows, begin, cnt = dev.batch_rows([qs[i] for i in mut], [1] * len(mut), [int(cols[i]) for i in mut])
+    for j, i in enumerate(mut):
+        assert res[j]["count"] == counts[j]
+    # a request larger than the whole budget is refused at submission
+    tiny = R.Server(dev, memory_budget=1 << 16)
+    with pytest.raises(R.RhyError):
+        tiny.submit(qs[mut[0]], 1, 0, 0.05)
+    tiny.stop()
+    srv.stop()
+
+
+def test_user_errors_surface_at_submit(setup):
+    _, dev, qs, _, _, _, _ = setup
+    srv = R.Server(dev)
+    with pytest.raises(R.IllegalQuery):
+        srv.submit("SymEq(main,99999999,A)")
+    with pytest.raises(R.RhyError):
+        srv.submit(qs[0], action=7)
+    with pytest.raises(R.RhyError):
+        srv.submit(qs[0], action=1, min_proportion=2.0)
+    r = srv.result(srv.submit(qs[0]))
+    assert r["count"] == dev.count(qs[0])
+    srv.stop()
