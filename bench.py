@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--planner-queries", type=int, default=1000,
                     help="queries (another seed) traced through the plain path to train the planner")
     ap.add_argument("--no-planner", action="store_true", help="rule-based ordering only")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
+    ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
     return ap.parse_args()
 
 
@@ -306,7 +308,9 @@ def main():
     barrier(ws)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, ws)
     value = n * args.steps * ws / total_s
-    launches_per_step = 1 + (5 if n_mut else 0)
+    # the persistent filter kernel, then per column with Mutations queries: transpose, container,
+    # coverage and final kernels
+    launches_per_step = 1 + 4 * len({int(c) for c, a in zip(columns, actions) if a == 1})
 
     # results of the batched path for the parity self-check against the plain path
     dev.batch_launch(sp, True, True)
@@ -397,6 +401,30 @@ def main():
     prog_bytes = info.n_instr * 16 + n * 16 + info.n_items * 8 + n_mut * 12
     d2h = n * 8 + n * 12 + len(rows) * 24
 
+    # ---------------- serving: Poisson arrivals, continuous batching ----------------
+    serving = None
+    if args.serve_seconds > 0:
+        srv = R.Server(dev, max_batch=512, streams=3)
+        rng = np.random.default_rng(args.qseed + 7)
+        runs = []
+        for rate in [float(x) for x in args.serve_rates.split(",") if x]:
+            nreq = max(1, int(rate * args.serve_seconds))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+            mix = rng.choice(3, nreq, p=[0.70, 0.25, 0.05]).astype(np.int32)
+            pick = rng.integers(0, n, nreq)
+            lat, wall = srv.replay([queries[i] for i in pick], mix, np.zeros(nreq, np.uint32), np.full(nreq, 0.05),
+                                   np.full(nreq, 1000, np.uint32), arrivals)
+            ok = lat[np.isfinite(lat)]
+            runs.append({"arrival_qps": rate, "requests": nreq, "achieved_qps": nreq / wall,
+                         "p50_ms": float(np.percentile(ok, 50)), "p99_ms": float(np.percentile(ok, 99)),
+                         "failed": int(nreq - len(ok))})
+        st = srv.stats()
+        srv.stop()
+        serving = {"mix": "70% count / 25% mutations (nucleotide, min proportion 0.05) / 5% details (first 1000 ids)",
+                   "arrivals": "Poisson, open loop (native submitter thread)", "rows": table.n_rows,
+                   "runs": runs, "mean_batch": st["mean_batch"], "batches": st["batches"],
+                   "peak_device_bytes": st["peak_bytes"], "planner": planner["mode"]}
+
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)
     # queries whose filter is neither empty nor every row: the pass reads the whole column
@@ -451,6 +479,7 @@ def main():
                       "e2e_p99_ms": float(np.percentile(e2e_plain_ms, 99))},
             "speedup_vs_plain": value / plain_qps,
             "planner": planner,
+            "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
                     "d2h_bytes_per_step": int(d2h), "output": "Mutations rows (min proportion 0.05) + counts",

@@ -295,6 +295,12 @@ int rhy_server_submit(RhyServer* s, const char* expr, int action, uint32_t colum
 int rhy_server_result(RhyServer* s, uint64_t id, double timeout_ms, uint64_t* count, RhyMutationRow* rows,
                       size_t rows_cap, size_t* n_rows, uint32_t* ids, size_t ids_cap, size_t* n_ids, double* latency_ms);
 int rhy_server_stats(RhyServer* s, RhyServerStats* out);
+/* Open-loop replay of a request trace: request i is submitted by a native thread at arrival_s[i]
+ * seconds after the call starts; then all are awaited. latency_ms[i] receives each latency (NaN if
+ * the request failed), *wall_s the time from the start to the last result. */
+int rhy_server_replay(RhyServer* s, const char* const* exprs, const int* actions, const uint32_t* columns,
+                      const double* min_proportions, const uint32_t* ks, const double* arrival_s, uint32_t n,
+                      double* latency_ms, double* wall_s);
 /* Finishes every queued request, stops the loop and frees the server. */
 void rhy_server_stop(RhyServer* s);
 

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -23,6 +24,9 @@ struct RhyTable {
    std::vector<RhyRawDictColumn> raw_dict;
    std::vector<RhyRawDateColumn> raw_date;
    std::vector<std::vector<const char*>> dict_values;
+   // planner features, built on first use
+   std::unique_ptr<rhygpu::FeatureContext> fctx;
+   std::mutex fctx_mu;
 };
 
 struct RhyDevice {
@@ -683,7 +687,12 @@ int rhy_plan_features(const RhyTable* t, const char* expr, float* x, size_t cap,
       need(t, "table");
       need(expr, "expression");
       need(n, "n");
-      const rhygpu::FeatureContext ctx = rhygpu::feature_context(t->image);
+      RhyTable* tt = const_cast<RhyTable*>(t);
+      {
+         std::lock_guard<std::mutex> lock(tt->fctx_mu);
+         if (!tt->fctx) tt->fctx = std::make_unique<rhygpu::FeatureContext>(rhygpu::feature_context(t->image));
+      }
+      const rhygpu::FeatureContext& ctx = *tt->fctx;
       rhygpu::OpPtr op = rhygpu::compile_filter(expr, t->image);
       std::vector<const rhygpu::Op*> nodes;
       std::function<void(const rhygpu::Op&)> walk = [&](const rhygpu::Op& o) {
@@ -881,6 +890,30 @@ int rhy_server_stats(RhyServer* s, RhyServerStats* out) {
       out->peak_bytes = st.peak_bytes;
       out->budget_bytes = st.budget_bytes;
       out->peak_inflight = st.peak_inflight;
+   });
+}
+
+int rhy_server_replay(RhyServer* s, const char* const* exprs, const int* actions, const uint32_t* columns,
+                      const double* min_proportions, const uint32_t* ks, const double* arrival_s, uint32_t n,
+                      double* latency_ms, double* wall_s) {
+   return guarded([&] {
+      need(s, "server");
+      if (n) {
+         need(exprs, "exprs");
+         need(arrival_s, "arrival_s");
+      }
+      std::vector<rhygpu::ServeRequest> reqs(n);
+      std::vector<double> arr(arrival_s, arrival_s + n);
+      for (uint32_t i = 0; i < n; ++i) {
+         need(exprs[i], "expression");
+         reqs[i].expr = exprs[i];
+         reqs[i].action = actions ? actions[i] : 0;
+         reqs[i].column = columns ? static_cast<int>(columns[i]) : 0;
+         reqs[i].min_proportion = min_proportions ? min_proportions[i] : 0.05;
+         reqs[i].k = ks ? ks[i] : 1000;
+      }
+      const std::vector<double> lat = s->server->replay(reqs, arr, wall_s);
+      if (latency_ms) std::copy(lat.begin(), lat.end(), latency_ms);
    });
 }
 

@@ -773,27 +773,12 @@ Estimator rule_estimator(const TableImage& t) {
          case OpT::EMPTY: return 0.0;
          case OpT::FULL: return rows;
          case OpT::INDEX_SCAN: {
-            const ContainerSet* cs;
-            uint32_t key;
-            uint32_t mask = 1;
-            if (op.leaf.kind == Leaf::SEQ) {
-               cs = &t.seq[op.leaf.col].vertical;
-               key = op.leaf.pos;
-               mask = op.leaf.symmask;
-            } else if (op.leaf.kind == Leaf::NULLS) {
-               return static_cast<double>(t.seq[op.leaf.col].null_rows.size());
-            } else {
-               cs = &t.dict[op.leaf.col].inverted;
-               key = op.leaf.value;
-            }
+            // exact: the containers of the symbols of one key are disjoint
+            if (op.leaf.kind == Leaf::NULLS) return static_cast<double>(t.seq[op.leaf.col].null_rows.size());
+            if (op.leaf.kind == Leaf::DICT) return t.dict[op.leaf.col].inverted.stat(op.leaf.value, 0).card;
+            const ContainerSet& cs = t.seq[op.leaf.col].vertical;
             double s = 0;
-            for (uint32_t v = 0; v < t.nchunks(); ++v) {
-               const size_t slot = static_cast<size_t>(v) * cs->nkeys + key;
-               for (uint32_t i = cs->off[slot]; i < cs->off[slot + 1]; ++i) {
-                  const CtrDesc& d = cs->ctrs[i];
-                  if (op.leaf.kind != Leaf::SEQ || (mask >> d.sym & 1)) s += d.card_m1 + 1.0;
-               }
-            }
+            for (uint32_t m = op.leaf.symmask; m; m &= m - 1) s += cs.stat(op.leaf.pos, __builtin_ctz(m)).card;
             return s;
          }
          case OpT::COMPLEMENT: return rows - rec(*op.children[0]);

@@ -92,29 +92,17 @@ void op_features(const Op& op, const FeatureContext& ctx, float* f) {
       f[16] = static_cast<float>(op.leaf.pos) / static_cast<float>(std::max(1u, c.L));
       f[17] = c.kind == SymKind::AA ? 1.0f : 0.0f;
       uint32_t n = 0, nb = 0;
-      for (uint32_t v = 0; v < t.nchunks(); ++v) {
-         const size_t slot = static_cast<size_t>(v) * c.vertical.nkeys + op.leaf.pos;
-         for (uint32_t i = c.vertical.off[slot]; i < c.vertical.off[slot + 1]; ++i) {
-            const CtrDesc& d = c.vertical.ctrs[i];
-            if (!((op.leaf.symmask >> d.sym) & 1)) continue;
-            ++n;
-            nb += d.type == CT_BITSET;
-         }
+      for (uint32_t m = op.leaf.symmask; m; m &= m - 1) {
+         const KeyStats& st = c.vertical.stat(op.leaf.pos, __builtin_ctz(m));
+         n += st.nctr;
+         nb += st.nbits;
       }
       f[18] = log2p(n) / 12.0f;
       f[19] = n ? static_cast<float>(nb) / static_cast<float>(n) : 0.0f;
    } else if (op.t == OpT::INDEX_SCAN && op.leaf.kind == Leaf::DICT) {
-      const ContainerSet& cs = t.dict[op.leaf.col].inverted;
-      uint32_t n = 0, nb = 0;
-      for (uint32_t v = 0; v < t.nchunks(); ++v) {
-         const size_t slot = static_cast<size_t>(v) * cs.nkeys + op.leaf.value;
-         for (uint32_t i = cs.off[slot]; i < cs.off[slot + 1]; ++i) {
-            ++n;
-            nb += cs.ctrs[i].type == CT_BITSET;
-         }
-      }
-      f[18] = log2p(n) / 12.0f;
-      f[19] = n ? static_cast<float>(nb) / static_cast<float>(n) : 0.0f;
+      const KeyStats& st = t.dict[op.leaf.col].inverted.stat(op.leaf.value, 0);
+      f[18] = log2p(st.nctr) / 12.0f;
+      f[19] = st.nctr ? static_cast<float>(st.nbits) / static_cast<float>(st.nctr) : 0.0f;
    } else if (op.t == OpT::SELECTION) {
       uint32_t ncov = 0;
       double width = 1.0;

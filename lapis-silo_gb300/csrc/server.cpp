@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
 
@@ -285,6 +286,40 @@ void Server::fail(Slot& slot, const std::string& what) {
    slot.bytes = 0;
    slot.phase = 0;
    cv_done_.notify_all();
+}
+
+std::vector<double> Server::replay(const std::vector<ServeRequest>& reqs, const std::vector<double>& arrival_s,
+                                   double* wall_s) {
+   if (reqs.size() != arrival_s.size()) throw std::invalid_argument("replay: one arrival time per request");
+   const size_t n = reqs.size();
+   std::vector<uint64_t> ids(n, 0);
+   std::vector<std::string> errors(n);
+   const double t0 = now_s();
+   std::thread producer([&] {
+      for (size_t i = 0; i < n; ++i) {
+         const double due = t0 + arrival_s[i];
+         for (double t = now_s(); t < due; t = now_s()) {
+            if (due - t > 200e-6) std::this_thread::sleep_for(std::chrono::microseconds(100));
+         }
+         try {
+            ids[i] = submit(reqs[i].expr, reqs[i].action, reqs[i].column, reqs[i].min_proportion, reqs[i].k);
+         } catch (const std::exception& e) {
+            errors[i] = e.what();
+         }
+      }
+   });
+   producer.join();
+   std::vector<double> lat(n, std::nan(""));
+   double t_end = t0;
+   for (size_t i = 0; i < n; ++i) {
+      if (!ids[i]) continue;
+      std::shared_ptr<ServeRequest> r = wait(ids[i], -1.0);
+      if (r->error.empty()) lat[i] = 1000.0 * (r->t_done - r->t_submit);
+      t_end = std::max(t_end, r->t_done);
+      release(ids[i]);
+   }
+   if (wall_s) *wall_s = t_end - t0;
+   return lat;
 }
 
 }  // namespace rhygpu

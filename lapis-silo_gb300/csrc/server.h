@@ -71,6 +71,10 @@ class Server {
    void release(uint64_t id);
    ServerStats stats();
    void stop();
+   // Open-loop replay of a request trace: every request is submitted at its arrival time (seconds
+   // from the start) by a native thread, then all are awaited and released. Returns each request's
+   // latency (ms, NaN if it failed) and the wall time from the first arrival to the last result.
+   std::vector<double> replay(const std::vector<ServeRequest>& reqs, const std::vector<double>& arrival_s, double* wall_s);
 
   private:
    struct Slot {

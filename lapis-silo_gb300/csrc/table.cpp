@@ -138,6 +138,13 @@ void assemble(std::vector<ChunkContainers>& chunks, uint32_t nkeys, ContainerSet
    // 16-byte loads that may cover up to seven u16 past a container's last element
    while (cs.payload.size() % 8) cs.payload.push_back(0);
    cs.payload.insert(cs.payload.end(), 8, 0);
+   cs.stats.assign(static_cast<size_t>(nkeys) * STAT_SYMS, KeyStats{});
+   for (const auto& d : cs.ctrs) {
+      KeyStats& st = cs.stats[static_cast<size_t>(d.key) * STAT_SYMS + d.sym];
+      st.card += d.card_m1 + 1u;
+      ++st.nctr;
+      st.nbits += d.type == CT_BITSET;
+   }
    const uint64_t nslots = static_cast<uint64_t>(chunks.size()) * nkeys;
    cs.off.assign(nslots + 1, 0);
    for (const auto& d : cs.ctrs) cs.off[static_cast<uint64_t>(d.v) * nkeys + d.key + 1]++;

@@ -70,12 +70,22 @@ struct NRunEntry {  // missing interval of one row clipped to one position block
    uint16_t hi;
 };
 
+// Totals over all chunks of the containers of one (key, symbol): rows, containers, bitsets.
+struct KeyStats {
+   uint32_t card = 0;
+   uint16_t nctr = 0;
+   uint16_t nbits = 0;
+};
+constexpr uint32_t STAT_SYMS = 32;  // stats slots per key (every alphabet has fewer symbols)
+
 struct ContainerSet {
    std::vector<CtrDesc> ctrs;       // sorted by (v, key, sym)
    std::vector<uint16_t> payload;   // bitset payloads start on 16-byte boundaries
    std::vector<uint32_t> off;       // [nchunks * nkeys + 1]: ctrs of (v, key) are [off[v*nkeys+key], off[...+1])
    uint32_t nkeys = 0;
+   std::vector<KeyStats> stats;     // [nkeys * STAT_SYMS]: planning statistics
    uint64_t payload_bytes() const;
+   const KeyStats& stat(uint32_t key, uint32_t sym) const { return stats[static_cast<size_t>(key) * STAT_SYMS + sym]; }
 };
 
 struct SeqColumnImage {

@@ -183,6 +183,7 @@ def lib():
         "rhy_server_result": (I, [P, U64, C.c_double, C.POINTER(U64), P, C.c_size_t, C.POINTER(C.c_size_t), P,
                                   C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_double)]),
         "rhy_server_stats": (I, [P, C.POINTER(ServerStats)]),
+        "rhy_server_replay": (I, [P, P, P, P, P, P, P, U32, P, C.POINTER(C.c_double)]),
         "rhy_server_stop": (None, [P]),
         "rhy_close": (None, [P]),
     }
@@ -566,6 +567,21 @@ class Server:
                 continue
             _check(rc)
             return {"count": cnt.value, "rows": rows[:nr.value], "ids": ids[:ni.value], "latency_ms": lat.value}
+
+    def replay(self, exprs, actions, columns, min_proportions, ks, arrival_s):
+        """Open-loop replay (native submitter thread): (latencies in ms, wall seconds)."""
+        n = len(exprs)
+        arr = (C.c_char_p * max(n, 1))(*[e.encode() for e in exprs])
+        act = np.ascontiguousarray(actions, np.int32)
+        col = np.ascontiguousarray(columns, np.uint32)
+        mp = np.ascontiguousarray(min_proportions, np.float64)
+        k = np.ascontiguousarray(ks, np.uint32)
+        at = np.ascontiguousarray(arrival_s, np.float64)
+        lat = np.zeros(max(n, 1), np.float64)
+        wall = C.c_double()
+        _check(lib().rhy_server_replay(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), _ptr(mp), _ptr(k),
+                                       _ptr(at), n, _ptr(lat), C.byref(wall)))
+        return lat[:n], wall.value
 
     def stats(self) -> dict:
         st = ServerStats()
