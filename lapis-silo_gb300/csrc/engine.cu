@@ -850,21 +850,21 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    }
    const FeatureContext& ctx = fctx();
    std::vector<OpPtr> ops(n);
-   parallel_for(n, threads, [&](uint32_t i) { ops[i] = compile_filter(exprs[i], table_); });
-   // every operator node of every expression, features in one table
+   std::vector<std::vector<const Op*>> qnodes(n);
+   std::vector<std::vector<std::array<float, PLAN_FEATURES>>> qx(n);
+   parallel_for(n, threads, [&](uint32_t i) {
+      ops[i] = compile_filter(exprs[i], table_);
+      tree_features(*ops[i], ctx, qnodes[i], qx[i]);
+   });
+   // every operator node of every expression in one table; the root of query i comes first
    std::vector<const Op*> nodes;
+   std::vector<std::array<float, PLAN_FEATURES>> x;
    std::vector<uint32_t> root_of(n);
-   std::function<void(const Op&)> walk = [&](const Op& op) {
-      nodes.push_back(&op);
-      for (const auto& c : op.children) walk(*c);
-      for (const auto& c : op.negated) walk(*c);
-   };
    for (uint32_t i = 0; i < n; ++i) {
       root_of[i] = static_cast<uint32_t>(nodes.size());
-      walk(*ops[i]);
+      nodes.insert(nodes.end(), qnodes[i].begin(), qnodes[i].end());
+      x.insert(x.end(), qx[i].begin(), qx[i].end());
    }
-   std::vector<std::array<float, PLAN_FEATURES>> x(nodes.size());
-   parallel_for(static_cast<uint32_t>(nodes.size()), threads, [&](uint32_t k) { op_features(*nodes[k], ctx, x[k].data()); });
    std::vector<double> sel, cost;
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
    planner_.predict(x, sel, cost);

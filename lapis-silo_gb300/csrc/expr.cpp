@@ -763,71 +763,72 @@ std::string Op::to_string() const {
 // =============================================================================================
 // Estimation (rule based): container cardinalities for leaves, independence for combinations.
 
-Estimator rule_estimator(const TableImage& t) {
+double rule_node_estimate(const Op& op, const TableImage& t, const std::function<double(const Op&)>& child) {
    const double rows = std::max(1u, t.n_rows);
    auto frac = [rows](double x) { return std::min(1.0, std::max(0.0, x / rows)); };
-   std::shared_ptr<std::function<double(const Op&)>> self = std::make_shared<std::function<double(const Op&)>>();
-   *self = [&t, rows, frac, self](const Op& op) -> double {
-      auto& rec = *self;
-      switch (op.t) {
-         case OpT::EMPTY: return 0.0;
-         case OpT::FULL: return rows;
-         case OpT::INDEX_SCAN: {
-            // exact: the containers of the symbols of one key are disjoint
-            if (op.leaf.kind == Leaf::NULLS) return static_cast<double>(t.seq[op.leaf.col].null_rows.size());
-            if (op.leaf.kind == Leaf::DICT) return t.dict[op.leaf.col].inverted.stat(op.leaf.value, 0).card;
-            const ContainerSet& cs = t.seq[op.leaf.col].vertical;
-            double s = 0;
-            for (uint32_t m = op.leaf.symmask; m; m &= m - 1) s += cs.stat(op.leaf.pos, __builtin_ctz(m)).card;
-            return s;
-         }
-         case OpT::COMPLEMENT: return rows - rec(*op.children[0]);
-         case OpT::INTERSECTION: {
-            double f = 1;
-            for (const auto& c : op.children) f *= frac(rec(*c));
-            for (const auto& c : op.negated) f *= 1 - frac(rec(*c));
-            return f * rows;
-         }
-         case OpT::UNION: {
-            double f = 1;
-            for (const auto& c : op.children) f *= 1 - frac(rec(*c));
-            return (1 - f) * rows;
-         }
-         case OpT::SELECTION: {
-            double f = op.children.empty() ? 1.0 : frac(rec(*op.children[0]));
-            for (const auto& p : op.preds) {
-               if (p.kind == Pred::COVERED) {
-                  f *= p.covered ? 0.97 : 0.03;
-               } else {
-                  f *= 0.5;
-               }
-            }
-            return f * rows;
-         }
-         case OpT::THRESHOLD: {
-            // Poisson-binomial distribution of the number of matching children.
-            std::vector<double> dist(1, 1.0);
-            auto add = [&](double p) {
-               std::vector<double> nd(dist.size() + 1, 0.0);
-               for (size_t i = 0; i < dist.size(); ++i) {
-                  nd[i] += dist[i] * (1 - p);
-                  nd[i + 1] += dist[i] * p;
-               }
-               dist.swap(nd);
-            };
-            for (const auto& c : op.children) add(frac(rec(*c)));
-            for (const auto& c : op.negated) add(1 - frac(rec(*c)));
-            double f = 0;
-            if (op.exact) {
-               f = static_cast<size_t>(op.n) < dist.size() ? dist[op.n] : 0.0;
-            } else {
-               for (size_t i = op.n; i < dist.size(); ++i) f += dist[i];
-            }
-            return f * rows;
-         }
+   switch (op.t) {
+      case OpT::EMPTY: return 0.0;
+      case OpT::FULL: return rows;
+      case OpT::INDEX_SCAN: {
+         // exact: the containers of the symbols of one key are disjoint
+         if (op.leaf.kind == Leaf::NULLS) return static_cast<double>(t.seq[op.leaf.col].null_rows.size());
+         if (op.leaf.kind == Leaf::DICT) return t.dict[op.leaf.col].inverted.stat(op.leaf.value, 0).card;
+         const ContainerSet& cs = t.seq[op.leaf.col].vertical;
+         double s = 0;
+         for (uint32_t m = op.leaf.symmask; m; m &= m - 1) s += cs.stat(op.leaf.pos, __builtin_ctz(m)).card;
+         return s;
       }
-      return rows;
-   };
+      case OpT::COMPLEMENT: return rows - child(*op.children[0]);
+      case OpT::INTERSECTION: {
+         double f = 1;
+         for (const auto& c : op.children) f *= frac(child(*c));
+         for (const auto& c : op.negated) f *= 1 - frac(child(*c));
+         return f * rows;
+      }
+      case OpT::UNION: {
+         double f = 1;
+         for (const auto& c : op.children) f *= 1 - frac(child(*c));
+         return (1 - f) * rows;
+      }
+      case OpT::SELECTION: {
+         double f = op.children.empty() ? 1.0 : frac(child(*op.children[0]));
+         for (const auto& p : op.preds) {
+            if (p.kind == Pred::COVERED) {
+               f *= p.covered ? 0.97 : 0.03;
+            } else {
+               f *= 0.5;
+            }
+         }
+         return f * rows;
+      }
+      case OpT::THRESHOLD: {
+         // Poisson-binomial distribution of the number of matching children.
+         std::vector<double> dist(1, 1.0);
+         auto add = [&](double p) {
+            std::vector<double> nd(dist.size() + 1, 0.0);
+            for (size_t i = 0; i < dist.size(); ++i) {
+               nd[i] += dist[i] * (1 - p);
+               nd[i + 1] += dist[i] * p;
+            }
+            dist.swap(nd);
+         };
+         for (const auto& c : op.children) add(frac(child(*c)));
+         for (const auto& c : op.negated) add(1 - frac(child(*c)));
+         double f = 0;
+         if (op.exact) {
+            f = static_cast<size_t>(op.n) < dist.size() ? dist[op.n] : 0.0;
+         } else {
+            for (size_t i = op.n; i < dist.size(); ++i) f += dist[i];
+         }
+         return f * rows;
+      }
+   }
+   return rows;
+}
+
+Estimator rule_estimator(const TableImage& t) {
+   std::shared_ptr<std::function<double(const Op&)>> self = std::make_shared<std::function<double(const Op&)>>();
+   *self = [&t, self](const Op& op) -> double { return rule_node_estimate(op, t, *self); };
    return [self](const Op& op) { return (*self)(op); };
 }
 

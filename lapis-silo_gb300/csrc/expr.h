@@ -104,6 +104,9 @@ OpPtr negate(OpPtr op);
 // never the result.
 using Estimator = std::function<double(const Op&)>;
 Estimator rule_estimator(const TableImage& t);
+// The rule estimate of one node given an estimator for its children (the children's estimates may
+// come from a memo; rule_estimator recurses).
+double rule_node_estimate(const Op& op, const TableImage& t, const std::function<double(const Op&)>& child);
 
 // Instructions [first, last] of one operator node: its result is on top of the stack after `last`.
 struct NodeSpan {

@@ -8,6 +8,7 @@
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 
 #include "alphabet.h"
 
@@ -62,7 +63,9 @@ FeatureContext feature_context(const TableImage& t) {
    return c;
 }
 
-void op_features(const Op& op, const FeatureContext& ctx, float* f) {
+namespace {
+
+void op_features_with(const Op& op, const FeatureContext& ctx, double rule_rows, const SubStats& ss, float* f) {
    const TableImage& t = *ctx.table;
    std::fill(f, f + PLAN_FEATURES, 0.0f);
    const double rows = std::max(1u, t.n_rows);
@@ -75,13 +78,12 @@ void op_features(const Op& op, const FeatureContext& ctx, float* f) {
       case OpT::THRESHOLD: f[6] = 1; break;
       default: f[7] = 1; break;
    }
-   const double sel = std::min(1.0, std::max(0.0, ctx.rule(op) / rows));
+   const double sel = std::min(1.0, std::max(0.0, rule_rows / rows));
    f[8] = static_cast<float>(std::log(std::max(sel, MIN_SEL)) / -std::log(MIN_SEL));
    f[9] = static_cast<float>(sel);
    const size_t nch = op.children.size() + op.negated.size();
    f[10] = log2p(static_cast<double>(nch)) / 6.0f;
    f[11] = nch ? static_cast<float>(op.negated.size()) / static_cast<float>(nch) : 0.0f;
-   const SubStats ss = subtree(op);
    f[12] = log2p(ss.nodes) / 8.0f;
    f[13] = static_cast<float>(ss.depth) / 8.0f;
    f[14] = log2p(ss.leaves) / 8.0f;
@@ -138,6 +140,44 @@ void op_features(const Op& op, const FeatureContext& ctx, float* f) {
       f[22] = nch ? static_cast<float>(op.n) / static_cast<float>(nch) : 0.0f;
       f[23] = op.exact ? 1.0f : 0.0f;
    }
+}
+
+}  // namespace
+
+void op_features(const Op& op, const FeatureContext& ctx, float* out) {
+   op_features_with(op, ctx, ctx.rule(op), subtree(op), out);
+}
+
+void tree_features(const Op& root, const FeatureContext& ctx, std::vector<const Op*>& nodes,
+                   std::vector<std::array<float, PLAN_FEATURES>>& x) {
+   // rule estimates and subtree statistics once per node, bottom up
+   std::unordered_map<const Op*, std::pair<double, SubStats>> memo;
+   std::function<void(const Op&)> post = [&](const Op& op) {
+      SubStats s{1, 1, 0};
+      if (op.t == OpT::INDEX_SCAN) s.leaves = 1;
+      if (op.t == OpT::SELECTION) s.leaves += static_cast<uint32_t>(op.preds.size());
+      auto add = [&](const OpPtr& c) {
+         post(*c);
+         const SubStats& cs = memo.at(c.get()).second;
+         s.nodes += cs.nodes;
+         s.leaves += cs.leaves;
+         s.depth = std::max(s.depth, cs.depth + 1);
+      };
+      for (const auto& c : op.children) add(c);
+      for (const auto& c : op.negated) add(c);
+      const double e = rule_node_estimate(op, *ctx.table, [&](const Op& c) { return memo.at(&c).first; });
+      memo.emplace(&op, std::make_pair(e, s));
+   };
+   post(root);
+   std::function<void(const Op&)> pre = [&](const Op& op) {
+      const auto& m = memo.at(&op);
+      nodes.push_back(&op);
+      x.emplace_back();
+      op_features_with(op, ctx, m.first, m.second, x.back().data());
+      for (const auto& c : op.children) pre(*c);
+      for (const auto& c : op.negated) pre(*c);
+   };
+   pre(root);
 }
 
 // ------------------------------------------------------------------------------------------------

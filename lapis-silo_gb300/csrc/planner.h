@@ -39,6 +39,10 @@ FeatureContext feature_context(const TableImage& t);
 // leaf statistics (symbols, position, container count and encodings), predicate and threshold
 // parameters. Every value lies roughly in [-1, 1].
 void op_features(const Op& op, const FeatureContext& ctx, float* out);
+// Every node of a tree (preorder) with its features, each node's rule estimate and subtree
+// statistics computed once.
+void tree_features(const Op& root, const FeatureContext& ctx, std::vector<const Op*>& nodes,
+                   std::vector<std::array<float, PLAN_FEATURES>>& x);
 
 struct PlannerSample {
    std::array<float, PLAN_FEATURES> x;
