@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <numeric>
 #include <unordered_map>
 
@@ -429,8 +431,19 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
          throw std::invalid_argument("no such sequence column");
       if (q.action < 0 || q.action > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
    }
-   const uint32_t W = fit_tile_bits(requested_tile_bits, depth, true);
-   const uint32_t tiles_per_query = nchunks() * (CHUNK_ROWS / W);
+   // Filter classes: the stack of the deepest program sizes every CTA's shared memory, so programs
+   // are grouped by tile width, chosen per program to keep the stack within 48 KiB (about four
+   // CTAs per SM) while the tile stays as wide as possible; one persistent launch per class.
+   auto class_w = [&](uint32_t d) {
+      if (requested_tile_bits) return fit_tile_bits(requested_tile_bits, depth, true);
+      uint32_t w = batch_tile_bits;
+      while (w > 16384 && static_cast<size_t>(d) * (w / 8) > 48 * 1024) w >>= 1;
+      return fit_tile_bits(w, d, true);
+   };
+   std::map<uint32_t, std::vector<uint32_t>, std::greater<uint32_t>> by_w;
+   for (uint32_t i = 0; i < n; ++i) by_w[class_w(qs[i].prog.max_depth)].push_back(i);
+   size_t nitems = 0;
+   for (const auto& [w, v] : by_w) nitems += static_cast<size_t>(v.size()) * nchunks() * (CHUNK_ROWS / w);
    // slots (queries whose row set is kept): Mutations grouped by column, then Details
    std::vector<std::vector<uint32_t>> by_col(table_.seq.size());
    std::vector<uint32_t> details;
@@ -465,7 +478,6 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    }
    const uint32_t nslots = static_cast<uint32_t>(slot_query.size());
    const uint32_t n_det = nslots - n_mut;
-   const size_t nitems = static_cast<size_t>(n) * tiles_per_query;
    if (nitems > 0xFFFFFFFFull) throw std::invalid_argument("batch too large");
    size_t n_ids = 0;
    for (uint32_t qi : details) n_ids += qs[qi].k;
@@ -480,7 +492,7 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    grow_device(b.d_slot_query, b.dc_slot_query, nslots);
    grow_host(b.h_counts, n, b.hc_counts);
    grow_device(b.d_counts, b.dc_counts, n);
-   grow_device(b.d_next, b.dc_next, 1);
+   grow_device(b.d_next, b.dc_next, by_w.size());
    grow_device(b.d_tiles, b.dc_tiles, static_cast<size_t>(nslots) * nchunks() * CHUNK_WORDS);
    grow_host(b.h_mcounts, counts_words, b.hc_mcounts);
    grow_device(b.d_mcounts, b.dc_mcounts, counts_words);
@@ -525,32 +537,45 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
                            p.n_ctr_leaves | (p.n_cov_leaves << 16)};
       off += p.code.size();
    }
-   // items: tile-major interleaving spreads the expensive queries over the whole launch; with
-   // predicted costs (learned planner) the queries go heaviest first so the long ones do not end
-   // the launch alone
-   std::vector<uint32_t> qorder(n);
-   std::iota(qorder.begin(), qorder.end(), 0u);
-   bool costed = false;
-   for (const auto& q : qs) costed |= q.cost > 0;
-   if (costed)
-      std::stable_sort(qorder.begin(), qorder.end(), [&](uint32_t x, uint32_t y) { return qs[x].cost > qs[y].cost; });
+   // items per class: tile-major interleaving spreads the expensive queries over the whole launch;
+   // with predicted costs (learned planner) the queries go heaviest first so the long ones do not
+   // end the launch alone
+   int props = 0;
+   cuda_check(cudaDeviceGetAttribute(&props, cudaDevAttrMultiProcessorCount, device_), "attribute");
+   b.fgroups.clear();
    size_t k = 0;
-   for (uint32_t t = 0; t < tiles_per_query; ++t)
-      for (uint32_t i = 0; i < n; ++i) b.h_items[k++] = WorkItem{qorder[i], t};
+   for (auto& [w, qv] : by_w) {
+      bool costed = false;
+      uint32_t gdepth = 1;
+      for (uint32_t qi : qv) {
+         costed |= qs[qi].cost > 0;
+         gdepth = std::max(gdepth, qs[qi].prog.max_depth);
+      }
+      if (costed)
+         std::stable_sort(qv.begin(), qv.end(), [&](uint32_t x, uint32_t y) { return qs[x].cost > qs[y].cost; });
+      const uint32_t tiles = nchunks() * (CHUNK_ROWS / w);
+      const size_t off = k;
+      for (uint32_t t = 0; t < tiles; ++t)
+         for (uint32_t qi : qv) b.h_items[k++] = WorkItem{qi, t};
+      const size_t smem = static_cast<size_t>(gdepth) * (w / 8);
+      b.fgroups.push_back(BatchState::FilterGroup{static_cast<uint32_t>(off), static_cast<uint32_t>(k - off), w, gdepth,
+                                                  static_cast<uint32_t>(props) *
+                                                     static_cast<uint32_t>(filter_batch_blocks_per_sm(smem))});
+   }
    std::memcpy(b.h_slot_query, slot_query.data(), slot_query.size() * sizeof(uint32_t));
    b.n_queries = n;
    b.n_slots = nslots;
    b.n_items = static_cast<uint32_t>(nitems);
    b.n_code = static_cast<uint32_t>(ncode);
    b.max_depth = depth;
-   b.tile_bits = W;
+   // reported shape: the class with the most items
+   const auto big = std::max_element(b.fgroups.begin(), b.fgroups.end(),
+                                     [](const auto& x, const auto& y) { return x.n_items < y.n_items; });
+   b.tile_bits = big != b.fgroups.end() ? big->tile_bits : batch_tile_bits;
+   b.grid = big != b.fgroups.end() ? big->grid : 0;
    b.counts_words = counts_words;
    b.scratch_words = scratch_words;
    b.mask_bytes = mask_bytes;
-   int props = 0;
-   cuda_check(cudaDeviceGetAttribute(&props, cudaDevAttrMultiProcessorCount, device_), "attribute");
-   const size_t smem = static_cast<size_t>(depth) * (W / 8);
-   b.grid = static_cast<uint32_t>(props) * static_cast<uint32_t>(filter_batch_blocks_per_sm(smem));
 }
 
 void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool copy_out, uint32_t parts) {
@@ -575,12 +600,15 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
    }
    if (parts & 1) {
       cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
-      cuda_check(cudaMemsetAsync(b.d_next, 0, sizeof(uint32_t), s), "memset");
+      cuda_check(cudaMemsetAsync(b.d_next, 0, b.fgroups.size() * sizeof(uint32_t), s), "memset");
       if (b.counts_words) cuda_check(cudaMemsetAsync(b.d_mcounts, 0, b.counts_words * 4, s), "memset");
       if (b.scratch_words) cuda_check(cudaMemsetAsync(b.d_mscratch, 0, b.scratch_words * 4, s), "memset");
-      cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.tile_bits, b.max_depth,
-                                     b.d_tiles, b.d_counts, b.d_next, b.grid, b.d_err, s),
-                 "filter batch launch");
+      for (size_t g = 0; g < b.fgroups.size(); ++g) {
+         const auto& fg = b.fgroups[g];
+         cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items + fg.item_off, fg.n_items,
+                                        fg.tile_bits, fg.max_depth, b.d_tiles, b.d_counts, b.d_next + g, fg.grid, b.d_err, s),
+                    "filter batch launch");
+      }
    }
    const size_t words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
    for (const auto& g : b.groups) {

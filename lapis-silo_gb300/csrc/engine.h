@@ -36,6 +36,11 @@ struct BatchQuery {
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
 struct BatchState {
+   // One persistent filter launch per class of programs sharing a tile width and stack depth.
+   struct FilterGroup {
+      uint32_t item_off, n_items, tile_bits, max_depth, grid;
+   };
+   std::vector<FilterGroup> fgroups;
    struct ColGroup {
       int column;
       uint32_t slot_begin, n;
