@@ -27,7 +27,7 @@ constexpr int MAX_DATE_COLS = 8;
 // range (SU_ARRAYS: up to SU elements of one chunk's array payloads; SU_BITSET: the bitset's 4096
 // u16); c0/c1: descriptor range (arrays: every descriptor overlapping [e0, e1); bitset / run: one).
 enum : uint32_t { SU_ARRAYS = 0, SU_BITSET = 1, SU_RUN = 2 };
-constexpr uint32_t SU = 8192;
+constexpr uint32_t SU = 4096;
 struct StreamUnit {
    uint32_t kind;
    uint32_t v;

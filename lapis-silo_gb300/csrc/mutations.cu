@@ -26,6 +26,12 @@ namespace {
 constexpr uint32_t MT = 256;
 constexpr uint32_t NW = MT / 32;
 
+constexpr uint32_t STAGED_UNITS = 64;  // units of one CTA staged in shared memory
+constexpr uint32_t EPT = SU / MT;      // array elements per thread in a unit (16)
+constexpr uint32_t DESC_CAP = 256;     // descriptors of an array unit copied beside its payload
+constexpr uint32_t BUF4 = SU / 8 + DESC_CAP;  // uint4 per buffer: payload, then descriptors
+static_assert(EPT == 16, "units hold 16 elements per thread");
+
 // Block-wide exclusive prefix sum of one value per thread; *total receives the sum. Contains
 // one barrier; the caller separates consecutive calls with another.
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, uint32_t* total) {
@@ -50,24 +56,26 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, 
 }
 
 // Container pass of the Mutations action, streaming the payload arena. Persistent CTAs walk a
-// contiguous range of the column's stream units (chunk-major):
+// contiguous range of the column's stream units (chunk-major), staged in shared memory:
 //   SU_ARRAYS  up to SU consecutive elements of a chunk's array payloads (arrays are stored back to
 //              back in descriptor order), with the descriptor range [c0, c1) overlapping them;
 //   SU_BITSET  one bitset container; SU_RUN one run container.
-// Array and bitset payloads are double-buffered into shared memory by TMA bulk copies (the copy
-// of the next unit is in flight while the current one is counted). For array units thread t
-// tests elements 32t..32t+31 against the filter tile of the chunk (staged in shared memory), a
+// Array and bitset payloads, and the first DESC_CAP descriptors of an array unit, are double-
+// buffered into shared memory by TMA bulk copies completing on one mbarrier (the copy of the next
+// unit is in flight while the current one is counted). For array units thread t tests elements
+// EPT t .. EPT t + EPT - 1 against the filter tile of the chunk (staged in shared memory), a
 // block prefix sum over the membership bits gives every container its |F ∩ c| as the difference
 // of two prefix values, added to counts[symbol][position] (containers cut by a unit boundary add
 // two partial counts). Full filters (|F| == rows) use the stored cardinalities
 // (reference: mutations_node.cpp:139-190, full path :240-266).
-__global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
+__global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                         const uint32_t* __restrict__ filter,
                                                         const unsigned long long* __restrict__ fcount,
                                                         uint32_t* counts, int* err) {
-   extern __shared__ __align__(128) uint4 sm4[];  // two SU-element buffers, then the filter tile
+   extern __shared__ __align__(128) uint4 sm4[];  // two buffers (payload + descriptors), then the filter tile
    __shared__ __align__(8) uint64_t bar[2];
    __shared__ uint32_t wsum[NW], msk[MT], exq[MT];
+   __shared__ StreamUnit su[STAGED_UNITS];  // this CTA's units, staged once
    const unsigned long long fc = *fcount;
    if (fc == 0) return;
    const bool full = fc == tab->n_rows;
@@ -76,24 +84,29 @@ __global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __res
    const uint32_t u0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * n_units / gridDim.x);
    const uint32_t u1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * n_units / gridDim.x);
    if (u0 >= u1) return;
-   const StreamUnit* __restrict__ units = cs->su;
+   const StreamUnit* __restrict__ gunits = cs->su;
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint16_t* __restrict__ payload = cs->payload;
    const uint32_t L = cs->L, tid = threadIdx.x;
-   uint32_t* F = reinterpret_cast<uint32_t*>(sm4 + 2 * (SU / 8));
+   uint32_t* F = reinterpret_cast<uint32_t*>(sm4 + 2 * BUF4);
    if (tid == 0) {
       mbar_init(&bar[0]);
       mbar_init(&bar[1]);
    }
+   for (uint32_t i = tid; i < u1 - u0 && i < STAGED_UNITS; i += MT) su[i] = gunits[u0 + i];
    __syncthreads();
+   auto unit = [&](uint32_t u) { return u - u0 < STAGED_UNITS ? su[u - u0] : gunits[u]; };
    auto copies = [&](const StreamUnit& U) { return !full && U.kind != SU_RUN; };
-   auto issue = [&](const StreamUnit& U, uint32_t b) {  // thread 0
+   auto issue = [&](const StreamUnit& U, uint32_t b) {  // thread 0: payload and descriptors on one barrier
       const uint32_t bytes = U.kind == SU_BITSET ? CHUNK_ROWS / 8 : ((U.e1 - U.e0) * 2u + 15u) & ~15u;
-      bulk_copy_g2s(sm4 + b * (SU / 8), payload + U.e0, bytes, &bar[b]);
+      const uint32_t nd = U.kind == SU_ARRAYS ? min(U.c1 - U.c0, DESC_CAP) : 0u;
+      mbar_expect(&bar[b], bytes + nd * 16u);
+      bulk_copy_g2s_tx(sm4 + b * BUF4, payload + U.e0, bytes, &bar[b]);
+      if (nd) bulk_copy_g2s_tx(sm4 + b * BUF4 + SU / 8, ctrs + U.c0, nd * 16u, &bar[b]);
    };
    uint32_t issued0 = 0, issued1 = 0;  // copies issued into each buffer (the same in every thread)
    {
-      const StreamUnit U = units[u0];
+      const StreamUnit U = unit(u0);
       if (copies(U)) {
          if (tid == 0) issue(U, 0);
          ++issued0;
@@ -103,14 +116,14 @@ __global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __res
    bool ok = true;
    for (uint32_t u = u0; u < u1 && ok; ++u) {
       const uint32_t b = (u - u0) & 1u;
-      const StreamUnit U = units[u];
+      const StreamUnit U = unit(u);
       if (!full && U.v != cur_v) {
          const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(U.v) * CHUNK_WORDS);
          for (uint32_t i = tid; i < CHUNK_WORDS / 4; i += MT) reinterpret_cast<uint4*>(F)[i] = __ldg(src + i);
          cur_v = U.v;
       }
       if (u + 1 < u1) {
-         const StreamUnit N = units[u + 1];
+         const StreamUnit N = unit(u + 1);
          if (copies(N)) {
             if (tid == 0) issue(N, b ^ 1u);
             if (b) ++issued0;
@@ -133,28 +146,32 @@ __global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __res
                if (s < e) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], e - s);
             }
          } else {
-            // this thread's first descriptor is loaded before the element tests hide its latency
-            const uint32_t c_first = U.c0 + tid;
-            uint4 raw0 = make_uint4(0, 0, 0, 0);
-            if (c_first < U.c1) raw0 = __ldg(reinterpret_cast<const uint4*>(ctrs) + c_first);
+            const uint4* sdesc = sm4 + b * BUF4 + SU / 8;
             const uint32_t n = U.e1 - U.e0;
-            const uint4* q = sm4 + b * (SU / 8) + 4 * tid;
+            const uint4* q = sm4 + b * BUF4 + 2 * tid;
             uint32_t m = 0;
+            // element r of the chunk sets mask bit k when row r is in F: the filter word holding r,
+            // rotated right by (r - k) mod 32, has that row's bit at position k
             if (n == SU) {
 #pragma unroll
-               for (uint32_t j = 0; j < 4; ++j) {
-                  const uint4 x = q[j];
-#pragma unroll
-                  for (uint32_t t = 0; t < 8; ++t) m |= test_bit(F, u16_of(x, t)) << (8 * j + t);
-               }
-            } else {
-#pragma unroll
-               for (uint32_t j = 0; j < 4; ++j) {
+               for (uint32_t j = 0; j < 2; ++j) {
                   const uint4 x = q[j];
 #pragma unroll
                   for (uint32_t t = 0; t < 8; ++t) {
-                     const uint32_t i = 32 * tid + 8 * j + t;
-                     if (i < n) m |= test_bit(F, u16_of(x, t)) << (8 * j + t);
+                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
+                     const uint32_t w = F[r >> 5];
+                     m |= __funnelshift_r(w, w, r - k) & (1u << k);
+                  }
+               }
+            } else {
+#pragma unroll
+               for (uint32_t j = 0; j < 2; ++j) {
+                  const uint4 x = q[j];
+#pragma unroll
+                  for (uint32_t t = 0; t < 8; ++t) {
+                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
+                     const uint32_t w = F[r >> 5];
+                     if (EPT * tid + k < n) m |= __funnelshift_r(w, w, r - k) & (1u << k);
                   }
                }
             }
@@ -164,11 +181,11 @@ __global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __res
             exq[tid] = ex;
             __syncthreads();
             auto prefix = [&](uint32_t i) -> uint32_t {  // members among elements [0, i)
-               if ((i >> 5) >= MT) return total;
-               return exq[i >> 5] + __popc(msk[i >> 5] & ((1u << (i & 31)) - 1u));
+               if (i / EPT >= MT) return total;
+               return exq[i / EPT] + __popc(msk[i / EPT] & ((1u << (i % EPT)) - 1u));
             };
-            for (uint32_t c = c_first; c < U.c1; c += MT) {
-               const uint4 raw = c == c_first ? raw0 : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
+            for (uint32_t c = U.c0 + tid; c < U.c1; c += MT) {
+               const uint4 raw = c - U.c0 < DESC_CAP ? sdesc[c - U.c0] : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
                const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
                if (d.type != CT_ARRAY) continue;
                const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
@@ -184,7 +201,7 @@ __global__ void __launch_bounds__(MT, 5) mut_stream_kernel(const DevTable* __res
          if (full) {
             k = tid == 0 ? d.card_m1 + 1u : 0u;
          } else if (U.kind == SU_BITSET) {
-            const uint4* x = sm4 + b * (SU / 8);
+            const uint4* x = sm4 + b * BUF4;
             const uint4* f = reinterpret_cast<const uint4*>(F);
 #pragma unroll
             for (uint32_t j = 0; j < CHUNK_WORDS / 4 / MT; ++j) {
@@ -303,7 +320,7 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
                       void* stream, uint32_t parts) {
    cudaStream_t s = static_cast<cudaStream_t>(stream);
    if ((parts & MUT_PART_CTR) && col_host.nsu > 0) {
-      const size_t smem = 2 * SU * 2 + CHUNK_WORDS * 4;
+      const size_t smem = 2 * BUF4 * 16 + CHUNK_WORDS * 4;
       // resident CTAs per device, computed once per device
       static std::atomic<uint32_t> resident[64];
       int dev = 0;

@@ -31,6 +31,22 @@ __device__ __forceinline__ void bulk_copy_g2s(void* smem, const void* gmem, uint
                 : "memory");
 }
 
+// One arrival that announces `bytes` of bulk copies completing on `bar`; the copies are then issued
+// with bulk_copy_g2s_tx. Called by one thread.
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(b), "r"(bytes)
+                : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s_tx(void* smem, const void* gmem, uint32_t bytes, uint64_t* bar) {
+   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(s),
+                "l"(gmem), "r"(bytes), "r"(b)
+                : "memory");
+}
+
 // Waits (bounded) for the phase with the given parity to complete. Returns false if it gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
