@@ -1,16 +1,13 @@
-// sm_103a kernels of the filter / count / mutations hot path.
+// sm_103a kernels of the filter and Count path (the Mutations kernels are in mutations.cu and
+// batch.cu, the output rows in rows.cu, Details in details.cu).
 //
 //  filter_kernel        one CTA per (chunk, tile of W rows): runs the postorder filter program over a
 //                       stack of W-bit tiles in shared memory; leaves expand array / bitset / run
 //                       containers straight into shared memory; writes the row-set tile and/or adds
 //                       its popcount (Count action, reference: copy_on_write_bitmap.cpp:108-118).
+//                       With a trace buffer it records every instruction's cycles and result size
+//                       (planner training).
 //  filter_batch_kernel  persistent variant: CTAs pull (query, tile) work items from a counter.
-//  mut_ctr_kernel       Mutations: every vertical container once, popcount against the filter tile of
-//                       its chunk staged in shared memory, integer counts per (symbol, position)
-//                       (reference: mutations_node.cpp:139-189).
-//  mut_cov_kernel       Mutations: rows of the filter outside coverage and inside missing intervals,
-//                       by position block (reference: mutations_node.cpp:51-136).
-//  mut_final_kernel     Mutations: local-reference counts (reference: mutations_node.cpp:192-203).
 // All arithmetic is integer; results are bit-exact with the CPU operators.
 #include <cuda_runtime.h>
 

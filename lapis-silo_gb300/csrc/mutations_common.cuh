@@ -7,28 +7,13 @@
 
 namespace rhygpu {
 
-constexpr uint32_t SMALL_ARRAY = 32;  // array containers up to this size are counted by one lane
-
 // mbarrier + TMA bulk-copy helpers. A barrier is initialised with one arrival; the issuing thread
-// arrives with the expected byte count and starts the copy, whose completion flips the phase.
+// arrives with the expected byte count of the copies it then starts, whose completion flips the
+// phase.
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Copies `bytes` (a multiple of 16, both addresses 16-byte aligned) from global to shared memory
-// and completes them on `bar`. Called by one thread.
-__device__ __forceinline__ void bulk_copy_g2s(void* smem, const void* gmem, uint32_t bytes, uint64_t* bar) {
-   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
-   // order earlier generic-proxy accesses of the buffer before the asynchronous write
-   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(b), "r"(bytes)
-                : "memory");
-   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(s),
-                "l"(gmem), "r"(bytes), "r"(b)
-                : "memory");
 }
 
 // One arrival that announces `bytes` of bulk copies completing on `bar`; the copies are then issued
@@ -62,8 +47,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
    return false;
 }
 
-__device__ __forceinline__ uint32_t test_bit(const uint32_t* F, uint32_t r) { return (F[r >> 5] >> (r & 31)) & 1u; }
-
 // popcount of F in [a, b)
 __device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, uint32_t b) {
    if (a >= b) return 0;
@@ -82,42 +65,6 @@ __device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, u
 __device__ __forceinline__ uint32_t u16_of(const uint4& w, uint32_t t) {
    const uint32_t x = t < 2 ? w.x : t < 4 ? w.y : t < 6 ? w.z : w.w;
    return (t & 1u) ? (x >> 16) : (x & 0xFFFFu);
-}
-
-__device__ __forceinline__ CtrDesc shfl_desc(const uint4& raw, int lane) {
-   uint4 r;
-   r.x = __shfl_sync(0xFFFFFFFFu, raw.x, lane);
-   r.y = __shfl_sync(0xFFFFFFFFu, raw.y, lane);
-   r.z = __shfl_sync(0xFFFFFFFFu, raw.z, lane);
-   r.w = __shfl_sync(0xFFFFFFFFu, raw.w, lane);
-   return *reinterpret_cast<const CtrDesc*>(&r);
-}
-
-// Calls f(row) for every element of a small array container (card <= SMALL_ARRAY) with at most five
-// independent 16-byte loads. The payload arena is padded so the covering words stay in bounds.
-template <typename Fn>
-__device__ __forceinline__ void small_array_for_each(const CtrDesc& d, const uint16_t* __restrict__ payload, Fn&& f) {
-   const uint32_t s = d.payload, e = s + d.card_m1 + 1u;
-   const uint4* pw = reinterpret_cast<const uint4*>(payload);
-   const uint32_t w0 = s >> 3, w1 = (e - 1) >> 3;
-   uint4 buf[5];
-#pragma unroll
-   for (uint32_t k = 0; k < 5; ++k) buf[k] = (w0 + k <= w1) ? __ldg(pw + w0 + k) : make_uint4(0, 0, 0, 0);
-#pragma unroll
-   for (uint32_t k = 0; k < 5; ++k) {
-#pragma unroll
-      for (uint32_t t = 0; t < 8; ++t) {
-         const uint32_t j = 8 * (w0 + k) + t;
-         if (j >= s && j < e) f(u16_of(buf[k], t));
-      }
-   }
-}
-
-__device__ __forceinline__ uint32_t small_array_count(const CtrDesc& d, const uint16_t* __restrict__ payload,
-                                                      const uint32_t* F) {
-   uint32_t c = 0;
-   small_array_for_each(d, payload, [&](uint32_t r) { c += test_bit(F, r); });
-   return c;
 }
 
 __device__ __forceinline__ uint32_t block_incl_scan_u32(uint32_t v, uint32_t* red) {
