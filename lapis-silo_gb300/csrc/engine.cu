@@ -432,12 +432,13 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
       if (q.action < 0 || q.action > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
    }
    // Filter classes: the stack of the deepest program sizes every CTA's shared memory, so programs
-   // are grouped by tile width, chosen per program to keep the stack within 48 KiB (about four
-   // CTAs per SM) while the tile stays as wide as possible; one persistent launch per class.
+   // are grouped by tile width, chosen per program to keep the stack within 40 KiB (with the leaf
+   // cache, four CTAs per SM) while the tile stays as wide as possible; one persistent launch per
+   // class.
    auto class_w = [&](uint32_t d) {
       if (requested_tile_bits) return fit_tile_bits(requested_tile_bits, depth, true);
       uint32_t w = batch_tile_bits;
-      while (w > 16384 && static_cast<size_t>(d) * (w / 8) > 48 * 1024) w >>= 1;
+      while (w > 16384 && static_cast<size_t>(d) * (w / 8) > 40 * 1024) w >>= 1;
       return fit_tile_bits(w, d, true);
    };
    std::map<uint32_t, std::vector<uint32_t>, std::greater<uint32_t>> by_w;

@@ -81,15 +81,23 @@ struct TileCtx {
 //    trip (its payload) instead of three;
 //  - coverage leaves (PUSH_COVERED, c = ordinal + 1): the tile's ranges of coverage exceptions and
 //    missing intervals.
-// Every staged payload and range is also handed to the TMA engine as a bulk L2 prefetch, so the
-// leaves find their data in L2 when the program reaches them.
+// Array payloads of at most LC_SMALL rows are copied into shared memory by TMA bulk copies; every
+// other staged payload and range is handed to the TMA engine as a bulk L2 prefetch, so the leaves
+// find their data in L2 when the program reaches them.
 constexpr uint32_t LC_LEAVES = 128;
 constexpr uint32_t LC_DESCS = 256;
 constexpr uint32_t LC_COV = 64;
 constexpr uint32_t LC_NONE = 0xFFFFFFFFu;
+constexpr uint32_t LC_PAY = 2048;   // u16 of small-array payloads copied into shared memory per item
+constexpr uint32_t LC_SMALL = 64;   // arrays up to this cardinality are copied
+constexpr uint16_t LC_NOPAY = 0xFFFF;
 
 struct LeafCache {
    uint4 desc[LC_DESCS];
+   uint4 pay4[LC_PAY / 8];   // small-array payloads (TMA bulk copies, 16-byte aligned runs)
+   uint16_t poff[LC_DESCS];  // u16 offset into pay4 of descriptor i's first element, or LC_NOPAY
+   uint32_t pay_used;        // u16 of pay4 reserved by this item's copies
+   uint64_t bar;             // completes the item's payload copies
    const uint4* src[LC_LEAVES];
    const uint16_t* pay[LC_LEAVES];
    uint32_t n[LC_LEAVES];
@@ -109,11 +117,21 @@ __device__ __forceinline__ void prefetch_l2(const void* a, const void* b) {
    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"(n) : "memory");
 }
 
+// Once per CTA, before the first item: the barrier of the payload copies.
+__device__ __forceinline__ void init_leaves(LeafCache& lc) {
+   if (threadIdx.x == 0) {
+      const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b));
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+}
+
 // Clears the leaf tables for nl container and ncov coverage leaves; a barrier must follow.
 __device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_t ncov) {
    if (threadIdx.x == 0) {
       lc.nl = nl;
       lc.ncov = ncov;
+      lc.pay_used = 0;
    }
    for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
       lc.n[k] = 0;
@@ -132,7 +150,28 @@ __device__ __forceinline__ uint4 cover_ranges(const DevTable* __restrict__ tab, 
    return make_uint4(__ldg(xo + k0), __ldg(xo + k1), __ldg(no + k0), __ldg(no + k1));
 }
 
-__device__ void stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __restrict__ code, uint32_t ncode) {
+// Waits (bounded) for phase `parity` of the copies' barrier; false if it gave up.
+__device__ __forceinline__ bool wait_copies(LeafCache& lc, uint32_t parity) {
+   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
+   for (uint32_t i = 0; i < (1u << 22); ++i) {
+      uint32_t done;
+      asm volatile(
+         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         : "=r"(done)
+         : "r"(b), "r"(parity)
+         : "memory");
+      if (done) return true;
+   }
+   return false;
+}
+
+// Stages the item's leaves (see LeafCache). Array containers of at most LC_SMALL rows are also
+// copied into shared memory by TMA bulk copies: each issuing thread announces its bytes on the
+// barrier (expect_tx) before starting its copy, and one thread arrives after every announcement,
+// so the phase completes when the last copy lands. `phase` is the parity of this item's wait,
+// flipped when copies were made. Returns false (error flag set) if the copies did not land.
+__device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __restrict__ code, uint32_t ncode,
+                             uint32_t& phase, int* err) {
    const DevTable* __restrict__ tab = c.tab;
    const uint32_t nl = lc.nl, ncov = lc.ncov;
    for (uint32_t i = threadIdx.x; i < ncode; i += blockDim.x) {
@@ -189,6 +228,7 @@ __device__ void stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
       }
    }
    __syncthreads();
+   const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
    for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
       const uint32_t b = lc.beg[k];
       if (b == LC_NONE) continue;
@@ -197,15 +237,43 @@ __device__ void stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
       for (uint32_t i = 0; i < lc.n[k]; ++i) {
          const uint4 raw = __ldg(s + i);
          lc.desc[b + i] = raw;
+         lc.poff[b + i] = LC_NOPAY;
          const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
          // the arena ends with 16 spare bytes, so rounding the end up stays inside it
          const uint16_t* p = pay + d.payload;
+         if (d.type == CT_ARRAY && d.card_m1 < LC_SMALL) {
+            const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+            const uintptr_t a0 = a & ~static_cast<uintptr_t>(15);
+            const uint32_t bytes = static_cast<uint32_t>(((a + 2u * (d.card_m1 + 1u) + 15) & ~static_cast<uintptr_t>(15)) - a0);
+            const uint32_t at = atomicAdd(&lc.pay_used, bytes / 2);
+            if (at + bytes / 2 <= LC_PAY) {
+               lc.poff[b + i] = static_cast<uint16_t>(at + (a - a0) / 2);
+               const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(lc.pay4)) + 2 * at;
+               asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+               asm volatile(
+                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                  "l"(a0), "r"(bytes), "r"(bar)
+                  : "memory");
+               continue;
+            }
+         }
          if (d.type == CT_ARRAY) prefetch_l2(p, p + d.card_m1 + 1u);
          else if (d.type == CT_BITSET) prefetch_l2(p + (c.row0 >> 4), p + ((c.row0 + c.W) >> 4));
          else prefetch_l2(p, p + 2u * d.nruns);
       }
    }
    __syncthreads();
+   if (lc.pay_used == 0) return true;  // no copies this item
+   if (threadIdx.x == 0)
+      asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
+   bool ok = wait_copies(lc, phase);
+   if (!ok) ok = wait_copies(lc, phase);  // once more before giving up with copies possibly in flight
+   phase ^= 1u;
+   if (!__syncthreads_and(ok)) {
+      if (threadIdx.x == 0) atomicExch(err, 6);
+      return false;
+   }
+   return true;
 }
 
 // OR of the containers of one slot whose symbol is in `mask` (all of them when !use_mask), from
@@ -223,11 +291,22 @@ __device__ void push_containers(uint32_t* t, const TileCtx& c, const CtrDesc* __
       src = reinterpret_cast<const uint4*>(ctrs) + b;
       n = e - b;
    }
+   const bool staged = leaf >= 1 && leaf <= lc.nl && lc.beg[leaf - 1] != LC_NONE;
    for (uint32_t i = 0; i < n; ++i) {
       const uint4 raw = src[i];
       const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
       if (use_mask && !((mask >> d.sym) & 1u)) continue;
-      or_container(t, d, payload, c.row0, c.W);
+      const uint16_t po = staged ? lc.poff[lc.beg[leaf - 1] + i] : LC_NOPAY;
+      if (po != LC_NOPAY) {  // array copied into shared memory with the item's leaves
+         const uint16_t* sp = reinterpret_cast<const uint16_t*>(lc.pay4) + po;
+         const uint32_t card = d.card_m1 + 1u;
+         for (uint32_t k = threadIdx.x; k < card; k += blockDim.x) {
+            const uint32_t r = static_cast<uint32_t>(sp[k]) - c.row0;
+            if (r < c.W) atomicOr(&t[r >> 5], 1u << (r & 31));
+         }
+      } else {
+         or_container(t, d, payload, c.row0, c.W);
+      }
    }
 }
 
@@ -628,9 +707,11 @@ __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__
       for (uint32_t w4 = threadIdx.x; w4 < (tile_bits >> 7); w4 += blockDim.x)
          reinterpret_cast<uint4*>(smem)[w4] = make_uint4(0, 0, 0, 0);
    } else {
+      init_leaves(lc);
       clear_leaves(lc, min(n_leaves & 0xFFFFu, LC_LEAVES), min(n_leaves >> 16, LC_COV));
       __syncthreads();
-      stage_leaves(lc, c, code, ncode);
+      uint32_t phase = 0;
+      if (!stage_leaves(lc, c, code, ncode, phase, err)) return;
       if (!run_program(c, code, ncode, smem, cap, lc, err,
                        trace ? trace + static_cast<size_t>(blockIdx.x) * ncode * 2 : nullptr))
          return;
@@ -654,6 +735,8 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
    __shared__ LeafCache lc;
    const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t per_query = static_cast<size_t>(tab->nchunks) * CHUNK_WORDS;
+   init_leaves(lc);
+   uint32_t phase = 0;
    for (;;) {
       if (threadIdx.x == 0) item_idx = atomicAdd(next_item, 1u);
       __syncthreads();
@@ -674,7 +757,7 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
          for (uint32_t w4 = threadIdx.x; w4 < (tile_bits >> 7); w4 += blockDim.x)
             reinterpret_cast<uint4*>(smem)[w4] = make_uint4(0, 0, 0, 0);
       } else {
-         stage_leaves(lc, c, code + q.code_off, q.code_len);
+         if (!stage_leaves(lc, c, code + q.code_off, q.code_len, phase, err)) return;
          if (!run_program(c, code + q.code_off, q.code_len, smem, cap, lc, err)) return;
       }
       uint32_t* dst = q.out_tiles ? out_tiles + static_cast<size_t>(q.out_tiles - 1) * per_query +
