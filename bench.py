@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--planner-queries", type=int, default=1000,
                     help="queries (another seed) traced through the plain path to train the planner")
     ap.add_argument("--no-planner", action="store_true", help="rule-based ordering only")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default filter schedule")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
     return ap.parse_args()
@@ -279,6 +280,17 @@ def main():
         if st["accepted"]:
             dev.planner_mode(1)
 
+    # ---------------- autotuner: schedule of the filter launches of this batch (untimed) ----------------
+    autotune = None
+    if not args.no_autotune and not args.tile_bits:
+        default_sched = dev.batch_schedule()
+        t0 = time.perf_counter()
+        tried = dev.batch_autotune(queries, actions, columns, reps=3, stream=sp)
+        autotune = {"candidates": len(tried), "tune_s": round(time.perf_counter() - t0, 2),
+                    "best_filter_ms": round(tried[0][1], 3),
+                    "default_filter_ms": next((round(ms, 3) for sc, ms in tried if sc == default_sched), None),
+                    "worst_filter_ms": round(tried[-1][1], 3)}
+
     # ---------------- batched path: device-resident ----------------
     dev.batch_prepare(queries, actions, columns, tile_bits=args.tile_bits)
     info = dev.batch_info()
@@ -375,14 +387,19 @@ def main():
 
     # ---------------- batched e2e through the C-ABI ----------------
     # rows of the Mutations action built on the device; the dense-count variant is kept for context
-    e2e_s = []
+    e2e_s, e2e_phases = [], []
     min_props = np.full(n, 0.05)
     for step in range(max(2, min(args.steps, 3))):
         t0 = time.perf_counter()
         r_counts, rows, r_begin, r_cnt = dev.batch_rows(queries, actions, columns, min_props,
                                                         tile_bits=args.tile_bits, stream=sp)
         e2e_s.append(time.perf_counter() - t0)
+        e2e_phases.append(dev.batch_times())
     e2e_qps = n * ws / max_over_ranks(statistics.median(e2e_s), ws)
+    # host wall time per phase of the median step; "other" is the binding's own time
+    mid = sorted(range(len(e2e_s)), key=lambda i: e2e_s[i])[len(e2e_s) // 2]
+    e2e_phase_ms = {k: round(v, 3) for k, v in e2e_phases[mid].items()}
+    e2e_phase_ms["other_ms"] = round(1000 * e2e_s[mid] - sum(e2e_phases[mid].values()), 3)
     dense_s = []
     for step in range(2):
         t0 = time.perf_counter()
@@ -470,6 +487,7 @@ def main():
                                    f"({n - n_mut} Aggregated count + {n_mut} nucleotide Mutations)",
                        "rows": args.rows, "batch": n, "mutations_per_batch": n_mut, "aa_genes": 12,
                        "tile_bits": info.tile_bits, "grid": info.grid, "planner": planner["mode"],
+                       "schedule": dev.batch_schedule(),
                        "l2": "flushed before every timed step (256 MiB write, outside the events)",
                        "parallelism": f"replicas x{ws}"},
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
@@ -479,12 +497,13 @@ def main():
                       "e2e_p99_ms": float(np.percentile(e2e_plain_ms, 99))},
             "speedup_vs_plain": value / plain_qps,
             "planner": planner,
+            "autotune": autotune,
             "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
                     "d2h_bytes_per_step": int(d2h), "output": "Mutations rows (min proportion 0.05) + counts",
                     "rows_per_step": int(len(rows)), "rows_mismatches": rows_mismatches,
-                    "dense_counts_qps": dense_qps},
+                    "dense_counts_qps": dense_qps, "phases_ms": e2e_phase_ms},
             "gpu_launches": launches_per_step * args.steps,
             "kernels_ms": kernels_ms,
             "roofline": {"kernel": "mut_stream_kernel (plain Mutations container pass, nucleotide column)",

@@ -136,9 +136,10 @@ int rhy_local_reference(const RhyTable* t, uint32_t column, char* out, size_t ca
  * chunk, symbol, cardinality and encoding (0 array, 1 bitset, 2 run). Pass cap = 0 to size. */
 int rhy_seq_containers(const RhyTable* t, uint32_t column, uint32_t* pos, uint16_t* chunk, uint8_t* sym, uint32_t* card,
                        uint8_t* type, size_t cap, size_t* n);
-/* Newline-separated seeded random filter expressions; *needed receives the byte count (incl. NUL). */
+/* Newline-separated seeded random filter expressions (trees of at most max_leaves leaves, 0 = no
+ * limit); *needed receives the byte count (incl. NUL). */
 int rhy_generate_queries(const RhyTable* t, uint64_t seed, uint32_t n, uint32_t max_depth, uint32_t max_nof_children,
-                         int use_aa, int use_metadata, char* buf, size_t cap, size_t* needed);
+                         uint32_t max_leaves, int use_aa, int use_metadata, char* buf, size_t cap, size_t* needed);
 void rhy_table_free(RhyTable* t);
 
 /* ---- planning ---- */
@@ -170,11 +171,21 @@ int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const 
  * order. counts[i] receives every query's filter cardinality; *n_rows the total number of rows,
  * which are copied when *n_rows <= rows_cap (otherwise rhy_batch_rows_fetch copies them without
  * recomputing). Query i's rows are rows[row_begin[i] .. row_begin[i] + row_count[i]).
- * min_proportions may be NULL (0.05 for every query); each must lie in [0, 1]. */
+ * min_proportions may be NULL (0.05 for every query); each must lie in [0, 1]. The batch is planned
+ * and run in parts (Mutations and Details first, then the counts in parts of about 512) so that
+ * planning a part overlaps the device work of the ones before it; results do not depend on it. */
 int rhy_batch_rows(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns,
                    const double* min_proportions, uint32_t n, uint32_t tile_bits, void* stream, uint64_t* counts,
                    RhyMutationRow* rows, size_t rows_cap, uint64_t* row_begin, uint32_t* row_count, size_t* n_rows);
 int rhy_batch_rows_fetch(RhyDevice* d, void* stream, RhyMutationRow* rows, size_t rows_cap);
+
+/* Host wall time of the phases of the last rhy_batch_rows call: planning (parse, rewrite, compile,
+ * estimates, lowering), staging (work items, device buffers), the batch on the device up to its
+ * counts and row sizes (one synchronisation), and the packed rows with their copy to the host. */
+typedef struct {
+   double plan_ms, prepare_ms, device_ms, output_ms;
+} RhyBatchTimes;
+int rhy_batch_times(RhyDevice* d, RhyBatchTimes* out);
 
 typedef struct {
    uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
@@ -192,6 +203,22 @@ int rhy_batch_capture(RhyDevice* d, void* stream);
 int rhy_batch_replay(RhyDevice* d, void* stream);
 int rhy_batch_results(RhyDevice* d, uint64_t* counts, uint32_t* const* mut_counts);
 int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out);
+
+/* Schedule of the batched filter launches (results never depend on it): the widest tile of a class
+ * (bits), the stack budget that narrows a class's tile (KiB), persistent CTAs per SM (0 = as many
+ * as fit) and the work-item order (0 = tile-major, 1 = every tile of one query in turn). */
+typedef struct {
+   uint32_t max_tile_bits, stack_kb, ctas_per_sm, query_major;
+} RhyBatchSchedule;
+/* Sets the schedule when `set` is not NULL, then reports the one in force when `get` is not NULL. */
+int rhy_batch_schedule(RhyDevice* d, const RhyBatchSchedule* set, RhyBatchSchedule* get);
+/* Autotuner: plans the batch, times its filter launches under every candidate schedule (tile widths
+ * 16 / 32 / 64 Kbit x stack budgets 24 / 40 / 64 KiB x all or two CTAs per SM x both item orders;
+ * `reps` timed runs each, median, CUDA events on `stream`), keeps the fastest in force and returns
+ * the candidates fastest first in tried[0 .. min(cap, *n_tried)) with their milliseconds. */
+int rhy_batch_autotune(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+                       uint32_t reps, void* stream, RhyBatchSchedule* tried, double* tried_ms, size_t cap,
+                       size_t* n_tried);
 /* Variants for timing: capture without the host copies; launch a subset of the kernels
  * (bit 0 filter, bits 1..4 transpose / container / coverage / final mutations kernels). */
 int rhy_batch_capture_ex(RhyDevice* d, void* stream, int copy_in, int copy_out);

@@ -307,7 +307,7 @@ int rhy_seq_containers(const RhyTable* t, uint32_t column, uint32_t* pos, uint16
 }
 
 int rhy_generate_queries(const RhyTable* t, uint64_t seed, uint32_t n, uint32_t max_depth, uint32_t max_nof_children,
-                         int use_aa, int use_metadata, char* buf, size_t cap, size_t* needed) {
+                         uint32_t max_leaves, int use_aa, int use_metadata, char* buf, size_t cap, size_t* needed) {
    return guarded([&] {
       need(t, "table");
       rhygpu::QueryGenConfig q;
@@ -315,6 +315,7 @@ int rhy_generate_queries(const RhyTable* t, uint64_t seed, uint32_t n, uint32_t 
       q.n_queries = n;
       q.max_depth = max_depth;
       q.max_nof_children = max_nof_children;
+      q.max_leaves = max_leaves;
       q.use_aa = use_aa != 0;
       q.use_metadata = use_metadata != 0;
       if (t->gen.pool.empty()) throw std::invalid_argument("queries can only be generated for generated tables");
@@ -477,17 +478,28 @@ int rhy_batch_rows(RhyDevice* d, const char* const* exprs, const int* actions, c
       need(n_rows, "n_rows");
       *n_rows = 0;
       if (n == 0) return;
+      need(exprs, "exprs");
+      std::vector<std::string> texts(n);
+      for (uint32_t i = 0; i < n; ++i) {
+         need(exprs[i], "expression");
+         texts[i] = exprs[i];
+      }
       std::lock_guard<std::mutex> lock(d->engine->mu);
       rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
-      std::vector<rhygpu::BatchQuery> qs = make_batch(d, exprs, actions, columns, n, 0);
-      if (min_proportions)
-         for (uint32_t i = 0; i < n; ++i) qs[i].min_proportion = min_proportions[i];
-      d->engine->batch_prepare(qs, tile_bits);
       cudaStream_t s = d->engine->stream_for(static_cast<cudaStream_t>(stream));
-      *n_rows = d->engine->batch_rows(s, reinterpret_cast<rhygpu::DevMutationRow*>(rows), rows ? rows_cap : 0, row_begin,
-                                      row_count);
-      if (counts)
-         for (uint32_t i = 0; i < n; ++i) counts[i] = d->engine->batch_count(i);
+      *n_rows = d->engine->batch_rows_pipelined(texts, actions, columns, min_proportions, tile_bits, s,
+                                                reinterpret_cast<rhygpu::DevMutationRow*>(rows), rows ? rows_cap : 0,
+                                                counts, row_begin, row_count);
+   });
+}
+
+int rhy_batch_times(RhyDevice* d, RhyBatchTimes* out) {
+   return guarded([&] {
+      need(d, "device");
+      need(out, "out");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      const auto& t = d->engine->batch_times;
+      *out = RhyBatchTimes{t.plan_ms, t.prepare_ms, t.device_ms, t.output_ms};
    });
 }
 
@@ -538,6 +550,41 @@ int rhy_batch_results(RhyDevice* d, uint64_t* counts, uint32_t* const* mut_count
    return guarded([&] {
       need(d, "device");
       copy_batch_results(d, d->engine->batch().n_queries, counts, mut_counts);
+   });
+}
+
+int rhy_batch_schedule(RhyDevice* d, const RhyBatchSchedule* set, RhyBatchSchedule* get) {
+   return guarded([&] {
+      need(d, "device");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::BatchSchedule& b = d->engine->batch_schedule;
+      if (set) {
+         if (set->max_tile_bits < 4096 || set->max_tile_bits > 65536 || (set->max_tile_bits & (set->max_tile_bits - 1)))
+            throw std::invalid_argument("max_tile_bits must be a power of two in [4096, 65536]");
+         if (set->stack_kb < 8 || set->stack_kb > 200) throw std::invalid_argument("stack_kb must lie in [8, 200]");
+         if (set->query_major > 1) throw std::invalid_argument("query_major must be 0 or 1");
+         b = rhygpu::BatchSchedule{set->max_tile_bits, set->stack_kb, set->ctas_per_sm, set->query_major};
+      }
+      if (get) *get = RhyBatchSchedule{b.max_tile_bits, b.stack_kb, b.ctas_per_sm, b.query_major};
+   });
+}
+
+int rhy_batch_autotune(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n,
+                       uint32_t reps, void* stream, RhyBatchSchedule* tried, double* tried_ms, size_t cap,
+                       size_t* n_tried) {
+   return guarded([&] {
+      need(d, "device");
+      if (n == 0) throw std::invalid_argument("autotune needs a batch");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      const std::vector<rhygpu::BatchQuery> qs = make_batch(d, exprs, actions, columns, n, 0);
+      const auto res = d->engine->autotune_batch(qs, static_cast<cudaStream_t>(stream), reps);
+      if (n_tried) *n_tried = res.size();
+      for (size_t i = 0; i < res.size() && i < cap; ++i) {
+         const auto& b = res[i].first;
+         if (tried) tried[i] = RhyBatchSchedule{b.max_tile_bits, b.stack_kb, b.ctas_per_sm, b.query_major};
+         if (tried_ms) tried_ms[i] = res[i].second;
+      }
    });
 }
 

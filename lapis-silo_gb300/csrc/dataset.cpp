@@ -557,24 +557,37 @@ struct QGen {
       return e;
    }
 
-   std::string expr(uint32_t depth) {
-      if (depth >= cfg.max_depth || r.uniform() < 0.25 + 0.15 * depth) return leaf();
+   // A subtree using at most `budget` leaves (decremented by the leaves used); with no leaf limit
+   // the budget never binds, so the random stream is the same as without one.
+   std::string expr(uint32_t depth, uint32_t& budget) {
+      if (depth >= cfg.max_depth || r.uniform() < 0.25 + 0.15 * depth || budget <= 1) {
+         --budget;
+         return leaf();
+      }
+      // children share the budget: each leaves one leaf for every later sibling
+      auto child = [&](uint32_t i, uint32_t k) {
+         uint32_t b = budget - (k - 1 - i);
+         const uint32_t before = b;
+         std::string c = expr(depth + 1, b);
+         budget -= before - b;
+         return c;
+      };
       const double u = r.uniform();
-      if (u < 0.15) return "Not(" + expr(depth + 1) + ")";
+      if (u < 0.15) return "Not(" + child(0, 1) + ")";
       if (u < 0.75) {
-         const uint32_t k = 2 + r.below(3);
+         const uint32_t k = std::min(2 + r.below(3), budget);
          std::string s = u < 0.45 ? "And(" : "Or(";
          for (uint32_t i = 0; i < k; ++i) {
             if (i) s += ",";
-            s += expr(depth + 1);
+            s += child(i, k);
          }
          return s + ")";
       }
-      const uint32_t k = 1 + r.below(std::max(1u, cfg.max_nof_children));
+      const uint32_t k = std::min(1 + r.below(std::max(1u, cfg.max_nof_children)), budget);
       const uint32_t n = r.below(k + 2);  // 0..k+1 exercises the trivial cases
       const bool exact = r.uniform() < 0.3;
       std::string s = "NOf(" + std::to_string(n) + (exact ? ",exactly" : ",atleast");
-      for (uint32_t i = 0; i < k; ++i) s += "," + expr(depth + 1);
+      for (uint32_t i = 0; i < k; ++i) s += "," + child(i, k);
       s += ")";
       if (cfg.use_ambiguity && r.uniform() < 0.05) return "Maybe(" + s + ")";
       return s;
@@ -587,7 +600,10 @@ std::vector<std::string> generate_queries(const GeneratedTable& g, const QueryGe
    QGen q{g, cfg, Rng(row_seed(cfg.seed, 3, 0))};
    std::vector<std::string> out;
    out.reserve(cfg.n_queries);
-   for (uint32_t i = 0; i < cfg.n_queries; ++i) out.push_back(q.expr(0));
+   for (uint32_t i = 0; i < cfg.n_queries; ++i) {
+      uint32_t budget = cfg.max_leaves ? cfg.max_leaves : 0x40000000u;
+      out.push_back(q.expr(0, budget));
+   }
    return out;
 }
 

@@ -97,6 +97,7 @@ struct QueryGenConfig {
    bool use_aa = false;        // amino-acid leaves
    bool use_metadata = false;  // country/lineage equality, date ranges
    bool use_ambiguity = true;  // Maybe/Exact wrappers and ambiguity symbols
+   uint32_t max_leaves = 0;    // leaves per tree at most (0 = no limit)
 };
 
 // Seeded random filter expressions in the textual expression syntax of expr.h.

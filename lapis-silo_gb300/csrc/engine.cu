@@ -2,6 +2,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -228,6 +229,7 @@ Engine::~Engine() {
    if (stream_) cudaStreamSynchronize(stream_);
    cudaDeviceSynchronize();
    batch_free(batch_);
+   for (auto& b : parts_) batch_free(*b);
    for (void* p : allocs_) cudaFree(p);
    if (h_code_) cudaFreeHost(h_code_);
    if (h_count_) cudaFreeHost(h_count_);
@@ -339,15 +341,6 @@ void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint
 
 namespace rhygpu {
 
-std::vector<Program> plan_many(const TableImage& t, const std::vector<std::string>& exprs, uint32_t threads,
-                               const LowerOptions& opt) {
-   std::vector<Program> out(exprs.size());
-   const Estimator est = rule_estimator(t);
-   parallel_for(static_cast<uint32_t>(exprs.size()), threads,
-                [&](uint32_t i) { out[i] = plan_filter(exprs[i], t, &est, opt, nullptr); });
-   return out;
-}
-
 uint32_t Engine::fit_tile_bits(uint32_t requested, uint32_t depth, bool batch) const {
    uint32_t W = requested ? requested : batch ? batch_tile_bits : tile_bits;
    while (W > 4096 && static_cast<size_t>(depth) * (W / 8) > 200 * 1024) W >>= 1;
@@ -432,13 +425,14 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
       if (q.action < 0 || q.action > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
    }
    // Filter classes: the stack of the deepest program sizes every CTA's shared memory, so programs
-   // are grouped by tile width, chosen per program to keep the stack within 40 KiB (with the leaf
-   // cache, four CTAs per SM) while the tile stays as wide as possible; one persistent launch per
-   // class.
+   // are grouped by tile width, chosen per program to keep the stack within the schedule's budget
+   // (40 KiB by default: with the leaf cache, four CTAs per SM) while the tile stays as wide as the
+   // schedule allows; one persistent launch per class.
+   const BatchSchedule& sch = batch_schedule;
    auto class_w = [&](uint32_t d) {
       if (requested_tile_bits) return fit_tile_bits(requested_tile_bits, depth, true);
-      uint32_t w = batch_tile_bits;
-      while (w > 16384 && static_cast<size_t>(d) * (w / 8) > 40 * 1024) w >>= 1;
+      uint32_t w = std::min(batch_tile_bits, std::max(sch.max_tile_bits, 4096u));
+      while (w > 16384 && static_cast<size_t>(d) * (w / 8) > static_cast<size_t>(sch.stack_kb) * 1024) w >>= 1;
       return fit_tile_bits(w, d, true);
    };
    std::map<uint32_t, std::vector<uint32_t>, std::greater<uint32_t>> by_w;
@@ -556,12 +550,18 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
          std::stable_sort(qv.begin(), qv.end(), [&](uint32_t x, uint32_t y) { return qs[x].cost > qs[y].cost; });
       const uint32_t tiles = nchunks() * (CHUNK_ROWS / w);
       const size_t off = k;
-      for (uint32_t t = 0; t < tiles; ++t)
-         for (uint32_t qi : qv) b.h_items[k++] = WorkItem{qi, t};
+      if (sch.query_major) {
+         for (uint32_t qi : qv)
+            for (uint32_t t = 0; t < tiles; ++t) b.h_items[k++] = WorkItem{qi, t};
+      } else {
+         for (uint32_t t = 0; t < tiles; ++t)
+            for (uint32_t qi : qv) b.h_items[k++] = WorkItem{qi, t};
+      }
       const size_t smem = static_cast<size_t>(gdepth) * (w / 8);
+      uint32_t per_sm = static_cast<uint32_t>(filter_batch_blocks_per_sm(smem));
+      if (sch.ctas_per_sm) per_sm = std::min(per_sm, sch.ctas_per_sm);
       b.fgroups.push_back(BatchState::FilterGroup{static_cast<uint32_t>(off), static_cast<uint32_t>(k - off), w, gdepth,
-                                                  static_cast<uint32_t>(props) *
-                                                     static_cast<uint32_t>(filter_batch_blocks_per_sm(smem))});
+                                                  static_cast<uint32_t>(props) * per_sm});
    }
    std::memcpy(b.h_slot_query, slot_query.data(), slot_query.size() * sizeof(uint32_t));
    b.n_queries = n;
@@ -712,11 +712,16 @@ const uint32_t* Engine::details_ids(const BatchState& b, uint32_t i, uint32_t* n
 size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count) {
    s = stream_for(s);
    BatchState& b = batch_;
+   rows_parts_.assign(1, &batch_);
    if (b.n_queries == 0) return 0;
+   const auto t0 = std::chrono::steady_clock::now();
    rows_phase1(b, s);
    cuda_check(cudaStreamSynchronize(s), "batch rows");
+   const auto t1 = std::chrono::steady_clock::now();
    const size_t total = rows_phase2(b, s, rows, cap);
    cuda_check(cudaStreamSynchronize(s), "batch rows");
+   batch_times.device_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+   batch_times.output_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
    for (uint32_t i = 0; i < b.n_queries; ++i) {
       uint64_t begin;
       uint32_t count;
@@ -729,12 +734,157 @@ size_t Engine::batch_rows(cudaStream_t s, DevMutationRow* rows, size_t cap, uint
 
 void Engine::batch_rows_fetch(cudaStream_t s, DevMutationRow* rows, size_t cap) {
    s = stream_for(s);
-   const BatchState& b = batch_;
-   if (b.n_rows > cap) throw std::invalid_argument("rows buffer holds " + std::to_string(cap) + " rows, " +
-                                                   std::to_string(b.n_rows) + " needed");
-   if (b.n_rows == 0) return;
-   cuda_check(cudaMemcpyAsync(rows, b.d_rows, b.n_rows * sizeof(DevMutationRow), cudaMemcpyDeviceToHost, s), "D2H");
+   size_t total = 0;
+   for (const BatchState* b : rows_parts_) total += b->n_rows;
+   if (total > cap)
+      throw std::invalid_argument("rows buffer holds " + std::to_string(cap) + " rows, " + std::to_string(total) +
+                                  " needed");
+   size_t off = 0;
+   for (const BatchState* b : rows_parts_) {
+      if (b->n_rows)
+         cuda_check(cudaMemcpyAsync(rows + off, b->d_rows, b->n_rows * sizeof(DevMutationRow), cudaMemcpyDeviceToHost, s),
+                    "D2H");
+      off += b->n_rows;
+   }
    cuda_check(cudaStreamSynchronize(s), "rows fetch");
+}
+
+size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
+                                    const double* min_proportions, uint32_t tile_bits, cudaStream_t s,
+                                    DevMutationRow* rows, size_t cap, uint64_t* counts, uint64_t* row_begin,
+                                    uint32_t* row_count) {
+   using clk = std::chrono::steady_clock;
+   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+   s = stream_for(s);
+   const uint32_t n = static_cast<uint32_t>(exprs.size());
+   // parts: the Mutations and Details queries, then the counts in parts of about PIPELINE_PART
+   std::vector<std::vector<uint32_t>> parts(1);
+   std::vector<uint32_t> light;
+   for (uint32_t i = 0; i < n; ++i) {
+      const int a = actions ? actions[i] : 0;
+      if (a < 0 || a > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
+      (a == 0 ? light : parts[0]).push_back(i);
+   }
+   const uint32_t nl = static_cast<uint32_t>(light.size());
+   const uint32_t nlp = std::max(1u, (nl + PIPELINE_PART / 2) / PIPELINE_PART);  // count parts
+   for (uint32_t k = 0; k < nlp; ++k) {
+      const uint32_t b0 = static_cast<uint32_t>(static_cast<uint64_t>(k) * nl / nlp);
+      const uint32_t b1 = static_cast<uint32_t>(static_cast<uint64_t>(k + 1) * nl / nlp);
+      if (parts[0].empty() && k == 0) parts[0].assign(light.begin() + b0, light.begin() + b1);
+      else if (b1 > b0) parts.emplace_back(light.begin() + b0, light.begin() + b1);
+   }
+   while (parts_.size() + 1 < parts.size()) parts_.push_back(std::make_unique<BatchState>());
+   std::vector<BatchState*> states(parts.size());
+   for (size_t p = 0; p < parts.size(); ++p) states[p] = p == 0 ? &batch_ : parts_[p - 1].get();
+   rows_parts_.assign(1, &batch_);
+   for (BatchState* b : states) b->n_rows = 0;
+   double plan_ms = 0, prepare_ms = 0;
+   clk::time_point launched;
+   try {
+      for (size_t p = 0; p < parts.size(); ++p) {
+         const auto t0 = clk::now();
+         std::vector<std::string> texts(parts[p].size());
+         for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
+         std::vector<BatchQuery> qs = plan_batch(texts, 0);
+         for (size_t j = 0; j < parts[p].size(); ++j) {
+            const uint32_t i = parts[p][j];
+            qs[j].action = actions ? actions[i] : 0;
+            qs[j].column = columns ? static_cast<int>(columns[i]) : 0;
+            if (min_proportions) qs[j].min_proportion = min_proportions[i];
+         }
+         const auto t1 = clk::now();
+         batch_prepare(*states[p], qs, tile_bits);
+         rows_phase1(*states[p], s);
+         launched = clk::now();
+         plan_ms += ms(t0, t1);
+         prepare_ms += ms(t1, launched);
+      }
+      cuda_check(cudaStreamSynchronize(s), "batch rows");
+   } catch (...) {
+      cudaStreamSynchronize(s);  // parts already enqueued finish before their buffers are reused
+      throw;
+   }
+   const auto t2 = clk::now();
+   rows_parts_ = states;
+   size_t total = 0;
+   std::vector<size_t> off(parts.size());
+   for (size_t p = 0; p < parts.size(); ++p) {
+      off[p] = total;
+      const bool fits = rows && total <= cap;
+      total += rows_phase2(*states[p], s, fits ? rows + total : nullptr, fits ? cap - total : 0);
+   }
+   cuda_check(cudaStreamSynchronize(s), "batch rows");  // total > cap: the caller refetches every part
+   for (size_t p = 0; p < parts.size(); ++p)
+      for (size_t j = 0; j < parts[p].size(); ++j) {
+         const uint32_t i = parts[p][j];
+         uint64_t begin;
+         uint32_t count;
+         row_range(*states[p], static_cast<uint32_t>(j), &begin, &count);
+         if (counts) counts[i] = states[p]->h_counts[j];
+         if (row_begin) row_begin[i] = begin + off[p];
+         if (row_count) row_count[i] = count;
+      }
+   batch_times = BatchTimes{plan_ms, prepare_ms, ms(launched, t2), ms(t2, clk::now())};
+   return total;
+}
+
+std::vector<std::pair<BatchSchedule, double>> Engine::autotune_batch(const std::vector<BatchQuery>& qs, cudaStream_t s,
+                                                                     uint32_t reps) {
+   s = stream_for(s);
+   reps = std::max(1u, reps);
+   std::vector<BatchSchedule> cands;
+   for (uint32_t w : {16384u, 32768u, 65536u})
+      for (uint32_t kb : {24u, 40u, 64u})
+         for (uint32_t cps : {0u, 2u})
+            for (uint32_t qm : {0u, 1u}) cands.push_back(BatchSchedule{w, kb, cps, qm});
+   const BatchSchedule saved = batch_schedule;
+   BatchState b;
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   std::vector<std::pair<BatchSchedule, double>> out;
+   std::map<std::string, double> seen;  // candidates that lay the launches out alike are timed once
+   try {
+      cuda_check(cudaEventCreate(&e0), "event");
+      cuda_check(cudaEventCreate(&e1), "event");
+      for (const BatchSchedule& c : cands) {
+         batch_schedule = c;
+         batch_prepare(b, qs);
+         std::string key = std::to_string(c.query_major);
+         for (const auto& g : b.fgroups)
+            key += "/" + std::to_string(g.tile_bits) + "x" + std::to_string(g.n_items) + "@" + std::to_string(g.grid);
+         if (const auto it = seen.find(key); it != seen.end()) {
+            out.emplace_back(c, it->second);
+            continue;
+         }
+         batch_enqueue(b, s, true, false, 1);  // copies the programs, warms the caches
+         std::vector<float> t(reps);
+         for (uint32_t r = 0; r < reps; ++r) {
+            cuda_check(cudaEventRecord(e0, s), "event");
+            batch_enqueue(b, s, false, false, 1);
+            cuda_check(cudaEventRecord(e1, s), "event");
+            cuda_check(cudaEventSynchronize(e1), "event");
+            cuda_check(cudaEventElapsedTime(&t[r], e0, e1), "event");
+         }
+         cuda_check(cudaMemcpyAsync(b.h_err, b.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+         cuda_check(cudaStreamSynchronize(s), "autotune");
+         check_batch_error(b);
+         std::nth_element(t.begin(), t.begin() + reps / 2, t.end());
+         seen.emplace(key, t[reps / 2]);
+         out.emplace_back(c, t[reps / 2]);
+      }
+   } catch (...) {
+      cudaStreamSynchronize(s);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      batch_free(b);
+      batch_schedule = saved;
+      throw;
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   batch_free(b);
+   std::stable_sort(out.begin(), out.end(), [](const auto& x, const auto& y) { return x.second < y.second; });
+   batch_schedule = out.empty() ? saved : out.front().first;
+   return out;
 }
 
 void Engine::batch_capture(cudaStream_t s, bool copy_in, bool copy_out) {
@@ -872,43 +1022,53 @@ void Engine::set_planner_mode(int mode) {
 std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs, uint32_t threads) {
    const uint32_t n = static_cast<uint32_t>(exprs.size());
    std::vector<BatchQuery> qs(n);
+   // threads == 0: the engine's persistent workers; otherwise that many threads of their own
+   auto each = [&](auto&& fn) {
+      if (threads == 0) plan_pool_.run(n, fn);
+      else parallel_for(n, threads, fn);
+   };
    if (!use_learned_) {
-      std::vector<Program> progs = plan_many(table_, exprs, threads);
-      for (uint32_t i = 0; i < n; ++i) qs[i].prog = std::move(progs[i]);
+      const Estimator est = rule_estimator(table_);
+      each([&](uint32_t i) { qs[i].prog = plan_filter(exprs[i], table_, &est, LowerOptions{}, nullptr); });
       return qs;
    }
+   // Learned: compile and featurise every expression, run the network once over every operator
+   // node of the batch (rows staged in pinned memory, each query's nodes at its own offset), then
+   // lower every expression with its nodes' predicted row counts.
    const FeatureContext& ctx = fctx();
    std::vector<OpPtr> ops(n);
    std::vector<std::vector<const Op*>> qnodes(n);
    std::vector<std::vector<std::array<float, PLAN_FEATURES>>> qx(n);
-   parallel_for(n, threads, [&](uint32_t i) {
+   each([&](uint32_t i) {
       ops[i] = compile_filter(exprs[i], table_);
       tree_features(*ops[i], ctx, qnodes[i], qx[i]);
    });
-   // every operator node of every expression in one table; the root of query i comes first
-   std::vector<const Op*> nodes;
-   std::vector<std::array<float, PLAN_FEATURES>> x;
-   std::vector<uint32_t> root_of(n);
-   for (uint32_t i = 0; i < n; ++i) {
-      root_of[i] = static_cast<uint32_t>(nodes.size());
-      nodes.insert(nodes.end(), qnodes[i].begin(), qnodes[i].end());
-      x.insert(x.end(), qx[i].begin(), qx[i].end());
-   }
-   std::vector<double> sel, cost;
+   std::vector<uint32_t> base(n + 1, 0);  // query i's nodes are rows base[i] .. base[i + 1]
+   for (uint32_t i = 0; i < n; ++i) base[i + 1] = base[i] + static_cast<uint32_t>(qnodes[i].size());
+   const uint32_t total = base[n];
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-   planner_.predict(x, sel, cost);
-   std::unordered_map<const Op*, double> est_rows;
-   est_rows.reserve(nodes.size());
+   float* X = planner_.net.staged_input(total);
+   each([&](uint32_t i) {
+      for (uint32_t k = 0; k < qnodes[i].size(); ++k)
+         planner_.normalize(qx[i][k].data(), X + static_cast<size_t>(base[i] + k) * PLAN_FEATURES);
+   });
+   const float* Y = total ? planner_.net.predict_staged(total) : nullptr;
    const double rows = std::max(1u, table_.n_rows);
-   for (size_t k = 0; k < nodes.size(); ++k)
-      if (std::isfinite(sel[k])) est_rows.emplace(nodes[k], sel[k] * rows);
-   const Estimator learned = [&](const Op& op) -> double {
-      const auto it = est_rows.find(&op);
-      return it != est_rows.end() ? it->second : ctx.rule(op);  // the rule where the network has no answer
-   };
-   parallel_for(n, threads, [&](uint32_t i) {
+   each([&](uint32_t i) {
+      // (node, estimated rows) sorted by node for lookup while lowering
+      std::vector<std::pair<const Op*, double>> est(qnodes[i].size());
+      for (uint32_t k = 0; k < qnodes[i].size(); ++k) {
+         const double sel = planner_.selectivity_of(qx[i][k].data(), Y + 2 * static_cast<size_t>(base[i] + k));
+         est[k] = {qnodes[i][k], std::isfinite(sel) ? sel * rows : -1.0};
+      }
+      const double c = qnodes[i].empty() ? 0.0 : planner_.cost_of(Y + 2 * static_cast<size_t>(base[i]));
+      std::sort(est.begin(), est.end());
+      const Estimator learned = [&](const Op& op) -> double {
+         const auto it = std::lower_bound(est.begin(), est.end(), std::make_pair(&op, -2.0));
+         if (it != est.end() && it->first == &op && it->second >= 0) return it->second;
+         return ctx.rule(op);  // the rule where the network has no answer
+      };
       qs[i].prog = lower(*ops[i], learned, LowerOptions{});
-      const double c = cost[root_of[i]];
       qs[i].cost = std::isfinite(c) ? c : 0.0;
    });
    return qs;

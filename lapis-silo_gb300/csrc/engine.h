@@ -13,6 +13,7 @@
 #include "device.h"
 #include "expr.h"
 #include "planner.h"
+#include "util.h"
 #include "table.h"
 
 namespace rhygpu {
@@ -32,6 +33,17 @@ struct BatchQuery {
    double min_proportion = 0.05;  // Mutations rows: minimum proportion of a reported mutation
    double cost = 0;               // predicted cycles per tile (learned planner); 0 = unknown
    uint32_t k = 1000;             // Details: number of row ids returned (the first ones)
+};
+
+// Schedule of the batched filter launches: the widest tile of a class, the stack budget that narrows
+// a class's tile (deep programs get narrower tiles, so more CTAs fit per SM), persistent CTAs per SM
+// (0 = as many as fit) and the order of the (query, tile) work items (tile-major interleaving, or
+// every tile of one query in turn). Results never depend on it.
+struct BatchSchedule {
+   uint32_t max_tile_bits = 65536;
+   uint32_t stack_kb = 40;
+   uint32_t ctas_per_sm = 0;
+   uint32_t query_major = 0;
 };
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
@@ -116,6 +128,13 @@ class Engine {
    // latency over wider tiles. rhy_set_tile_bits sets both.
    uint32_t tile_bits = 16384;
    uint32_t batch_tile_bits = 65536;
+   BatchSchedule batch_schedule;  // used by batch_prepare unless a tile width is requested
+   // Autotuner: prepares the batch under every candidate schedule (tile widths 16, 32 and 64 Kbit,
+   // stack budgets 24, 40 and 64 KiB, all or two CTAs per SM, both item orders), times its filter
+   // launches `reps` times with CUDA events on `stream` and keeps the fastest as batch_schedule.
+   // Returns every candidate with its median milliseconds, the chosen one first. The caller holds mu.
+   std::vector<std::pair<BatchSchedule, double>> autotune_batch(const std::vector<BatchQuery>& qs, cudaStream_t stream,
+                                                                uint32_t reps);
 
    Program plan(const std::string& expr, const LowerOptions& opt = {}, std::string* tree = nullptr) const;
 
@@ -171,7 +190,24 @@ class Engine {
    size_t batch_rows(cudaStream_t stream, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count);
    // Copies the rows of the last batch_rows again (for a caller whose buffer was too small).
    void batch_rows_fetch(cudaStream_t stream, DevMutationRow* rows, size_t cap);
+   // batch_rows of a whole batch given as text, planned and run in parts so that the host plans
+   // part k + 1 while the device runs part k: part 0 holds the Mutations and Details queries (a
+   // Mutations pass reads the column once per 256 queries, so they stay together), then come the
+   // Aggregated counts in parts of about PIPELINE_PART queries. Results equal batch_rows of the
+   // whole batch; the rows of part 0 come first. Batches too small for two parts run as one.
+   // The caller holds mu.
+   static constexpr uint32_t PIPELINE_PART = 512;
+   size_t batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
+                               const double* min_proportions, uint32_t tile_bits, cudaStream_t stream,
+                               DevMutationRow* rows, size_t cap, uint64_t* counts, uint64_t* row_begin,
+                               uint32_t* row_count);
    uint64_t batch_count(uint32_t query) const { return batch_.h_counts[query]; }
+   // Host wall time of the phases of the last batch call made through the C-ABI: planning
+   // (parse, rewrite, compile, estimates, lowering), staging (work items, device buffers), the
+   // batch on the device up to its counts and row sizes, and the packed rows with their copy.
+   struct BatchTimes {
+      double plan_ms = 0, prepare_ms = 0, device_ms = 0, output_ms = 0;
+   } batch_times;
    // Tile width that fits the batch's deepest program in the shared-memory budget.
    uint32_t fit_tile_bits(uint32_t requested, uint32_t depth, bool batch = false) const;
 
@@ -223,17 +259,16 @@ class Engine {
    int* h_err_ = nullptr;                  // pinned
    uint64_t device_bytes_ = 0;
    BatchState batch_;
+   std::vector<std::unique_ptr<BatchState>> parts_;      // parts 1.. of batch_rows_pipelined
+   std::vector<BatchState*> rows_parts_{&batch_};        // states holding the last rows, in row order
    void copy_details(BatchState& b, cudaStream_t s);
    Planner planner_;
    bool use_learned_ = false;
    std::unique_ptr<FeatureContext> fctx_;  // built on first use
    const FeatureContext& fctx();
+   WorkerPool plan_pool_;  // planning threads, one per hardware thread
 
 };
-
-// Plans many expressions on host threads (rewrite -> compile -> lower per expression).
-std::vector<Program> plan_many(const TableImage& t, const std::vector<std::string>& exprs, uint32_t threads,
-                               const LowerOptions& opt = {});
 
 // Occupancy of the persistent filter kernel for a given shared-memory stack size.
 int filter_batch_blocks_per_sm(size_t smem_bytes);

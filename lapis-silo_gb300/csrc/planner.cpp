@@ -191,6 +191,8 @@ PlannerNet::~PlannerNet() {
                    static_cast<void*>(d_grad_), static_cast<void*>(d_loss_), static_cast<void*>(d_w_),
                    static_cast<void*>(d_X_), static_cast<void*>(d_T_), static_cast<void*>(d_Y_)})
       if (p) cudaFree(p);
+   if (h_X_) cudaFreeHost(h_X_);
+   if (h_Y_) cudaFreeHost(h_Y_);
    if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -209,7 +211,11 @@ void PlannerNet::init(uint64_t seed) {
 
 void PlannerNet::reserve(uint32_t n) {
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-   if (!stream_) cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+   if (!stream_) {  // high priority: inference during planning runs between the batch kernels' blocks
+      int lo = 0, hi = 0;
+      cuda_check(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+      cuda_check(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, hi), "stream");
+   }
    if (!d_master_) {
       for (float** p : {&d_master_, &d_m_, &d_v_, &d_grad_})
          cuda_check(cudaMalloc(p, MLP_NPARAM * sizeof(float)), "cudaMalloc (planner)");
@@ -310,6 +316,27 @@ void PlannerNet::predict(const float* X, uint32_t n, float* Y) {
    cuda_check(cudaStreamSynchronize(s), "mlp forward");
 }
 
+float* PlannerNet::staged_input(uint32_t n) {
+   reserve(n);
+   if (n > hcap_) {
+      if (h_X_) cudaFreeHost(h_X_);
+      if (h_Y_) cudaFreeHost(h_Y_);
+      h_X_ = h_Y_ = nullptr;
+      hcap_ = 0;
+      const uint32_t c = std::max(n + n / 4, 1024u);
+      cuda_check(cudaMallocHost(&h_X_, static_cast<size_t>(c) * MLP_IN * sizeof(float)), "cudaMallocHost (planner)");
+      cuda_check(cudaMallocHost(&h_Y_, static_cast<size_t>(c) * MLP_OUT * sizeof(float)), "cudaMallocHost (planner)");
+      hcap_ = c;
+   }
+   return h_X_;
+}
+
+const float* PlannerNet::predict_staged(uint32_t n) {
+   if (n > hcap_) throw std::logic_error("planner: staged rows exceed the staging buffer");
+   predict(h_X_, n, h_Y_);
+   return h_Y_;
+}
+
 // ------------------------------------------------------------------------------------------------
 // Planner
 
@@ -408,16 +435,24 @@ void Planner::predict(const std::vector<std::array<float, PLAN_FEATURES>>& x, st
    cost.assign(n, std::nan(""));
    if (!trained || n == 0) return;
    std::vector<float> X(static_cast<size_t>(n) * PLAN_FEATURES), Y(static_cast<size_t>(n) * 2);
-   for (uint32_t i = 0; i < n; ++i)
-      for (uint32_t k = 0; k < PLAN_FEATURES; ++k) X[static_cast<size_t>(i) * PLAN_FEATURES + k] = (x[i][k] - fmean[k]) / fstd[k];
+   for (uint32_t i = 0; i < n; ++i) normalize(x[i].data(), X.data() + static_cast<size_t>(i) * PLAN_FEATURES);
    net.predict(X.data(), n, Y.data());
    for (uint32_t i = 0; i < n; ++i) {
-      const double rl = rule_log_sel_of(x[i].data());
-      const double ls = exact_by_rule(x[i].data()) ? rl : rl + static_cast<double>(Y[2 * i]) * tstd[0] + tmean[0];
-      const double lc = static_cast<double>(Y[2 * i + 1]) * tstd[1] + tmean[1];
-      sel[i] = std::exp(std::max(std::log(MIN_SEL), std::min(0.0, ls)));
-      cost[i] = std::exp(lc);
+      sel[i] = selectivity_of(x[i].data(), Y.data() + 2 * i);
+      cost[i] = cost_of(Y.data() + 2 * i);
    }
 }
+
+void Planner::normalize(const float* x, float* out) const {
+   for (uint32_t k = 0; k < PLAN_FEATURES; ++k) out[k] = (x[k] - fmean[k]) / fstd[k];
+}
+
+double Planner::selectivity_of(const float* x, const float* y) const {
+   const double rl = rule_log_sel_of(x);
+   const double ls = exact_by_rule(x) ? rl : rl + static_cast<double>(y[0]) * tstd[0] + tmean[0];
+   return std::exp(std::max(std::log(MIN_SEL), std::min(0.0, ls)));
+}
+
+double Planner::cost_of(const float* y) const { return std::exp(static_cast<double>(y[1]) * tstd[1] + tmean[1]); }
 
 }  // namespace rhygpu

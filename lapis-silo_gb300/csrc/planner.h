@@ -79,9 +79,16 @@ class PlannerNet {
    float train(const std::vector<float>& X, const std::vector<float>& T, uint32_t n, uint32_t epochs, uint32_t batch,
                float lr, uint64_t seed);
    void predict(const float* X, uint32_t n, float* Y);
+   // Pinned host rows (n x MLP_IN) to fill before predict_staged, which runs the network on them
+   // and returns its outputs (n x MLP_OUT, pinned, valid until the next call).
+   float* staged_input(uint32_t n);
+   const float* predict_staged(uint32_t n);
 
   private:
    void reserve(uint32_t n);
+   float* h_X_ = nullptr;  // pinned staging
+   float* h_Y_ = nullptr;
+   uint32_t hcap_ = 0;
    int device_;
    float* d_master_ = nullptr;
    float* d_m_ = nullptr;
@@ -112,6 +119,11 @@ class Planner {
    // Selectivity (fraction of rows) and cycles per tile for each feature row.
    void predict(const std::vector<std::array<float, PLAN_FEATURES>>& x, std::vector<double>& sel,
                 std::vector<double>& cost);
+   // The same one row at a time around the network: its normalised input, then the selectivity
+   // and cost from the raw features and the network's two outputs.
+   void normalize(const float* x, float* out) const;
+   double selectivity_of(const float* x, const float* y) const;
+   double cost_of(const float* y) const;
 };
 
 }  // namespace rhygpu

@@ -63,6 +63,19 @@ class RawTable(C.Structure):
                 ("date", C.POINTER(RawDateColumn))]
 
 
+class BatchTimes(C.Structure):
+    _fields_ = [("plan_ms", C.c_double), ("prepare_ms", C.c_double), ("device_ms", C.c_double),
+                ("output_ms", C.c_double)]
+
+
+class BatchSchedule(C.Structure):
+    _fields_ = [("max_tile_bits", C.c_uint32), ("stack_kb", C.c_uint32), ("ctas_per_sm", C.c_uint32),
+                ("query_major", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class GenConfig(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("n_rows", C.c_uint32), ("genome_len", C.c_uint32),
                 ("pool_sites", C.c_uint32), ("n_aa_genes", C.c_uint32), ("null_fraction", C.c_double),
@@ -144,7 +157,7 @@ def lib():
         "rhy_table_raw": (I, [P, C.POINTER(RawTable)]),
         "rhy_local_reference": (I, [P, U32, C.c_char_p, C.c_size_t]),
         "rhy_seq_containers": (I, [P, U32, P, P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
-        "rhy_generate_queries": (I, [P, U64, U32, U32, U32, I, I, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_generate_queries": (I, [P, U64, U32, U32, U32, U32, I, I, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_table_free": (None, [P]),
         "rhy_plan": (I, [P, C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(U32), C.POINTER(U32)]),
         "rhy_open": (I, [P, I, C.POINTER(P)]),
@@ -157,6 +170,10 @@ def lib():
         "rhy_batch": (I, [P, P, P, P, U32, U32, P, P, P]),
         "rhy_batch_rows": (I, [P, P, P, P, P, U32, U32, P, P, P, C.c_size_t, P, P, C.POINTER(C.c_size_t)]),
         "rhy_batch_rows_fetch": (I, [P, P, P, C.c_size_t]),
+        "rhy_batch_times": (I, [P, C.POINTER(BatchTimes)]),
+        "rhy_batch_schedule": (I, [P, C.POINTER(BatchSchedule), C.POINTER(BatchSchedule)]),
+        "rhy_batch_autotune": (I, [P, P, P, P, U32, U32, P, C.POINTER(BatchSchedule), P, C.c_size_t,
+                                   C.POINTER(C.c_size_t)]),
         "rhy_batch_prepare": (I, [P, P, P, P, U32, U32, U32]),
         "rhy_batch_launch": (I, [P, P, I, I]),
         "rhy_batch_capture": (I, [P, P]),
@@ -301,12 +318,13 @@ class Table:
         return pos, chunk, sym, card, typ
 
     def queries(self, n: int, seed: int = 43, max_depth: int = 4, max_nof_children: int = 8, use_aa: bool = False,
-                use_metadata: bool = False) -> list[str]:
+                use_metadata: bool = False, max_leaves: int = 0) -> list[str]:
+        """Seeded random filter expressions; max_leaves bounds the leaves per tree (0 = no limit)."""
         need = C.c_size_t()
-        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, int(use_aa),
+        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, max_leaves, int(use_aa),
                                           int(use_metadata), None, 0, C.byref(need)))
         buf = C.create_string_buffer(need.value)
-        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, int(use_aa),
+        _check(lib().rhy_generate_queries(self._h, seed, n, max_depth, max_nof_children, max_leaves, int(use_aa),
                                           int(use_metadata), buf, need.value, None))
         return [q for q in buf.value.decode().split("\n") if q]
 
@@ -386,7 +404,7 @@ class Device:
     @staticmethod
     def _query_arrays(exprs, actions, columns):
         n = len(exprs)
-        arr = (C.c_char_p * max(n, 1))(*[e.encode() for e in exprs])
+        arr = _text_array(exprs)
         act = np.asarray(actions if actions is not None else [0] * n, dtype=np.int32)
         col = np.asarray(columns if columns is not None else [0] * n, dtype=np.uint32)
         return n, arr, act, col
@@ -420,7 +438,7 @@ class Device:
         begin = np.zeros(max(n, 1), np.uint64)
         cnt = np.zeros(max(n, 1), np.uint32)
         mp = None if min_proportions is None else np.ascontiguousarray(min_proportions, dtype=np.float64)
-        rows = np.zeros(max(rows_cap, 1), self.ROW_DTYPE)
+        rows = np.empty(max(rows_cap, 1), self.ROW_DTYPE)  # written by the library up to the row count
         total = C.c_size_t()
         _check(lib().rhy_batch_rows(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col),
                                     None if mp is None else _ptr(mp), n, tile_bits, stream, _ptr(counts),
@@ -429,6 +447,12 @@ class Device:
             rows = np.zeros(total.value, self.ROW_DTYPE)
             _check(lib().rhy_batch_rows_fetch(self._h, stream, rows.ctypes.data, total.value))
         return counts[:n], rows[:total.value], begin[:n], cnt[:n]
+
+    def batch_times(self) -> dict:
+        """Host wall time (ms) of the phases of the last batch_rows call."""
+        t = BatchTimes()
+        _check(lib().rhy_batch_times(self._h, C.byref(t)))
+        return {k: t.__getattribute__(k) for k, _ in BatchTimes._fields_}
 
     def batch_prepare(self, exprs, actions=None, columns=None, tile_bits: int = 0, plan_threads: int = 0):
         n, arr, act, col = self._query_arrays(exprs, actions, columns)
@@ -460,6 +484,28 @@ class Device:
         _check(lib().rhy_batch_results(self._h, _ptr(counts), C.cast(ptrs, C.c_void_p)))
         return counts[:n], outs
 
+    def batch_schedule(self, **set_fields) -> dict:
+        """The schedule of the batched filter launches; keyword arguments set fields first."""
+        cur = BatchSchedule()
+        _check(lib().rhy_batch_schedule(self._h, None, C.byref(cur)))
+        if set_fields:
+            for k, v in set_fields.items():
+                setattr(cur, k, v)
+            _check(lib().rhy_batch_schedule(self._h, C.byref(cur), C.byref(cur)))
+        return cur.as_dict()
+
+    def batch_autotune(self, exprs, actions=None, columns=None, reps: int = 5, stream=None) -> list:
+        """Times every candidate schedule on this batch and keeps the fastest; returns
+        [(schedule dict, median ms)] fastest first."""
+        n, arr, act, col = self._query_arrays(exprs, actions, columns)
+        cap = 128
+        tried = (BatchSchedule * cap)()
+        ms = np.zeros(cap, np.float64)
+        nt = C.c_size_t()
+        _check(lib().rhy_batch_autotune(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), n, reps, stream, tried,
+                                        _ptr(ms), cap, C.byref(nt)))
+        return [(tried[i].as_dict(), float(ms[i])) for i in range(min(nt.value, cap))]
+
     def batch_info(self) -> BatchInfo:
         info = BatchInfo()
         _check(lib().rhy_batch_info(self._h, C.byref(info)))
@@ -486,7 +532,7 @@ class Device:
 
     # ---- learned planner ----
     def planner_collect(self, exprs) -> int:
-        arr = (C.c_char_p * max(len(exprs), 1))(*[e.encode() for e in exprs])
+        arr = _text_array(exprs)
         n = C.c_size_t()
         _check(lib().rhy_planner_collect(self._h, C.cast(arr, C.c_void_p), len(exprs), C.byref(n)))
         return n.value
@@ -571,7 +617,7 @@ class Server:
     def replay(self, exprs, actions, columns, min_proportions, ks, arrival_s):
         """Open-loop replay (native submitter thread): (latencies in ms, wall seconds)."""
         n = len(exprs)
-        arr = (C.c_char_p * max(n, 1))(*[e.encode() for e in exprs])
+        arr = _text_array(exprs)
         act = np.ascontiguousarray(actions, np.int32)
         col = np.ascontiguousarray(columns, np.uint32)
         mp = np.ascontiguousarray(min_proportions, np.float64)
@@ -598,6 +644,23 @@ class Server:
             self.stop()
         except Exception:
             pass
+
+
+def _text_array(texts) -> C.Array:
+    """A `const char* const*` array over the strings: one encoded buffer, pointers computed in bulk
+    (keeps the buffer alive as an attribute of the array)."""
+    n = len(texts)
+    blob = "\0".join(texts).encode() + b"\0"
+    ends = np.flatnonzero(np.frombuffer(blob, np.uint8) == 0)
+    if len(ends) != max(n, 1):  # a string holding NUL: one pointer per string, cut at the NUL
+        arr = (C.c_char_p * max(n, 1))(*[t.encode() for t in texts])
+        return arr
+    ptrs = np.zeros(len(ends), np.uint64)
+    ptrs[1:] = ends[:-1] + 1
+    ptrs += np.uint64(C.cast(C.c_char_p(blob), C.c_void_p).value)
+    arr = (C.c_void_p * len(ptrs)).from_buffer(ptrs)
+    arr._keep = (blob, ptrs)
+    return arr
 
 
 def bits_to_rows(bits: np.ndarray) -> np.ndarray:

@@ -118,6 +118,56 @@ def test_batched_mutation_rows(config2_small):
         dev.batch_rows(qs[:4], [1, 1, 0, 0], None, [0.05, 1.5, 0.05, 0.05])
 
 
+def test_batch_rows_in_parts(config2_small):
+    """A batch large enough to run in several parts (Mutations and Details first, then three
+    count parts, planned while earlier parts run) gives every query the counts and rows of the
+    single-part dense batch, and a refetch returns the rows of every part."""
+    t, orc, dev, qs = config2_small
+    big = (qs * 6)[:1700]
+    rng = np.random.default_rng(11)
+    act = np.where(rng.random(len(big)) < 0.12, 1, np.where(rng.random(len(big)) < 0.05, 2, 0)).astype(np.int32)
+    col = rng.integers(0, t.n_seq, len(big)).astype(np.uint32)
+    counts, rows, begin, cnt = dev.batch_rows(big, act, col, None, rows_cap=10)
+    dense_act = np.where(act == 2, 0, act).astype(np.int32)
+    dcounts, muts = dev.batch(big, dense_act, col)
+    assert np.array_equal(counts, dcounts)
+    assert int(cnt.sum()) == len(rows)
+    ranges = sorted((int(begin[i]), int(cnt[i])) for i in range(len(big)) if cnt[i])
+    assert all(a + n <= b for (a, n), (b, _) in zip(ranges, ranges[1:]))  # disjoint
+    for i in range(len(big)):
+        if act[i] != 1:
+            assert cnt[i] == 0
+            continue
+        got = rows[int(begin[i]):int(begin[i]) + int(cnt[i])]
+        want = t.mutation_rows(int(col[i]), muts[i], 0.05)
+        assert [(int(r["position"]), r["from_"].decode(), r["to"].decode(), int(r["count"]), int(r["coverage"]),
+                 float(r["proportion"])) for r in got] == want, big[i]
+    times = dev.batch_times()
+    assert all(v >= 0 for v in times.values())
+
+
+def test_autotuned_schedule_keeps_results(config2_small):
+    """The autotuner times all 36 candidate schedules, keeps the fastest in force, and every
+    schedule gives the same counts and Mutations tables."""
+    t, orc, dev, qs = config2_small
+    act = np.array([i % 4 == 3 for i in range(len(qs))], np.int32)
+    default = dev.batch_schedule()
+    ref_c, ref_m = dev.batch(qs, act)
+    tried = dev.batch_autotune(qs, act, reps=3)
+    assert len(tried) == 36
+    assert all(np.isfinite(ms) and ms > 0 for _, ms in tried)
+    assert [ms for _, ms in tried] == sorted(ms for _, ms in tried)
+    assert dev.batch_schedule() == tried[0][0]
+    for sch in (tried[0][0], tried[-1][0], dict(max_tile_bits=16384, stack_kb=24, ctas_per_sm=2, query_major=1)):
+        dev.batch_schedule(**sch)
+        c, m = dev.batch(qs, act)
+        assert np.array_equal(c, ref_c)
+        assert all(np.array_equal(m[k], ref_m[k]) for k in ref_m)
+    with pytest.raises(R.RhyError):
+        dev.batch_schedule(max_tile_bits=3000)
+    dev.batch_schedule(**default)
+
+
 def test_tile_widths(config2_small):
     t, orc, dev, qs = config2_small
     for tb in (4096, 8192, 32768, 65536):
@@ -203,4 +253,37 @@ def test_complement_identity_at_scale():
     m, _ = dev.mutations(qs[3], 0)
     om, _ = orc.mutations(qs[3], 0)
     assert np.array_equal(m, om)
+    dev.close()
+
+
+def test_batching_shapes_in_one_captured_launch():
+    """The batching shape: 4,096 trees of 1-64 leaves (NOf up to 64 children) with selectivities
+    log-uniform over [1e-5, 0.9], evaluated by the persistent kernels inside one captured CUDA graph,
+    bit-exact with the oracle for every query (counts) and for a sample of Mutations tables."""
+    import re
+
+    import workloads
+
+    t = R.Table.generate(100000, seed=42, n_aa_genes=12, null_fraction=0.002)
+    dev = R.Device(t, 0)
+    qs = workloads.batching_workload(t, dev, n=4096, seed=44, candidates=40000)
+    leaves = np.array([len(re.findall(r"SymEq|HasMut|StrEq|DateBetween", q)) for q in qs])
+    assert leaves.min() >= 1 and leaves.max() <= 64 and (leaves == 64).sum() > 100
+    assert max(len(re.findall(r",", q)) for q in qs if q.startswith("NOf")) > 40
+    act = np.array([i % 8 == 7 for i in range(len(qs))], np.int32)
+    dev.batch_prepare(qs, act)
+    dev.batch_capture()
+    dev.batch_replay()
+    counts, muts = dev.batch_results()
+    sel = counts / t.n_rows
+    decades = np.histogram(np.log10(sel), bins=[-5, -4, -3, -2, -1, np.log10(0.9)])[0]
+    assert decades.min() >= 600, decades   # log-uniform: about 820 per decade
+    orc = oracle_for(t)
+    import os
+
+    _, _, want = orc.run_batch(qs, [0] * len(qs), [0] * len(qs), os.cpu_count() or 4)
+    assert np.array_equal(counts, want)
+    for i in np.flatnonzero(act)[::64]:
+        om, _ = orc.mutations(qs[i], 0)
+        assert np.array_equal(muts[int(i)], om), qs[i]
     dev.close()
