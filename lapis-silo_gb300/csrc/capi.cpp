@@ -499,7 +499,7 @@ int rhy_batch_times(RhyDevice* d, RhyBatchTimes* out) {
       need(out, "out");
       std::lock_guard<std::mutex> lock(d->engine->mu);
       const auto& t = d->engine->batch_times;
-      *out = RhyBatchTimes{t.plan_ms, t.prepare_ms, t.device_ms, t.output_ms};
+      *out = RhyBatchTimes{t.plan_ms, t.prepare_ms, t.device_ms, t.output_ms, t.compile_ms, t.predict_ms, t.lower_ms};
    });
 }
 

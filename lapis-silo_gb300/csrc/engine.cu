@@ -757,7 +757,8 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
    s = stream_for(s);
    const uint32_t n = static_cast<uint32_t>(exprs.size());
-   // parts: the Mutations and Details queries, then the counts in parts of about PIPELINE_PART
+   // part 0: the Mutations and Details queries (or, without any, the first quarter of the counts);
+   // part 1: the counts, planned while part 0 runs
    std::vector<std::vector<uint32_t>> parts(1);
    std::vector<uint32_t> light;
    for (uint32_t i = 0; i < n; ++i) {
@@ -765,19 +766,21 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
       if (a < 0 || a > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
       (a == 0 ? light : parts[0]).push_back(i);
    }
-   const uint32_t nl = static_cast<uint32_t>(light.size());
-   const uint32_t nlp = std::max(1u, (nl + PIPELINE_PART / 2) / PIPELINE_PART);  // count parts
-   for (uint32_t k = 0; k < nlp; ++k) {
-      const uint32_t b0 = static_cast<uint32_t>(static_cast<uint64_t>(k) * nl / nlp);
-      const uint32_t b1 = static_cast<uint32_t>(static_cast<uint64_t>(k + 1) * nl / nlp);
-      if (parts[0].empty() && k == 0) parts[0].assign(light.begin() + b0, light.begin() + b1);
-      else if (b1 > b0) parts.emplace_back(light.begin() + b0, light.begin() + b1);
+   size_t first = 0;
+   if (parts[0].empty()) {
+      first = light.size() < 2 * PIPELINE_PART ? light.size() : light.size() / 4;
+      parts[0].assign(light.begin(), light.begin() + first);
+   }
+   if (first < light.size()) {
+      if (light.size() - first < PIPELINE_PART) parts[0].insert(parts[0].end(), light.begin() + first, light.end());
+      else parts.emplace_back(light.begin() + first, light.end());
    }
    while (parts_.size() + 1 < parts.size()) parts_.push_back(std::make_unique<BatchState>());
    std::vector<BatchState*> states(parts.size());
    for (size_t p = 0; p < parts.size(); ++p) states[p] = p == 0 ? &batch_ : parts_[p - 1].get();
    rows_parts_.assign(1, &batch_);
    for (BatchState* b : states) b->n_rows = 0;
+   batch_times = BatchTimes{};
    double plan_ms = 0, prepare_ms = 0;
    clk::time_point launched;
    try {
@@ -824,7 +827,10 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
          if (row_begin) row_begin[i] = begin + off[p];
          if (row_count) row_count[i] = count;
       }
-   batch_times = BatchTimes{plan_ms, prepare_ms, ms(launched, t2), ms(t2, clk::now())};
+   batch_times.plan_ms = plan_ms;
+   batch_times.prepare_ms = prepare_ms;
+   batch_times.device_ms = ms(launched, t2);
+   batch_times.output_ms = ms(t2, clk::now());
    return total;
 }
 
@@ -1027,9 +1033,13 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
       if (threads == 0) plan_pool_.run(n, fn);
       else parallel_for(n, threads, fn);
    };
+   using clk = std::chrono::steady_clock;
+   auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+   auto t0 = clk::now();
    if (!use_learned_) {
       const Estimator est = rule_estimator(table_);
       each([&](uint32_t i) { qs[i].prog = plan_filter(exprs[i], table_, &est, LowerOptions{}, nullptr); });
+      batch_times.compile_ms += since(t0);
       return qs;
    }
    // Learned: compile and featurise every expression, run the network once over every operator
@@ -1043,6 +1053,8 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
       ops[i] = compile_filter(exprs[i], table_);
       tree_features(*ops[i], ctx, qnodes[i], qx[i]);
    });
+   batch_times.compile_ms += since(t0);
+   t0 = clk::now();
    std::vector<uint32_t> base(n + 1, 0);  // query i's nodes are rows base[i] .. base[i + 1]
    for (uint32_t i = 0; i < n; ++i) base[i + 1] = base[i] + static_cast<uint32_t>(qnodes[i].size());
    const uint32_t total = base[n];
@@ -1053,6 +1065,8 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
          planner_.normalize(qx[i][k].data(), X + static_cast<size_t>(base[i] + k) * PLAN_FEATURES);
    });
    const float* Y = total ? planner_.net.predict_staged(total) : nullptr;
+   batch_times.predict_ms += since(t0);
+   t0 = clk::now();
    const double rows = std::max(1u, table_.n_rows);
    each([&](uint32_t i) {
       // (node, estimated rows) sorted by node for lookup while lowering
@@ -1070,7 +1084,13 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
       };
       qs[i].prog = lower(*ops[i], learned, LowerOptions{});
       qs[i].cost = std::isfinite(c) ? c : 0.0;
+      // free the query's tree and features here, in parallel: a serial teardown of every tree on
+      // the calling thread costs as much as the planning
+      ops[i].reset();
+      std::vector<const Op*>().swap(qnodes[i]);
+      std::vector<std::array<float, PLAN_FEATURES>>().swap(qx[i]);
    });
+   batch_times.lower_ms += since(t0);
    return qs;
 }
 

@@ -190,13 +190,13 @@ class Engine {
    size_t batch_rows(cudaStream_t stream, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count);
    // Copies the rows of the last batch_rows again (for a caller whose buffer was too small).
    void batch_rows_fetch(cudaStream_t stream, DevMutationRow* rows, size_t cap);
-   // batch_rows of a whole batch given as text, planned and run in parts so that the host plans
-   // part k + 1 while the device runs part k: part 0 holds the Mutations and Details queries (a
-   // Mutations pass reads the column once per 256 queries, so they stay together), then come the
-   // Aggregated counts in parts of about PIPELINE_PART queries. Results equal batch_rows of the
-   // whole batch; the rows of part 0 come first. Batches too small for two parts run as one.
-   // The caller holds mu.
-   static constexpr uint32_t PIPELINE_PART = 512;
+   // batch_rows of a whole batch given as text, planned and run in two parts so that the host
+   // plans the second while the device runs the first: part 0 holds the Mutations and Details
+   // queries (a Mutations pass reads the column once per 256 queries, so they stay together; the
+   // first quarter of the counts when there are none), part 1 the Aggregated counts. Results equal
+   // batch_rows of the whole batch; the rows of part 0 come first. A part 1 of fewer than
+   // PIPELINE_PART queries joins part 0. The caller holds mu.
+   static constexpr uint32_t PIPELINE_PART = 256;
    size_t batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
                                const double* min_proportions, uint32_t tile_bits, cudaStream_t stream,
                                DevMutationRow* rows, size_t cap, uint64_t* counts, uint64_t* row_begin,
@@ -205,8 +205,11 @@ class Engine {
    // Host wall time of the phases of the last batch call made through the C-ABI: planning
    // (parse, rewrite, compile, estimates, lowering), staging (work items, device buffers), the
    // batch on the device up to its counts and row sizes, and the packed rows with their copy.
+   // plan_ms splits into compile (parse, rewrite, compile, features), predict (network inference,
+   // learned planner only) and lower.
    struct BatchTimes {
       double plan_ms = 0, prepare_ms = 0, device_ms = 0, output_ms = 0;
+      double compile_ms = 0, predict_ms = 0, lower_ms = 0;
    } batch_times;
    // Tile width that fits the batch's deepest program in the shared-memory budget.
    uint32_t fit_tile_bits(uint32_t requested, uint32_t depth, bool batch = false) const;

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <map>
+#include <string_view>
 
 namespace rhygpu {
 
@@ -82,11 +83,12 @@ struct Parser {
    const TableImage& t;
    size_t i = 0;
 
+   static bool space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v'; }
    [[noreturn]] void fail(const std::string& msg) const {
       throw IllegalQuery("cannot parse expression at offset " + std::to_string(i) + ": " + msg);
    }
    void ws() {
-      while (i < s.size() && std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+      while (i < s.size() && space(s[i])) ++i;
    }
    bool eat(char c) {
       ws();
@@ -99,23 +101,31 @@ struct Parser {
    void expect(char c) {
       if (!eat(c)) fail(std::string("expected '") + c + "'");
    }
-   std::string token() {
+   // The next token, a view into the text (valid while the text is).
+   std::string_view token() {
       ws();
-      size_t b = i;
-      while (i < s.size() && s[i] != ',' && s[i] != '(' && s[i] != ')' && !std::isspace(static_cast<unsigned char>(s[i]))) ++i;
+      const size_t b = i;
+      while (i < s.size() && s[i] != ',' && s[i] != '(' && s[i] != ')' && !space(s[i])) ++i;
       if (b == i) fail("expected a token");
-      return s.substr(b, i - b);
+      return std::string_view(s).substr(b, i - b);
    }
+   // A base-10 integer with an optional sign, the whole token, within the range of long long.
    long long integer() {
-      const std::string tok = token();
-      try {
-         size_t used = 0;
-         long long v = std::stoll(tok, &used);
-         if (used != tok.size()) fail("expected an integer, got '" + tok + "'");
-         return v;
-      } catch (const std::logic_error&) {
-         fail("expected an integer, got '" + tok + "'");
+      const std::string_view tok = token();
+      size_t k = 0;
+      const bool neg = tok[0] == '-';
+      if (tok[0] == '-' || tok[0] == '+') k = 1;
+      unsigned long long v = 0;
+      const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
+      bool ok = k < tok.size();
+      for (; ok && k < tok.size(); ++k) {
+         const char c = tok[k];
+         if (c < '0' || c > '9') ok = false;
+         else if (v > (lim - static_cast<unsigned long long>(c - '0')) / 10) ok = false;
+         else v = v * 10 + static_cast<unsigned long long>(c - '0');
       }
+      if (!ok) fail("expected an integer, got '" + std::string(tok) + "'");
+      return neg ? static_cast<long long>(0ull - v) : static_cast<long long>(v);
    }
    uint32_t position() {
       const long long p = integer();
@@ -130,14 +140,14 @@ struct Parser {
    }
 
    void seq_column(Expr& e) {
-      e.column = token();
+      e.column = std::string(token());
       const int c = t.find_seq(e.column);
       if (c < 0) throw IllegalQuery("the database does not contain the sequence column '" + e.column + "'");
       e.sym_kind = t.seq[c].kind;
    }
 
    ExprPtr parse() {
-      const std::string name = token();
+      const std::string_view name = token();
       if (name == "True" || name == "False") {
          auto e = node(EK::BOOL);
          e->truth = name == "True";
@@ -164,7 +174,7 @@ struct Parser {
          if (n < -1000000 || n > 1000000) fail("NOf count out of range");
          e->n = static_cast<int>(n);
          expect(',');
-         const std::string mode = token();
+         const std::string_view mode = token();
          if (mode != "exactly" && mode != "atleast") fail("NOf mode must be exactly or atleast");
          e->exact = mode == "exactly";
          while (eat(',')) e->children.push_back(parse());
@@ -174,13 +184,13 @@ struct Parser {
          expect(',');
          e->pos = position();
          expect(',');
-         const std::string c = token();
+         const std::string_view c = token();
          if (c.size() != 1) fail("a symbol is a single character");
          if (c[0] == '.') {
             e->sym = -1;
          } else {
             e->sym = alphabet(e->sym_kind).sym(c[0]);
-            if (e->sym < 0) throw IllegalQuery("illegal symbol '" + c + "' for column " + e->column);
+            if (e->sym < 0) throw IllegalQuery("illegal symbol '" + std::string(c) + "' for column " + e->column);
          }
       } else if (name == "HasMut") {
          e = node(EK::HAS_MUT);
@@ -189,12 +199,12 @@ struct Parser {
          e->pos = position();
       } else if (name == "StrEq") {
          e = node(EK::STR_EQ);
-         e->column = token();
+         e->column = std::string(token());
          expect(',');
-         e->value = token();
+         e->value = std::string(token());
       } else if (name == "DateBetween") {
          e = node(EK::DATE_BETWEEN);
-         e->column = token();
+         e->column = std::string(token());
          expect(',');
          if (eat('*')) {
             e->has_from = false;
@@ -210,7 +220,7 @@ struct Parser {
             e->to = static_cast<int32_t>(integer());
          }
       } else {
-         fail("unknown function '" + name + "'");
+         fail("unknown function '" + std::string(name) + "'");
       }
       expect(')');
       return e;

@@ -65,7 +65,8 @@ class RawTable(C.Structure):
 
 class BatchTimes(C.Structure):
     _fields_ = [("plan_ms", C.c_double), ("prepare_ms", C.c_double), ("device_ms", C.c_double),
-                ("output_ms", C.c_double)]
+                ("output_ms", C.c_double), ("compile_ms", C.c_double), ("predict_ms", C.c_double),
+                ("lower_ms", C.c_double)]
 
 
 class BatchSchedule(C.Structure):

@@ -119,9 +119,9 @@ def test_batched_mutation_rows(config2_small):
 
 
 def test_batch_rows_in_parts(config2_small):
-    """A batch large enough to run in several parts (Mutations and Details first, then three
-    count parts, planned while earlier parts run) gives every query the counts and rows of the
-    single-part dense batch, and a refetch returns the rows of every part."""
+    """A batch run in two parts (Mutations and Details first, then the counts, planned while the
+    first part runs) gives every query the counts and rows of the single-part dense batch, and a
+    refetch returns the rows of both parts."""
     t, orc, dev, qs = config2_small
     big = (qs * 6)[:1700]
     rng = np.random.default_rng(11)
