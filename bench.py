@@ -60,12 +60,18 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--tile-bits", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--planner-queries", type=int, default=1000,
-                    help="queries (another seed) traced through the plain path to train the planner")
+    ap.add_argument("--planner-samples", type=int, default=200_000,
+                    help="operator-node traces of the plain path to train the planner on (0: no planner)")
+    ap.add_argument("--planner-trace-rows", type=int, default=500_000,
+                    help="sequences of the table the traces come from (its own seeded table)")
+    ap.add_argument("--planner-heldout", type=int, default=10_000,
+                    help="held-out queries on the benchmark table that judge the trained network")
     ap.add_argument("--no-planner", action="store_true", help="rule-based ordering only")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default filter schedule")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
+    ap.add_argument("--serve-rows", type=int, default=8_000_000,
+                    help="sequences of the serving table (its own seeded table when it differs from --rows)")
     return ap.parse_args()
 
 
@@ -263,22 +269,39 @@ def main():
         return statistics.median(ms)
 
     # ---------------- learned planner: traces of the plain path, trained on the GPU ----------------
+    # traces on their own table, the trained model imported here and judged on held-out queries
     planner = {"mode": "rule-based ordering"}
-    if not args.no_planner and args.planner_queries > 0:
-        train_q = table.queries(args.planner_queries, seed=args.qseed + 1000, use_aa=True, use_metadata=True)
+    if not args.no_planner and args.planner_samples > 0:
         t0 = time.perf_counter()
-        n_samples = dev.planner_collect(train_q)
+        own = args.planner_trace_rows != args.rows
+        tr_table = R.Table.generate(args.planner_trace_rows, seed=args.seed + 1, n_aa_genes=12) if own else table
+        tr_dev = R.Device(tr_table, dev_index) if own else dev
+        n_samples, n_trace_q, k = 0, 0, 0
+        while n_samples < args.planner_samples and k < 64:
+            qk = tr_table.queries(2000, seed=args.qseed + 1000 + k, use_aa=True, use_metadata=True)
+            n_samples += tr_dev.planner_collect(qk)
+            n_trace_q += len(qk)
+            k += 1
         collect_s = time.perf_counter() - t0
-        st = dev.planner_train(epochs=80, batch=1024, lr=2e-3, seed=7)
-        rule_ms = time_batch(5, 2)
-        planner = {"mode": "learned" if st["accepted"] else "rule-based ordering (network rejected by the judge)",
-                   "trace_queries": len(train_q), "samples": n_samples, "collect_s": round(collect_s, 3),
-                   "train_ms": round(st["train_ms"], 1), "val_qerr_median": [st["qerr_learned_median"],
-                                                                            st["qerr_rule_median"]],
-                   "val_qerr_p90": [st["qerr_learned_p90"], st["qerr_rule_p90"]],
-                   "cost_ln_err_median": st["cost_err_median"], "rule_ms_per_step": rule_ms}
-        if st["accepted"]:
-            dev.planner_mode(1)
+        st = tr_dev.planner_train(epochs=40, batch=1024, lr=2e-3, seed=7)
+        model = tr_dev.planner_export()
+        if own:
+            tr_dev.close()
+            del tr_table
+        dev.planner_import(model)
+        held = table.queries(args.planner_heldout, seed=args.qseed + 5000, use_aa=True, use_metadata=True)
+        t1 = time.perf_counter()
+        judged = dev.planner_evaluate(held)
+        planner = {"mode": "learned" if judged["accepted"] else "rule-based ordering (network rejected by the judge)",
+                   "trace_rows": args.planner_trace_rows, "trace_queries": n_trace_q, "samples": n_samples,
+                   "collect_s": round(collect_s, 2), "train_ms": round(st["train_ms"], 1),
+                   "train_split_qerr_median": [st["qerr_learned_median"], st["qerr_rule_median"]],
+                   "train_split_qerr_p90": [st["qerr_learned_p90"], st["qerr_rule_p90"]],
+                   "heldout_queries": len(held), "heldout_nodes": judged["n_val"],
+                   "heldout_evaluate_s": round(time.perf_counter() - t1, 2),
+                   "heldout_qerr_median": [judged["qerr_learned_median"], judged["qerr_rule_median"]],
+                   "heldout_qerr_p90": [judged["qerr_learned_p90"], judged["qerr_rule_p90"]],
+                   "heldout_cost_ln_err_median": judged["cost_err_median"]}
 
     # ---------------- autotuner: schedule of the filter launches of this batch (untimed) ----------------
     autotune = None
@@ -290,6 +313,11 @@ def main():
                     "best_filter_ms": round(tried[0][1], 3),
                     "default_filter_ms": next((round(ms, 3) for sc, ms in tried if sc == default_sched), None),
                     "worst_filter_ms": round(tried[-1][1], 3)}
+
+    if planner["mode"] == "learned":
+        planner["rule_ms_per_step"] = time_batch(10, 3)  # the same batch and schedule, rule-based plans
+        dev.planner_mode(1)
+        planner["learned_ms_per_step"] = time_batch(10, 3)
 
     # ---------------- batched path: device-resident ----------------
     dev.batch_prepare(queries, actions, columns, tile_bits=args.tile_bits)
@@ -320,9 +348,9 @@ def main():
     barrier(ws)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, ws)
     value = n * args.steps * ws / total_s
-    # the persistent filter kernel, then per column with Mutations queries: transpose, container,
-    # coverage and final kernels
-    launches_per_step = 1 + 4 * len({int(c) for c, a in zip(columns, actions) if a == 1})
+    # a persistent filter launch per class of programs, then per column with Mutations queries:
+    # transpose, container, coverage and final kernels
+    launches_per_step = info.n_filter_launches + 4 * len({int(c) for c, a in zip(columns, actions) if a == 1})
 
     # results of the batched path for the parity self-check against the plain path
     dev.batch_launch(sp, True, True)
@@ -422,7 +450,15 @@ def main():
     # ---------------- serving: Poisson arrivals, continuous batching ----------------
     serving = None
     if args.serve_seconds > 0:
-        srv = R.Server(dev, max_batch=512, streams=3)
+        t_setup = time.perf_counter()
+        s_table, s_dev, s_queries, s_planner = table, dev, queries, planner["mode"]
+        if args.serve_rows != args.rows:
+            s_table = R.Table.generate(args.serve_rows, seed=args.seed, n_aa_genes=12)
+            s_dev = R.Device(s_table, dev_index)
+            s_queries = s_table.queries(n, seed=args.qseed, use_aa=True, use_metadata=True)
+            s_planner = "rule-based ordering"
+        setup_s = time.perf_counter() - t_setup
+        srv = R.Server(s_dev, max_batch=512, streams=3)
         rng = np.random.default_rng(args.qseed + 7)
         runs = []
         for rate in [float(x) for x in args.serve_rates.split(",") if x]:
@@ -430,7 +466,7 @@ def main():
             arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
             mix = rng.choice(3, nreq, p=[0.70, 0.25, 0.05]).astype(np.int32)
             pick = rng.integers(0, n, nreq)
-            lat, wall = srv.replay([queries[i] for i in pick], mix, np.zeros(nreq, np.uint32), np.full(nreq, 0.05),
+            lat, wall = srv.replay([s_queries[i] for i in pick], mix, np.zeros(nreq, np.uint32), np.full(nreq, 0.05),
                                    np.full(nreq, 1000, np.uint32), arrivals)
             ok = lat[np.isfinite(lat)]
             runs.append({"arrival_qps": rate, "requests": nreq, "achieved_qps": nreq / wall,
@@ -439,9 +475,12 @@ def main():
         st = srv.stats()
         srv.stop()
         serving = {"mix": "70% count / 25% mutations (nucleotide, min proportion 0.05) / 5% details (first 1000 ids)",
-                   "arrivals": "Poisson, open loop (native submitter thread)", "rows": table.n_rows,
-                   "runs": runs, "mean_batch": st["mean_batch"], "batches": st["batches"],
-                   "peak_device_bytes": st["peak_bytes"], "planner": planner["mode"]}
+                   "arrivals": "Poisson, open loop (native submitter thread)", "rows": s_table.n_rows,
+                   "table_setup_s": round(setup_s, 1), "runs": runs, "mean_batch": st["mean_batch"],
+                   "batches": st["batches"], "peak_device_bytes": st["peak_bytes"], "planner": s_planner}
+        if s_dev is not dev:
+            s_dev.close()
+            del s_table
 
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)

@@ -191,6 +191,7 @@ int rhy_batch_times(RhyDevice* d, RhyBatchTimes* out);
 typedef struct {
    uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
    uint64_t device_bytes;
+   uint32_t n_filter_launches; /* one persistent filter launch per class of programs */
 } RhyBatchInfo;
 
 /* Split form of rhy_batch for callers that reuse one batch shape: prepare plans and stages the
@@ -280,6 +281,20 @@ int rhy_planner_mode(RhyDevice* d, int mode);
 /* Samples: x[n][24] features; y[n][3] = ln selectivity, ln cycles per tile, ln rule selectivity. */
 int rhy_planner_samples(RhyDevice* d, float* x, float* y, size_t cap, size_t* n);
 int rhy_planner_weights(RhyDevice* d, float* w /* RHY_MLP_NPARAM FP32 master weights */);
+/* A trained planner as plain values, to train on one table and plan on another: the FP32 master
+ * weights, the feature and target normalisation, and the verdict of the judge. */
+typedef struct {
+   float weights[RHY_MLP_NPARAM];
+   float feature_mean[RHY_PLANNER_FEATURES], feature_std[RHY_PLANNER_FEATURES];
+   double target_mean[2], target_std[2];
+   int accepted;
+} RhyPlannerModel;
+int rhy_planner_export(RhyDevice* d, RhyPlannerModel* out);
+int rhy_planner_import(RhyDevice* d, const RhyPlannerModel* in);
+/* Traces the expressions on this device (they do not join the training samples) and judges the
+ * current network on them against the rule-based estimates (q-errors in out, n_val = samples); the
+ * verdict replaces the planner's acceptance, and a rejected network leaves mode 1. */
+int rhy_planner_evaluate(RhyDevice* d, const char* const* exprs, uint32_t n, RhyPlannerStats* out);
 /* Network predictions (GPU inference) for feature rows: selectivity (fraction of rows) and cycles
  * per tile. */
 int rhy_planner_predict(RhyDevice* d, const float* x, uint32_t n, double* sel, double* cost);

@@ -601,6 +601,7 @@ int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out) {
       out->tile_bits = b.tile_bits;
       out->grid = b.grid;
       out->device_bytes = d->engine->device_bytes();
+      out->n_filter_launches = static_cast<uint32_t>(b.fgroups.size());
    });
 }
 
@@ -767,24 +768,86 @@ int rhy_planner_collect(RhyDevice* d, const char* const* exprs, uint32_t n, size
    });
 }
 
+namespace {
+void copy_stats(const rhygpu::PlannerStats& st, RhyPlannerStats* out) {
+   if (!out) return;
+   out->n_train = st.n_train;
+   out->n_val = st.n_val;
+   out->epochs = st.epochs;
+   out->train_loss = st.train_loss;
+   out->val_loss = st.val_loss;
+   out->qerr_learned_median = st.qerr_learned_median;
+   out->qerr_rule_median = st.qerr_rule_median;
+   out->qerr_learned_p90 = st.qerr_learned_p90;
+   out->qerr_rule_p90 = st.qerr_rule_p90;
+   out->cost_err_median = st.cost_err_median;
+   out->train_ms = st.train_ms;
+   out->accepted = st.accepted;
+}
+}  // namespace
+
 int rhy_planner_train(RhyDevice* d, uint32_t epochs, uint32_t batch, float lr, uint64_t seed, RhyPlannerStats* out) {
    return guarded([&] {
       need(d, "device");
-      const rhygpu::PlannerStats st = d->engine->planner_train(epochs, batch, lr, seed);
-      if (out) {
-         out->n_train = st.n_train;
-         out->n_val = st.n_val;
-         out->epochs = st.epochs;
-         out->train_loss = st.train_loss;
-         out->val_loss = st.val_loss;
-         out->qerr_learned_median = st.qerr_learned_median;
-         out->qerr_rule_median = st.qerr_rule_median;
-         out->qerr_learned_p90 = st.qerr_learned_p90;
-         out->qerr_rule_p90 = st.qerr_rule_p90;
-         out->cost_err_median = st.cost_err_median;
-         out->train_ms = st.train_ms;
-         out->accepted = st.accepted;
+      copy_stats(d->engine->planner_train(epochs, batch, lr, seed), out);
+   });
+}
+
+int rhy_planner_evaluate(RhyDevice* d, const char* const* exprs, uint32_t n, RhyPlannerStats* out) {
+   return guarded([&] {
+      need(d, "device");
+      if (n) need(exprs, "exprs");
+      std::vector<std::string> texts;
+      for (uint32_t i = 0; i < n; ++i) {
+         need(exprs[i], "expression");
+         texts.emplace_back(exprs[i]);
       }
+      copy_stats(d->engine->planner_evaluate(texts), out);
+   });
+}
+
+int rhy_planner_export(RhyDevice* d, RhyPlannerModel* out) {
+   return guarded([&] {
+      need(d, "device");
+      need(out, "out");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::Planner& p = d->engine->planner();
+      if (!p.trained) throw std::invalid_argument("the planner network is not trained");
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      p.net.get_master(out->weights);
+      std::copy(p.fmean.begin(), p.fmean.end(), out->feature_mean);
+      std::copy(p.fstd.begin(), p.fstd.end(), out->feature_std);
+      for (int k = 0; k < 2; ++k) {
+         out->target_mean[k] = p.tmean[k];
+         out->target_std[k] = p.tstd[k];
+      }
+      out->accepted = p.accepted ? 1 : 0;
+   });
+}
+
+int rhy_planner_import(RhyDevice* d, const RhyPlannerModel* in) {
+   return guarded([&] {
+      need(d, "device");
+      need(in, "model");
+      for (int k = 0; k < RHY_PLANNER_FEATURES; ++k)
+         if (!(std::isfinite(in->feature_mean[k]) && in->feature_std[k] > 0))
+            throw std::invalid_argument("model: feature normalisation must be finite with positive deviations");
+      for (int k = 0; k < 2; ++k)
+         if (!(std::isfinite(in->target_mean[k]) && in->target_std[k] > 0))
+            throw std::invalid_argument("model: target normalisation must be finite with positive deviations");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      rhygpu::Planner& p = d->engine->planner();
+      p.net.set_master(in->weights);
+      std::copy(in->feature_mean, in->feature_mean + RHY_PLANNER_FEATURES, p.fmean.begin());
+      std::copy(in->feature_std, in->feature_std + RHY_PLANNER_FEATURES, p.fstd.begin());
+      for (int k = 0; k < 2; ++k) {
+         p.tmean[k] = in->target_mean[k];
+         p.tstd[k] = in->target_std[k];
+      }
+      p.trained = true;
+      p.accepted = in->accepted != 0;
+      if (!p.accepted) d->engine->set_planner_mode(0);
    });
 }
 

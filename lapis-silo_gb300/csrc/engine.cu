@@ -944,6 +944,21 @@ const FeatureContext& Engine::fctx() {
 
 size_t Engine::planner_collect(const std::vector<std::string>& exprs) {
    std::lock_guard<std::mutex> lock(mu);
+   return collect_traces(exprs, planner_.samples);
+}
+
+PlannerStats Engine::planner_evaluate(const std::vector<std::string>& exprs) {
+   std::lock_guard<std::mutex> lock(mu);
+   std::vector<PlannerSample> held_out;
+   collect_traces(exprs, held_out);
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   const PlannerStats st = planner_.evaluate(held_out);
+   planner_.accepted = st.accepted != 0;
+   if (!planner_.accepted) use_learned_ = false;
+   return st;
+}
+
+size_t Engine::collect_traces(const std::vector<std::string>& exprs, std::vector<PlannerSample>& out) {
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
    const FeatureContext& ctx = fctx();
    const uint32_t W = tile_bits;
@@ -1000,7 +1015,7 @@ size_t Engine::planner_collect(const std::vector<std::string>& exprs) {
             smp.log_sel = static_cast<float>(std::log(std::max(popc / rows, 1e-7)));
             smp.log_cost = static_cast<float>(std::log(std::max(cyc / live, 1.0)));
             smp.rule_log_sel = static_cast<float>(std::log(std::max(std::min(1.0, ctx.rule(*sp.op) / rows), 1e-7)));
-            planner_.samples.push_back(smp);
+            out.push_back(smp);
             ++added;
          }
       }

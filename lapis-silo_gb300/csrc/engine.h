@@ -219,6 +219,10 @@ class Engine {
    // early exits) and appends one training sample per operator node. Returns the samples added.
    size_t planner_collect(const std::vector<std::string>& exprs);
    PlannerStats planner_train(uint32_t epochs, uint32_t batch, float lr, uint64_t seed);
+   // Traces the expressions (not added to the training samples) and judges the current network on
+   // them against the rule; the verdict replaces the planner's acceptance (a rejected network
+   // leaves the learned mode).
+   PlannerStats planner_evaluate(const std::vector<std::string>& exprs);
    // 0: rule-based ordering; 1: learned (only once a trained network was accepted by the judge).
    void set_planner_mode(int mode);
    int planner_mode() const { return use_learned_ ? 1 : 0; }
@@ -270,6 +274,8 @@ class Engine {
    std::unique_ptr<FeatureContext> fctx_;  // built on first use
    const FeatureContext& fctx();
    WorkerPool plan_pool_;  // planning threads, one per hardware thread
+   // Runs the expressions through the single-query path in trace mode; one sample per node.
+   size_t collect_traces(const std::vector<std::string>& exprs, std::vector<PlannerSample>& out);
 
 };
 

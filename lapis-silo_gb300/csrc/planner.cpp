@@ -340,6 +340,67 @@ const float* PlannerNet::predict_staged(uint32_t n) {
 // ------------------------------------------------------------------------------------------------
 // Planner
 
+namespace {
+// output 0: residual of the rule estimate, ln(measured / rule); output 1: ln cycles per tile
+double target_of(const PlannerSample& sm, int k) {
+   return k ? sm.log_cost : static_cast<double>(sm.log_sel) - rule_log_sel_of(sm.x.data());
+}
+}  // namespace
+
+void Planner::judge(const std::vector<const PlannerSample*>& set, const float* Y, PlannerStats& st) const {
+   std::vector<float> ql, qr, ce;
+   for (size_t i = 0; i < set.size(); ++i) {
+      const PlannerSample& sm = *set[i];
+      const double rl = rule_log_sel_of(sm.x.data());
+      const double ls = exact_by_rule(sm.x.data()) ? rl : rl + static_cast<double>(Y[2 * i]) * tstd[0] + tmean[0];
+      const double lc = static_cast<double>(Y[2 * i + 1]) * tstd[1] + tmean[1];
+      const double truth = sm.log_sel;
+      ql.push_back(static_cast<float>(std::exp(std::fabs(std::max(std::log(MIN_SEL), std::min(0.0, ls)) - truth))));
+      qr.push_back(static_cast<float>(std::exp(std::fabs(sm.rule_log_sel - truth))));
+      ce.push_back(static_cast<float>(std::fabs(lc - sm.log_cost)));
+   }
+   auto pct = [](std::vector<float> v, double q) {
+      if (v.empty()) return std::nanf("");
+      std::sort(v.begin(), v.end());
+      return v[static_cast<size_t>(q * (v.size() - 1))];
+   };
+   st.qerr_learned_median = pct(ql, 0.5);
+   st.qerr_rule_median = pct(qr, 0.5);
+   st.qerr_learned_p90 = pct(ql, 0.9);
+   st.qerr_rule_p90 = pct(qr, 0.9);
+   st.cost_err_median = pct(ce, 0.5);
+   // the judge: not worse than the rule at the median (index scans are exact for both, so ties
+   // there are common) and not worse at the 90th percentile
+   st.accepted = !set.empty() && std::isfinite(st.val_loss) &&
+                       st.qerr_learned_median <= st.qerr_rule_median * (1.0f + 1e-4f) &&
+                       st.qerr_learned_p90 <= st.qerr_rule_p90 * (1.0f + 1e-4f)
+                    ? 1
+                    : 0;
+}
+
+PlannerStats Planner::evaluate(const std::vector<PlannerSample>& set) {
+   if (!trained) throw std::invalid_argument("the planner network is not trained");
+   PlannerStats st{};
+   st.n_val = static_cast<uint32_t>(set.size());
+   const uint32_t n = st.n_val;
+   std::vector<float> X(static_cast<size_t>(n) * PLAN_FEATURES), Y(static_cast<size_t>(n) * 2);
+   std::vector<const PlannerSample*> ptrs(n);
+   double loss = 0;
+   for (uint32_t i = 0; i < n; ++i) {
+      ptrs[i] = &set[i];
+      normalize(set[i].x.data(), X.data() + static_cast<size_t>(i) * PLAN_FEATURES);
+   }
+   if (n) net.predict(X.data(), n, Y.data());
+   for (uint32_t i = 0; i < n; ++i)
+      for (int k = 0; k < 2; ++k) {
+         const double t = (target_of(set[i], k) - tmean[k]) / tstd[k];
+         loss += (Y[2 * i + k] - t) * (Y[2 * i + k] - t);
+      }
+   st.val_loss = n ? static_cast<float>(loss / n) : std::nanf("");
+   judge(ptrs, Y.data(), st);
+   return st;
+}
+
 PlannerStats Planner::train(uint32_t epochs, uint32_t batch, float lr, uint64_t seed) {
    const auto t0 = std::chrono::steady_clock::now();
    const uint32_t n = static_cast<uint32_t>(samples.size());
@@ -358,10 +419,7 @@ PlannerStats Planner::train(uint32_t epochs, uint32_t batch, float lr, uint64_t 
       fmean[k] = static_cast<float>(m);
       fstd[k] = static_cast<float>(std::max(std::sqrt(v / n_tr), 1e-3));
    }
-   // output 0: residual of the rule estimate, ln(measured / rule); output 1: ln cycles per tile
-   auto target = [&](const PlannerSample& sm, int k) -> double {
-      return k ? sm.log_cost : static_cast<double>(sm.log_sel) - rule_log_sel_of(sm.x.data());
-   };
+   auto target = target_of;
    for (int k = 0; k < 2; ++k) {
       double m = 0, v = 0;
       for (uint32_t i = 0; i < n_tr; ++i) m += target(samples[idx[i]], k);
@@ -398,32 +456,11 @@ PlannerStats Planner::train(uint32_t epochs, uint32_t batch, float lr, uint64_t 
    std::vector<float> Y(static_cast<size_t>(n_val) * 2);
    net.gradient(Xva.data(), Tva.data(), n_val, nullptr, &vloss, Y.data());
    st.val_loss = vloss;
-   std::vector<float> ql, qr, ce;
-   for (uint32_t i = 0; i < n_val; ++i) {
-      const PlannerSample& sm = samples[idx[n_tr + i]];
-      const double rl = rule_log_sel_of(sm.x.data());
-      const double ls = exact_by_rule(sm.x.data()) ? rl : rl + static_cast<double>(Y[2 * i]) * tstd[0] + tmean[0];
-      const double lc = static_cast<double>(Y[2 * i + 1]) * tstd[1] + tmean[1];
-      const double truth = sm.log_sel;
-      ql.push_back(static_cast<float>(std::exp(std::fabs(std::max(std::log(MIN_SEL), std::min(0.0, ls)) - truth))));
-      qr.push_back(static_cast<float>(std::exp(std::fabs(sm.rule_log_sel - truth))));
-      ce.push_back(static_cast<float>(std::fabs(lc - sm.log_cost)));
-   }
-   auto pct = [](std::vector<float> v, double q) {
-      std::sort(v.begin(), v.end());
-      return v[static_cast<size_t>(q * (v.size() - 1))];
-   };
-   st.qerr_learned_median = pct(ql, 0.5);
-   st.qerr_rule_median = pct(qr, 0.5);
-   st.qerr_learned_p90 = pct(ql, 0.9);
-   st.qerr_rule_p90 = pct(qr, 0.9);
-   st.cost_err_median = pct(ce, 0.5);
+   std::vector<const PlannerSample*> val(n_val);
+   for (uint32_t i = 0; i < n_val; ++i) val[i] = &samples[idx[n_tr + i]];
+   judge(val, Y.data(), st);
    trained = true;
-   // the judge: not worse than the rule at the median (index scans are exact for both, so ties
-   // there are common) and not worse at the 90th percentile
-   accepted = std::isfinite(st.val_loss) && st.qerr_learned_median <= st.qerr_rule_median * (1.0f + 1e-4f) &&
-              st.qerr_learned_p90 <= st.qerr_rule_p90 * (1.0f + 1e-4f);
-   st.accepted = accepted ? 1 : 0;
+   accepted = st.accepted != 0;
    st.train_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
    return st;
 }

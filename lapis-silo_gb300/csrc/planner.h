@@ -116,6 +116,10 @@ class Planner {
 
    // Trains on `samples` (a seeded 80/20 split) and judges the result on the held-out part.
    PlannerStats train(uint32_t epochs, uint32_t batch, float lr, uint64_t seed);
+   // Judges the current network on another sample set (traces of held-out queries, possibly on
+   // another table) with the statistics and the acceptance rule of train's held-out split; the
+   // verdict is returned, not applied.
+   PlannerStats evaluate(const std::vector<PlannerSample>& set);
    // Selectivity (fraction of rows) and cycles per tile for each feature row.
    void predict(const std::vector<std::array<float, PLAN_FEATURES>>& x, std::vector<double>& sel,
                 std::vector<double>& cost);
@@ -124,6 +128,11 @@ class Planner {
    void normalize(const float* x, float* out) const;
    double selectivity_of(const float* x, const float* y) const;
    double cost_of(const float* y) const;
+
+  private:
+   // q-errors of the network's outputs Y (two per sample) and of the rule estimates against the
+   // measured selectivities, the cost error, and the verdict (st.val_loss must be set).
+   void judge(const std::vector<const PlannerSample*>& set, const float* Y, PlannerStats& st) const;
 };
 
 }  // namespace rhygpu

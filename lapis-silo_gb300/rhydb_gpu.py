@@ -98,7 +98,7 @@ class SeqColumnInfo(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [("n_queries", C.c_uint32), ("n_mutation_slots", C.c_uint32), ("n_items", C.c_uint32),
                 ("n_instr", C.c_uint32), ("max_depth", C.c_uint32), ("tile_bits", C.c_uint32), ("grid", C.c_uint32),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("n_filter_launches", C.c_uint32)]
 
 
 class PlannerStats(C.Structure):
@@ -110,6 +110,11 @@ class PlannerStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PlannerModel(C.Structure):
+    _fields_ = [("weights", C.c_float * 5890), ("feature_mean", C.c_float * 24), ("feature_std", C.c_float * 24),
+                ("target_mean", C.c_double * 2), ("target_std", C.c_double * 2), ("accepted", C.c_int)]
 
 
 class ServerConfig(C.Structure):
@@ -194,6 +199,9 @@ def lib():
         "rhy_planner_mode": (I, [P, I]),
         "rhy_planner_samples": (I, [P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_planner_weights": (I, [P, P]),
+        "rhy_planner_export": (I, [P, C.POINTER(PlannerModel)]),
+        "rhy_planner_import": (I, [P, C.POINTER(PlannerModel)]),
+        "rhy_planner_evaluate": (I, [P, P, U32, C.POINTER(PlannerStats)]),
         "rhy_planner_predict": (I, [P, P, U32, P, P]),
         "rhy_mlp_gradient": (I, [P, P, P, P, U32, P, P, P]),
         "rhy_server_start": (I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
@@ -566,6 +574,22 @@ class Device:
         w = np.zeros(MLP_NPARAM, np.float32)
         _check(lib().rhy_planner_weights(self._h, _ptr(w)))
         return w
+
+    def planner_export(self) -> PlannerModel:
+        m = PlannerModel()
+        _check(lib().rhy_planner_export(self._h, C.byref(m)))
+        return m
+
+    def planner_import(self, model: PlannerModel):
+        _check(lib().rhy_planner_import(self._h, C.byref(model)))
+
+    def planner_evaluate(self, exprs) -> dict:
+        """Judges the current network on traces of these expressions on this device (the verdict
+        replaces the acceptance)."""
+        arr = _text_array(exprs)
+        st = PlannerStats()
+        _check(lib().rhy_planner_evaluate(self._h, C.cast(arr, C.c_void_p), len(exprs), C.byref(st)))
+        return st.as_dict()
 
     def mlp_gradient(self, w: np.ndarray, x: np.ndarray, t: np.ndarray):
         """One forward + backward of the planner network on the device: (gradient, loss, outputs)."""

@@ -101,3 +101,46 @@ def test_mode_requires_accepted_network():
     with pytest.raises(R.RhyError):
         dev.planner_train()  # no samples
     dev.close()
+
+
+def test_model_trained_on_one_table_plans_another(setup):
+    """Train on one table's traces, export, import into a device over a larger table with another
+    seed, judge there on held-out queries, and plan: results are identical under both planners."""
+    t, dev, train_q, _ = setup
+    src = R.Device(t, 0)
+    src.planner_collect(train_q)
+    st = src.planner_train(epochs=80, batch=1024, lr=2e-3, seed=7)
+    model = src.planner_export()
+    src.close()
+    assert model.accepted == st["accepted"] == 1
+    big = R.Table.generate(400000, seed=21, n_aa_genes=12, null_fraction=0.002)
+    dst = R.Device(big, 0)
+    with pytest.raises(R.RhyError):
+        dst.planner_mode(1)  # nothing trained here yet
+    dst.planner_import(model)
+    assert np.array_equal(dst.planner_weights(), np.ctypeslib.as_array(model.weights))
+    held = big.queries(600, seed=22, use_aa=True, use_metadata=True)
+    ev = dst.planner_evaluate(held)
+    print("judged on the other table:", ev)
+    assert ev["n_val"] > 3000
+    assert np.isfinite(ev["qerr_learned_median"]) and np.isfinite(ev["qerr_rule_p90"])
+    if ev["accepted"]:
+        dst.planner_mode(1)
+    else:
+        with pytest.raises(R.RhyError):
+            dst.planner_mode(1)
+    act = (np.arange(len(held)) % 4 == 3).astype(np.int32)
+    learned = dst.batch(held, act)
+    dst.planner_mode(0)
+    rule = dst.batch(held, act)
+    assert np.array_equal(learned[0], rule[0])
+    assert all(np.array_equal(learned[1][i], rule[1][i]) for i in rule[1])
+    # a model whose verdict was negative cannot enable the learned mode
+    model.accepted = 0
+    dst.planner_import(model)
+    with pytest.raises(R.RhyError):
+        dst.planner_mode(1)
+    bad = R.PlannerModel()
+    with pytest.raises(R.RhyError):
+        dst.planner_import(bad)  # zero deviations
+    dst.close()
