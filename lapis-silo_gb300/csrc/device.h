@@ -120,6 +120,7 @@ struct QueryDesc {
    uint32_t code_len;
    uint32_t out_tiles;    // 1 = write the row set to the query's output tiles
    uint32_t n_leaves;     // container leaves | coverage leaves << 16 (numbered 1.. in their c field)
+   uint32_t depth;        // stack tiles the program uses; the rest of its class's stack stages payloads
 };
 
 // ---- launchers (kernels.cu) ----

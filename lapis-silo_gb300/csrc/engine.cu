@@ -529,7 +529,7 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
       std::memcpy(b.h_code + off, p.code.data(), p.code.size() * sizeof(Instr));
       b.h_q[i] = QueryDesc{static_cast<uint32_t>(off), static_cast<uint32_t>(p.code.size()),
                            b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1,
-                           p.n_ctr_leaves | (p.n_cov_leaves << 16)};
+                           p.n_ctr_leaves | (p.n_cov_leaves << 16), std::max(p.max_depth, 1u)};
       off += p.code.size();
    }
    // items per class: tile-major interleaving spreads the expensive queries over the whole launch;

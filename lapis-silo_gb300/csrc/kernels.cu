@@ -95,8 +95,14 @@ constexpr uint16_t LC_NOPAY = 0xFFFF;
 struct LeafCache {
    uint4 desc[LC_DESCS];
    uint4 pay4[LC_PAY / 8];   // small-array payloads (TMA bulk copies, 16-byte aligned runs)
-   uint16_t poff[LC_DESCS];  // u16 offset into pay4 of descriptor i's first element, or LC_NOPAY
+   uint16_t poff[LC_DESCS];  // descriptor i's first element: u16 offset into pay4 (below LC_PAY), or
+                             // LC_PAY + offset into ext; LC_NOPAY when not copied
+   uint8_t dleaf[LC_DESCS];  // leaf (0-based) of staged descriptor i
+   uint32_t nstaged;         // staged descriptors: the staged leaves are a prefix of the leaves
    uint32_t pay_used;        // u16 of pay4 reserved by this item's copies
+   uint16_t* ext;            // the stack tiles the item's program leaves free (16-byte aligned)
+   uint32_t ext_cap;         // their size in u16
+   uint32_t ext_used;        // u16 of ext reserved by this item's copies
    uint64_t bar;             // completes the item's payload copies
    const uint4* src[LC_LEAVES];
    const uint16_t* pay[LC_LEAVES];
@@ -127,11 +133,15 @@ __device__ __forceinline__ void init_leaves(LeafCache& lc) {
 }
 
 // Clears the leaf tables for nl container and ncov coverage leaves; a barrier must follow.
-__device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_t ncov) {
+__device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_t ncov, uint16_t* ext = nullptr,
+                                             uint32_t ext_cap = 0) {
    if (threadIdx.x == 0) {
       lc.nl = nl;
       lc.ncov = ncov;
       lc.pay_used = 0;
+      lc.ext = ext;
+      lc.ext_cap = ext ? ext_cap : 0u;
+      lc.ext_used = 0;
    }
    for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
       lc.n[k] = 0;
@@ -174,6 +184,9 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
                              uint32_t& phase, int* err) {
    const DevTable* __restrict__ tab = c.tab;
    const uint32_t nl = lc.nl, ncov = lc.ncov;
+   // this thread's earlier shared-memory accesses (stack tiles, staged payloads of the previous
+   // item) are ordered before the bulk copies into the same memory issued after the next barrier
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
    for (uint32_t i = threadIdx.x; i < ncode; i += blockDim.x) {
       const uint4 raw = __ldg(reinterpret_cast<const uint4*>(code) + i);
       const Instr in = *reinterpret_cast<const Instr*>(&raw);
@@ -212,7 +225,7 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
    __syncthreads();
    if (threadIdx.x < 32) {  // exclusive scan of the counts; leaves that do not fit stay unstaged
       const uint32_t lane = threadIdx.x;
-      uint32_t carry = 0;
+      uint32_t carry = 0, staged = 0;
       for (uint32_t k0 = 0; k0 < nl; k0 += 32) {
          const uint32_t k = k0 + lane;
          const uint32_t x = k < nl ? lc.n[k] : 0u;
@@ -223,47 +236,62 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
             if (lane >= o) incl += y;
          }
          const uint32_t ex = carry + incl - x;
-         if (k < nl) lc.beg[k] = (x > 0 && ex + x <= LC_DESCS) ? ex : LC_NONE;
+         const bool fits = x > 0 && ex + x <= LC_DESCS;  // the leaves that fit are a prefix of them
+         if (k < nl) lc.beg[k] = fits ? ex : LC_NONE;
+         if (fits) {
+            for (uint32_t i = 0; i < x; ++i) lc.dleaf[ex + i] = static_cast<uint8_t>(k);
+         }
+         staged = max(staged, __reduce_max_sync(0xFFFFFFFFu, fits ? ex + x : 0u));
          carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
       }
+      if (lane == 0) lc.nstaged = staged;
    }
    __syncthreads();
+   // one staged descriptor per thread: its load, and the copy or prefetch of its payload
    const uint32_t bar = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
-   for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
-      const uint32_t b = lc.beg[k];
-      if (b == LC_NONE) continue;
-      const uint4* s = lc.src[k];
-      const uint16_t* pay = lc.pay[k];
-      for (uint32_t i = 0; i < lc.n[k]; ++i) {
-         const uint4 raw = __ldg(s + i);
-         lc.desc[b + i] = raw;
-         lc.poff[b + i] = LC_NOPAY;
-         const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
-         // the arena ends with 16 spare bytes, so rounding the end up stays inside it
-         const uint16_t* p = pay + d.payload;
-         if (d.type == CT_ARRAY && d.card_m1 < LC_SMALL) {
-            const uintptr_t a = reinterpret_cast<uintptr_t>(p);
-            const uintptr_t a0 = a & ~static_cast<uintptr_t>(15);
-            const uint32_t bytes = static_cast<uint32_t>(((a + 2u * (d.card_m1 + 1u) + 15) & ~static_cast<uintptr_t>(15)) - a0);
+   for (uint32_t j = threadIdx.x; j < lc.nstaged; j += blockDim.x) {
+      const uint32_t k = lc.dleaf[j];
+      const uint4 raw = __ldg(lc.src[k] + (j - lc.beg[k]));
+      lc.desc[j] = raw;
+      lc.poff[j] = LC_NOPAY;
+      const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+      // the arena ends with 16 spare bytes, so rounding the end up stays inside it
+      const uint16_t* p = lc.pay[k] + d.payload;
+      if (d.type == CT_ARRAY) {  // small arrays into pay4, any array into the free stack tiles
+         const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+         const uintptr_t a0 = a & ~static_cast<uintptr_t>(15);
+         const uint32_t bytes = static_cast<uint32_t>(((a + 2u * (d.card_m1 + 1u) + 15) & ~static_cast<uintptr_t>(15)) - a0);
+         uint32_t dst = 0, po = LC_NOPAY;
+         if (d.card_m1 < LC_SMALL) {
             const uint32_t at = atomicAdd(&lc.pay_used, bytes / 2);
             if (at + bytes / 2 <= LC_PAY) {
-               lc.poff[b + i] = static_cast<uint16_t>(at + (a - a0) / 2);
-               const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(lc.pay4)) + 2 * at;
-               asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-               asm volatile(
-                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                  "l"(a0), "r"(bytes), "r"(bar)
-                  : "memory");
-               continue;
+               po = at + static_cast<uint32_t>(a - a0) / 2;
+               dst = static_cast<uint32_t>(__cvta_generic_to_shared(lc.pay4)) + 2 * at;
             }
          }
-         if (d.type == CT_ARRAY) prefetch_l2(p, p + d.card_m1 + 1u);
-         else if (d.type == CT_BITSET) prefetch_l2(p + (c.row0 >> 4), p + ((c.row0 + c.W) >> 4));
-         else prefetch_l2(p, p + 2u * d.nruns);
+         if (po == LC_NOPAY && lc.ext_cap) {
+            const uint32_t at = atomicAdd(&lc.ext_used, bytes / 2);
+            if (at + bytes / 2 <= lc.ext_cap) {
+               po = LC_PAY + at + static_cast<uint32_t>(a - a0) / 2;
+               dst = static_cast<uint32_t>(__cvta_generic_to_shared(lc.ext)) + 2 * at;
+            }
+         }
+         if (po != LC_NOPAY) {
+            lc.poff[j] = static_cast<uint16_t>(po);
+            asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+            asm volatile(
+               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(a0), "r"(bytes), "r"(bar)
+               : "memory");
+            continue;
+         }
       }
+      if (d.type == CT_ARRAY) prefetch_l2(p, p + d.card_m1 + 1u);
+      else if (d.type == CT_BITSET) prefetch_l2(p + (c.row0 >> 4), p + ((c.row0 + c.W) >> 4));
+      else prefetch_l2(p, p + 2u * d.nruns);
    }
    __syncthreads();
-   if (lc.pay_used == 0) return true;  // no copies this item
+   if (lc.pay_used == 0 && lc.ext_used == 0) return true;  // no copies this item
    if (threadIdx.x == 0)
       asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
    bool ok = wait_copies(lc, phase);
@@ -298,7 +326,7 @@ __device__ void push_containers(uint32_t* t, const TileCtx& c, const CtrDesc* __
       if (use_mask && !((mask >> d.sym) & 1u)) continue;
       const uint16_t po = staged ? lc.poff[lc.beg[leaf - 1] + i] : LC_NOPAY;
       if (po != LC_NOPAY) {  // array copied into shared memory with the item's leaves
-         const uint16_t* sp = reinterpret_cast<const uint16_t*>(lc.pay4) + po;
+         const uint16_t* sp = po < LC_PAY ? reinterpret_cast<const uint16_t*>(lc.pay4) + po : lc.ext + (po - LC_PAY);
          const uint32_t card = d.card_m1 + 1u;
          for (uint32_t k = threadIdx.x; k < card; k += blockDim.x) {
             const uint32_t r = static_cast<uint32_t>(sp[k]) - c.row0;
@@ -744,7 +772,11 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
       if (it >= n_items) return;
       const WorkItem wi = items[it];
       const QueryDesc q = queries[wi.query];
-      clear_leaves(lc, min(q.n_leaves & 0xFFFFu, LC_LEAVES), min(q.n_leaves >> 16, LC_COV));
+      // the program uses q.depth stack tiles; the class's other tiles take this item's payloads
+      const uint32_t depth = min(max(q.depth, 1u), cap);
+      const uint32_t ext_cap = min((cap - depth) * (tile_bits / 16), 65535u - LC_PAY - 16u) & ~7u;
+      clear_leaves(lc, min(q.n_leaves & 0xFFFFu, LC_LEAVES), min(q.n_leaves >> 16, LC_COV),
+                   reinterpret_cast<uint16_t*>(smem + static_cast<size_t>(depth) * (tile_bits >> 5)), ext_cap);
       __syncthreads();
       TileCtx c;
       c.tab = tab;
@@ -758,7 +790,8 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
             reinterpret_cast<uint4*>(smem)[w4] = make_uint4(0, 0, 0, 0);
       } else {
          if (!stage_leaves(lc, c, code + q.code_off, q.code_len, phase, err)) return;
-         if (!run_program(c, code + q.code_off, q.code_len, smem, cap, lc, err)) return;
+         // the stack may not grow past the program's depth into the staged payloads
+         if (!run_program(c, code + q.code_off, q.code_len, smem, depth, lc, err)) return;
       }
       uint32_t* dst = q.out_tiles ? out_tiles + static_cast<size_t>(q.out_tiles - 1) * per_query +
                                        static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5)
