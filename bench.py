@@ -68,6 +68,8 @@ def parse():
                     help="held-out queries on the benchmark table that judge the trained network")
     ap.add_argument("--no-planner", action="store_true", help="rule-based ordering only")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default filter schedule")
+    ap.add_argument("--schedule", default="",
+                    help="max_tile_bits,stack_kb,ctas_per_sm,query_major: this filter schedule instead of the autotuner's")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
     ap.add_argument("--serve-rows", type=int, default=8_000_000,
@@ -305,7 +307,10 @@ def main():
 
     # ---------------- autotuner: schedule of the filter launches of this batch (untimed) ----------------
     autotune = None
-    if not args.no_autotune and not args.tile_bits:
+    if args.schedule:
+        w, kb, cps, qm = (int(x) for x in args.schedule.split(","))
+        dev.batch_schedule(max_tile_bits=w, stack_kb=kb, ctas_per_sm=cps, query_major=qm)
+    elif not args.no_autotune and not args.tile_bits:
         default_sched = dev.batch_schedule()
         t0 = time.perf_counter()
         tried = dev.batch_autotune(queries, actions, columns, reps=3, stream=sp)

@@ -107,6 +107,8 @@ struct LeafCache {
    const uint4* src[LC_LEAVES];
    const uint16_t* pay[LC_LEAVES];
    uint32_t n[LC_LEAVES];
+   uint32_t symmask[LC_LEAVES];  // symbols the leaf ORs (every container for dictionary leaves)
+   uint32_t match[LC_LEAVES];    // staged leaves of at most 32 descriptors: bit i = descriptor i matches
    uint32_t beg[LC_LEAVES];  // LC_NONE: not staged (the leaf reads its descriptors from global memory)
    uint4 cov[LC_COV];        // exception range (x, y) and missing-interval range (z, w) of the tile
    uint32_t nl;              // container leaves 1..nl are described by the table
@@ -146,6 +148,7 @@ __device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_
    for (uint32_t k = threadIdx.x; k < nl; k += blockDim.x) {
       lc.n[k] = 0;
       lc.src[k] = nullptr;
+      lc.match[k] = 0;
    }
    for (uint32_t k = threadIdx.x; k < ncov; k += blockDim.x) lc.cov[k] = make_uint4(0, 0, 0, 0);
 }
@@ -221,6 +224,7 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
       lc.src[in.c - 1] = reinterpret_cast<const uint4*>(ctrs) + b;
       lc.pay[in.c - 1] = payload;
       lc.n[in.c - 1] = e - b;
+      lc.symmask[in.c - 1] = in.op == OP_PUSH_SCAN ? in.b : 0xFFFFFFFFu;
    }
    __syncthreads();
    if (threadIdx.x < 32) {  // exclusive scan of the counts; leaves that do not fit stay unstaged
@@ -255,6 +259,8 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
       lc.desc[j] = raw;
       lc.poff[j] = LC_NOPAY;
       const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+      if (!((lc.symmask[k] >> d.sym) & 1u)) continue;  // a symbol the leaf does not OR: no payload
+      if (lc.n[k] <= 32) atomicOr(&lc.match[k], 1u << (j - lc.beg[k]));
       // the arena ends with 16 spare bytes, so rounding the end up stays inside it
       const uint16_t* p = lc.pay[k] + d.payload;
       if (d.type == CT_ARRAY) {  // small arrays into pay4, any array into the free stack tiles
@@ -320,7 +326,14 @@ __device__ void push_containers(uint32_t* t, const TileCtx& c, const CtrDesc* __
       n = e - b;
    }
    const bool staged = leaf >= 1 && leaf <= lc.nl && lc.beg[leaf - 1] != LC_NONE;
-   for (uint32_t i = 0; i < n; ++i) {
+   // staged leaves of at most 32 descriptors visit only the matching ones
+   uint32_t todo = staged && n <= 32 ? lc.match[leaf - 1] : 0u;
+   const bool listed = staged && n <= 32;
+   for (uint32_t i = 0; listed ? todo != 0u : i < n; ++i) {
+      if (listed) {
+         i = __ffs(todo) - 1;
+         todo &= todo - 1;
+      }
       const uint4 raw = src[i];
       const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
       if (use_mask && !((mask >> d.sym) & 1u)) continue;

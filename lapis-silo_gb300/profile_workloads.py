@@ -29,6 +29,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--qseed", type=int, default=43)
+    ap.add_argument("--query-major", action="store_true", help="batch: query-major work items")
     args = ap.parse_args()
 
     import torch
@@ -49,6 +50,8 @@ def main():
         stream.synchronize()
         print(f"plain-mutations: {len(idx)} queries over {table.n_rows} rows")
     else:
+        if args.query_major:
+            dev.batch_schedule(query_major=1)
         dev.batch_prepare(queries, actions, columns)
         for _ in range(args.steps):
             dev.batch_launch(sp, True, True)
