@@ -361,6 +361,9 @@ def main():
     dev.batch_launch(sp, True, True)
     torch.cuda.synchronize()
     b_counts, b_muts = dev.batch_results()
+    # row x position cells the batch's Mutations queries count: |F| x L per query
+    cells = sum(int(b_counts[i]) * table.columns[int(columns[i])].L for i in range(n) if actions[i] == 1)
+    step_s = statistics.median(step_ms) / 1000.0
 
     # per-kernel times of the batched path
     kernels_ms = {}
@@ -541,6 +544,7 @@ def main():
                       "p99_ms": float(np.percentile(plain_ms, 99)), "queries": m, "e2e_qps": plain_e2e_qps,
                       "e2e_p99_ms": float(np.percentile(e2e_plain_ms, 99))},
             "speedup_vs_plain": value / plain_qps,
+            "row_position_counts_per_s": cells * ws / max_over_ranks(step_s, ws),
             "planner": planner,
             "autotune": autotune,
             "serving": serving,
