@@ -353,9 +353,10 @@ def main():
     barrier(ws)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, ws)
     value = n * args.steps * ws / total_s
-    # a persistent filter launch per class of programs, then per column with Mutations queries:
-    # transpose, container, coverage and final kernels
-    launches_per_step = info.n_filter_launches + 4 * len({int(c) for c, a in zip(columns, actions) if a == 1})
+    # a persistent filter launch per class of programs, then per column with Mutations queries: the
+    # slot split, transpose, container, coverage, row-index (when on) and final kernels
+    per_col = 5 + (1 if dev.sparse_rows()[1] > 0 else 0)
+    launches_per_step = info.n_filter_launches + per_col * len({int(c) for c, a in zip(columns, actions) if a == 1})
 
     # results of the batched path for the parity self-check against the plain path
     dev.batch_launch(sp, True, True)
@@ -368,7 +369,7 @@ def main():
     # per-kernel times of the batched path
     kernels_ms = {}
     for name, parts in (("filter_batch", 1), ("transpose", 2), ("mut_ctr_batch", 4), ("mut_cov_batch", 8),
-                        ("mut_final_batch", 16)):
+                        ("mut_final_batch", 16), ("mut_sparse_batch", 32)):
         ts = []
         for _ in range(2):
             dev.batch_launch_parts(1, sp) if parts != 1 else None

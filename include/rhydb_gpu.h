@@ -155,6 +155,11 @@ int rhy_count(RhyDevice* d, const char* expr, void* stream, uint64_t* out);
 int rhy_eval(RhyDevice* d, const char* expr, void* stream, uint32_t* out_bits, uint64_t* out_count);
 /* counts: n_symbols * L words, counts[symbol * L + position]; filter_count may be NULL. */
 int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream, uint32_t* counts, uint64_t* filter_count);
+/* Mutations filters of 1..set[0] rows (single queries) or 1..set[1] rows (slots of a batch) are
+ * counted from the row index (each filtered row adds its entries) instead of by the passes over
+ * every container; 0 turns that path off. Results are the same either way. `set` and `get` point
+ * to two values each and may be NULL. Defaults: rows / 32 and rows / 64. */
+int rhy_sparse_rows(RhyDevice* d, const uint64_t* set, uint64_t* get);
 /* ---- batched path (no reference counterpart: the reference runs one query per worker thread,
  * app/src/api.cpp:39-51) ----
  * n queries; actions[i] 0 = count, 1 = mutations of columns[i]. counts[i] receives the filter
@@ -222,7 +227,9 @@ int rhy_batch_autotune(RhyDevice* d, const char* const* exprs, const int* action
                        uint32_t reps, void* stream, RhyBatchSchedule* tried, double* tried_ms, size_t cap,
                        size_t* n_tried);
 /* Variants for timing: capture without the host copies; launch a subset of the kernels
- * (bit 0 filter, bits 1..4 transpose / container / coverage / final mutations kernels). */
+ * (bit 0 filter, bits 1..4 transpose / container / coverage / final mutations kernels, bit 5 the
+ * row-index pass of the slots whose filters have few rows; without bit 5 the dense kernels count
+ * every slot). */
 int rhy_batch_capture_ex(RhyDevice* d, void* stream, int copy_in, int copy_out);
 int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts);
 
@@ -231,7 +238,9 @@ int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts);
  * a mutations query) into the handle's scratch without synchronising. */
 int rhy_plain_prepare(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns, uint32_t n);
 int rhy_plain_launch(RhyDevice* d, uint32_t i, void* stream);
-/* parts: bit 0 zeroing + filter kernel, bits 1..3 container / coverage / final mutations kernels. */
+/* parts: bit 0 zeroing + filter kernel, bits 1..3 container / coverage / final mutations kernels,
+ * bit 4 the row-index pass for filters of few rows (rhy_sparse_rows; without it the container and
+ * coverage kernels count every filter). */
 int rhy_plain_launch_parts(RhyDevice* d, uint32_t i, void* stream, uint32_t parts);
 /* Bytes a mutations pass over `column` must read: container payloads plus descriptors. */
 int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_bytes, uint64_t* descriptor_bytes);

@@ -12,7 +12,13 @@
 //   mut_cov_batch_kernel   missing-interval and coverage boundary events (reference:
 //                          mutations_node.cpp:51-136)
 //   mut_final_batch_kernel prefix sums and reference counts per query
+//   mut_select_kernel      splits the slots by their filter's cardinality: none for empty filters,
+//                          the row-index pass for filters of at most sparse_max rows, the dense
+//                          passes above (over a compacted slot list) for the others
+//   mut_sparse_batch_kernel the row-index pass of the sparse slots
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "device.h"
 #include "mutations_common.cuh"
@@ -38,9 +44,11 @@ __device__ __forceinline__ uint32_t pass_width_u32(uint32_t nqc, uint32_t pass) 
 constexpr uint32_t TR_WORDS = BT / 32;
 constexpr uint32_t TR_CHUNKS = 32;  // query chunks of 32 staged per round (a multiple of 8)
 
-__global__ void __launch_bounds__(BT) transpose_kernel(const uint32_t* __restrict__ tiles, uint32_t nq, uint32_t nchunks,
-                                                       uint32_t* __restrict__ R) {
+__global__ void __launch_bounds__(BT) transpose_kernel(const uint32_t* __restrict__ tiles,
+                                                       const uint32_t* __restrict__ lists, uint32_t nq_max,
+                                                       uint32_t nchunks, uint32_t* __restrict__ R) {
    __shared__ uint32_t stage[TR_WORDS * 32 * (TR_CHUNKS + 1)];
+   const uint32_t nq = lists[2 * nq_max];  // dense slots: lists[0 .. nq)
    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
    const uint32_t words = nchunks * CHUNK_WORDS;
    const uint32_t nqc = (nq + 31) / 32;
@@ -52,7 +60,7 @@ __global__ void __launch_bounds__(BT) transpose_kernel(const uint32_t* __restric
       const uint32_t P = nc | 1u;  // odd stride: the 32 lanes of a warp hit 32 banks
       for (uint32_t c = 0; c < nc; ++c) {
          const uint32_t q = 32 * (c0 + c) + lane;
-         const uint32_t x = q < nq ? __ldg(tiles + static_cast<size_t>(q) * words + w) : 0u;
+         const uint32_t x = q < nq ? __ldg(tiles + static_cast<size_t>(lists[q]) * words + w) : 0u;
          uint32_t mine = 0;
 #pragma unroll
          for (uint32_t b = 0; b < 32; ++b) {
@@ -133,12 +141,14 @@ __device__ __forceinline__ void count_window(NibbleCounter& k, uint32_t x, uint3
 // Bitset containers are expanded 1024 rows at a time into a per-warp row list in shared memory.
 __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                            const CtrUnit* __restrict__ units, uint32_t n_units,
-                                                           const uint16_t* __restrict__ R, uint32_t nq,
+                                                           const uint16_t* __restrict__ R,
+                                                           const uint32_t* __restrict__ lists, uint32_t nq_max,
                                                            uint32_t* __restrict__ counts) {
    __shared__ uint16_t list[BT / 32][1024];
    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
    const uint32_t u = blockIdx.x * (BT / 32) + warp;
-   if (u >= n_units) return;  // the whole warp leaves
+   const uint32_t nq = lists[2 * nq_max];  // dense slots: lists[0 .. nq)
+   if (u >= n_units || blockIdx.y * PASS_GROUPS * MUT_GROUP >= nq) return;  // the whole warp leaves
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t L = cs->L;
    const size_t per_query = static_cast<size_t>(cs->nsym) * L;
@@ -230,10 +240,11 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
       for (uint32_t q = 0; q < MUT_GROUP; ++q)
          for (uint32_t o = 16; o >= gsz; o >>= 1) k.c[q] += __shfl_down_sync(0xFFFFFFFFu, k.c[q], o);
       if (sub == 0 && gvalid) {
-         uint32_t* dst = counts + static_cast<size_t>(MUT_GROUP) * g * per_query + static_cast<size_t>(s) * L + p;
 #pragma unroll
          for (uint32_t q = 0; q < MUT_GROUP; ++q)
-            if (k.c[q] && MUT_GROUP * g + q < nq) atomicAdd(dst + q * per_query, k.c[q]);
+            if (k.c[q] && MUT_GROUP * g + q < nq)
+               atomicAdd(counts + static_cast<size_t>(lists[MUT_GROUP * g + q]) * per_query + static_cast<size_t>(s) * L + p,
+                         k.c[q]);
       }
    }
 }
@@ -246,8 +257,11 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
 // Events are read once for all groups of the pass.
 __global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                               const EvItem* __restrict__ items,
-                                                              const uint16_t* __restrict__ R, uint32_t nq,
+                                                              const uint16_t* __restrict__ R,
+                                                              const uint32_t* __restrict__ lists, uint32_t nq_max,
                                                               uint32_t* __restrict__ scratch) {
+   const uint32_t nq = lists[2 * nq_max];  // dense slots: lists[0 .. nq)
+   if (blockIdx.y * 32 * MUT_GROUP >= nq) return;
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t L = cs->L, nseg = mut_nseg(L);
    const size_t per_query = mut_scratch_words(L);
@@ -277,7 +291,8 @@ __global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __
    const uint32_t hist = missing ? 2 * (L + 1) : (it.list == EV_CSTART ? 0u : L + 1);
    const uint32_t segb = 3 * (L + 1) + (missing ? 2 * nseg : (it.list == EV_CSTART ? 0u : nseg));
    const uint32_t sign = it.list == EV_MEND ? 0xFFFFFFFFu : 1u;  // multiplier modulo 2^32
-   uint32_t* sc = scratch + static_cast<size_t>(g) * MUT_GROUP * per_query;
+   // scratch of query q of this lane's group: that dense slot's
+   auto sc_of = [&](uint32_t q) { return scratch + static_cast<size_t>(lists[MUT_GROUP * g + q]) * per_query; };
 
    NibbleCounter k;
    k.clear();
@@ -291,7 +306,7 @@ __global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __
       if (curseg == NONE) return;
 #pragma unroll
       for (uint32_t q = 0; q < MUT_GROUP; ++q) {
-         if (seg[q] && MUT_GROUP * g + q < nq) atomicAdd(sc + q * per_query + segb + curseg, seg[q] * sign);
+         if (seg[q] && MUT_GROUP * g + q < nq) atomicAdd(sc_of(q) + segb + curseg, seg[q] * sign);
          seg[q] = 0;
       }
    };
@@ -300,7 +315,7 @@ __global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __
       if (cur != NONE && cur <= L) {
 #pragma unroll
          for (uint32_t q = 0; q < MUT_GROUP; ++q) {
-            if (k.c[q] && MUT_GROUP * g + q < nq) atomicAdd(sc + q * per_query + hist + cur, k.c[q] * sign);
+            if (k.c[q] && MUT_GROUP * g + q < nq) atomicAdd(sc_of(q) + hist + cur, k.c[q] * sign);
             seg[q] += k.c[q];
          }
       }
@@ -356,6 +371,61 @@ __global__ void __launch_bounds__(BT, 3) mut_cov_batch_kernel(const DevTable* __
    flush_seg();
 }
 
+// One CTA: the dense slot list, the sparse slot list and their lengths, in slot order.
+__global__ void __launch_bounds__(1024) mut_select_kernel(const unsigned long long* __restrict__ fcounts,
+                                                          const uint32_t* __restrict__ slot_query, uint32_t nq,
+                                                          unsigned long long sparse_max, uint32_t* __restrict__ lists) {
+   __shared__ uint32_t wd[32], wsp[32];
+   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+   uint32_t nd = 0, ns = 0;  // the same in every thread
+   for (uint32_t q0 = 0; q0 < nq; q0 += blockDim.x) {
+      const uint32_t q = q0 + threadIdx.x;
+      const unsigned long long fc = q < nq ? fcounts[slot_query[q]] : 0ull;
+      const bool dense = fc > sparse_max, sparse = fc > 0 && fc <= sparse_max;
+      const uint32_t bd = __ballot_sync(0xFFFFFFFFu, dense), bs = __ballot_sync(0xFFFFFFFFu, sparse);
+      if (lane == 0) {
+         wd[warp] = __popc(bd);
+         wsp[warp] = __popc(bs);
+      }
+      __syncthreads();
+      uint32_t pd = 0, ps = 0, td = 0, ts = 0;
+      for (uint32_t w = 0; w < nw; ++w) {
+         pd += w < warp ? wd[w] : 0u;
+         ps += w < warp ? wsp[w] : 0u;
+         td += wd[w];
+         ts += wsp[w];
+      }
+      const uint32_t below = (1u << lane) - 1u;
+      if (dense) lists[nd + pd + __popc(bd & below)] = q;
+      if (sparse) lists[nq + ns + ps + __popc(bs & below)] = q;
+      nd += td;
+      ns += ts;
+      __syncthreads();
+   }
+   if (threadIdx.x == 0) {
+      lists[2 * nq] = nd;
+      lists[2 * nq + 1] = ns;
+   }
+}
+
+// grid (CTAs per slot, nq): the row-index pass of sparse slot blockIdx.y, if there is one.
+__global__ void __launch_bounds__(BT) mut_sparse_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                              const uint32_t* __restrict__ filters,
+                                                              const uint32_t* __restrict__ lists, uint32_t nq,
+                                                              uint32_t* counts, uint32_t* scratch) {
+   __shared__ uint32_t list[BT / 32][1024];
+   if (blockIdx.y >= lists[2 * nq + 1]) return;
+   const uint32_t slot = lists[nq + blockIdx.y];
+   const DevSeqCol* cs = &tab->seq[col];
+   const uint32_t words = tab->nchunks * CHUNK_WORDS;
+   const uint32_t warp = threadIdx.x >> 5, nwarps = gridDim.x * (BT / 32);
+   const uint32_t* F = filters + static_cast<size_t>(slot) * words;
+   uint32_t* cnt = counts + static_cast<size_t>(slot) * cs->nsym * cs->L;
+   uint32_t* sc = scratch + static_cast<size_t>(slot) * mut_scratch_words(cs->L);
+   for (uint32_t w = (blockIdx.x * (BT / 32) + warp) * 32; w < words; w += nwarps * 32)
+      row_index_pass32(cs, F, w, words, cnt, sc, list[warp]);
+}
+
 // grid (ceil(L / MUT_SEG), nq): reference counts of slot blockIdx.y.
 __global__ void __launch_bounds__(MUT_SEG) mut_final_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                                   const unsigned long long* __restrict__ fcounts,
@@ -380,20 +450,31 @@ size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks) {
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                             const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
                             const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
-                            uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
-                            uint32_t parts) {
+                            uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
+                            uint32_t* d_lists, uint64_t sparse_max, void* stream, uint32_t parts) {
    if (nq == 0) return;
    cudaStream_t s = static_cast<cudaStream_t>(stream);
-   const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;
-   if (parts & BMUT_PART_TRANSPOSE)
-      transpose_kernel<<<nchunks * CHUNK_WORDS / TR_WORDS, BT, 0, s>>>(d_filters, nq, nchunks,
+   const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;  // grids for the largest dense list
+   // the slot lists are made with the transpose part, which every timed part follows; the split
+   // does not depend on which parts run (without the row-index part its slots stay uncounted)
+   if (parts & BMUT_PART_TRANSPOSE) {
+      mut_select_kernel<<<1, 1024, 0, s>>>(d_fcounts, d_slot_query, nq, static_cast<unsigned long long>(sparse_max),
+                                           d_lists);
+      transpose_kernel<<<nchunks * CHUNK_WORDS / TR_WORDS, BT, 0, s>>>(d_filters, d_lists, nq, nchunks,
                                                                        reinterpret_cast<uint32_t*>(d_masks));
+   }
    if ((parts & BMUT_PART_CTR) && n_units > 0) {
       const dim3 grid((n_units + BT / 32 - 1) / (BT / 32), (ngroups + PASS_GROUPS - 1) / PASS_GROUPS);
-      mut_ctr_batch_kernel<<<grid, BT, 0, s>>>(d_table, col, d_units, n_units, d_masks, nq, d_counts);
+      mut_ctr_batch_kernel<<<grid, BT, 0, s>>>(d_table, col, d_units, n_units, d_masks, d_lists, nq, d_counts);
    }
    if ((parts & BMUT_PART_COV) && n_ev > 0)
-      mut_cov_batch_kernel<<<dim3(n_ev, (ngroups + 31) / 32), BT, 0, s>>>(d_table, col, d_ev, d_masks, nq, d_scratch);
+      mut_cov_batch_kernel<<<dim3(n_ev, (ngroups + 31) / 32), BT, 0, s>>>(d_table, col, d_ev, d_masks, d_lists, nq,
+                                                                          d_scratch);
+   if ((parts & BMUT_PART_SPARSE) && sparse_max > 0) {
+      const uint32_t per_slot = std::max(1u, std::min(nchunks * CHUNK_WORDS / 32 / (BT / 32), 64u));
+      mut_sparse_batch_kernel<<<dim3(per_slot, nq), BT, 0, s>>>(d_table, col, d_filters, d_lists, nq, d_counts,
+                                                                d_scratch);
+   }
    if (parts & BMUT_PART_FINAL) {
       dim3 fin((col_host.L + MUT_SEG - 1) / MUT_SEG, nq);
       mut_final_batch_kernel<<<fin, MUT_SEG, 0, s>>>(d_table, col, d_fcounts, d_slot_query, d_counts, d_scratch);

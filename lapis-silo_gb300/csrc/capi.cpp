@@ -644,14 +644,29 @@ int rhy_plain_launch_parts(RhyDevice* d, uint32_t i, void* stream, uint32_t part
          }
          if (parts >> 1)
             e.launch_mutations(static_cast<int>(q.column), e.d_filter, e.d_count, e.d_counts, e.d_scratch, s,
-                               (parts >> 1) & rhygpu::MUT_PART_ALL);
+                               (parts >> 1) & (rhygpu::MUT_PART_ALL | rhygpu::MUT_PART_SPARSE));
       } else if (parts & 1) {
          e.launch_count(d->d_plain_code + q.code_off, q.prog, e.d_count, nullptr, s);
       }
    });
 }
 
-int rhy_plain_launch(RhyDevice* d, uint32_t i, void* stream) { return rhy_plain_launch_parts(d, i, stream, 15); }
+int rhy_plain_launch(RhyDevice* d, uint32_t i, void* stream) { return rhy_plain_launch_parts(d, i, stream, 31); }
+
+int rhy_sparse_rows(RhyDevice* d, const uint64_t* set, uint64_t* get) {
+   return guarded([&] {
+      need(d, "device");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      if (set) {
+         d->engine->sparse_rows_plain = set[0];
+         d->engine->sparse_rows_batch = set[1];
+      }
+      if (get) {
+         get[0] = d->engine->sparse_rows_plain;
+         get[1] = d->engine->sparse_rows_batch;
+      }
+   });
+}
 
 int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_bytes, uint64_t* descriptor_bytes) {
    return guarded([&] {

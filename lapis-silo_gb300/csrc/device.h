@@ -53,6 +53,8 @@ struct DevSeqCol {
    const uint32_t* mend;       // missing-interval end events
    const CovEvent* cstart;     // coverage starts > 0
    const CovEvent* cend;       // coverage ends < L
+   const uint32_t* hrow_off;   // row index: nchunks * CHUNK_ROWS + 1 offsets into hent
+   const uint32_t* hent;       // row index entries (position << 5 | code)
    uint32_t L;
    uint32_t nblocks;
    uint32_t nsym;
@@ -144,10 +146,13 @@ enum : uint32_t { BMUT_PART_TRANSPOSE = 1, BMUT_PART_CTR = 2, BMUT_PART_COV = 4,
 // Mutations. counts: nsym * L u32 and scratch: mut_scratch_words(L) u32, both zeroed by the caller.
 // The filter count decides on the device between the full path (|F| == rows: stored cardinalities),
 // the empty path and the mixed path, so no host round trip sits between filter and mutations.
+// Filters of at most sparse_max rows (0: none) take the row-index pass (part MUT_PART_SPARSE) instead
+// of the container and coverage passes: their rows read their row-index entries.
+enum : uint32_t { MUT_PART_SPARSE = 8 };
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
-                      void* stream, uint32_t parts = MUT_PART_ALL);
+                      void* stream, uint32_t parts = MUT_PART_ALL | MUT_PART_SPARSE, uint64_t sparse_max = 0);
 
 // One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),
 // at most CTR_UNIT_CHUNKS chunks and, unless a single chunk exceeds it, CTR_UNIT_ELEMENTS elements.
@@ -162,12 +167,18 @@ constexpr uint32_t CTR_UNIT_ELEMENTS = 4096;
 // counts[slot][nsym][L] and scratch[slot][mut_scratch_words(L)] zeroed by the caller;
 // d_fcounts[d_slot_query[slot]] is the cardinality of the slot's filter; d_masks holds
 // mutations_batch_mask_bytes(nq, nchunks); d_units lists the column's container units, heaviest first.
+// On the device, once the filters are known, the slots split by their filter's cardinality: empty
+// filters need no pass, filters of at most sparse_max rows (0: none) take the row-index pass (part
+// BMUT_PART_SPARSE), the others the dense passes over the slots listed in d_lists (2 * nq + 2 u32
+// of scratch: the dense and the sparse slot lists and their lengths).
+enum : uint32_t { BMUT_PART_SPARSE = 16 };
 size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks);
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                             const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
                             const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
-                            uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch, void* stream,
-                            uint32_t parts = BMUT_PART_ALL);
+                            uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
+                            uint32_t* d_lists, uint64_t sparse_max, void* stream,
+                            uint32_t parts = BMUT_PART_ALL | BMUT_PART_SPARSE);
 
 // Output rows of the Mutations action (same layout as RhyMutationRow in the C-ABI header).
 struct DevMutationRow {

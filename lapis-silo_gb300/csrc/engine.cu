@@ -127,6 +127,8 @@ void Engine::upload_dates(const DateColumnImage& dc, uint32_t nchunks, DevDateCo
 Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), planner_(device) {
    if (t.seq.size() > MAX_SEQ_COLS || t.dict.size() > MAX_DICT_COLS || t.date.size() > MAX_DATE_COLS)
       throw std::invalid_argument("too many columns for the device image");
+   sparse_rows_plain = t.n_rows / SPARSE_PLAIN_DIV;
+   sparse_rows_batch = t.n_rows / SPARSE_BATCH_DIV;
    cuda_check(cudaSetDevice(device), "cudaSetDevice");
    try {
       cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -172,6 +174,8 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
          d.mend = upload(s.mend);
          d.cstart = upload(s.cstart);
          d.cend = upload(s.cend);
+         d.hrow_off = upload(s.hrow_off);
+         d.hent = upload(s.hent);
          // coverage-pass work items: event ranges of at most EV_PER_CTA, never spanning two blocks
          std::vector<EvItem> items;
          auto split = [&](uint32_t list, uint32_t block, uint32_t b, uint32_t e) {
@@ -268,7 +272,7 @@ void Engine::launch_mutations(int column, const uint32_t* filter, const unsigned
                               uint32_t* scratch, cudaStream_t stream, uint32_t parts) {
    const DevSeqCol& c = view_.seq[column];
    rhygpu::launch_mutations(d_table_, c, static_cast<uint32_t>(column), nchunks(), d_ev_[column], n_ev_[column],
-                            filter, count, counts, scratch, d_err, stream, parts);
+                            filter, count, counts, scratch, d_err, stream, parts, sparse_rows_plain);
    cuda_check(cudaGetLastError(), "mutations kernel launch");
 }
 
@@ -381,7 +385,7 @@ void Engine::batch_free(BatchState& b) {
                    static_cast<void*>(b.d_tiles), static_cast<void*>(b.d_mcounts), static_cast<void*>(b.d_mscratch),
                    static_cast<void*>(b.d_masks), static_cast<void*>(b.d_minprop), static_cast<void*>(b.d_rowblk),
                    static_cast<void*>(b.d_rows), static_cast<void*>(b.d_err), static_cast<void*>(b.d_k),
-                   static_cast<void*>(b.d_ids), static_cast<void*>(b.d_nids)})
+                   static_cast<void*>(b.d_ids), static_cast<void*>(b.d_nids), static_cast<void*>(b.d_lists)})
       if (p) cudaFree(p);
    b = BatchState{};
 }
@@ -396,7 +400,7 @@ size_t Engine::batch_device_bytes(const std::vector<BatchQuery>& qs, uint32_t ti
       bytes += q.prog.code.size() * sizeof(Instr) + sizeof(QueryDesc) + tiles * sizeof(WorkItem) + 8;
       if (q.action == 1 && q.column >= 0 && static_cast<size_t>(q.column) < per_col.size()) {
          const DevSeqCol& dc = view_.seq[q.column];
-         bytes += tile_bytes + static_cast<size_t>(dc.nsym) * dc.L * 4 + mut_scratch_words(dc.L) * 4 + 16 +
+         bytes += tile_bytes + static_cast<size_t>(dc.nsym) * dc.L * 4 + mut_scratch_words(dc.L) * 4 + 16 + 8 +
                   (rows_blocks(dc.L) + 1) * 4 + static_cast<size_t>(dc.L) * 2 * sizeof(DevMutationRow);
          ++per_col[q.column];
       } else if (q.action == 2) {
@@ -449,12 +453,13 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    b.groups.clear();
    b.slot_of_query.assign(n, UINT32_MAX);
    std::vector<uint32_t> slot_query;
-   size_t counts_words = 0, scratch_words = 0, mask_bytes = 0;
+   size_t counts_words = 0, scratch_words = 0, mask_bytes = 0, lists_words = 0;
    uint32_t n_blk = 0;
    for (size_t c = 0; c < by_col.size(); ++c) {
       if (by_col[c].empty()) continue;
       BatchState::ColGroup g{static_cast<int>(c), static_cast<uint32_t>(slot_query.size()),
-                             static_cast<uint32_t>(by_col[c].size()), counts_words, scratch_words, n_blk};
+                             static_cast<uint32_t>(by_col[c].size()), counts_words, scratch_words, lists_words, n_blk};
+      lists_words += 2 * static_cast<size_t>(g.n) + 2;
       n_blk += g.n * rows_blocks(view_.seq[c].L);
       for (uint32_t qi : by_col[c]) {
          b.slot_of_query[qi] = static_cast<uint32_t>(slot_query.size());
@@ -493,6 +498,7 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    grow_device(b.d_mcounts, b.dc_mcounts, counts_words);
    grow_device(b.d_mscratch, b.dc_mscratch, scratch_words);
    grow_device(b.d_masks, b.dc_masks, mask_bytes / 2 + 8);
+   grow_device(b.d_lists, b.dc_lists, lists_words + 2);
    grow_host(b.h_minprop, nslots, b.hc_minprop);
    grow_device(b.d_minprop, b.dc_minprop, nslots);
    grow_host(b.h_rowblk, static_cast<size_t>(n_blk) + 1, b.hc_rowblk);
@@ -616,8 +622,9 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
       launch_mutations_batch(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), nchunks(),
                              b.d_tiles + static_cast<size_t>(g.slot_begin) * words, g.n, b.d_counts,
                              b.d_slot_query + g.slot_begin, d_ev_[g.column], n_ev_[g.column], d_cu_[g.column],
-                             n_cu_[g.column], b.d_masks, b.d_mcounts + g.counts_off, b.d_mscratch + g.scratch_off, s,
-                             (parts >> 1) & BMUT_PART_ALL);
+                             n_cu_[g.column], b.d_masks, b.d_mcounts + g.counts_off, b.d_mscratch + g.scratch_off,
+                             b.d_lists + g.lists_off, sparse_rows_batch, s,
+                             (parts >> 1) & (BMUT_PART_ALL | BMUT_PART_SPARSE));
       cuda_check(cudaGetLastError(), "mutations batch launch");
    }
    if (b.n_details && (parts & 1)) {

@@ -57,6 +57,7 @@ struct BatchState {
       int column;
       uint32_t slot_begin, n;
       size_t counts_off, scratch_off;  // u32 offsets into the arenas
+      size_t lists_off;                // u32 offset of the group's slot lists (2 n + 2)
       uint32_t blk_off;                // first entry of the group's slots in the row-block table
    };
    uint32_t n_queries = 0, n_slots = 0, n_items = 0, n_code = 0, max_depth = 1, tile_bits = 16384, grid = 0;
@@ -83,6 +84,7 @@ struct BatchState {
    uint32_t* d_mcounts = nullptr;
    uint32_t* d_mscratch = nullptr;
    uint16_t* d_masks = nullptr;
+   uint32_t* d_lists = nullptr;       // per column group: dense and sparse slot lists, their lengths
    double* d_minprop = nullptr;
    uint32_t* d_rowblk = nullptr;
    DevMutationRow* d_rows = nullptr;
@@ -103,12 +105,13 @@ struct BatchState {
           hc_rowblk = 0, hc_err = 0, hc_k = 0, hc_ids = 0, hc_nids = 0;
    size_t dc_code = 0, dc_q = 0, dc_items = 0, dc_slot_query = 0, dc_counts = 0, dc_next = 0, dc_tiles = 0,
           dc_mcounts = 0, dc_mscratch = 0, dc_masks = 0, dc_minprop = 0, dc_rowblk = 0, dc_rows = 0, dc_err = 0, dc_k = 0,
-          dc_ids = 0, dc_nids = 0;
+          dc_ids = 0, dc_nids = 0, dc_lists = 0;
    cudaGraphExec_t graph = nullptr;
 };
 
 class Engine {
   public:
+   static constexpr uint32_t BATCH_ALL = 63;  // batch_enqueue parts: the whole batch
    Engine(const TableImage& table, int device);
    ~Engine();
    Engine(const Engine&) = delete;
@@ -128,6 +131,11 @@ class Engine {
    // latency over wider tiles. rhy_set_tile_bits sets both.
    uint32_t tile_bits = 16384;
    uint32_t batch_tile_bits = 65536;
+   // Mutations filters of at most this many rows take the row-index pass instead of the dense
+   // passes: single queries, and slots of a batch (0: never). Defaults: rows / SPARSE_PLAIN_DIV and
+   // rows / SPARSE_BATCH_DIV.
+   static constexpr uint32_t SPARSE_PLAIN_DIV = 32, SPARSE_BATCH_DIV = 64;
+   uint64_t sparse_rows_plain = 0, sparse_rows_batch = 0;
    BatchSchedule batch_schedule;  // used by batch_prepare unless a tile width is requested
    // Autotuner: prepares the batch under every candidate schedule (tile widths 16, 32 and 64 Kbit,
    // stack budgets 24, 40 and 64 KiB, all or two CTAs per SM, both item orders), times its filter
@@ -163,11 +171,13 @@ class Engine {
    // Stream-ordered: optional H2D of the staged programs, the persistent filter kernel, the batched
    // mutations kernels per column, optional D2H of the results into the pinned host buffers.
    // parts: bit 0 = zeroing + filter kernel, bits 1..4 = transpose, container, coverage and final
-   // mutations kernels (all set = the whole batch); used to time kernels one by one.
-   void batch_enqueue(cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31) {
+   // mutations kernels, bit 5 = the row-index pass of the slots whose filters have few rows (all set
+   // = the whole batch; without bit 5 the dense passes count every slot); used to time kernels one
+   // by one.
+   void batch_enqueue(cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = BATCH_ALL) {
       batch_enqueue(batch_, stream, copy_in, copy_out, parts);
    }
-   void batch_enqueue(BatchState& b, cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = 31);
+   void batch_enqueue(BatchState& b, cudaStream_t stream, bool copy_in, bool copy_out, uint32_t parts = BATCH_ALL);
    // Row pass of a batch in two stream-ordered phases around one host step: phase 1 enqueues the
    // batch, the D2H of the counts / Details ids and the count + scan of the rows; once the stream
    // has passed it, phase 2 sizes the rows, enqueues their write and copies them to `rows`.

@@ -9,6 +9,9 @@
 //                    (reference: mutations_node.cpp:51-136).
 //  mut_final_kernel  prefix sums and the local-reference count per position
 //                    (reference: mutations_node.cpp:192-203).
+//  mut_sparse_kernel filters of few rows: each row of F adds its row-index entries, the same counts
+//                    the two passes above add for it (the reference's mixed path walks the filtered
+//                    rows for coverage the same way, mutations_node.cpp:111-136).
 // The filter count decides on the device between the full path (|F| == rows: stored
 // cardinalities, reference: mutations_node.cpp:240-266), the empty path and the mixed path.
 #include <cuda_runtime.h>
@@ -71,13 +74,13 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, 
 __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                         const uint32_t* __restrict__ filter,
                                                         const unsigned long long* __restrict__ fcount,
-                                                        uint32_t* counts, int* err) {
+                                                        unsigned long long sparse_max, uint32_t* counts, int* err) {
    extern __shared__ __align__(128) uint4 sm4[];  // two buffers (payload + descriptors), then the filter tile
    __shared__ __align__(8) uint64_t bar[2];
    __shared__ uint32_t wsum[NW], msk[MT], exq[MT];
    __shared__ StreamUnit su[STAGED_UNITS];  // this CTA's units, staged once
    const unsigned long long fc = *fcount;
-   if (fc == 0) return;
+   if (fc == 0 || fc <= sparse_max) return;  // empty, or counted by the row-index pass
    const bool full = fc == tab->n_rows;
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t n_units = cs->nsu;
@@ -234,10 +237,11 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
 __global__ void __launch_bounds__(MT) mut_cov_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                      const EvItem* __restrict__ items,
                                                      const uint32_t* __restrict__ filter,
-                                                     const unsigned long long* __restrict__ fcount, uint32_t* scratch) {
+                                                     const unsigned long long* __restrict__ fcount,
+                                                     unsigned long long sparse_max, uint32_t* scratch) {
    __shared__ int cnt[NBLOCK + 1];
    const unsigned long long fc = *fcount;
-   if (fc == 0) return;
+   if (fc == 0 || fc <= sparse_max) return;  // empty, or counted by the row-index pass
    const bool full = fc == tab->n_rows;
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t L = cs->L, nseg = mut_nseg(L);
@@ -304,6 +308,22 @@ __global__ void __launch_bounds__(MT) mut_cov_kernel(const DevTable* __restrict_
    }
 }
 
+// Filters of 1..sparse_max rows: one warp per 32 filter words at a time.
+__global__ void __launch_bounds__(MT) mut_sparse_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                        const uint32_t* __restrict__ filter,
+                                                        const unsigned long long* __restrict__ fcount,
+                                                        unsigned long long sparse_max, uint32_t* counts,
+                                                        uint32_t* scratch) {
+   __shared__ uint32_t list[NW][1024];
+   const unsigned long long fc = *fcount;
+   if (fc == 0 || fc > sparse_max) return;
+   const DevSeqCol* cs = &tab->seq[col];
+   const uint32_t words = tab->nchunks * CHUNK_WORDS;
+   const uint32_t warp = threadIdx.x >> 5, nwarps = gridDim.x * NW;
+   for (uint32_t w = (blockIdx.x * NW + warp) * 32; w < words; w += nwarps * 32)
+      row_index_pass32(cs, filter, w, words, counts, scratch, list[warp]);
+}
+
 __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                             const unsigned long long* __restrict__ fcount,
                                                             uint32_t* counts, const uint32_t* __restrict__ scratch) {
@@ -317,8 +337,14 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __re
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
-                      void* stream, uint32_t parts) {
+                      void* stream, uint32_t parts, uint64_t sparse_max) {
    cudaStream_t s = static_cast<cudaStream_t>(stream);
+   if (!(parts & MUT_PART_SPARSE)) sparse_max = 0;  // the dense passes count every filter
+   if (sparse_max) {
+      const uint32_t groups = nchunks * CHUNK_WORDS / 32;  // 32-word groups, one per warp and step
+      mut_sparse_kernel<<<std::max(1u, std::min(groups / NW, 2048u)), MT, 0, s>>>(
+         d_table, col, d_filter, d_filter_count, static_cast<unsigned long long>(sparse_max), d_counts, d_scratch);
+   }
    if ((parts & MUT_PART_CTR) && col_host.nsu > 0) {
       const size_t smem = 2 * BUF4 * 16 + CHUNK_WORDS * 4;
       // resident CTAs per device, computed once per device
@@ -336,10 +362,12 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
          if (dev >= 0 && dev < 64) resident[dev].store(res, std::memory_order_relaxed);
       }
       const uint32_t grid = std::min<uint32_t>(col_host.nsu, res);
-      mut_stream_kernel<<<grid, MT, smem, s>>>(d_table, col, d_filter, d_filter_count, d_counts, d_err);
+      mut_stream_kernel<<<grid, MT, smem, s>>>(d_table, col, d_filter, d_filter_count,
+                                               static_cast<unsigned long long>(sparse_max), d_counts, d_err);
    }
    if ((parts & MUT_PART_COV) && n_ev > 0)
-      mut_cov_kernel<<<n_ev, MT, 0, s>>>(d_table, col, d_ev, d_filter, d_filter_count, d_scratch);
+      mut_cov_kernel<<<n_ev, MT, 0, s>>>(d_table, col, d_ev, d_filter, d_filter_count,
+                                         static_cast<unsigned long long>(sparse_max), d_scratch);
    if (parts & MUT_PART_FINAL)
       mut_final_kernel<<<(col_host.L + MUT_SEG - 1) / MUT_SEG, MUT_SEG, 0, s>>>(d_table, col, d_filter_count, d_counts,
                                                                                d_scratch);

@@ -132,4 +132,94 @@ __device__ __forceinline__ void final_position_counts(const DevSeqCol* cs, uint3
    counts[static_cast<size_t>(cs->local_ref[p]) * L + p] += ref;
 }
 
+// Row-index pass over 32 words [w, w + 32) of a dense filter F (words in all): every row of F there
+// adds its row-index entries, which are exactly what the container and coverage passes add for
+// that row: symbol entries to counts[symbol][position]; coverage starts and ends to their
+// histograms, missing-interval starts (+1) and ends (-1, modulo 2^32) to the difference array, each
+// also to its segment total. The warp gathers the rows into `list` (1,024 entries), then takes them
+// 32 at a time: one lane loads one row's entry range, and the rows' entries, numbered across the
+// warp, are read four per lane at a time (each lane finds the row of an entry by a binary search
+// over the lanes' first entry numbers). Called by a whole warp.
+__device__ __forceinline__ void row_index_pass32(const DevSeqCol* __restrict__ cs, const uint32_t* __restrict__ F,
+                                                 uint32_t w, uint32_t words, uint32_t* counts, uint32_t* scratch,
+                                                 uint32_t* list) {
+   const uint32_t lane = threadIdx.x & 31;
+   const uint32_t L = cs->L, nseg = mut_nseg(L);
+   uint32_t x = w + lane < words ? __ldg(F + w + lane) : 0u;
+   const uint32_t c = __popc(x);
+   uint32_t incl = c;
+#pragma unroll
+   for (uint32_t o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += y;
+   }
+   const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+   if (total == 0) return;
+   uint32_t at = incl - c;
+   while (x) {
+      list[at++] = 32 * (w + lane) + (__ffs(x) - 1);
+      x &= x - 1;
+   }
+   __syncwarp();
+   uint32_t* start_hist = scratch;
+   uint32_t* end_hist = scratch + (L + 1);
+   uint32_t* ndiff = scratch + 2 * (L + 1);
+   uint32_t* seg_s = scratch + 3 * (L + 1);
+   uint32_t* seg_e = seg_s + nseg;
+   uint32_t* seg_n = seg_e + nseg;
+   for (uint32_t r0 = 0; r0 < total; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      uint32_t b = 0, n = 0;
+      if (j < total) {
+         const uint32_t r = list[j];
+         b = __ldg(cs->hrow_off + r);
+         n = __ldg(cs->hrow_off + r + 1) - b;
+      }
+      uint32_t first = n;  // exclusive prefix of the entry counts after the scan
+#pragma unroll
+      for (uint32_t o = 1; o < 32; o <<= 1) {
+         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, first, o);
+         if (lane >= o) first += y;
+      }
+      const uint32_t E = __shfl_sync(0xFFFFFFFFu, first, 31);
+      first -= n;
+      constexpr uint32_t U = 4;
+      for (uint32_t k0 = 0; k0 < E; k0 += 32 * U) {
+         uint32_t ent[U];
+#pragma unroll
+         for (uint32_t u = 0; u < U; ++u) {
+            const uint32_t k = k0 + 32 * u + lane;
+            // the last lane whose first entry number is <= k holds entry k
+            uint32_t lo = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+               const uint32_t f = __shfl_sync(0xFFFFFFFFu, first, lo + step);
+               if (f <= k) lo += step;
+            }
+            const uint32_t bl = __shfl_sync(0xFFFFFFFFu, b, lo), fl = __shfl_sync(0xFFFFFFFFu, first, lo);
+            ent[u] = k < E ? __ldg(cs->hent + bl + (k - fl)) : 0xFFFFFFFFu;
+         }
+#pragma unroll
+         for (uint32_t u = 0; u < U; ++u) {
+            if (ent[u] == 0xFFFFFFFFu) continue;
+            const uint32_t code = ent[u] & 31u, pos = ent[u] >> 5;
+            if (code < ROW_COV_START) {
+               atomicAdd(counts + static_cast<size_t>(code) * L + pos, 1u);
+            } else if (code == ROW_COV_START) {
+               atomicAdd(start_hist + pos, 1u);
+               atomicAdd(seg_s + pos / MUT_SEG, 1u);
+            } else if (code == ROW_COV_END) {
+               atomicAdd(end_hist + pos, 1u);
+               atomicAdd(seg_e + pos / MUT_SEG, 1u);
+            } else {
+               const uint32_t d = code == ROW_MISS_START ? 1u : 0xFFFFFFFFu;
+               atomicAdd(ndiff + pos, d);
+               atomicAdd(seg_n + pos / MUT_SEG, d);
+            }
+         }
+      }
+   }
+   __syncwarp();
+}
+
 }  // namespace rhygpu

@@ -305,6 +305,66 @@ void build_mutation_events(SeqColumnImage& col, const std::vector<ChunkRows>& ch
    std::sort(col.cend.begin(), col.cend.end(), by_pos);
 }
 
+// The row index (see SeqColumnImage::hrow_off): every entry the dense passes would count for a row,
+// from the same containers, coverage exceptions and missing intervals.
+void build_row_index(SeqColumnImage& col, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
+   const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
+   const ContainerSet& V = col.vertical;
+   const uint32_t nkeys = V.nkeys, L = col.L;
+   if (alphabet(col.kind).count > ROW_COV_START) throw std::logic_error("row index: too many symbols");
+   auto for_chunk = [&](uint32_t v, auto&& emit) {  // emit(row within chunk, entry)
+      for (uint32_t i = V.off[static_cast<size_t>(v) * nkeys]; i < V.off[static_cast<size_t>(v + 1) * nkeys]; ++i) {
+         const CtrDesc& d = V.ctrs[i];
+         const uint32_t e = d.key << 5 | d.sym;
+         const uint16_t* p = V.payload.data() + d.payload;
+         if (d.type == CT_ARRAY) {
+            for (uint32_t k = 0; k <= d.card_m1; ++k) emit(p[k], e);
+         } else if (d.type == CT_BITSET) {
+            for (uint32_t w = 0; w < CHUNK_WORDS; ++w) {
+               uint32_t x = static_cast<uint32_t>(p[2 * w]) | static_cast<uint32_t>(p[2 * w + 1]) << 16;
+               while (x) {
+                  emit(32 * w + static_cast<uint32_t>(__builtin_ctz(x)), e);
+                  x &= x - 1;
+               }
+            }
+         } else {
+            for (uint32_t k = 0; k < d.nruns; ++k)
+               for (uint32_t r = p[2 * k]; r <= static_cast<uint32_t>(p[2 * k]) + p[2 * k + 1]; ++r) emit(r, e);
+         }
+      }
+      for (uint32_t i = col.cov_exc_off[v]; i < col.cov_exc_off[v + 1]; ++i) {
+         const CovExc& x = col.cov_exc[i];
+         if (x.start > 0) emit(x.row, x.start << 5 | ROW_COV_START);
+         if (x.end < L) emit(x.row, x.end << 5 | ROW_COV_END);
+      }
+      for (uint32_t r = 0; r < chunk_sizes[v]; ++r) {
+         const size_t g = static_cast<size_t>(v) * CHUNK_ROWS + r;
+         for (uint32_t q = col.nrow_off[g]; q < col.nrow_off[g + 1]; ++q) {
+            emit(r, col.nrow_start[q] << 5 | ROW_MISS_START);
+            emit(r, col.nrow_end[q] << 5 | ROW_MISS_END);
+         }
+      }
+   };
+   std::vector<uint32_t>& off = col.hrow_off;
+   off.assign(static_cast<size_t>(nchunks) * CHUNK_ROWS + 1, 0);
+   parallel_for(nchunks, threads, [&](uint32_t v) {
+      uint32_t* o = off.data() + static_cast<size_t>(v) * CHUNK_ROWS + 1;
+      for_chunk(v, [&](uint32_t r, uint32_t) { ++o[r]; });
+   });
+   uint64_t total = 0;
+   for (size_t i = 1; i < off.size(); ++i) {
+      total += off[i];
+      if (total > 0xFFFFFFFFull) throw std::invalid_argument("row index: more than 2^32 entries in one column");
+      off[i] = static_cast<uint32_t>(total);
+   }
+   col.hent.resize(total);
+   parallel_for(nchunks, threads, [&](uint32_t v) {
+      std::vector<uint32_t> at(off.begin() + static_cast<size_t>(v) * CHUNK_ROWS,
+                               off.begin() + static_cast<size_t>(v + 1) * CHUNK_ROWS);
+      for_chunk(v, [&](uint32_t r, uint32_t e) { col.hent[at[r]++] = e; });
+   });
+}
+
 SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
    SeqColumnImage col;
    col.name = raw.name;
@@ -495,6 +555,7 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
       toff(&col.nblk_toff[bv * TOFF_N], col.nblk_off[bv], col.nblk_off[bv + 1],
            [&](uint32_t i) { return col.nblk[i].row & 0xFFFFu; });
    build_mutation_events(col, chunks, chunk_sizes);
+   build_row_index(col, chunk_sizes, threads);
    return col;
 }
 

@@ -118,8 +118,16 @@ struct SeqColumnImage {
    // Coverage boundaries of rows whose covered region is not the whole genome, sorted by
    // position: starts above 0 and ends below L (a row without coverage has end 0).
    std::vector<CovEvent> cstart, cend;
+   // Row index of the same counts, for filters of few rows: per row (global id, chunk stride) one
+   // entry (position << 5 | code) per container holding the row (code = its symbol), per coverage
+   // boundary above (ROW_COV_START, ROW_COV_END) and per missing interval (ROW_MISS_START at its
+   // first position, ROW_MISS_END after its last). Rows of F read their entries instead of every
+   // container being tested against F.
+   std::vector<uint32_t> hrow_off;     // nchunks * CHUNK_ROWS + 1
+   std::vector<uint32_t> hent;
    uint32_t flipped_positions = 0;
 };
+constexpr uint32_t ROW_COV_START = 28, ROW_COV_END = 29, ROW_MISS_START = 30, ROW_MISS_END = 31;
 
 struct DictColumnImage {
    std::string name;

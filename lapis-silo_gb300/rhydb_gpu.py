@@ -177,6 +177,7 @@ def lib():
         "rhy_batch_rows": (I, [P, P, P, P, P, U32, U32, P, P, P, C.c_size_t, P, P, C.POINTER(C.c_size_t)]),
         "rhy_batch_rows_fetch": (I, [P, P, P, C.c_size_t]),
         "rhy_batch_times": (I, [P, C.POINTER(BatchTimes)]),
+        "rhy_sparse_rows": (I, [P, P, P]),
         "rhy_batch_schedule": (I, [P, C.POINTER(BatchSchedule), C.POINTER(BatchSchedule)]),
         "rhy_batch_autotune": (I, [P, P, P, P, U32, U32, P, C.POINTER(BatchSchedule), P, C.c_size_t,
                                    C.POINTER(C.c_size_t)]),
@@ -492,6 +493,16 @@ class Device:
                     ptrs[i] = outs[i].ctypes.data
         _check(lib().rhy_batch_results(self._h, _ptr(counts), C.cast(ptrs, C.c_void_p)))
         return counts[:n], outs
+
+    def sparse_rows(self, plain=None, batch=None) -> tuple:
+        """Row limits of the row-index Mutations path (single queries, batch slots); arguments set
+        them first (0 turns the path off)."""
+        cur = np.zeros(2, np.uint64)
+        _check(lib().rhy_sparse_rows(self._h, None, _ptr(cur)))
+        if plain is not None or batch is not None:
+            new = np.array([cur[0] if plain is None else plain, cur[1] if batch is None else batch], np.uint64)
+            _check(lib().rhy_sparse_rows(self._h, _ptr(new), _ptr(cur)))
+        return int(cur[0]), int(cur[1])
 
     def batch_schedule(self, **set_fields) -> dict:
         """The schedule of the batched filter launches; keyword arguments set fields first."""

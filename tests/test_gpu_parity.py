@@ -168,6 +168,34 @@ def test_autotuned_schedule_keeps_results(config2_small):
     dev.batch_schedule(**default)
 
 
+@pytest.mark.parametrize("limit", ["dense", "sparse", "default"])
+def test_row_index_and_dense_passes_agree(config2_small, limit):
+    """Mutations counts from the row index (every filtered row adds its entries), from the dense
+    passes over every container, and from the default split by filter size are the oracle's, for
+    single queries and batch slots over every column (empty and full filters included)."""
+    t, orc, dev, qs = config2_small
+    default = dev.sparse_rows()
+    lim = {"dense": (0, 0), "sparse": (t.n_rows, t.n_rows), "default": default}[limit]
+    dev.sparse_rows(*lim)
+    try:
+        extra = ["True", "False", "SymEq(main,1,N)", "Not(HasMut(main,5))"]
+        sample = qs[:40] + extra
+        rng = np.random.default_rng(9)
+        col = rng.integers(0, t.n_seq, len(sample)).astype(np.uint32)
+        for q, c in zip(sample, col):
+            m, n = dev.mutations(q, int(c))
+            om, on = orc.mutations(q, int(c))
+            assert n == on and np.array_equal(m, om), (limit, q, c)
+        act = np.ones(len(sample), np.int32)
+        counts, muts = dev.batch(sample, act, col)
+        for i, q in enumerate(sample):
+            om, on = orc.mutations(q, int(col[i]))
+            assert counts[i] == on and np.array_equal(muts[i], om), (limit, q, col[i])
+    finally:
+        dev.sparse_rows(*default)
+    assert default == (t.n_rows // 32, t.n_rows // 64)
+
+
 def test_tile_widths(config2_small):
     t, orc, dev, qs = config2_small
     for tb in (4096, 8192, 32768, 65536):
