@@ -155,6 +155,21 @@ int rhy_count(RhyDevice* d, const char* expr, void* stream, uint64_t* out);
 int rhy_eval(RhyDevice* d, const char* expr, void* stream, uint32_t* out_bits, uint64_t* out_count);
 /* counts: n_symbols * L words, counts[symbol * L + position]; filter_count may be NULL. */
 int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream, uint32_t* counts, uint64_t* filter_count);
+/* Grouped counts of the filter's rows (replaces BitmapAggregationNode, reference
+ * bitmap_aggregation_node.cpp:51-140): one dimension per sequence position (kind 0: column,
+ * 1-based position; groups = the column's symbols in alphabet order, then null rows) or dictionary
+ * column (kind 1: groups = its values in string order, then null rows). Row i of the output is one
+ * nonzero combination, in the reference's depth-first order: groups[i * n_dims + d] is its group in
+ * dimension d (a symbol index, a value id, or -1 for the null group), counts[i] its rows. *n_out
+ * receives the number of combinations; the first min(cap, *n_out) are copied. At most 8
+ * dimensions and 2^26 group combinations. */
+typedef struct {
+   int kind;
+   uint32_t column;
+   uint32_t position;
+} RhyAggDimension;
+int rhy_aggregate(RhyDevice* d, const char* expr, const RhyAggDimension* dims, uint32_t n_dims, void* stream,
+                  int32_t* groups, uint64_t* counts, size_t cap, size_t* n_out, uint64_t* filter_count);
 /* Mutations filters of 1..set[0] rows (single queries) or 1..set[1] rows (slots of a batch) are
  * counted from the row index (each filtered row adds its entries) instead of by the passes over
  * every container; 0 turns that path off. Results are the same either way. `set` and `get` point

@@ -1,5 +1,6 @@
 // extern "C" boundary (include/rhydb_gpu.h). No exception crosses it: every entry point maps
 // exceptions to a status code and a thread-local message.
+#include <algorithm>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -407,6 +408,29 @@ int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream,
       if (column >= d->table->image.seq.size()) throw std::invalid_argument("no such sequence column");
       const rhygpu::Program p = d->engine->plan(expr);
       d->engine->mutations(p, static_cast<int>(column), counts, filter_count, static_cast<cudaStream_t>(stream));
+   });
+}
+
+int rhy_aggregate(RhyDevice* d, const char* expr, const RhyAggDimension* dims, uint32_t n_dims, void* stream,
+                  int32_t* groups, uint64_t* counts, size_t cap, size_t* n_out, uint64_t* filter_count) {
+   return guarded([&] {
+      need(d, "device");
+      need(expr, "expr");
+      need(n_out, "n_out");
+      if (n_dims) need(dims, "dims");
+      std::vector<rhygpu::Engine::AggSpec> spec(n_dims);
+      for (uint32_t i = 0; i < n_dims; ++i) {
+         if (dims[i].kind == 0 && dims[i].position == 0) throw rhygpu::IllegalQuery("positions are 1-based");
+         spec[i] = {static_cast<uint32_t>(dims[i].kind), dims[i].column, dims[i].kind == 0 ? dims[i].position - 1 : 0u};
+      }
+      const rhygpu::Program p = d->engine->plan(expr);
+      std::vector<int32_t> g;
+      std::vector<uint64_t> c;
+      d->engine->aggregate(p, spec, g, c, filter_count, static_cast<cudaStream_t>(stream));
+      *n_out = c.size();
+      const size_t m = std::min(cap, c.size());
+      if (groups && m) std::copy(g.begin(), g.begin() + m * n_dims, groups);
+      if (counts && m) std::copy(c.begin(), c.begin() + m, counts);
    });
 }
 

@@ -200,6 +200,29 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
          d.payload = upload(s.inverted.payload, 8);
          d.off = upload(s.inverted.off);
          d.nkeys = s.inverted.nkeys;
+         // for aggregation: every row's value id (from the inverted index) and the string order
+         std::vector<uint32_t> ids(static_cast<size_t>(nchunks) * CHUNK_ROWS, 0xFFFFFFFFu);
+         for (const CtrDesc& x : s.inverted.ctrs) {
+            const uint16_t* pl = s.inverted.payload.data() + x.payload;
+            const size_t base = static_cast<size_t>(x.v) * CHUNK_ROWS;
+            if (x.type == CT_ARRAY) {
+               for (uint32_t k = 0; k <= x.card_m1; ++k) ids[base + pl[k]] = x.key;
+            } else if (x.type == CT_BITSET) {
+               for (uint32_t r = 0; r < CHUNK_ROWS; ++r)
+                  if ((pl[r >> 4] >> (r & 15)) & 1u) ids[base + r] = x.key;
+            } else {
+               for (uint32_t k = 0; k < x.nruns; ++k)
+                  for (uint32_t r = pl[2 * k]; r <= static_cast<uint32_t>(pl[2 * k]) + pl[2 * k + 1]; ++r) ids[base + r] = x.key;
+            }
+         }
+         std::vector<uint32_t> by_rank(s.values.size());
+         std::iota(by_rank.begin(), by_rank.end(), 0u);
+         std::sort(by_rank.begin(), by_rank.end(), [&](uint32_t a, uint32_t b) { return s.values[a] < s.values[b]; });
+         std::vector<uint32_t> rank(std::max<size_t>(1, s.values.size()));
+         for (uint32_t r = 0; r < by_rank.size(); ++r) rank[by_rank[r]] = r;
+         d_dict_ids_.push_back(upload(ids));
+         d_dict_rank_.push_back(upload(rank));
+         dict_by_rank_.push_back(std::move(by_rank));
       }
       for (size_t c = 0; c < t.date.size(); ++c) upload_dates(t.date[c], nchunks, view_.date[c]);
       d_table_ = static_cast<DevTable*>(alloc(sizeof(DevTable)));
@@ -234,6 +257,9 @@ Engine::~Engine() {
    cudaDeviceSynchronize();
    batch_free(batch_);
    for (auto& b : parts_) batch_free(*b);
+   for (void* p : {static_cast<void*>(d_agg_dims_), static_cast<void*>(d_agg_counters_), static_cast<void*>(d_agg_blocks_),
+                   static_cast<void*>(d_agg_out_)})
+      if (p) cudaFree(p);
    for (void* p : allocs_) cudaFree(p);
    if (h_code_) cudaFreeHost(h_code_);
    if (h_count_) cudaFreeHost(h_count_);
@@ -1114,6 +1140,91 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    });
    batch_times.lower_ms += since(t0);
    return qs;
+}
+
+void Engine::aggregate(const Program& p, const std::vector<AggSpec>& spec, std::vector<int32_t>& groups,
+                       std::vector<uint64_t>& counts, uint64_t* filter_count, cudaStream_t stream) {
+   if (spec.empty() || spec.size() > 8) throw std::invalid_argument("aggregation needs 1 to 8 dimensions");
+   std::vector<AggDim> dims(spec.size());
+   for (size_t d = 0; d < spec.size(); ++d) {
+      const AggSpec& x = spec[d];
+      AggDim& a = dims[d];
+      a.kind = x.kind;
+      a.col = x.col;
+      a.pos = x.pos;
+      if (x.kind == AGG_SEQUENCE) {
+         if (x.col >= table_.seq.size()) throw IllegalQuery("no such sequence column");
+         if (x.pos >= table_.seq[x.col].L) throw IllegalQuery("position out of range for the sequence column");
+         a.ngroups = view_.seq[x.col].nsym + 1;
+         a.ids = a.rank = nullptr;
+      } else if (x.kind == AGG_DICTIONARY) {
+         if (x.col >= table_.dict.size()) throw IllegalQuery("no such dictionary column");
+         a.ngroups = static_cast<uint32_t>(table_.dict[x.col].values.size()) + 1;
+         a.ids = d_dict_ids_[x.col];
+         a.rank = d_dict_rank_[x.col];
+      } else {
+         throw std::invalid_argument("dimension kind must be 0 (sequence position) or 1 (dictionary column)");
+      }
+   }
+   uint64_t keys = 1;  // dimension 0 most significant: key order = the reference's depth-first order
+   for (size_t d = dims.size(); d-- > 0;) {
+      dims[d].stride = keys;
+      keys *= dims[d].ngroups;
+      if (keys > AGG_MAX_KEYS) throw std::invalid_argument("aggregation: more than 2^26 group combinations");
+   }
+   std::lock_guard<std::mutex> lock(mu);
+   cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+   if (!stream) stream = stream_;
+   const uint64_t nblocks = (keys + AGG_BLOCK - 1) / AGG_BLOCK;
+   grow_device(d_agg_dims_, agg_dims_cap_, 8);
+   grow_device(d_agg_counters_, agg_counters_cap_, keys);
+   grow_device(d_agg_blocks_, agg_blocks_cap_, nblocks);
+   cuda_check(cudaMemcpyAsync(d_agg_dims_, dims.data(), dims.size() * sizeof(AggDim), cudaMemcpyHostToDevice, stream),
+              "H2D");
+   upload_program(p, d_code, stream);
+   cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream), "memset");
+   cuda_check(cudaMemsetAsync(d_agg_counters_, 0, keys * sizeof(uint32_t), stream), "memset");
+   launch_count(d_code, p, d_count, d_filter, stream);
+   launch_agg_keys(d_table_, nchunks(), d_filter, d_agg_dims_, static_cast<uint32_t>(dims.size()), d_agg_counters_,
+                   stream);
+   launch_agg_nonzero(d_agg_counters_, keys, d_agg_blocks_, stream);
+   cuda_check(cudaGetLastError(), "aggregation launch");
+   std::vector<uint32_t> block(nblocks);
+   cuda_check(cudaMemcpyAsync(block.data(), d_agg_blocks_, nblocks * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
+              "D2H");
+   cuda_check(cudaMemcpyAsync(h_count_, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "D2H");
+   cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream), "D2H");
+   cuda_check(cudaStreamSynchronize(stream), "aggregation");
+   check_error_flag();
+   uint64_t total = 0;
+   for (uint64_t b = 0; b < nblocks; ++b) {
+      const uint32_t n = block[b];
+      block[b] = static_cast<uint32_t>(total);
+      total += n;
+   }
+   std::vector<AggCount> out(total);
+   if (total) {
+      grow_device(d_agg_out_, agg_out_cap_, total);
+      cuda_check(cudaMemcpyAsync(d_agg_blocks_, block.data(), nblocks * sizeof(uint32_t), cudaMemcpyHostToDevice, stream),
+                 "H2D");
+      launch_agg_write(d_agg_counters_, keys, d_agg_blocks_, d_agg_out_, stream);
+      cuda_check(cudaGetLastError(), "aggregation launch");
+      cuda_check(cudaMemcpyAsync(out.data(), d_agg_out_, total * sizeof(AggCount), cudaMemcpyDeviceToHost, stream), "D2H");
+      cuda_check(cudaStreamSynchronize(stream), "aggregation");
+   }
+   groups.resize(total * dims.size());
+   counts.resize(total);
+   for (uint64_t i = 0; i < total; ++i) {
+      counts[i] = out[i].count;
+      for (size_t d = 0; d < dims.size(); ++d) {
+         const uint32_t g = static_cast<uint32_t>((out[i].key / dims[d].stride) % dims[d].ngroups);
+         int32_t v = -1;  // the null group is the last one
+         if (g + 1 < dims[d].ngroups) v = dims[d].kind == AGG_SEQUENCE ? static_cast<int32_t>(g)
+                                                                       : static_cast<int32_t>(dict_by_rank_[dims[d].col][g]);
+         groups[i * dims.size() + d] = v;
+      }
+   }
+   if (filter_count) *filter_count = *h_count_;
 }
 
 }  // namespace rhygpu

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "aggregate.h"
 #include "device.h"
 #include "expr.h"
 #include "planner.h"
@@ -151,6 +152,14 @@ class Engine {
    void eval(const Program& p, uint32_t* host_bits /* nchunks * 2048 */, uint64_t* host_count, cudaStream_t stream);
    void mutations(const Program& p, int column, uint32_t* host_counts /* nsym * L */, uint64_t* filter_count,
                   cudaStream_t stream);
+   // Grouped counts of the filter's rows (BitmapAggregation): one dimension per sequence position
+   // (kind AGG_SEQUENCE, 0-based position) or dictionary column (AGG_DICTIONARY). Output rows in the
+   // reference's order, groups[i * dims + d] = symbol index / value id / -1 for the null group.
+   struct AggSpec {
+      uint32_t kind, col, pos;
+   };
+   void aggregate(const Program& p, const std::vector<AggSpec>& dims, std::vector<int32_t>& groups,
+                  std::vector<uint64_t>& counts, uint64_t* filter_count, cudaStream_t stream);
 
    // Device-side building blocks (no host synchronisation); used by the timed benchmark legs.
    void upload_program(const Program& p, Instr* d_code, cudaStream_t stream);
@@ -284,6 +293,14 @@ class Engine {
    std::unique_ptr<FeatureContext> fctx_;  // built on first use
    const FeatureContext& fctx();
    WorkerPool plan_pool_;  // planning threads, one per hardware thread
+   // aggregation: per dictionary column the value id of every row and the values' string order
+   std::vector<const uint32_t*> d_dict_ids_, d_dict_rank_;
+   std::vector<std::vector<uint32_t>> dict_by_rank_;
+   AggDim* d_agg_dims_ = nullptr;
+   uint32_t* d_agg_counters_ = nullptr;
+   uint32_t* d_agg_blocks_ = nullptr;
+   AggCount* d_agg_out_ = nullptr;
+   size_t agg_dims_cap_ = 0, agg_counters_cap_ = 0, agg_blocks_cap_ = 0, agg_out_cap_ = 0;
    // Runs the expressions through the single-query path in trace mode; one sample per node.
    size_t collect_traces(const std::vector<std::string>& exprs, std::vector<PlannerSample>& out);
 

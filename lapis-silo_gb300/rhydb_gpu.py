@@ -69,6 +69,10 @@ class BatchTimes(C.Structure):
                 ("lower_ms", C.c_double)]
 
 
+class AggDimension(C.Structure):
+    _fields_ = [("kind", C.c_int), ("column", C.c_uint32), ("position", C.c_uint32)]
+
+
 class BatchSchedule(C.Structure):
     _fields_ = [("max_tile_bits", C.c_uint32), ("stack_kb", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("query_major", C.c_uint32)]
@@ -178,6 +182,7 @@ def lib():
         "rhy_batch_rows_fetch": (I, [P, P, P, C.c_size_t]),
         "rhy_batch_times": (I, [P, C.POINTER(BatchTimes)]),
         "rhy_sparse_rows": (I, [P, P, P]),
+        "rhy_aggregate": (I, [P, C.c_char_p, P, U32, P, P, P, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(U64)]),
         "rhy_batch_schedule": (I, [P, C.POINTER(BatchSchedule), C.POINTER(BatchSchedule)]),
         "rhy_batch_autotune": (I, [P, P, P, P, U32, U32, P, C.POINTER(BatchSchedule), P, C.c_size_t,
                                    C.POINTER(C.c_size_t)]),
@@ -493,6 +498,43 @@ class Device:
                     ptrs[i] = outs[i].ctypes.data
         _check(lib().rhy_batch_results(self._h, _ptr(counts), C.cast(ptrs, C.c_void_p)))
         return counts[:n], outs
+
+    def aggregate(self, expr: str, dims, stream=None):
+        """Grouped counts of the filter's rows (BitmapAggregation). dims: ("seq", column, 1-based
+        position) or ("dict", column) per dimension. Returns ([(group label per dimension, count)],
+        filter count) in the reference's order; labels are symbol characters or dictionary values,
+        None for the null group."""
+        nd = len(dims)
+        arr = (AggDimension * max(nd, 1))()
+        for i, d in enumerate(dims):
+            if d[0] == "seq":
+                arr[i] = AggDimension(0, int(d[1]), int(d[2]))
+            elif d[0] == "dict":
+                arr[i] = AggDimension(1, int(d[1]), 0)
+            else:
+                raise ValueError(f"unknown dimension kind {d[0]!r}")
+        n = C.c_size_t()
+        fc = C.c_uint64()
+        _check(lib().rhy_aggregate(self._h, expr.encode(), arr, nd, stream, None, None, 0, C.byref(n), C.byref(fc)))
+        m = n.value
+        groups = np.zeros(max(m * nd, 1), np.int32)
+        counts = np.zeros(max(m, 1), np.uint64)
+        _check(lib().rhy_aggregate(self._h, expr.encode(), arr, nd, stream, _ptr(groups), _ptr(counts), m, C.byref(n),
+                                   C.byref(fc)))
+        raw = self.table.raw()
+        out = []
+        for i in range(m):
+            labels = []
+            for j, d in enumerate(dims):
+                g = int(groups[i * nd + j])
+                if g < 0:
+                    labels.append(None)
+                elif d[0] == "seq":
+                    labels.append(self.table.columns[int(d[1])].symbols[g])
+                else:
+                    labels.append(raw.dict[int(d[1])].values[g].decode())
+            out.append((tuple(labels), int(counts[i])))
+        return out, fc.value
 
     def sparse_rows(self, plain=None, batch=None) -> tuple:
         """Row limits of the row-index Mutations path (single queries, batch slots); arguments set

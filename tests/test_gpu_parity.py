@@ -315,3 +315,88 @@ def test_batching_shapes_in_one_captured_launch():
         om, _ = orc.mutations(qs[i], 0)
         assert np.array_equal(muts[int(i)], om), qs[i]
     dev.close()
+
+
+def _expected_aggregation(t, orc, expr, dims):
+    """The reference's grouping restated on the oracle: a sequence dimension's group of a row is the
+    symbol c for which And(filter, SymEq(col, pos, c)) holds it (compileSymbolInSet for {c}), null
+    rows last; a dictionary dimension's group is the row's value, values in string order, null last;
+    combinations in depth-first (lexicographic group) order."""
+    import ctypes as C
+
+    bits, n = orc.compute_filter(expr)
+    rows = R.bits_to_rows(bits)
+    raw = t.raw()
+    gid = {int(g): i for i, g in enumerate(rows)}
+    per_dim = []
+    for d in dims:
+        g = np.full(len(rows), -2, np.int64)
+        if d[0] == "seq":
+            col = t.columns[d[1]]
+            for s, ch in enumerate(col.symbols):
+                b, _ = orc.compute_filter(f"And({expr},SymEq({col.name},{d[2]},{ch}))")
+                for r in R.bits_to_rows(b):
+                    assert g[gid[int(r)]] == -2, "symbol groups overlap"
+                    g[gid[int(r)]] = s
+            nulls = np.ctypeslib.as_array(C.cast(raw.seq[d[1]].is_null, C.POINTER(C.c_uint8)), shape=(t.n_rows,))
+            order = list(range(col.n_symbols)) + [-1]
+            labels = {s: col.symbols[s] for s in range(col.n_symbols)}
+        else:
+            rc = raw.dict[d[1]]
+            ids = np.ctypeslib.as_array(C.cast(rc.ids, C.POINTER(C.c_uint32)), shape=(t.n_rows,))
+            values = [rc.values[i].decode() for i in range(rc.n_values)]
+            order = sorted(range(len(values)), key=lambda i: values[i]) + [-1]
+            labels = {i: values[i] for i in range(len(values))}
+            nulls = (ids == 0xFFFFFFFF).astype(np.uint8)
+        for k, r in enumerate(rows):
+            i = (int(r) >> 16) * 65536 + (int(r) & 0xFFFF)  # raw row index = chunk * 2^16 + row
+            if d[0] == "seq":
+                if nulls[i]:
+                    assert g[k] == -2
+                    g[k] = -1
+            else:
+                g[k] = -1 if nulls[i] else int(ids[i])
+        assert (g != -2).all(), "every filtered row falls in one group"
+        per_dim.append((g, {v: j for j, v in enumerate(order)}, labels))
+    combos = {}
+    for k in range(len(rows)):
+        key = tuple(pd[1][int(pd[0][k])] for pd in per_dim)
+        combos[key] = combos.get(key, 0) + 1
+    out = []
+    for key in sorted(combos):
+        lab = []
+        for j, pd in enumerate(per_dim):
+            inv = {v: kk for kk, v in pd[1].items()}
+            gg = inv[key[j]]
+            lab.append(None if gg == -1 else pd[2][gg])
+        out.append((tuple(lab), combos[key]))
+    return out, n
+
+
+def test_aggregation_matches_the_oracle(config2_small):
+    """BitmapAggregation over sequence positions (nucleotide and amino-acid, pool sites and N runs)
+    and dictionary columns, one to three dimensions, against the oracle's row sets."""
+    t, orc, dev, qs = config2_small
+    names = [c.name for c in t.columns]
+    aa = names.index("S") if "S" in names else 1
+    cases = [
+        ("True", [("seq", 0, 1)]),
+        (qs[0], [("seq", 0, 21618)]),
+        (qs[1], [("seq", 0, 3037), ("dict", 0)]),
+        (qs[2], [("dict", 1), ("seq", aa, 5)]),
+        (qs[3], [("seq", 0, 241), ("seq", 0, 14408), ("dict", 0)]),
+        ("Not(HasMut(main,23403))", [("seq", 0, 23403)]),
+        ("False", [("seq", 0, 100)]),
+    ]
+    for expr, dims in cases:
+        got, n = dev.aggregate(expr, dims)
+        want, on = _expected_aggregation(t, orc, expr, dims)
+        assert n == on, expr
+        assert got == want, (expr, dims)
+        assert sum(c for _, c in got) == n
+    with pytest.raises(R.RhyError):
+        dev.aggregate("True", [("seq", 0, 0)])
+    with pytest.raises(R.RhyError):
+        dev.aggregate("True", [("seq", 0, t.columns[0].L + 1)])
+    with pytest.raises(R.RhyError):
+        dev.aggregate("True", [("dict", 99)])
