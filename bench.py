@@ -493,6 +493,17 @@ def main():
             s_dev.close()
             del s_table
 
+    # ---------------- aggregation: grouped counts of one filter (BitmapAggregation) ----------------
+    agg_q = next(queries[i] for i in range(n) if 0.01 * table.n_rows < int(b_counts[i]) < 0.5 * table.n_rows)
+    agg_dims = [("seq", 0, 21618), ("dict", 0)]
+    agg_ms = []
+    for _ in range(6):
+        t0 = time.perf_counter()
+        agg_rows, agg_n = dev.aggregate(agg_q, agg_dims)
+        agg_ms.append(1000 * (time.perf_counter() - t0))
+    aggregate = {"dimensions": "nucleotide position 21618 x country", "filter_rows": agg_n,
+                 "combinations": len(agg_rows), "ms_per_call": round(statistics.median(agg_ms[1:]), 3)}
+
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)
     # queries whose filter is neither empty nor every row: the pass reads the whole column
@@ -550,6 +561,7 @@ def main():
             "row_position_counts_per_s": cells * ws / max_over_ranks(step_s, ws),
             "planner": planner,
             "autotune": autotune,
+            "aggregate": aggregate,
             "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
