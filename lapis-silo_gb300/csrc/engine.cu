@@ -790,14 +790,21 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
    s = stream_for(s);
    const uint32_t n = static_cast<uint32_t>(exprs.size());
-   // part 0: the Mutations and Details queries (or, without any, the first quarter of the counts);
-   // part 1: the counts, planned while part 0 runs
+   // first the Mutations and Details queries, in parts of about PIPELINE_PART (one dense pass each)
+   // so that the device starts after the first of them is planned (without any: the first quarter
+   // of the counts); then the counts, planned while the first parts run
    std::vector<std::vector<uint32_t>> parts(1);
-   std::vector<uint32_t> light;
+   std::vector<uint32_t> light, heavy;
    for (uint32_t i = 0; i < n; ++i) {
       const int a = actions ? actions[i] : 0;
       if (a < 0 || a > 2) throw std::invalid_argument("action must be 0 (count), 1 (mutations) or 2 (details)");
-      (a == 0 ? light : parts[0]).push_back(i);
+      (a == 0 ? light : heavy).push_back(i);
+   }
+   {
+      const size_t k = std::max<size_t>(1, heavy.size() / PIPELINE_PART);  // heavy parts
+      parts.assign(k, {});
+      for (size_t j = 0; j < k; ++j)
+         parts[j].assign(heavy.begin() + heavy.size() * j / k, heavy.begin() + heavy.size() * (j + 1) / k);
    }
    size_t first = 0;
    if (parts[0].empty()) {
@@ -805,7 +812,7 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
       parts[0].assign(light.begin(), light.begin() + first);
    }
    if (first < light.size()) {
-      if (light.size() - first < PIPELINE_PART) parts[0].insert(parts[0].end(), light.begin() + first, light.end());
+      if (light.size() - first < PIPELINE_PART) parts.back().insert(parts.back().end(), light.begin() + first, light.end());
       else parts.emplace_back(light.begin() + first, light.end());
    }
    while (parts_.size() + 1 < parts.size()) parts_.push_back(std::make_unique<BatchState>());

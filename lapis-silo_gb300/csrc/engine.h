@@ -209,12 +209,12 @@ class Engine {
    size_t batch_rows(cudaStream_t stream, DevMutationRow* rows, size_t cap, uint64_t* row_begin, uint32_t* row_count);
    // Copies the rows of the last batch_rows again (for a caller whose buffer was too small).
    void batch_rows_fetch(cudaStream_t stream, DevMutationRow* rows, size_t cap);
-   // batch_rows of a whole batch given as text, planned and run in two parts so that the host
-   // plans the second while the device runs the first: part 0 holds the Mutations and Details
-   // queries (a Mutations pass reads the column once per 256 queries, so they stay together; the
-   // first quarter of the counts when there are none), part 1 the Aggregated counts. Results equal
-   // batch_rows of the whole batch; the rows of part 0 come first. A part 1 of fewer than
-   // PIPELINE_PART queries joins part 0. The caller holds mu.
+   // batch_rows of a whole batch given as text, planned and run in parts so that the host plans a
+   // part while the device runs the ones before it: first the Mutations and Details queries in
+   // parts of about PIPELINE_PART (a dense Mutations pass takes up to 256 queries; the first
+   // quarter of the counts when there are none), then the Aggregated counts. Results equal
+   // batch_rows of the whole batch; the rows come in part order. A counts part of fewer than
+   // PIPELINE_PART queries joins the part before it. The caller holds mu.
    static constexpr uint32_t PIPELINE_PART = 256;
    size_t batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
                                const double* min_proportions, uint32_t tile_bits, cudaStream_t stream,

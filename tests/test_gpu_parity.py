@@ -118,14 +118,15 @@ def test_batched_mutation_rows(config2_small):
         dev.batch_rows(qs[:4], [1, 1, 0, 0], None, [0.05, 1.5, 0.05, 0.05])
 
 
-def test_batch_rows_in_parts(config2_small):
-    """A batch run in two parts (Mutations and Details first, then the counts, planned while the
-    first part runs) gives every query the counts and rows of the single-part dense batch, and a
-    refetch returns the rows of both parts."""
+@pytest.mark.parametrize("heavy", [0.12, 0.5])
+def test_batch_rows_in_parts(config2_small, heavy):
+    """A batch run in parts (Mutations and Details first, about 256 at a time, then the counts,
+    each planned while the earlier parts run) gives every query the counts and rows of the
+    single-part dense batch, and a refetch returns the rows of every part."""
     t, orc, dev, qs = config2_small
     big = (qs * 6)[:1700]
     rng = np.random.default_rng(11)
-    act = np.where(rng.random(len(big)) < 0.12, 1, np.where(rng.random(len(big)) < 0.05, 2, 0)).astype(np.int32)
+    act = np.where(rng.random(len(big)) < heavy, 1, np.where(rng.random(len(big)) < 0.05, 2, 0)).astype(np.int32)
     col = rng.integers(0, t.n_seq, len(big)).astype(np.uint32)
     counts, rows, begin, cnt = dev.batch_rows(big, act, col, None, rows_cap=10)
     dense_act = np.where(act == 2, 0, act).astype(np.int32)
