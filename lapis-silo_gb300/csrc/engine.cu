@@ -270,7 +270,9 @@ Engine::~Engine() {
 uint64_t Engine::mutation_payload_bytes(int column) const { return table_.seq.at(column).vertical.payload_bytes(); }
 
 Program Engine::plan(const std::string& expr, const LowerOptions& opt, std::string* tree) const {
-   return plan_filter(expr, table_, nullptr, opt, tree);
+   LowerOptions o = opt;
+   if (o.rows <= 0) o.rows = table_.n_rows;  // early-exit tests where the estimates say they can fire
+   return plan_filter(expr, table_, nullptr, o, tree);
 }
 
 void Engine::upload_program(const Program& p, Instr* dst, cudaStream_t stream) {
@@ -1093,7 +1095,9 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    auto t0 = clk::now();
    if (!use_learned_) {
       const Estimator est = rule_estimator(table_);
-      each([&](uint32_t i) { qs[i].prog = plan_filter(exprs[i], table_, &est, LowerOptions{}, nullptr); });
+      LowerOptions lo;
+      lo.rows = table_.n_rows;
+      each([&](uint32_t i) { qs[i].prog = plan_filter(exprs[i], table_, &est, lo, nullptr); });
       batch_times.compile_ms += since(t0);
       return qs;
    }
@@ -1137,7 +1141,9 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
          if (it != est.end() && it->first == &op && it->second >= 0) return it->second;
          return ctx.rule(op);  // the rule where the network has no answer
       };
-      qs[i].prog = lower(*ops[i], learned, LowerOptions{});
+      LowerOptions lo;
+      lo.rows = table_.n_rows;
+      qs[i].prog = lower(*ops[i], learned, lo);
       qs[i].cost = std::isfinite(c) ? c : 0.0;
       // free the query's tree and features here, in parallel: a serial teardown of every tree on
       // the calling thread costs as much as the planning

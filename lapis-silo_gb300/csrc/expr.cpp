@@ -863,6 +863,12 @@ struct Lowerer {
    }
    void pop(uint32_t n = 1) { depth -= n; }
 
+   // Estimated fraction of the table's rows in an operator's result (1 without the row count).
+   double sel(const Op& o) const {
+      if (opt.rows <= 0) return 1.0;
+      return std::min(1.0, std::max(0.0, est(o) / opt.rows));
+   }
+
    std::vector<const Op*> order(const std::vector<OpPtr>& v, bool ascending) {
       std::vector<std::pair<double, const Op*>> e;
       for (const auto& c : v) e.emplace_back(opt.reorder ? est(*c) : 0.0, c.get());
@@ -966,17 +972,20 @@ struct Lowerer {
             auto neg = order(op.negated, false);
             std::vector<size_t> jumps;
             node(*pos[0]);
+            double part = sel(*pos[0]);  // estimated selectivity of the partial result
             for (size_t i = 1; i < pos.size(); ++i) {
-               if (opt.early_exit) jumps.push_back(jump(OP_JZ));
+               if (opt.early_exit && (opt.rows <= 0 || part <= opt.exit_sel)) jumps.push_back(jump(OP_JZ));
                node(*pos[i]);
                emit(OP_AND);
                pop();
+               part *= sel(*pos[i]);
             }
             for (const Op* c : neg) {
-               if (opt.early_exit) jumps.push_back(jump(OP_JZ));
+               if (opt.early_exit && (opt.rows <= 0 || part <= opt.exit_sel)) jumps.push_back(jump(OP_JZ));
                node(*c);
                emit(OP_ANDNOT);
                pop();
+               part *= 1.0 - sel(*c);
             }
             patch(jumps);
             return;
@@ -990,11 +999,13 @@ struct Lowerer {
             auto ch = order(op.children, false);
             std::vector<size_t> jumps;
             node(*ch[0]);
+            double miss = 1.0 - sel(*ch[0]);  // estimated fraction of rows the partial union misses
             for (size_t i = 1; i < ch.size(); ++i) {
-               if (opt.early_exit) jumps.push_back(jump(OP_JFULL));
+               if (opt.early_exit && (opt.rows <= 0 || miss <= opt.exit_sel)) jumps.push_back(jump(OP_JFULL));
                node(*ch[i]);
                emit(OP_OR);
                pop();
+               miss *= 1.0 - sel(*ch[i]);
             }
             patch(jumps);
             return;
@@ -1030,6 +1041,7 @@ struct Lowerer {
                first = 1;
             }
             for (size_t i = first; i < parts.size(); ++i) {
+               // the predicates are not estimated one by one: keep every test
                if (opt.early_exit) jumps.push_back(jump(OP_JZ));
                parts[i]();
                emit(OP_AND);

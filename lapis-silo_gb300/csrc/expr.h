@@ -127,6 +127,11 @@ struct LowerOptions {
    bool early_exit = true;   // emit JZ/JFULL after partial intersections/unions
    bool reorder = true;      // order children by the estimator
    bool record_spans = false;  // fill Program::spans
+   // With the table's rows (> 0), an early-exit test is emitted only where the estimates (children
+   // independent) put the partial result within exit_sel of empty (JZ) or of every row (JFULL);
+   // elsewhere a tile practically never exits there and the test would cost a barrier for nothing.
+   double rows = 0;
+   double exit_sel = 0.01;
 };
 
 // parse -> rewrite(NONE) -> compile, without lowering.
