@@ -504,6 +504,20 @@ def main():
     aggregate = {"dimensions": "nucleotide position 21618 x country", "filter_rows": agg_n,
                  "combinations": len(agg_rows), "ms_per_call": round(statistics.median(agg_ms[1:]), 3)}
 
+    # ---------------- MutationProfile: rows within a distance of a profile (one row-index pass) ----------------
+    prng = np.random.default_rng(17)
+    pmuts = ",".join(f"{p + 1}:{'ACGT'[p % 4]}" for p in sorted(prng.choice(table.columns[0].L, 25, replace=False)))
+    profile = {"profile": "reference + 25 substitutions, nucleotide column", "distances": {}}
+    for d in (0, 5, 50, 200):
+        pq = f"MutProfileMutations(main,{d},{pmuts})"
+        pn = dev.count(pq)
+        p_ms = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            dev.count(pq)
+            p_ms.append(1000 * (time.perf_counter() - t0))
+        profile["distances"][str(d)] = {"rows": int(pn), "ms_per_count": round(statistics.median(p_ms), 3)}
+
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)
     # queries whose filter is neither empty nor every row: the pass reads the whole column
@@ -562,6 +576,7 @@ def main():
             "planner": planner,
             "autotune": autotune,
             "aggregate": aggregate,
+            "mutation_profile": profile,
             "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),

@@ -123,7 +123,20 @@ struct QueryDesc {
    uint32_t out_tiles;    // 1 = write the row set to the query's output tiles
    uint32_t n_leaves;     // container leaves | coverage leaves << 16 (numbered 1.. in their c field)
    uint32_t depth;        // stack tiles the program uses; the rest of its class's stack stages payloads
+   uint32_t aux_base;     // its PUSH_AUX row sets are aux tiles aux_base + a
 };
+
+// A MutationProfile row set to compute before the filter programs (see ProfileSpec): the column,
+// the distance and the counting terms (mask[L], ploc[L + 1], pmis[L + 1]) in device memory.
+struct DevProfile {
+   uint32_t col, distance, base, pad;
+   const uint32_t* mask;
+   const uint32_t* ploc;
+   const uint32_t* pmis;
+};
+// aux[k] (nchunks * CHUNK_WORDS words each) = the rows of profiles[k] within its distance.
+void launch_profiles(const DevTable* d_table, uint32_t nchunks, const DevProfile* d_profiles, uint32_t n,
+                     uint32_t* d_aux, void* stream);
 
 // ---- launchers (kernels.cu) ----
 // tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth. n_leaves: container
@@ -131,13 +144,14 @@ struct QueryDesc {
 // tiles x ncode x 2 u32 (cycles, result popcount per executed instruction), zeroed by the caller.
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
                           uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles,
-                          unsigned long long* d_count, int* d_err, void* stream, uint32_t* d_trace = nullptr);
+                          unsigned long long* d_count, int* d_err, void* stream, uint32_t* d_trace = nullptr,
+                          const uint32_t* d_aux = nullptr);
 
 // Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.
 cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
                          const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
                          uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
-                         uint32_t* d_next, uint32_t grid, int* d_err, void* stream);
+                         uint32_t* d_next, uint32_t grid, int* d_err, void* stream, const uint32_t* d_aux = nullptr);
 
 // Kernel selection masks (all bits set = the whole pass); used to time the kernels one by one.
 enum : uint32_t { MUT_PART_CTR = 1, MUT_PART_COV = 2, MUT_PART_FINAL = 4, MUT_PART_ALL = 7 };

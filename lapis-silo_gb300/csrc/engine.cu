@@ -13,6 +13,53 @@
 #include "util.h"
 
 namespace rhygpu {
+namespace {
+template <typename T>
+void grow_device(T*& p, size_t& cap, size_t n) {
+   if (n <= cap && p) return;
+   if (p) cudaFree(p);
+   p = nullptr;
+   const size_t want = std::max<size_t>(n + n / 4, 16);
+   cuda_check(cudaMalloc(&p, want * sizeof(T)), "cudaMalloc (batch)");
+   cap = want;
+}
+template <typename T>
+void grow_host(T*& p, size_t n, size_t& cap) {
+   if (n <= cap && p) return;
+   if (p) cudaFreeHost(p);
+   p = nullptr;
+   const size_t want = std::max<size_t>(n + n / 4, 16);
+   cuda_check(cudaMallocHost(&p, want * sizeof(T)), "cudaMallocHost (batch)");
+   cap = want;
+}
+// The profiles of a program as DevProfile entries whose arrays start at `base` (device memory of
+// profile_words(aux) words) and the words to copy there.
+size_t profile_words(const std::vector<std::shared_ptr<const ProfileSpec>>& aux) {
+   size_t n = 0;
+   for (const auto& x : aux) n += x->mask.size() + x->ploc.size() + x->pmis.size();
+   return n;
+}
+void pack_profiles(const std::vector<std::shared_ptr<const ProfileSpec>>& aux, const uint32_t* base,
+                   DevProfile* profs, uint32_t* data) {
+   size_t off = 0;
+   for (size_t k = 0; k < aux.size(); ++k) {
+      const ProfileSpec& x = *aux[k];
+      DevProfile d{static_cast<uint32_t>(x.col), x.distance, x.base, 0, base + off, nullptr, nullptr};
+      std::copy(x.mask.begin(), x.mask.end(), data + off);
+      off += x.mask.size();
+      d.ploc = base + off;
+      std::copy(x.ploc.begin(), x.ploc.end(), data + off);
+      off += x.ploc.size();
+      d.pmis = base + off;
+      std::copy(x.pmis.begin(), x.pmis.end(), data + off);
+      off += x.pmis.size();
+      profs[k] = d;
+   }
+}
+}  // namespace
+}  // namespace rhygpu
+
+namespace rhygpu {
 
 void cuda_check(cudaError_t e, const char* what) {
    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
@@ -258,7 +305,8 @@ Engine::~Engine() {
    batch_free(batch_);
    for (auto& b : parts_) batch_free(*b);
    for (void* p : {static_cast<void*>(d_agg_dims_), static_cast<void*>(d_agg_counters_), static_cast<void*>(d_agg_blocks_),
-                   static_cast<void*>(d_agg_out_)})
+                   static_cast<void*>(d_agg_out_), static_cast<void*>(d_prof_), static_cast<void*>(d_prof_data_),
+                   static_cast<void*>(d_aux_)})
       if (p) cudaFree(p);
    for (void* p : allocs_) cudaFree(p);
    if (h_code_) cudaFreeHost(h_code_);
@@ -288,9 +336,25 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
    while (W > 4096 && static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) W >>= 1;
    if (static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
    cudaGetLastError();  // an error left by an unrelated earlier call must not be reported here
+   const uint32_t* aux = nullptr;
+   if (!p.aux.empty()) {  // MutationProfile row sets, before the program that reads them
+      const uint32_t n = static_cast<uint32_t>(p.aux.size());
+      const size_t nw = profile_words(p.aux);
+      grow_device(d_prof_, prof_cap_, n);
+      grow_device(d_prof_data_, prof_data_cap_, nw);
+      grow_device(d_aux_, aux_cap_, static_cast<size_t>(n) * nchunks() * CHUNK_WORDS);
+      std::vector<DevProfile> profs(n);
+      std::vector<uint32_t> data(nw);
+      pack_profiles(p.aux, d_prof_data_, profs.data(), data.data());
+      cuda_check(cudaMemcpyAsync(d_prof_, profs.data(), n * sizeof(DevProfile), cudaMemcpyHostToDevice, stream), "H2D");
+      cuda_check(cudaMemcpyAsync(d_prof_data_, data.data(), nw * 4, cudaMemcpyHostToDevice, stream), "H2D");
+      cuda_check(cudaStreamSynchronize(stream), "profile upload");  // the host arrays go out of scope
+      launch_profiles(d_table_, nchunks(), d_prof_, n, d_aux_, stream);
+      aux = d_aux_;
+   }
    const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()),
                                                p.n_ctr_leaves | (p.n_cov_leaves << 16), W,
-                                               p.max_depth, tiles, count, d_err, stream);
+                                               p.max_depth, tiles, count, d_err, stream, nullptr, aux);
    if (e != cudaSuccess)
       throw CudaError("filter kernel launch (tile " + std::to_string(W) + " rows, stack " + std::to_string(p.max_depth) +
                       " tiles): " + cudaGetErrorString(e));
@@ -380,40 +444,22 @@ uint32_t Engine::fit_tile_bits(uint32_t requested, uint32_t depth, bool batch) c
    return W;
 }
 
-namespace {
-template <typename T>
-void grow_device(T*& p, size_t& cap, size_t n) {
-   if (n <= cap && p) return;
-   if (p) cudaFree(p);
-   p = nullptr;
-   const size_t want = std::max<size_t>(n + n / 4, 16);
-   cuda_check(cudaMalloc(&p, want * sizeof(T)), "cudaMalloc (batch)");
-   cap = want;
-}
-template <typename T>
-void grow_host(T*& p, size_t n, size_t& cap) {
-   if (n <= cap && p) return;
-   if (p) cudaFreeHost(p);
-   p = nullptr;
-   const size_t want = std::max<size_t>(n + n / 4, 16);
-   cuda_check(cudaMallocHost(&p, want * sizeof(T)), "cudaMallocHost (batch)");
-   cap = want;
-}
-}  // namespace
 
 void Engine::batch_free(BatchState& b) {
    if (b.graph) cudaGraphExecDestroy(b.graph);
    for (void* p : {static_cast<void*>(b.h_code), static_cast<void*>(b.h_q), static_cast<void*>(b.h_items),
                    static_cast<void*>(b.h_slot_query), static_cast<void*>(b.h_counts), static_cast<void*>(b.h_mcounts),
                    static_cast<void*>(b.h_minprop), static_cast<void*>(b.h_rowblk), static_cast<void*>(b.h_err),
-                   static_cast<void*>(b.h_k), static_cast<void*>(b.h_ids), static_cast<void*>(b.h_nids)})
+                   static_cast<void*>(b.h_k), static_cast<void*>(b.h_ids), static_cast<void*>(b.h_nids),
+                   static_cast<void*>(b.h_prof), static_cast<void*>(b.h_prof_data)})
       if (p) cudaFreeHost(p);
    for (void* p : {static_cast<void*>(b.d_code), static_cast<void*>(b.d_q), static_cast<void*>(b.d_items),
                    static_cast<void*>(b.d_slot_query), static_cast<void*>(b.d_counts), static_cast<void*>(b.d_next),
                    static_cast<void*>(b.d_tiles), static_cast<void*>(b.d_mcounts), static_cast<void*>(b.d_mscratch),
                    static_cast<void*>(b.d_masks), static_cast<void*>(b.d_minprop), static_cast<void*>(b.d_rowblk),
                    static_cast<void*>(b.d_rows), static_cast<void*>(b.d_err), static_cast<void*>(b.d_k),
-                   static_cast<void*>(b.d_ids), static_cast<void*>(b.d_nids), static_cast<void*>(b.d_lists)})
+                   static_cast<void*>(b.d_ids), static_cast<void*>(b.d_nids), static_cast<void*>(b.d_lists),
+                   static_cast<void*>(b.d_prof), static_cast<void*>(b.d_prof_data), static_cast<void*>(b.d_aux)})
       if (p) cudaFree(p);
    b = BatchState{};
 }
@@ -426,6 +472,7 @@ size_t Engine::batch_device_bytes(const std::vector<BatchQuery>& qs, uint32_t ti
    std::vector<uint32_t> per_col(table_.seq.size(), 0);
    for (const auto& q : qs) {
       bytes += q.prog.code.size() * sizeof(Instr) + sizeof(QueryDesc) + tiles * sizeof(WorkItem) + 8;
+      bytes += q.prog.aux.size() * (tile_bytes + sizeof(DevProfile)) + profile_words(q.prog.aux) * 4;
       if (q.action == 1 && q.column >= 0 && static_cast<size_t>(q.column) < per_col.size()) {
          const DevSeqCol& dc = view_.seq[q.column];
          bytes += tile_bytes + static_cast<size_t>(dc.nsym) * dc.L * 4 + mut_scratch_words(dc.L) * 4 + 16 + 8 +
@@ -510,6 +557,18 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    size_t n_ids = 0;
    for (uint32_t qi : details) n_ids += qs[qi].k;
    if (n_ids > 0xFFFFFFFFull) throw std::invalid_argument("details: too many row ids requested");
+   size_t n_aux = 0, n_prof_data = 0;
+   for (const auto& q : qs) {
+      n_aux += q.prog.aux.size();
+      n_prof_data += profile_words(q.prog.aux);
+   }
+   grow_host(b.h_prof, n_aux, b.hc_prof);
+   grow_device(b.d_prof, b.dc_prof, n_aux);
+   grow_host(b.h_prof_data, n_prof_data, b.hc_prof_data);
+   grow_device(b.d_prof_data, b.dc_prof_data, n_prof_data);
+   grow_device(b.d_aux, b.dc_aux, n_aux * nchunks() * CHUNK_WORDS);
+   b.n_aux = static_cast<uint32_t>(n_aux);
+   b.n_prof_data = n_prof_data;
    grow_host(b.h_code, ncode, b.hc_code);
    grow_device(b.d_code, b.dc_code, ncode);
    grow_host(b.h_q, n, b.hc_q);
@@ -556,15 +615,21 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    b.n_mut_slots = n_mut;
    b.n_details = n_det;
    b.n_ids = static_cast<uint32_t>(n_ids);
-   // programs, query descriptors, work items
-   size_t off = 0;
+   // programs, query descriptors, profile row sets, work items
+   size_t off = 0, aux_off = 0, data_off = 0;
    for (uint32_t i = 0; i < n; ++i) {
       const Program& p = qs[i].prog;
       std::memcpy(b.h_code + off, p.code.data(), p.code.size() * sizeof(Instr));
       b.h_q[i] = QueryDesc{static_cast<uint32_t>(off), static_cast<uint32_t>(p.code.size()),
                            b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1,
-                           p.n_ctr_leaves | (p.n_cov_leaves << 16), std::max(p.max_depth, 1u)};
+                           p.n_ctr_leaves | (p.n_cov_leaves << 16), std::max(p.max_depth, 1u),
+                           static_cast<uint32_t>(aux_off)};
       off += p.code.size();
+      if (!p.aux.empty()) {
+         pack_profiles(p.aux, b.d_prof_data + data_off, b.h_prof + aux_off, b.h_prof_data + data_off);
+         aux_off += p.aux.size();
+         data_off += profile_words(p.aux);
+      }
    }
    // items per class: tile-major interleaving spreads the expensive queries over the whole launch;
    // with predicted costs (learned planner) the queries go heaviest first so the long ones do not
@@ -631,7 +696,15 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
          cuda_check(cudaMemcpyAsync(b.d_k, b.h_k, 2 * static_cast<size_t>(b.n_details) * sizeof(uint32_t),
                                     cudaMemcpyHostToDevice, s),
                     "H2D");
+      if (b.n_aux) {
+         cuda_check(cudaMemcpyAsync(b.d_prof, b.h_prof, b.n_aux * sizeof(DevProfile), cudaMemcpyHostToDevice, s), "H2D");
+         cuda_check(cudaMemcpyAsync(b.d_prof_data, b.h_prof_data, b.n_prof_data * 4, cudaMemcpyHostToDevice, s), "H2D");
+      }
       cuda_check(cudaMemsetAsync(b.d_err, 0, sizeof(int), s), "memset");
+   }
+   if ((parts & 1) && b.n_aux) {
+      launch_profiles(d_table_, nchunks(), b.d_prof, b.n_aux, b.d_aux, s);
+      cuda_check(cudaGetLastError(), "profile launch");
    }
    if (parts & 1) {
       cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
@@ -641,7 +714,8 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
       for (size_t g = 0; g < b.fgroups.size(); ++g) {
          const auto& fg = b.fgroups[g];
          cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items + fg.item_off, fg.n_items,
-                                        fg.tile_bits, fg.max_depth, b.d_tiles, b.d_counts, b.d_next + g, fg.grid, b.d_err, s),
+                                        fg.tile_bits, fg.max_depth, b.d_tiles, b.d_counts, b.d_next + g, fg.grid, b.d_err, s,
+                                        b.n_aux ? b.d_aux : nullptr),
                     "filter batch launch");
       }
    }
@@ -1018,6 +1092,7 @@ size_t Engine::collect_traces(const std::vector<std::string>& exprs, std::vector
          o.early_exit = false;
          o.record_spans = true;
          const Program p = lower(*op, ctx.rule, o);
+         if (!p.aux.empty()) continue;  // MutationProfile row sets are not traced
          const uint32_t nc = static_cast<uint32_t>(p.code.size());
          const size_t words = static_cast<size_t>(ntiles) * nc * 2;
          if (words > cap) {

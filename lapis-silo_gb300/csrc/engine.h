@@ -100,7 +100,15 @@ struct BatchState {
    uint32_t n_blk = 0;                // row-block table entries (Mutations slots)
    size_t n_rows = 0;                 // rows of the last row pass
    uint32_t n_mut_slots = 0, n_details = 0, n_ids = 0;
-   // capacities
+   // MutationProfile row sets of the batch's programs (QueryDesc.aux_base numbers them)
+   DevProfile* h_prof = nullptr;      // pinned; arrays point into d_prof_data
+   uint32_t* h_prof_data = nullptr;   // pinned
+   DevProfile* d_prof = nullptr;
+   uint32_t* d_prof_data = nullptr;
+   uint32_t* d_aux = nullptr;         // n_aux row sets of nchunks * CHUNK_WORDS words
+   uint32_t n_aux = 0;
+   size_t n_prof_data = 0;
+   size_t hc_prof = 0, hc_prof_data = 0, dc_prof = 0, dc_prof_data = 0, dc_aux = 0;
    // capacities (elements), one per buffer
    size_t hc_code = 0, hc_q = 0, hc_items = 0, hc_slot_query = 0, hc_counts = 0, hc_mcounts = 0, hc_minprop = 0,
           hc_rowblk = 0, hc_err = 0, hc_k = 0, hc_ids = 0, hc_nids = 0;
@@ -301,6 +309,11 @@ class Engine {
    uint32_t* d_agg_blocks_ = nullptr;
    AggCount* d_agg_out_ = nullptr;
    size_t agg_dims_cap_ = 0, agg_counters_cap_ = 0, agg_blocks_cap_ = 0, agg_out_cap_ = 0;
+   // MutationProfile row sets of the single-query path
+   DevProfile* d_prof_ = nullptr;
+   uint32_t* d_prof_data_ = nullptr;
+   uint32_t* d_aux_ = nullptr;
+   size_t prof_cap_ = 0, prof_data_cap_ = 0, aux_cap_ = 0;
    // Runs the expressions through the single-query path in trace mode; one sample per node.
    size_t collect_traces(const std::vector<std::string>& exprs, std::vector<PlannerSample>& out);
 

@@ -30,6 +30,7 @@ ExprPtr Expr::clone() const {
    e->to = to;
    e->truth = truth;
    e->sym_kind = sym_kind;
+   e->muts = muts;
    return e;
 }
 
@@ -69,6 +70,12 @@ std::string Expr::to_string() const {
          return "DateBetween(" + column + "," + (has_from ? std::to_string(from) : "*") + "," +
                 (has_to ? std::to_string(to) : "*") + ")";
       case EK::BOOL: return truth ? "True" : "False";
+      case EK::MUT_PROFILE: {
+         if (!value.empty()) return "MutProfile(" + column + "," + std::to_string(n) + "," + value + ")";
+         std::string s = "MutProfileMutations(" + column + "," + std::to_string(n);
+         for (uint32_t m : muts) s += "," + std::to_string((m >> 8) + 1) + ":" + A.chars[m & 0xFFu];
+         return s + ")";
+      }
    }
    return "?";
 }
@@ -218,6 +225,34 @@ struct Parser {
          } else {
             e->has_to = true;
             e->to = static_cast<int32_t>(integer());
+         }
+      } else if (name == "MutProfile" || name == "MutProfileMutations") {
+         // MutProfile(column, distance, query sequence) / MutProfileMutations(column, distance,
+         // position:symbol, ...) (reference: mutation_profile.cpp, querySequence and mutations input)
+         e = node(EK::MUT_PROFILE);
+         seq_column(*e);
+         expect(',');
+         const long long d = integer();
+         if (d < 0 || d > 0x7FFFFFFFll) fail("the distance must not be negative");
+         e->n = static_cast<int>(d);
+         if (name == "MutProfile") {
+            expect(',');
+            e->value = std::string(token());
+         } else {
+            while (eat(',')) {
+               const std::string_view m = token();
+               const size_t colon = m.find(':');
+               if (colon == std::string_view::npos || colon + 2 != m.size()) fail("a mutation is position:symbol");
+               uint64_t p = 0;
+               for (size_t k = 0; k < colon; ++k) {
+                  if (m[k] < '0' || m[k] > '9' || p > 0xFFFFFFull) fail("a mutation is position:symbol");
+                  p = p * 10 + static_cast<uint64_t>(m[k] - '0');
+               }
+               if (p < 1) fail("positions are 1-based");
+               const int sy = alphabet(e->sym_kind).sym(m[colon + 1]);
+               if (sy < 0) throw IllegalQuery("illegal symbol '" + std::string(1, m[colon + 1]) + "' for column " + e->column);
+               e->muts.push_back(static_cast<uint32_t>(p - 1) << 8 | static_cast<uint32_t>(sy));
+            }
          }
       } else {
          fail("unknown function '" + std::string(name) + "'");
@@ -414,6 +449,10 @@ ExprPtr rewrite(const Expr& e, const TableImage& t, Ambiguity mode) {
          if (t.find_date(e.column) < 0) throw IllegalQuery("the database does not contain the date column '" + e.column + "'");
          return e.clone();
       case EK::BOOL: return e.clone();
+      case EK::MUT_PROFILE:
+         // the ambiguity mode does not apply (mutation_profile.cpp:198-201)
+         seq_col(t, e.column);
+         return e.clone();
    }
    throw CompilationError("unknown expression kind");
 }
@@ -593,6 +632,58 @@ OpPtr negate(OpPtr op) {
    }
 }
 
+namespace {
+
+// The profile (query sequence, or the reference with the mutations applied), the symbols that
+// differ from it at each position (every symbol not in AMBIGUITY_SYMBOLS of the profile's symbol;
+// none where the profile holds the missing symbol) and the per-row counting terms
+// (reference: mutation_profile.cpp:62-89, 160-196, 198-257).
+OpPtr compile_profile(const TableImage& t, const Expr& e) {
+   const int ci = t.find_seq(e.column);
+   if (ci < 0) throw IllegalQuery("the database does not contain the sequence column '" + e.column + "'");
+   const SeqColumnImage& col = t.seq[ci];
+   const Alphabet& A = alphabet(col.kind);
+   const uint32_t L = col.L;
+   std::vector<uint8_t> profile;
+   if (!e.value.empty()) {
+      if (e.value.size() != L)
+         throw IllegalQuery("querySequence length " + std::to_string(e.value.size()) +
+                            " does not match the reference sequence length " + std::to_string(L));
+      profile.resize(L);
+      for (uint32_t p = 0; p < L; ++p) {
+         const int sy = A.sym(e.value[p]);
+         if (sy < 0) throw IllegalQuery(std::string("Invalid symbol '") + e.value[p] + "' in querySequence for MutationProfile");
+         profile[p] = static_cast<uint8_t>(sy);
+      }
+   } else {
+      profile = col.global_ref;
+      for (uint32_t m : e.muts) {
+         if ((m >> 8) >= L)
+            throw IllegalQuery("MutationProfile mutation position " + std::to_string((m >> 8) + 1) +
+                               " is out of bounds (reference length " + std::to_string(L) + ")");
+         profile[m >> 8] = static_cast<uint8_t>(m & 0xFFu);
+      }
+   }
+   auto spec = std::make_shared<ProfileSpec>();
+   spec->col = ci;
+   spec->distance = static_cast<uint32_t>(e.n);
+   spec->mask.resize(L);
+   spec->ploc.assign(L + 1, 0);
+   spec->pmis.assign(L + 1, 0);
+   for (uint32_t p = 0; p < L; ++p) {
+      const uint32_t m = profile[p] == A.missing ? 0u : A.all_mask & ~A.ambiguity[profile[p]];
+      spec->mask[p] = m;
+      spec->ploc[p + 1] = spec->ploc[p] + ((m >> col.local_ref[p]) & 1u);
+      spec->pmis[p + 1] = spec->pmis[p] + ((m >> A.missing) & 1u);
+   }
+   spec->base = spec->ploc[L];
+   auto o = mk(OpT::PROFILE);
+   o->profile = std::move(spec);
+   return o;
+}
+
+}  // namespace
+
 OpPtr compile(const Expr& e, const TableImage& t) {
    switch (e.kind) {
       case EK::AND: {
@@ -720,6 +811,7 @@ OpPtr compile(const Expr& e, const TableImage& t) {
          return selection_of(nullptr, {lo, hi});
       }
       case EK::BOOL: return mk(e.truth ? OpT::FULL : OpT::EMPTY);
+      case EK::MUT_PROFILE: return compile_profile(t, e);
       case EK::SYM_EQ: throw CompilationError("SymbolEquals should have been rewritten before compilation");
       case EK::HAS_MUT: throw CompilationError("HasMutation expression must be eliminated in query rewrite phase");
       case EK::MAYBE: throw CompilationError("Maybe expression must be elimitated in query rewrite phase");
@@ -766,6 +858,8 @@ std::string Op::to_string() const {
          }
          return s + "](" + list(children) + ")";
       }
+      case OpT::PROFILE:
+         return "Profile(" + std::to_string(profile->col) + ",<=" + std::to_string(profile->distance) + ")";
    }
    return "?";
 }
@@ -811,6 +905,9 @@ double rule_node_estimate(const Op& op, const TableImage& t, const std::function
          }
          return f * rows;
       }
+      case OpT::PROFILE:
+         // no statistics of the profile distances: an even chance
+         return 0.5 * rows;
       case OpT::THRESHOLD: {
          // Poisson-binomial distribution of the number of matching children.
          std::vector<double> dist(1, 1.0);
@@ -1071,6 +1168,12 @@ struct Lowerer {
             push();
             return;
          }
+         case OpT::PROFILE:
+            emit(OP_PUSH_AUX, static_cast<uint8_t>(op.profile->col), 0, static_cast<uint32_t>(prog.aux.size()));
+            prog.aux.push_back(op.profile);
+            push();
+            ++prog.n_leaves;
+            return;
       }
    }
 };

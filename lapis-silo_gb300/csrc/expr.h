@@ -32,7 +32,8 @@ namespace rhygpu {
 
 enum class Ambiguity : uint8_t { UPPER_BOUND, LOWER_BOUND, NONE };
 
-enum class EK : uint8_t { AND, OR, NOT, NOF, MAYBE, EXACT, SYM_EQ, HAS_MUT, SYM_IN_SET, STR_EQ, DATE_BETWEEN, BOOL };
+enum class EK : uint8_t { AND, OR, NOT, NOF, MAYBE, EXACT, SYM_EQ, HAS_MUT, SYM_IN_SET, STR_EQ, DATE_BETWEEN, BOOL,
+                          MUT_PROFILE };
 
 struct Expr;
 using ExprPtr = std::unique_ptr<Expr>;
@@ -51,6 +52,9 @@ struct Expr {
    int32_t from = 0, to = 0;  // DATE_BETWEEN
    bool truth = false;      // BOOL
    SymKind sym_kind = SymKind::NUC;
+   // MUT_PROFILE: n = distance; the profile is `value` (a query sequence) when not empty, else the
+   // reference with `muts` applied (position << 8 | symbol)
+   std::vector<uint32_t> muts;
 
    ExprPtr clone() const;
    std::string to_string() const;
@@ -61,7 +65,22 @@ ExprPtr parse_expression(const std::string& text, const TableImage& table);
 // ---------------------------------------------------------------------------------------------
 // Operator trees
 
-enum class OpT : uint8_t { EMPTY, FULL, INDEX_SCAN, INTERSECTION, UNION, COMPLEMENT, THRESHOLD, SELECTION };
+enum class OpT : uint8_t { EMPTY, FULL, INDEX_SCAN, INTERSECTION, UNION, COMPLEMENT, THRESHOLD, SELECTION, PROFILE };
+
+// A MutationProfile as one operator: the rows with at most `distance` positions whose symbol is
+// not compatible with the profile's symbol there, which is the row set of the reference's rewrite
+// Not(NOf(distance + 1, SymbolInSet(position, incompatible symbols) for every position))
+// (reference: src/rhydb/query_engine/scalar_expressions/mutation_profile.cpp:198-257). Counted per
+// row from the row index: `base` differences for a covered row holding the local reference
+// everywhere, corrected by the row's own symbols and by the positions it does not cover.
+struct ProfileSpec {
+   int col = 0;
+   uint32_t distance = 0;
+   uint32_t base = 0;
+   std::vector<uint32_t> mask;        // L: symbols counted as a difference at each position
+   std::vector<uint32_t> ploc, pmis;  // L + 1: prefix counts of positions where the local reference
+                                      // symbol (ploc) or the missing symbol (pmis) is a difference
+};
 
 struct Pred {
    enum Kind : uint8_t { COVERED, DATE } kind = COVERED;
@@ -93,6 +112,7 @@ struct Op {
    Leaf leaf;                    // INDEX_SCAN
    int n = 0;                    // THRESHOLD
    bool exact = false;           // THRESHOLD
+   std::shared_ptr<const ProfileSpec> profile;  // PROFILE
    std::string to_string() const;
 };
 
@@ -121,6 +141,8 @@ struct Program {
    uint32_t n_leaves = 0;
    uint32_t n_ctr_leaves = 0;  // PUSH_SCAN / PUSH_DICT leaves, numbered 1.. in their c field
    uint32_t n_cov_leaves = 0;  // PUSH_COVERED leaves, numbered 1.. in their c field
+   // row sets computed before the program runs (PUSH_AUX leaves, numbered 0.. in their a field)
+   std::vector<std::shared_ptr<const ProfileSpec>> aux;
 };
 
 struct LowerOptions {

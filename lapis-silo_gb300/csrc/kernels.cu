@@ -73,6 +73,7 @@ struct TileCtx {
    uint32_t row0;
    uint32_t W;
    uint32_t nvalid;
+   const uint32_t* aux;  // the query's precomputed row sets (PUSH_AUX), nchunks * CHUNK_WORDS words each
 };
 
 // Per-item staging of the program's leaves for the chunk and row range of the current tile:
@@ -500,7 +501,8 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
          case OP_PUSH_NULLS:
          case OP_PUSH_DICT:
          case OP_PUSH_COVERED:
-         case OP_PUSH_DATE: {
+         case OP_PUSH_DATE:
+         case OP_PUSH_AUX: {
             if (sp >= cap) {
                if (threadIdx.x == 0) atomicExch(err, 1);
                return false;
@@ -517,6 +519,16 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             } else if (in.op == OP_PUSH_NULLS) {
                const uint4* src = reinterpret_cast<const uint4*>(c.tab->seq[in.col].null_tiles +
                                                                  static_cast<size_t>(c.v) * CHUNK_WORDS + (c.row0 >> 5));
+               for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = __ldg(src + w4);
+               synced = false;
+            } else if (in.op == OP_PUSH_AUX) {
+               if (c.aux == nullptr) {
+                  if (threadIdx.x == 0) atomicExch(err, 5);
+                  return false;
+               }
+               const uint4* src = reinterpret_cast<const uint4*>(
+                  c.aux + static_cast<size_t>(in.a) * c.tab->nchunks * CHUNK_WORDS + static_cast<size_t>(c.v) * CHUNK_WORDS +
+                  (c.row0 >> 5));
                for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = __ldg(src + w4);
                synced = false;
             } else if (in.op == OP_PUSH_COVERED) {
@@ -732,7 +744,7 @@ __device__ __forceinline__ uint32_t result_popc(const uint32_t* smem, uint32_t W
 __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__ tab, const Instr* __restrict__ code,
                                                     uint32_t ncode, uint32_t n_leaves, uint32_t tile_bits, uint32_t cap,
                                                     uint32_t* __restrict__ out_tiles, unsigned long long* count, int* err,
-                                                    uint32_t* trace) {
+                                                    uint32_t* trace, const uint32_t* __restrict__ aux) {
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
    __shared__ LeafCache lc;
@@ -742,6 +754,7 @@ __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__
    c.v = blockIdx.x / T;
    c.W = tile_bits;
    c.row0 = (blockIdx.x % T) * tile_bits;
+   c.aux = aux;
    const uint32_t csize = __ldg(tab->chunk_sizes + c.v);
    c.nvalid = csize > c.row0 ? min(tile_bits, csize - c.row0) : 0u;
    if (c.nvalid == 0) {
@@ -769,7 +782,8 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
                                                           const QueryDesc* __restrict__ queries,
                                                           const WorkItem* __restrict__ items, uint32_t n_items,
                                                           uint32_t tile_bits, uint32_t cap, uint32_t* __restrict__ out_tiles,
-                                                          unsigned long long* counts, uint32_t* next_item, int* err) {
+                                                          unsigned long long* counts, uint32_t* next_item, int* err,
+                                                          const uint32_t* __restrict__ aux) {
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
    __shared__ uint32_t item_idx;
@@ -796,6 +810,7 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
       c.v = wi.tile / T;
       c.W = tile_bits;
       c.row0 = (wi.tile % T) * tile_bits;
+      c.aux = aux ? aux + static_cast<size_t>(q.aux_base) * per_query : nullptr;
       const uint32_t csize = __ldg(tab->chunk_sizes + c.v);
       c.nvalid = csize > c.row0 ? min(tile_bits, csize - c.row0) : 0u;
       if (c.nvalid == 0) {
@@ -822,14 +837,14 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
 
 cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, uint32_t ncode,
                           uint32_t n_leaves, uint32_t tile_bits, uint32_t stack_tiles, uint32_t* d_out_tiles, unsigned long long* d_count,
-                          int* d_err, void* stream, uint32_t* d_trace) {
+                          int* d_err, void* stream, uint32_t* d_trace, const uint32_t* d_aux) {
    const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
    cudaError_t e = cudaFuncSetAttribute(filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
    if (e != cudaSuccess) return e;
    filter_kernel<<<nchunks * T, FT, smem, static_cast<cudaStream_t>(stream)>>>(
-      d_table, d_code, ncode, n_leaves, tile_bits, stack_tiles, d_out_tiles, d_count, d_err, d_trace);
+      d_table, d_code, ncode, n_leaves, tile_bits, stack_tiles, d_out_tiles, d_count, d_err, d_trace, d_aux);
    return cudaGetLastError();
 }
 
@@ -850,14 +865,14 @@ int filter_batch_blocks_per_sm(size_t smem_bytes) {
 cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
                          const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
                          uint32_t* d_out_tiles, unsigned long long* d_counts, uint32_t* d_next, uint32_t grid, int* d_err,
-                         void* stream) {
+                         void* stream, const uint32_t* d_aux) {
    (void)nchunks;
    const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
    cudaError_t e = cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
    if (e != cudaSuccess) return e;
    filter_batch_kernel<<<grid, FT, smem, static_cast<cudaStream_t>(stream)>>>(
-      d_table, d_code, d_queries, d_items, n_items, tile_bits, stack_tiles, d_out_tiles, d_counts, d_next, d_err);
+      d_table, d_code, d_queries, d_items, n_items, tile_bits, stack_tiles, d_out_tiles, d_counts, d_next, d_err, d_aux);
    return cudaGetLastError();
 }
 

@@ -24,7 +24,7 @@ struct SubStats {
 
 SubStats subtree(const Op& op) {
    SubStats s{1, 1, 0};
-   if (op.t == OpT::INDEX_SCAN) s.leaves = 1;
+   if (op.t == OpT::INDEX_SCAN || op.t == OpT::PROFILE) s.leaves = 1;
    if (op.t == OpT::SELECTION) s.leaves += static_cast<uint32_t>(op.preds.size());
    auto add = [&](const OpPtr& c) {
       const SubStats x = subtree(*c);
@@ -154,7 +154,7 @@ void tree_features(const Op& root, const FeatureContext& ctx, std::vector<const 
    std::unordered_map<const Op*, std::pair<double, SubStats>> memo;
    std::function<void(const Op&)> post = [&](const Op& op) {
       SubStats s{1, 1, 0};
-      if (op.t == OpT::INDEX_SCAN) s.leaves = 1;
+      if (op.t == OpT::INDEX_SCAN || op.t == OpT::PROFILE) s.leaves = 1;
       if (op.t == OpT::SELECTION) s.leaves += static_cast<uint32_t>(op.preds.size());
       auto add = [&](const OpPtr& c) {
          post(*c);

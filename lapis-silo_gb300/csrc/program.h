@@ -31,6 +31,7 @@ enum OpCode : uint8_t {
    OP_THR_END = 13,      // a = planes, b = n, flags&1 = exactly: pop planes, push count >= n (== n)
    OP_JZ = 14,           // a = target: jump if the top tile is all zero
    OP_JFULL = 15,        // a = target: jump if the top tile holds every valid row
+   OP_PUSH_AUX = 16,     // a = index of a row set computed before the program (a MutationProfile)
 };
 
 // Comparators of the date predicate (reference: src/rhydb/query_engine/filter/operators/selection.h:40-72).

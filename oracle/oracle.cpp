@@ -1028,7 +1028,7 @@ RowSet Operator::evaluate() const {
 enum class Mode { UPPER, LOWER, NONE };
 Mode invert(Mode m) { return m == Mode::UPPER ? Mode::LOWER : m == Mode::LOWER ? Mode::UPPER : m; }
 
-enum class EK { AND, OR, NOT, NOF, MAYBE, EXACT, SYM_EQ, HAS_MUT, SYM_IN_SET, STR_EQ, DATE_BETWEEN, BOOL };
+enum class EK { AND, OR, NOT, NOF, MAYBE, EXACT, SYM_EQ, HAS_MUT, SYM_IN_SET, STR_EQ, DATE_BETWEEN, BOOL, MUT_PROFILE };
 
 struct Expr;
 using EP = std::unique_ptr<Expr>;
@@ -1038,7 +1038,7 @@ struct Expr {
    std::string column;
    uint32_t pos = 0;
    int sym = -1;  // -1 = '.'
-   std::vector<int> symbols;  // SYM_IN_SET, may repeat
+   std::vector<int> symbols;  // SYM_IN_SET, may repeat; MUT_PROFILE: position << 8 | symbol
    int n = 0;
    bool exact = false;
    std::string value;
@@ -1147,6 +1147,27 @@ struct Parser {
          if (!eat('*')) e->from = static_cast<int32_t>(num());
          expect(',');
          if (!eat('*')) e->to = static_cast<int32_t>(num());
+      } else if (name == "MutProfile" || name == "MutProfileMutations") {
+         e = node(EK::MUT_PROFILE);
+         e->column = tok();
+         const Alpha& A = alpha_of(e->column);
+         expect(',');
+         e->n = static_cast<int>(num());
+         if (e->n < 0) throw IllegalQuery("negative distance");
+         if (name == "MutProfile") {
+            expect(',');
+            e->value = tok();
+         } else {
+            while (eat(',')) {
+               const std::string m = tok();
+               const size_t colon = m.find(':');
+               if (colon == std::string::npos || colon + 2 != m.size()) throw IllegalQuery("a mutation is position:symbol");
+               const long long p = std::stoll(m.substr(0, colon));
+               const int sy = A.sym(m[colon + 1]);
+               if (p < 1 || sy < 0) throw IllegalQuery("bad mutation");
+               e->symbols.push_back(static_cast<int>((p - 1) << 8 | sy));
+            }
+         }
       } else {
          throw IllegalQuery("unknown function " + name);
       }
@@ -1169,6 +1190,8 @@ EP sym_in_set(const std::string& col, uint32_t pos, std::vector<int> syms) {
    e->symbols = std::move(syms);
    return e;
 }
+
+bool has(const std::vector<int>& v, int s) { return std::find(v.begin(), v.end(), s) != v.end(); }
 
 EP rewrite(const Expr& e, const Table& t, Mode mode) {
    switch (e.k) {
@@ -1297,6 +1320,38 @@ EP rewrite(const Expr& e, const Table& t, Mode mode) {
          }
          return sym_in_set(e.column, e.pos, syms);
       }
+      case EK::MUT_PROFILE: {  // mutation_profile.cpp:172-257
+         const SeqColumn& c = seq_of(t, e.column);
+         const Alpha& A = *c.A;
+         std::vector<int> profile(c.reference.begin(), c.reference.end());
+         if (!e.value.empty()) {
+            if (e.value.size() != profile.size()) throw IllegalQuery("querySequence length does not match");
+            for (size_t p = 0; p < profile.size(); ++p) {
+               profile[p] = A.sym(e.value[p]);
+               if (profile[p] < 0) throw IllegalQuery("Invalid symbol in querySequence");
+            }
+         } else {
+            for (int m : e.symbols) {
+               if (static_cast<size_t>(m >> 8) >= profile.size()) throw IllegalQuery("mutation position out of bounds");
+               profile[m >> 8] = m & 0xFF;
+            }
+         }
+         auto nof = std::make_unique<Expr>();
+         nof->k = EK::NOF;
+         nof->n = e.n + 1;
+         for (size_t p = 0; p < profile.size(); ++p) {
+            if (profile[p] == A.missing) continue;
+            std::vector<int> diff;
+            for (int y = 0; y < A.count; ++y)
+               if (!has(A.ambiguity[profile[p]], y)) diff.push_back(y);
+            if (diff.empty()) continue;
+            nof->ch.push_back(sym_in_set(e.column, static_cast<uint32_t>(p), diff));
+         }
+         auto o = std::make_unique<Expr>();
+         o->k = EK::NOT;
+         o->ch.push_back(std::move(nof));
+         return o;
+      }
       case EK::SYM_IN_SET: throw CompileError("Cannot rewrite SymbolInSet");
       case EK::STR_EQ:
       case EK::DATE_BETWEEN:
@@ -1304,8 +1359,6 @@ EP rewrite(const Expr& e, const Table& t, Mode mode) {
    }
    throw CompileError("unknown expression");
 }
-
-bool has(const std::vector<int>& v, int s) { return std::find(v.begin(), v.end(), s) != v.end(); }
 
 OpP compile(const Expr& e, const Table& t);
 

@@ -168,6 +168,29 @@ class Table:
                 S = set(col.alpha) - ({ref} if mode == UPPER else col.amb[ref])
             ids = [col.alpha.index(s) for s in S]
             return ~col.null & np.isin(col.sym[:, p], ids)
+        if k in ("MutProfile", "MutProfileMutations"):
+            # at most `distance` positions whose symbol is not compatible with the profile's
+            # (not in its ambiguity set; positions where the profile is missing never count);
+            # a row without a sequence differs nowhere
+            col = self.cols[e[1]]
+            dist = int(e[2])
+            if k == "MutProfile":
+                prof = e[3].upper()
+            else:
+                prof = list(col.reference.upper())
+                for m in e[3:]:
+                    pos, sym = m.split(":")
+                    prof[int(pos) - 1] = sym.upper()
+            cnt = np.zeros(self.n, np.int64)
+            for p, c in enumerate(prof):
+                if col.kind == 0 and c == "U":
+                    c = "T"
+                if c == col.missing:
+                    continue
+                ok = [col.alpha.index(y) for y in col.amb[c]]
+                cnt += ~np.isin(col.sym[:, p], ok)
+            cnt[col.null] = 0
+            return cnt <= dist
         if k == "StrEq":
             vals = self.dicts[e[1]]
             return np.array([v == e[2] for v in vals])
@@ -208,3 +231,27 @@ def from_raw(raw) -> Table:
         d = raw.date[c]
         dates[d.name.decode()] = np.array([d.days[r] for r in range(n)], np.int64)
     return Table(n, cols, dicts, dates)
+
+
+def profile_queries(sem, rng):
+    """MutationProfile queries: near a row's own sequence, the reference with mutations, missing
+    and ambiguous profile symbols, distances 0 .. 50."""
+    col = sem.cols["main"]
+    L = len(col.reference)
+    out = []
+    rows = rng.choice(np.flatnonzero(~col.null), 4, replace=False)
+    for i, r in enumerate(rows):
+        prof = [col.alpha[x] for x in col.sym[r]]
+        for p in rng.choice(L, 3 * i, replace=False):
+            prof[p] = "ACGTN-RY"[rng.integers(8)]
+        for d in (0, 1, 5, 50):
+            out.append(f"MutProfile(main,{d},{''.join(prof)})")
+    out.append(f"MutProfile(main,0,{'N' * L})")
+    out.append(f"MutProfile(main,3,{col.reference.lower()})")
+    muts = ",".join(f"{p + 1}:{'ACGTN'[p % 5]}" for p in rng.choice(L, 12, replace=False))
+    for d in (0, 2, 12, 200):
+        out.append(f"MutProfileMutations(main,{d},{muts})")
+    out.append("MutProfileMutations(main,0)")
+    out.append("Not(MutProfileMutations(ORF1a,1,5:K,7:X))")
+    out.append(f"And(StrEq(country,country_001),MutProfileMutations(main,4,{muts}))")
+    return out

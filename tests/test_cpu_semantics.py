@@ -54,3 +54,13 @@ def test_handwritten_edge_queries(small):
         expect = gid[sem.evaluate(q)]
         bits, cnt = orc.compute_filter(q)
         assert np.array_equal(R.bits_to_rows(bits), expect), q
+
+
+def test_mutation_profile(small):
+    t, orc, sem = small
+    n = t.n_rows
+    gid = np.array([(i >> 16) << 16 | (i & 0xFFFF) for i in range(n)], np.uint32)
+    for q in semantic.profile_queries(sem, np.random.default_rng(3)):
+        expect = gid[sem.evaluate(q)]
+        bits, cnt = orc.compute_filter(q)
+        assert cnt == len(expect) and np.array_equal(R.bits_to_rows(bits), expect), q[:80]

@@ -3,6 +3,7 @@ import numpy as np
 import pytest
 
 import rhydb_gpu as R
+import semantic
 from rawtable import RawBuilder, oracle_for
 
 pytestmark = pytest.mark.gpu
@@ -401,3 +402,73 @@ def test_aggregation_matches_the_oracle(config2_small):
         dev.aggregate("True", [("seq", 0, t.columns[0].L + 1)])
     with pytest.raises(R.RhyError):
         dev.aggregate("True", [("dict", 99)])
+
+
+@pytest.fixture(scope="module")
+def profile_table():
+    """70,000 rows over a 600-nt genome with null rows; the row-level semantics for the profiles."""
+    t = R.Table.generate(70000, seed=3, genome_len=600, pool_sites=120, n_aa_genes=2, null_fraction=0.002)
+    raw = t.raw()
+    orc = oracle_for(t, raw)
+    dev = R.Device(t, 0)
+    yield t, orc, dev, semantic.from_raw(raw)
+    dev.close()
+
+
+def test_mutation_profile(profile_table):
+    """MutationProfile row sets (one pass over the row index) against the oracle's rewrite into
+    Not(NOf(distance + 1, SymbolInSet per position)), alone, nested and in a batch."""
+    t, orc, dev, sem = profile_table
+    qs = semantic.profile_queries(sem, np.random.default_rng(3))
+    for q in qs:
+        check_filter(dev, orc, q)
+        assert dev.count(q) == orc.count(q), q[:80]
+    for q in (qs[1], qs[-1]):
+        m, n = dev.mutations(q, 0)
+        om, on = orc.mutations(q, 0)
+        assert n == on and np.array_equal(m, om), q[:80]
+    two = f"Or({qs[0]},{qs[5]})"  # two profiles in one program
+    check_filter(dev, orc, two)
+    mixed = qs + [two] + t.queries(40, seed=9, use_aa=True, use_metadata=True)
+    act = np.array([1 if i % 3 == 1 else 0 for i in range(len(mixed))], np.int32)
+    counts, muts = dev.batch(mixed, act)
+    for i, q in enumerate(mixed):
+        assert counts[i] == orc.count(q), q[:80]
+    for i in np.flatnonzero(act):
+        om, _ = orc.mutations(mixed[i], 0)
+        assert np.array_equal(muts[int(i)], om), mixed[i][:80]
+    L = len(sem.cols["main"].reference)
+    for bad in (f"MutProfile(main,1,{'A' * (L - 1)})", f"MutProfile(main,1,{'A' * (L - 1)}!)",
+                f"MutProfileMutations(main,1,{L + 1}:A)", "MutProfileMutations(main,-1,3:A)",
+                "MutProfileMutations(nosuch,1,3:A)", "MutProfileMutations(main,1,3:J)"):
+        with pytest.raises(R.RhyError):
+            dev.count(bad)
+
+
+def test_mutation_profile_full_genome(config2_small):
+    """Profiles over the 29,903-nt genome and an amino-acid gene, distances 0, 5, 50 and 200."""
+    t, orc, dev, _ = config2_small
+    raw = t.raw()
+    rng = np.random.default_rng(11)
+    ref = raw.seq[0].reference[: raw.seq[0].L].decode()
+    L = len(ref)
+    muts = ",".join(f"{p + 1}:{'ACGTN-'[p % 6]}" for p in sorted(rng.choice(L, 25, replace=False)))
+    prof = list(ref)
+    for p in rng.choice(L, 40, replace=False):
+        prof[p] = "ACGTNRY-"[rng.integers(8)]
+    aa = raw.seq[1].name.decode()
+    qs = [f"MutProfileMutations(main,{d},{muts})" for d in (0, 5, 50, 200)]
+    qs += [f"MutProfile(main,{d},{''.join(prof)})" for d in (0, 5, 50)]
+    qs += [f"MutProfileMutations({aa},2,3:X,10:K,11:*)", f"And(HasMut(main,241),MutProfileMutations(main,5,{muts}))"]
+    want = []
+    for q in qs:  # the oracle's NOf over ~30,000 children takes seconds: one call per query
+        bits, n = dev.compute_filter(q)
+        obits, on = orc.compute_filter(q)
+        assert n == on and np.array_equal(bits, obits), q[:80]
+        want.append(on)
+    act = np.array([1 if i in (1, 5) else 0 for i in range(len(qs))], np.int32)
+    counts, muts_out = dev.batch(qs, act)
+    assert list(counts) == want
+    for i in np.flatnonzero(act):
+        om, _ = orc.mutations(qs[i], 0)
+        assert np.array_equal(muts_out[int(i)], om), qs[i][:80]
