@@ -232,6 +232,7 @@ def main():
     import torch
 
     import rhydb_gpu as R
+    import workloads
 
     R.lib()
     torch.cuda.set_device(local)
@@ -505,16 +506,22 @@ def main():
                  "combinations": len(agg_rows), "ms_per_call": round(statistics.median(agg_ms[1:]), 3)}
 
     # ---------------- MutationProfile: rows within a distance of a profile (one row-index pass) ----------------
-    prng = np.random.default_rng(17)
-    pmuts = ",".join(f"{p + 1}:{'ACGT'[p % 4]}" for p in sorted(prng.choice(table.columns[0].L, 25, replace=False)))
-    profile = {"profile": "reference + 25 substitutions, nucleotide column", "distances": {}}
+    # The profile is one row's own aligned sequence with 20 substitutions, given as a query
+    # sequence (the reference's nof_sequence_filter case: a ~genome-length NOf after its rewrite).
+    pseq = workloads.profile_query_sequence(table, row=123457, substitutions=20, seed=17)
+    pstats = table.column_stats(0)
+    p_bytes = 4 * (table.n_chunks * 65536 + pstats.n_row_index_entries) + table.n_chunks * 8192 * 2
+    profile = {"profile": "row 123457's nucleotide sequence + 20 substitutions, as a query sequence",
+               "row_index_entries": pstats.n_row_index_entries, "row_index_bytes": p_bytes, "distances": {}}
     for d in (0, 5, 50, 200):
-        pq = f"MutProfileMutations(main,{d},{pmuts})"
-        pn = dev.count(pq)
+        pq = f"MutProfile(main,{d},{pseq})"
+        pn = dev.count(pq, sp)
         p_ms = []
         for _ in range(5):
+            flush_l2()
+            torch.cuda.synchronize()
             t0 = time.perf_counter()
-            dev.count(pq)
+            dev.count(pq, sp)
             p_ms.append(1000 * (time.perf_counter() - t0))
         profile["distances"][str(d)] = {"rows": int(pn), "ms_per_count": round(statistics.median(p_ms), 3)}
 

@@ -109,6 +109,7 @@ typedef struct {
    uint64_t n_missing_intervals;
    uint64_t n_coverage_exceptions;
    uint64_t n_null_rows;
+   uint64_t n_row_index_entries;  /* per-row entries (own symbols, coverage and missing-interval events) */
 } RhySeqColumnInfo;
 
 typedef struct {

@@ -245,6 +245,7 @@ int rhy_seq_column_info(const RhyTable* t, uint32_t column, RhySeqColumnInfo* ou
       out->n_missing_intervals = c.nrow_start.size();
       out->n_coverage_exceptions = c.cov_exc.size();
       out->n_null_rows = c.null_rows.size();
+      out->n_row_index_entries = c.hent.size();
    });
 }
 

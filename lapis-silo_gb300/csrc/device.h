@@ -127,16 +127,16 @@ struct QueryDesc {
 };
 
 // A MutationProfile row set to compute before the filter programs (see ProfileSpec): the column,
-// the distance and the counting terms (mask[L], ploc[L + 1], pmis[L + 1]) in device memory.
+// the distance and the counting terms in device memory, terms[p] = (mask[p], diff[p]) for
+// p <= L (mask[L] = 0), so that any row-index entry needs one 8-byte load.
 struct DevProfile {
    uint32_t col, distance, base, pad;
-   const uint32_t* mask;
-   const uint32_t* ploc;
-   const uint32_t* pmis;
+   const uint2* terms;
 };
 // aux[k] (nchunks * CHUNK_WORDS words each) = the rows of profiles[k] within its distance.
+// max_L: the longest genome among the profiles' columns.
 void launch_profiles(const DevTable* d_table, uint32_t nchunks, const DevProfile* d_profiles, uint32_t n,
-                     uint32_t* d_aux, void* stream);
+                     uint32_t max_L, uint32_t* d_aux, void* stream);
 
 // ---- launchers (kernels.cu) ----
 // tile_bits: 4096, 8192, 16384, 32768 or 65536. stack_tiles: program depth. n_leaves: container

@@ -33,10 +33,16 @@ void grow_host(T*& p, size_t n, size_t& cap) {
    cap = want;
 }
 // The profiles of a program as DevProfile entries whose arrays start at `base` (device memory of
-// profile_words(aux) words) and the words to copy there.
+// profile_words(aux) words, 8-byte aligned) and the words to copy there: per profile the
+// interleaved (mask, diff) pairs of positions 0 .. L.
+uint32_t profile_max_L(const std::vector<std::shared_ptr<const ProfileSpec>>& aux) {
+   uint32_t L = 0;
+   for (const auto& x : aux) L = std::max(L, static_cast<uint32_t>(x->mask.size()));
+   return L;
+}
 size_t profile_words(const std::vector<std::shared_ptr<const ProfileSpec>>& aux) {
    size_t n = 0;
-   for (const auto& x : aux) n += x->mask.size() + x->ploc.size() + x->pmis.size();
+   for (const auto& x : aux) n += 2 * x->diff.size();
    return n;
 }
 void pack_profiles(const std::vector<std::shared_ptr<const ProfileSpec>>& aux, const uint32_t* base,
@@ -44,16 +50,13 @@ void pack_profiles(const std::vector<std::shared_ptr<const ProfileSpec>>& aux, c
    size_t off = 0;
    for (size_t k = 0; k < aux.size(); ++k) {
       const ProfileSpec& x = *aux[k];
-      DevProfile d{static_cast<uint32_t>(x.col), x.distance, x.base, 0, base + off, nullptr, nullptr};
-      std::copy(x.mask.begin(), x.mask.end(), data + off);
-      off += x.mask.size();
-      d.ploc = base + off;
-      std::copy(x.ploc.begin(), x.ploc.end(), data + off);
-      off += x.ploc.size();
-      d.pmis = base + off;
-      std::copy(x.pmis.begin(), x.pmis.end(), data + off);
-      off += x.pmis.size();
-      profs[k] = d;
+      profs[k] = DevProfile{static_cast<uint32_t>(x.col), x.distance, x.base, 0,
+                            reinterpret_cast<const uint2*>(base + off)};
+      for (size_t p = 0; p < x.diff.size(); ++p) {
+         data[off + 2 * p] = p < x.mask.size() ? x.mask[p] : 0u;
+         data[off + 2 * p + 1] = x.diff[p];
+      }
+      off += 2 * x.diff.size();
    }
 }
 }  // namespace
@@ -222,7 +225,7 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
          d.cstart = upload(s.cstart);
          d.cend = upload(s.cend);
          d.hrow_off = upload(s.hrow_off);
-         d.hent = upload(s.hent);
+         d.hent = upload(s.hent, s.hent.size() + 8);  // 8 entries of tail: the profile pass reads whole uint4 pairs
          // coverage-pass work items: event ranges of at most EV_PER_CTA, never spanning two blocks
          std::vector<EvItem> items;
          auto split = [&](uint32_t list, uint32_t block, uint32_t b, uint32_t e) {
@@ -349,7 +352,7 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
       cuda_check(cudaMemcpyAsync(d_prof_, profs.data(), n * sizeof(DevProfile), cudaMemcpyHostToDevice, stream), "H2D");
       cuda_check(cudaMemcpyAsync(d_prof_data_, data.data(), nw * 4, cudaMemcpyHostToDevice, stream), "H2D");
       cuda_check(cudaStreamSynchronize(stream), "profile upload");  // the host arrays go out of scope
-      launch_profiles(d_table_, nchunks(), d_prof_, n, d_aux_, stream);
+      launch_profiles(d_table_, nchunks(), d_prof_, n, profile_max_L(p.aux), d_aux_, stream);
       aux = d_aux_;
    }
    const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()),
@@ -558,9 +561,11 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    for (uint32_t qi : details) n_ids += qs[qi].k;
    if (n_ids > 0xFFFFFFFFull) throw std::invalid_argument("details: too many row ids requested");
    size_t n_aux = 0, n_prof_data = 0;
+   b.profile_max_L = 0;
    for (const auto& q : qs) {
       n_aux += q.prog.aux.size();
       n_prof_data += profile_words(q.prog.aux);
+      b.profile_max_L = std::max(b.profile_max_L, profile_max_L(q.prog.aux));
    }
    grow_host(b.h_prof, n_aux, b.hc_prof);
    grow_device(b.d_prof, b.dc_prof, n_aux);
@@ -703,7 +708,7 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
       cuda_check(cudaMemsetAsync(b.d_err, 0, sizeof(int), s), "memset");
    }
    if ((parts & 1) && b.n_aux) {
-      launch_profiles(d_table_, nchunks(), b.d_prof, b.n_aux, b.d_aux, s);
+      launch_profiles(d_table_, nchunks(), b.d_prof, b.n_aux, b.profile_max_L, b.d_aux, s);
       cuda_check(cudaGetLastError(), "profile launch");
    }
    if (parts & 1) {

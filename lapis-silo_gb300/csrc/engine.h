@@ -106,7 +106,7 @@ struct BatchState {
    DevProfile* d_prof = nullptr;
    uint32_t* d_prof_data = nullptr;
    uint32_t* d_aux = nullptr;         // n_aux row sets of nchunks * CHUNK_WORDS words
-   uint32_t n_aux = 0;
+   uint32_t n_aux = 0, profile_max_L = 0;
    size_t n_prof_data = 0;
    size_t hc_prof = 0, hc_prof_data = 0, dc_prof = 0, dc_prof_data = 0, dc_aux = 0;
    // capacities (elements), one per buffer

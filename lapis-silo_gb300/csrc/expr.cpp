@@ -668,15 +668,16 @@ OpPtr compile_profile(const TableImage& t, const Expr& e) {
    spec->col = ci;
    spec->distance = static_cast<uint32_t>(e.n);
    spec->mask.resize(L);
-   spec->ploc.assign(L + 1, 0);
-   spec->pmis.assign(L + 1, 0);
+   spec->diff.assign(L + 1, 0);
+   uint32_t loc = 0;
    for (uint32_t p = 0; p < L; ++p) {
       const uint32_t m = profile[p] == A.missing ? 0u : A.all_mask & ~A.ambiguity[profile[p]];
-      spec->mask[p] = m;
-      spec->ploc[p + 1] = spec->ploc[p] + ((m >> col.local_ref[p]) & 1u);
-      spec->pmis[p + 1] = spec->pmis[p] + ((m >> A.missing) & 1u);
+      const uint32_t lbit = (m >> col.local_ref[p]) & 1u;
+      spec->mask[p] = m | lbit << 31;
+      spec->diff[p + 1] = spec->diff[p] + ((m >> A.missing) & 1u) - lbit;
+      loc += lbit;
    }
-   spec->base = spec->ploc[L];
+   spec->base = loc;
    auto o = mk(OpT::PROFILE);
    o->profile = std::move(spec);
    return o;

@@ -77,9 +77,12 @@ struct ProfileSpec {
    int col = 0;
    uint32_t distance = 0;
    uint32_t base = 0;
-   std::vector<uint32_t> mask;        // L: symbols counted as a difference at each position
-   std::vector<uint32_t> ploc, pmis;  // L + 1: prefix counts of positions where the local reference
-                                      // symbol (ploc) or the missing symbol (pmis) is a difference
+   // L: bit s = symbol s counts as a difference at the position; bit 31 = the local reference
+   // symbol does (alphabets have at most 28 symbols)
+   std::vector<uint32_t> mask;
+   // L + 1: diff[p] = (positions < p where the missing symbol is a difference) - (positions < p
+   // where the local reference symbol is one), stored as two's complement
+   std::vector<uint32_t> diff;
 };
 
 struct Pred {

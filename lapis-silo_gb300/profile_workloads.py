@@ -4,6 +4,8 @@
   plain-mutations  single-query path: filter, then the Mutations passes, for Mutations queries whose
                    filter is neither empty nor every row (the container pass reads the whole column)
   batch            the batched path: prepare once, then launch the whole batch `--steps` times
+  profile          MutationProfile counts (one row's sequence + 20 substitutions) at distances
+                   0, 5, 50 and 200
 
 The table and queries are the benchmark's seeded synthetic workload (sizes on the command line).
 """
@@ -18,11 +20,12 @@ import numpy as np
 
 sys.path.insert(0, str(Path(__file__).resolve().parent))
 import rhydb_gpu as R  # noqa: E402
+import workloads  # noqa: E402
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["plain-mutations", "batch"])
+    ap.add_argument("workload", choices=["plain-mutations", "batch", "profile"])
     ap.add_argument("--rows", type=int, default=2_000_000)
     ap.add_argument("--batch", type=int, default=2048)
     ap.add_argument("--queries", type=int, default=8, help="plain-mutations: queries to run")
@@ -49,6 +52,11 @@ def main():
             dev.plain_launch(i, sp)
         stream.synchronize()
         print(f"plain-mutations: {len(idx)} queries over {table.n_rows} rows")
+    elif args.workload == "profile":
+        seq = workloads.profile_query_sequence(table)
+        for d in (0, 5, 50, 200):
+            n = dev.count(f"MutProfile(main,{d},{seq})", sp)
+            print(f"profile: distance {d}: {n} of {table.n_rows} rows")
     else:
         if args.query_major:
             dev.batch_schedule(query_major=1)

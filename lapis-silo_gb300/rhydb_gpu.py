@@ -96,7 +96,8 @@ class SeqColumnInfo(C.Structure):
     _fields_ = [("L", C.c_uint32), ("n_symbols", C.c_uint32), ("kind", C.c_uint32), ("flipped_positions", C.c_uint32),
                 ("n_containers", C.c_uint64), ("payload_bytes", C.c_uint64), ("n_array", C.c_uint64),
                 ("n_bitset", C.c_uint64), ("n_run", C.c_uint64), ("n_missing_intervals", C.c_uint64),
-                ("n_coverage_exceptions", C.c_uint64), ("n_null_rows", C.c_uint64)]
+                ("n_coverage_exceptions", C.c_uint64), ("n_null_rows", C.c_uint64),
+                ("n_row_index_entries", C.c_uint64)]
 
 
 class BatchInfo(C.Structure):
@@ -257,6 +258,7 @@ class SeqColumnStats:
     n_missing_intervals: int
     n_coverage_exceptions: int
     n_null_rows: int
+    n_row_index_entries: int
 
     @property
     def symbols(self) -> str:
@@ -301,7 +303,8 @@ class Table:
         _check(lib().rhy_seq_column_name(self._h, i, buf, 256))
         return SeqColumnStats(buf.value.decode(), info.L, info.n_symbols, info.kind, info.flipped_positions,
                               info.n_containers, info.payload_bytes, info.n_array, info.n_bitset, info.n_run,
-                              info.n_missing_intervals, info.n_coverage_exceptions, info.n_null_rows)
+                              info.n_missing_intervals, info.n_coverage_exceptions, info.n_null_rows,
+                              info.n_row_index_entries)
 
     def column_index(self, name: str) -> int:
         for i, c in enumerate(self.columns):

@@ -5,6 +5,10 @@ to 64 children, whose selectivities spread log-uniformly over [1e-5, 0.9]. The g
 aim at a selectivity, so a larger seeded candidate set is drawn, every candidate is counted on the
 device, and the batch takes, for targets evenly spaced in log(selectivity), the unused candidate
 nearest to each target.
+
+profile_query_sequence: a MutationProfile query sequence near the data, one row's own aligned
+sequence with a few seeded substitutions (the shape of the reference's nof_sequence_filter
+benchmark, whose profile is an evolved sequence).
 """
 from __future__ import annotations
 
@@ -48,3 +52,19 @@ def batching_workload(table, device, n: int = 4096, seed: int = 44, candidates: 
                        use_metadata=use_metadata)
     counts, _ = device.batch(qs)
     return [qs[i] for i in log_uniform_pick(counts, table.n_rows, n)]
+
+
+def profile_query_sequence(table, row: int = 123457, substitutions: int = 20, seed: int = 17,
+                           column: int = 0) -> str:
+    """Row `row`'s aligned sequence in sequence column `column` (its runs over the reference),
+    with `substitutions` seeded positions set to a random A/C/G/T."""
+    raw = table.raw()
+    s = raw.seq[column]
+    row = row % table.n_rows
+    seq = bytearray(s.reference[: s.L])
+    for k in range(s.row_off[row], s.row_off[row + 1]):
+        seq[s.run_pos[k]: s.run_pos[k] + s.run_len[k]] = s.run_char[k] * s.run_len[k]
+    rng = np.random.default_rng(seed)
+    for p in rng.choice(s.L, substitutions, replace=False):
+        seq[p] = ord("ACGT"[rng.integers(4)])
+    return seq.decode()

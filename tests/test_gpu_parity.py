@@ -472,3 +472,21 @@ def test_mutation_profile_full_genome(config2_small):
     for i in np.flatnonzero(act):
         om, _ = orc.mutations(qs[i], 0)
         assert np.array_equal(muts_out[int(i)], om), qs[i][:80]
+
+
+def test_mutation_profile_long_genome():
+    """A 40,000-position genome: the profile terms do not fit shared memory, so the row-index pass
+    reads them through the caches instead."""
+    t = R.Table.generate(20000, seed=5, genome_len=40000, pool_sites=300, n_aa_genes=1, null_fraction=0.01)
+    orc = oracle_for(t)
+    dev = R.Device(t, 0)
+    try:
+        rng = np.random.default_rng(2)
+        muts = ",".join(f"{p + 1}:{'ACGTN'[p % 5]}" for p in sorted(rng.choice(40000, 30, replace=False)))
+        for d in (0, 20, 60):
+            check_filter(dev, orc, f"MutProfileMutations(main,{d},{muts})")
+        qs = [f"MutProfileMutations(main,{d},{muts})" for d in (10, 40)]
+        counts, _ = dev.batch(qs, np.zeros(2, np.int32))
+        assert list(counts) == [orc.count(q) for q in qs]
+    finally:
+        dev.close()
