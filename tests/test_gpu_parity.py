@@ -4,6 +4,7 @@ import pytest
 
 import rhydb_gpu as R
 import semantic
+import workloads
 from rawtable import RawBuilder, oracle_for
 
 pytestmark = pytest.mark.gpu
@@ -277,9 +278,26 @@ def test_complement_identity_at_scale():
         assert np.array_equal(m, muts[int(i)])
         # every covered, filtered row holds exactly one symbol per position
         assert int(m.sum(axis=0).max()) <= plain[int(i)]
+    # MutationProfile at scale: row sets grow with the distance, the source row of the profile is
+    # within its 20 substitutions, every row is within the genome's length, batched == plain
+    seq = workloads.profile_query_sequence(t, row=123457, substitutions=20, seed=17)
+    prev, sets = None, []
+    for d in (0, 20, 50, 100, 200, t.columns[0].L):
+        bits, n = dev.compute_filter(f"MutProfile(main,{d},{seq})")
+        if prev is not None:
+            assert np.array_equal(prev & bits, prev), d
+        prev = bits
+        sets.append(n)
+        if d == 20:
+            assert (bits[123457 // 32] >> (123457 % 32)) & 1
+    assert sets == sorted(sets) and sets[-1] == t.n_rows
+    pq = [f"MutProfile(main,{d},{seq})" for d in (0, 20, 50, 100, 200)]
+    counts, _ = dev.batch(pq, np.zeros(len(pq), np.int32))
+    assert counts.tolist() == sets[:-1]
     orc = oracle_for(t)
     for q in qs[:3]:
         check_filter(dev, orc, q)
+    check_filter(dev, orc, pq[0])
     m, _ = dev.mutations(qs[3], 0)
     om, _ = orc.mutations(qs[3], 0)
     assert np.array_equal(m, om)
