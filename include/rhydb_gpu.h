@@ -212,7 +212,7 @@ int rhy_batch_times(RhyDevice* d, RhyBatchTimes* out);
 typedef struct {
    uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
    uint64_t device_bytes;
-   uint32_t n_filter_launches; /* one persistent filter launch per class of programs */
+   uint32_t n_filter_launches; /* persistent filter launches per batch (one for all program classes) */
 } RhyBatchInfo;
 
 /* Split form of rhy_batch for callers that reuse one batch shape: prepare plans and stages the

@@ -626,7 +626,7 @@ int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out) {
       out->tile_bits = b.tile_bits;
       out->grid = b.grid;
       out->device_bytes = d->engine->device_bytes();
-      out->n_filter_launches = static_cast<uint32_t>(b.fgroups.size());
+      out->n_filter_launches = b.n_items ? 1u : 0u;
    });
 }
 

@@ -122,8 +122,9 @@ struct QueryDesc {
    uint32_t code_len;
    uint32_t out_tiles;    // 1 = write the row set to the query's output tiles
    uint32_t n_leaves;     // container leaves | coverage leaves << 16 (numbered 1.. in their c field)
-   uint32_t depth;        // stack tiles the program uses; the rest of its class's stack stages payloads
+   uint32_t depth;        // stack tiles the program uses; the rest of the CTA's stack stages payloads
    uint32_t aux_base;     // its PUSH_AUX row sets are aux tiles aux_base + a
+   uint32_t tile_bits;    // rows per work item of this query (its class's tile width)
 };
 
 // A MutationProfile row set to compute before the filter programs (see ProfileSpec): the column,
@@ -147,9 +148,11 @@ cudaError_t launch_filter(const DevTable* d_table, uint32_t nchunks, const Instr
                           unsigned long long* d_count, int* d_err, void* stream, uint32_t* d_trace = nullptr,
                           const uint32_t* d_aux = nullptr);
 
-// Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next.
+// Batched: n_items work items over the programs in d_code; CTAs pull items from *d_next. Every
+// item uses its query's tile width (QueryDesc.tile_bits); stack_bytes of shared memory per CTA hold
+// the program stack of any of them (depth x tile bytes) and staged payloads in the rest.
 cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
-                         const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
+                         const WorkItem* d_items, uint32_t n_items, uint32_t stack_bytes,
                          uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
                          uint32_t* d_next, uint32_t grid, int* d_err, void* stream, const uint32_t* d_aux = nullptr);
 

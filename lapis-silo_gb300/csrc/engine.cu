@@ -518,7 +518,11 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
       return fit_tile_bits(w, d, true);
    };
    std::map<uint32_t, std::vector<uint32_t>, std::greater<uint32_t>> by_w;
-   for (uint32_t i = 0; i < n; ++i) by_w[class_w(qs[i].prog.max_depth)].push_back(i);
+   std::vector<uint32_t> width(n);
+   for (uint32_t i = 0; i < n; ++i) {
+      width[i] = class_w(qs[i].prog.max_depth);
+      by_w[width[i]].push_back(i);
+   }
    size_t nitems = 0;
    for (const auto& [w, v] : by_w) nitems += static_cast<size_t>(v.size()) * nchunks() * (CHUNK_ROWS / w);
    // slots (queries whose row set is kept): Mutations grouped by column, then Details
@@ -628,7 +632,7 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
       b.h_q[i] = QueryDesc{static_cast<uint32_t>(off), static_cast<uint32_t>(p.code.size()),
                            b.slot_of_query[i] == UINT32_MAX ? 0u : b.slot_of_query[i] + 1,
                            p.n_ctr_leaves | (p.n_cov_leaves << 16), std::max(p.max_depth, 1u),
-                           static_cast<uint32_t>(aux_off)};
+                           static_cast<uint32_t>(aux_off), width[i]};
       off += p.code.size();
       if (!p.aux.empty()) {
          pack_profiles(p.aux, b.d_prof_data + data_off, b.h_prof + aux_off, b.h_prof_data + data_off);
@@ -636,9 +640,10 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
          data_off += profile_words(p.aux);
       }
    }
-   // items per class: tile-major interleaving spreads the expensive queries over the whole launch;
-   // with predicted costs (learned planner) the queries go heaviest first so the long ones do not
-   // end the launch alone
+   // items per class (widest tiles first), all in one persistent launch whose CTAs hold the stack
+   // of any class: tile-major interleaving spreads the expensive queries over the launch; with
+   // predicted costs (learned planner) the queries go heaviest first so the long ones do not end
+   // their class alone
    int props = 0;
    cuda_check(cudaDeviceGetAttribute(&props, cudaDevAttrMultiProcessorCount, device_), "attribute");
    b.fgroups.clear();
@@ -661,23 +666,24 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
          for (uint32_t t = 0; t < tiles; ++t)
             for (uint32_t qi : qv) b.h_items[k++] = WorkItem{qi, t};
       }
-      const size_t smem = static_cast<size_t>(gdepth) * (w / 8);
-      uint32_t per_sm = static_cast<uint32_t>(filter_batch_blocks_per_sm(smem));
-      if (sch.ctas_per_sm) per_sm = std::min(per_sm, sch.ctas_per_sm);
-      b.fgroups.push_back(BatchState::FilterGroup{static_cast<uint32_t>(off), static_cast<uint32_t>(k - off), w, gdepth,
-                                                  static_cast<uint32_t>(props) * per_sm});
+      b.fgroups.push_back(BatchState::FilterGroup{static_cast<uint32_t>(off), static_cast<uint32_t>(k - off), w, gdepth});
    }
+   size_t stack = 0;
+   for (const auto& g : b.fgroups) stack = std::max(stack, static_cast<size_t>(g.max_depth) * (g.tile_bits / 8));
+   uint32_t per_sm = static_cast<uint32_t>(filter_batch_blocks_per_sm(stack));
+   if (sch.ctas_per_sm) per_sm = std::min(per_sm, sch.ctas_per_sm);
+   b.stack_bytes = static_cast<uint32_t>(stack);
+   b.grid = static_cast<uint32_t>(props) * per_sm;
    std::memcpy(b.h_slot_query, slot_query.data(), slot_query.size() * sizeof(uint32_t));
    b.n_queries = n;
    b.n_slots = nslots;
    b.n_items = static_cast<uint32_t>(nitems);
    b.n_code = static_cast<uint32_t>(ncode);
    b.max_depth = depth;
-   // reported shape: the class with the most items
+   // reported tile width: the class with the most items
    const auto big = std::max_element(b.fgroups.begin(), b.fgroups.end(),
                                      [](const auto& x, const auto& y) { return x.n_items < y.n_items; });
    b.tile_bits = big != b.fgroups.end() ? big->tile_bits : batch_tile_bits;
-   b.grid = big != b.fgroups.end() ? big->grid : 0;
    b.counts_words = counts_words;
    b.scratch_words = scratch_words;
    b.mask_bytes = mask_bytes;
@@ -713,16 +719,13 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
    }
    if (parts & 1) {
       cuda_check(cudaMemsetAsync(b.d_counts, 0, b.n_queries * sizeof(unsigned long long), s), "memset");
-      cuda_check(cudaMemsetAsync(b.d_next, 0, b.fgroups.size() * sizeof(uint32_t), s), "memset");
+      cuda_check(cudaMemsetAsync(b.d_next, 0, sizeof(uint32_t), s), "memset");
       if (b.counts_words) cuda_check(cudaMemsetAsync(b.d_mcounts, 0, b.counts_words * 4, s), "memset");
       if (b.scratch_words) cuda_check(cudaMemsetAsync(b.d_mscratch, 0, b.scratch_words * 4, s), "memset");
-      for (size_t g = 0; g < b.fgroups.size(); ++g) {
-         const auto& fg = b.fgroups[g];
-         cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items + fg.item_off, fg.n_items,
-                                        fg.tile_bits, fg.max_depth, b.d_tiles, b.d_counts, b.d_next + g, fg.grid, b.d_err, s,
-                                        b.n_aux ? b.d_aux : nullptr),
+      if (b.n_items)
+         cuda_check(launch_filter_batch(d_table_, nchunks(), b.d_code, b.d_q, b.d_items, b.n_items, b.stack_bytes, b.d_tiles,
+                                        b.d_counts, b.d_next, b.grid, b.d_err, s, b.n_aux ? b.d_aux : nullptr),
                     "filter batch launch");
-      }
    }
    const size_t words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
    for (const auto& g : b.groups) {
@@ -977,7 +980,8 @@ std::vector<std::pair<BatchSchedule, double>> Engine::autotune_batch(const std::
          batch_prepare(b, qs);
          std::string key = std::to_string(c.query_major);
          for (const auto& g : b.fgroups)
-            key += "/" + std::to_string(g.tile_bits) + "x" + std::to_string(g.n_items) + "@" + std::to_string(g.grid);
+            key += "/" + std::to_string(g.tile_bits) + "x" + std::to_string(g.n_items);
+         key += "@" + std::to_string(b.grid);
          if (const auto it = seen.find(key); it != seen.end()) {
             out.emplace_back(c, it->second);
             continue;

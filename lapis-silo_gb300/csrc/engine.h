@@ -49,11 +49,13 @@ struct BatchSchedule {
 
 // Batched path state: device buffers and pinned staging, grown on demand and reused across batches.
 struct BatchState {
-   // One persistent filter launch per class of programs sharing a tile width and stack depth.
+   // Classes of programs sharing a tile width (their work items are consecutive); one persistent
+   // filter launch of `grid` CTAs with `stack_bytes` of stack takes the items of every class.
    struct FilterGroup {
-      uint32_t item_off, n_items, tile_bits, max_depth, grid;
+      uint32_t item_off, n_items, tile_bits, max_depth;
    };
    std::vector<FilterGroup> fgroups;
+   uint32_t stack_bytes = 0;
    struct ColGroup {
       int column;
       uint32_t slot_begin, n;

@@ -781,14 +781,13 @@ __global__ void __launch_bounds__(FT) filter_kernel(const DevTable* __restrict__
 __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __restrict__ tab, const Instr* __restrict__ code,
                                                           const QueryDesc* __restrict__ queries,
                                                           const WorkItem* __restrict__ items, uint32_t n_items,
-                                                          uint32_t tile_bits, uint32_t cap, uint32_t* __restrict__ out_tiles,
+                                                          uint32_t stack_words, uint32_t* __restrict__ out_tiles,
                                                           unsigned long long* counts, uint32_t* next_item, int* err,
                                                           const uint32_t* __restrict__ aux) {
    extern __shared__ __align__(16) uint32_t smem[];
    __shared__ uint32_t red[FT / 32];
    __shared__ uint32_t item_idx;
    __shared__ LeafCache lc;
-   const uint32_t T = CHUNK_ROWS / tile_bits;
    const size_t per_query = static_cast<size_t>(tab->nchunks) * CHUNK_WORDS;
    init_leaves(lc);
    uint32_t phase = 0;
@@ -799,7 +798,9 @@ __global__ void __launch_bounds__(FT) filter_batch_kernel(const DevTable* __rest
       if (it >= n_items) return;
       const WorkItem wi = items[it];
       const QueryDesc q = queries[wi.query];
-      // the program uses q.depth stack tiles; the class's other tiles take this item's payloads
+      const uint32_t tile_bits = q.tile_bits, T = CHUNK_ROWS / tile_bits;
+      const uint32_t cap = stack_words / (tile_bits >> 5);  // stack tiles of this width
+      // the program uses q.depth stack tiles; the CTA's other tiles take this item's payloads
       const uint32_t depth = min(max(q.depth, 1u), cap);
       const uint32_t ext_cap = min((cap - depth) * (tile_bits / 16), 65535u - LC_PAY - 16u) & ~7u;
       clear_leaves(lc, min(q.n_leaves & 0xFFFFu, LC_LEAVES), min(q.n_leaves >> 16, LC_COV),
@@ -863,16 +864,16 @@ int filter_batch_blocks_per_sm(size_t smem_bytes) {
 }
 
 cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const Instr* d_code, const QueryDesc* d_queries,
-                         const WorkItem* d_items, uint32_t n_items, uint32_t tile_bits, uint32_t stack_tiles,
-                         uint32_t* d_out_tiles, unsigned long long* d_counts, uint32_t* d_next, uint32_t grid, int* d_err,
-                         void* stream, const uint32_t* d_aux) {
+                         const WorkItem* d_items, uint32_t n_items, uint32_t stack_bytes, uint32_t* d_out_tiles,
+                         unsigned long long* d_counts, uint32_t* d_next, uint32_t grid, int* d_err, void* stream,
+                         const uint32_t* d_aux) {
    (void)nchunks;
-   const size_t smem = static_cast<size_t>(stack_tiles) * (tile_bits / 8);
+   const size_t smem = stack_bytes;
    cudaError_t e = cudaFuncSetAttribute(filter_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
    if (e != cudaSuccess) return e;
    filter_batch_kernel<<<grid, FT, smem, static_cast<cudaStream_t>(stream)>>>(
-      d_table, d_code, d_queries, d_items, n_items, tile_bits, stack_tiles, d_out_tiles, d_counts, d_next, d_err, d_aux);
+      d_table, d_code, d_queries, d_items, n_items, stack_bytes / 4, d_out_tiles, d_counts, d_next, d_err, d_aux);
    return cudaGetLastError();
 }
 
