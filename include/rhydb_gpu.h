@@ -127,6 +127,10 @@ const char* rhy_last_error(void);
 int rhy_generate(const RhyGenConfig* cfg, RhyTable** out);
 int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out);
 int rhy_table_info(const RhyTable* t, RhyTableInfo* out);
+/* Names the dictionary column holding the table's primary key (the schema's primary_key, used by
+ * MutProfileSequenceId; reference: src/rhydb/query_engine/scalar_expressions/mutation_profile.cpp:127-150).
+ * NULL clears it. Call it before queries that use it run, not concurrently with them. */
+int rhy_table_set_primary_key(RhyTable* t, const char* dict_column);
 int rhy_seq_column_info(const RhyTable* t, uint32_t column, RhySeqColumnInfo* out);
 int rhy_seq_column_name(const RhyTable* t, uint32_t column, char* buf, size_t cap);
 /* Views of the raw input of a generated table (valid until rhy_table_free). */

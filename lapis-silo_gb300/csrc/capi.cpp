@@ -225,6 +225,19 @@ int rhy_table_info(const RhyTable* t, RhyTableInfo* out) {
    });
 }
 
+int rhy_table_set_primary_key(RhyTable* t, const char* dict_column) {
+   return guarded([&] {
+      need(t, "table");
+      if (dict_column == nullptr) {
+         t->image.primary_key = -1;
+         return;
+      }
+      const int c = t->image.find_dict(dict_column);
+      if (c < 0) throw rhygpu::IllegalQuery(std::string("no dictionary column '") + dict_column + "'");
+      t->image.primary_key = c;
+   });
+}
+
 int rhy_seq_column_info(const RhyTable* t, uint32_t column, RhySeqColumnInfo* out) {
    return guarded([&] {
       need(t, "table");

@@ -31,6 +31,7 @@ ExprPtr Expr::clone() const {
    e->truth = truth;
    e->sym_kind = sym_kind;
    e->muts = muts;
+   e->by_id = by_id;
    return e;
 }
 
@@ -71,6 +72,7 @@ std::string Expr::to_string() const {
                 (has_to ? std::to_string(to) : "*") + ")";
       case EK::BOOL: return truth ? "True" : "False";
       case EK::MUT_PROFILE: {
+         if (by_id) return "MutProfileSequenceId(" + column + "," + std::to_string(n) + "," + value + ")";
          if (!value.empty()) return "MutProfile(" + column + "," + std::to_string(n) + "," + value + ")";
          std::string s = "MutProfileMutations(" + column + "," + std::to_string(n);
          for (uint32_t m : muts) s += "," + std::to_string((m >> 8) + 1) + ":" + A.chars[m & 0xFFu];
@@ -226,18 +228,20 @@ struct Parser {
             e->has_to = true;
             e->to = static_cast<int32_t>(integer());
          }
-      } else if (name == "MutProfile" || name == "MutProfileMutations") {
+      } else if (name == "MutProfile" || name == "MutProfileMutations" || name == "MutProfileSequenceId") {
          // MutProfile(column, distance, query sequence) / MutProfileMutations(column, distance,
-         // position:symbol, ...) (reference: mutation_profile.cpp, querySequence and mutations input)
+         // position:symbol, ...) / MutProfileSequenceId(column, distance, primary key)
+         // (reference: mutation_profile.cpp, querySequence, mutations and sequenceId input)
          e = node(EK::MUT_PROFILE);
          seq_column(*e);
          expect(',');
          const long long d = integer();
          if (d < 0 || d > 0x7FFFFFFFll) fail("the distance must not be negative");
          e->n = static_cast<int>(d);
-         if (name == "MutProfile") {
+         if (name == "MutProfile" || name == "MutProfileSequenceId") {
             expect(',');
             e->value = std::string(token());
+            e->by_id = name == "MutProfileSequenceId";
          } else {
             while (eat(',')) {
                const std::string_view m = token();
@@ -634,6 +638,59 @@ OpPtr negate(OpPtr op) {
 
 namespace {
 
+// The aligned sequence of the row whose primary key is `id`: the first row holding that value in
+// the table's primary-key dictionary column. It is rebuilt from the row index: the local reference,
+// overwritten by the row's own symbols, and the missing symbol wherever the row is not covered or
+// lies in a missing interval, so a null row is missing everywhere (reference:
+// mutation_profile.cpp:95-150, reconstructSequenceAtRow and buildProfileFromSequenceId).
+std::vector<uint8_t> sequence_of_primary_key(const TableImage& t, const SeqColumnImage& col, const std::string& id) {
+   const Alphabet& A = alphabet(col.kind);
+   if (t.primary_key < 0 || static_cast<size_t>(t.primary_key) >= t.dict.size())
+      throw IllegalQuery("MutationProfile sequenceId: the table has no primary key column");
+   const DictColumnImage& pk = t.dict[t.primary_key];
+   const auto it = pk.index.find(id);
+   const ContainerSet& V = pk.inverted;
+   uint32_t row = UINT32_MAX;
+   if (it != pk.index.end() && it->second < V.nkeys) {
+      for (uint32_t v = 0; v < t.nchunks() && row == UINT32_MAX; ++v) {
+         const size_t k = static_cast<size_t>(v) * V.nkeys + it->second;
+         uint32_t first = UINT32_MAX;
+         for (uint32_t i = V.off[k]; i < V.off[k + 1]; ++i) {
+            const CtrDesc& d = V.ctrs[i];
+            const uint16_t* p = V.payload.data() + d.payload;
+            uint32_t m = UINT32_MAX;
+            if (d.type == CT_ARRAY || d.type == CT_RUN) {
+               m = p[0];  // arrays ascend; runs are (start, length - 1) pairs in order
+            } else {
+               for (uint32_t w = 0; w < CHUNK_WORDS && m == UINT32_MAX; ++w) {
+                  const uint32_t x = static_cast<uint32_t>(p[2 * w]) | static_cast<uint32_t>(p[2 * w + 1]) << 16;
+                  if (x) m = 32 * w + static_cast<uint32_t>(__builtin_ctz(x));
+               }
+            }
+            first = std::min(first, m);
+         }
+         if (first != UINT32_MAX) row = v * CHUNK_ROWS + first;
+      }
+   }
+   if (row == UINT32_MAX)
+      throw IllegalQuery("No sequence found with primary key '" + id + "' in " +
+                         (col.kind == SymKind::NUC ? "Nucleotide" : "AminoAcid") + " MutationProfile");
+   std::vector<uint8_t> seq = col.local_ref;
+   std::vector<uint8_t> missing(col.L, 0);
+   uint32_t start = 0, end = col.L, miss_a = 0;
+   for (uint32_t i = col.hrow_off[row]; i < col.hrow_off[row + 1]; ++i) {
+      const uint32_t code = col.hent[i] & 31u, p = col.hent[i] >> 5;
+      if (code < ROW_COV_START) seq[p] = static_cast<uint8_t>(code);
+      else if (code == ROW_COV_START) start = p;
+      else if (code == ROW_COV_END) end = p;
+      else if (code == ROW_MISS_START) miss_a = p;
+      else std::fill(missing.begin() + miss_a, missing.begin() + p, 1);
+   }
+   for (uint32_t p = 0; p < col.L; ++p)
+      if (p < start || p >= end || missing[p]) seq[p] = static_cast<uint8_t>(A.missing);
+   return seq;
+}
+
 // The profile (query sequence, or the reference with the mutations applied), the symbols that
 // differ from it at each position (every symbol not in AMBIGUITY_SYMBOLS of the profile's symbol;
 // none where the profile holds the missing symbol) and the per-row counting terms
@@ -645,7 +702,9 @@ OpPtr compile_profile(const TableImage& t, const Expr& e) {
    const Alphabet& A = alphabet(col.kind);
    const uint32_t L = col.L;
    std::vector<uint8_t> profile;
-   if (!e.value.empty()) {
+   if (e.by_id) {
+      profile = sequence_of_primary_key(t, col, e.value);
+   } else if (!e.value.empty()) {
       if (e.value.size() != L)
          throw IllegalQuery("querySequence length " + std::to_string(e.value.size()) +
                             " does not match the reference sequence length " + std::to_string(L));

@@ -52,9 +52,11 @@ struct Expr {
    int32_t from = 0, to = 0;  // DATE_BETWEEN
    bool truth = false;      // BOOL
    SymKind sym_kind = SymKind::NUC;
-   // MUT_PROFILE: n = distance; the profile is `value` (a query sequence) when not empty, else the
-   // reference with `muts` applied (position << 8 | symbol)
+   // MUT_PROFILE: n = distance; the profile is the sequence of the row whose primary key is
+   // `value` when `by_id`, else `value` (a query sequence) when not empty, else the reference with
+   // `muts` applied (position << 8 | symbol)
    std::vector<uint32_t> muts;
+   bool by_id = false;
 
    ExprPtr clone() const;
    std::string to_string() const;

@@ -147,6 +147,7 @@ struct TableImage {
    std::vector<SeqColumnImage> seq;
    std::vector<DictColumnImage> dict;
    std::vector<DateColumnImage> date;
+   int primary_key = -1;  // dictionary column holding the primary key (schema primary_key), -1 = none
    uint32_t nchunks() const { return static_cast<uint32_t>(chunk_sizes.size()); }
    int find_seq(const std::string& name) const;
    int find_dict(const std::string& name) const;

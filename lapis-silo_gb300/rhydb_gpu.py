@@ -163,6 +163,7 @@ def lib():
         "rhy_generate": (I, [C.POINTER(GenConfig), C.POINTER(P)]),
         "rhy_table_from_raw": (I, [C.POINTER(RawTable), U32, C.POINTER(P)]),
         "rhy_table_info": (I, [P, C.POINTER(TableInfo)]),
+        "rhy_table_set_primary_key": (I, [P, C.c_char_p]),
         "rhy_seq_column_info": (I, [P, U32, C.POINTER(SeqColumnInfo)]),
         "rhy_seq_column_name": (I, [P, U32, C.c_char_p, C.c_size_t]),
         "rhy_table_raw": (I, [P, C.POINTER(RawTable)]),
@@ -295,6 +296,10 @@ class Table:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.rhy_table_free(self._h)
             self._h = None
+
+    def set_primary_key(self, dict_column: str | None) -> None:
+        """Names the dictionary column holding the primary key (MutProfileSequenceId)."""
+        _check(lib().rhy_table_set_primary_key(self._h, None if dict_column is None else dict_column.encode()))
 
     def column_stats(self, i: int) -> SeqColumnStats:
         info = SeqColumnInfo()

@@ -508,6 +508,7 @@ struct Table {
    std::vector<SeqColumn> seq;
    std::vector<DictColumn> dict;
    std::vector<DateColumn> date;
+   int primary_key = -1;  // dictionary column of the schema's primary key
    int find_seq(const std::string& n) const {
       for (size_t i = 0; i < seq.size(); ++i)
          if (seq[i].name == n) return static_cast<int>(i);
@@ -1044,6 +1045,7 @@ struct Expr {
    std::string value;
    std::optional<int32_t> from, to;
    bool truth = false;
+   bool by_id = false;  // MUT_PROFILE: `value` is a primary key
    EP clone() const {
       auto e = std::make_unique<Expr>();
       e->k = k;
@@ -1058,6 +1060,7 @@ struct Expr {
       e->from = from;
       e->to = to;
       e->truth = truth;
+      e->by_id = by_id;
       return e;
    }
 };
@@ -1147,16 +1150,17 @@ struct Parser {
          if (!eat('*')) e->from = static_cast<int32_t>(num());
          expect(',');
          if (!eat('*')) e->to = static_cast<int32_t>(num());
-      } else if (name == "MutProfile" || name == "MutProfileMutations") {
+      } else if (name == "MutProfile" || name == "MutProfileMutations" || name == "MutProfileSequenceId") {
          e = node(EK::MUT_PROFILE);
          e->column = tok();
          const Alpha& A = alpha_of(e->column);
          expect(',');
          e->n = static_cast<int>(num());
          if (e->n < 0) throw IllegalQuery("negative distance");
-         if (name == "MutProfile") {
+         if (name == "MutProfile" || name == "MutProfileSequenceId") {
             expect(',');
             e->value = tok();
+            e->by_id = name == "MutProfileSequenceId";
          } else {
             while (eat(',')) {
                const std::string m = tok();
@@ -1192,6 +1196,34 @@ EP sym_in_set(const std::string& col, uint32_t pos, std::vector<int> syms) {
 }
 
 bool has(const std::vector<int>& v, int s) { return std::find(v.begin(), v.end(), s) != v.end(); }
+
+// buildProfileFromSequenceId / reconstructSequenceAtRow (mutation_profile.cpp:95-150): the first
+// row holding `id` in the primary-key dictionary column; the local reference overwritten by the
+// row's vertical-index symbols, then the missing symbol outside its covered region and inside its
+// missing intervals.
+std::vector<int> sequence_at_primary_key(const Table& t, const SeqColumn& c, const std::string& id) {
+   if (t.primary_key < 0) throw IllegalQuery("the table has no primary key column");
+   const DictColumn& pk = t.dict[t.primary_key];
+   const auto it = pk.index.find(id);
+   if (it == pk.index.end() || it->second.empty()) throw IllegalQuery("No sequence found with primary key");
+   const auto& [chunk, ctr] = it->second.c.front();
+   uint32_t first = 0;
+   if (ctr.is_bitset) {
+      uint32_t w = 0;
+      while (ctr.bits[w] == 0) ++w;
+      first = 64 * w + static_cast<uint32_t>(__builtin_ctzll(ctr.bits[w]));
+   } else {
+      first = ctr.arr.front();
+   }
+   const uint32_t row = static_cast<uint32_t>(chunk) << 16 | first;
+   std::vector<int> seq = c.local_reference;
+   for (const auto& [key, x] : c.vertical)
+      if (key.v_index == chunk && x.contains(static_cast<uint16_t>(first))) seq[key.position] = key.symbol;
+   const auto [s, e] = c.coverage_range(row);
+   for (uint32_t p = 0; p < c.L; ++p)
+      if (p < s || p >= e || c.horizontal_contains(row, p)) seq[p] = c.A->missing;
+   return seq;
+}
 
 EP rewrite(const Expr& e, const Table& t, Mode mode) {
    switch (e.k) {
@@ -1324,7 +1356,9 @@ EP rewrite(const Expr& e, const Table& t, Mode mode) {
          const SeqColumn& c = seq_of(t, e.column);
          const Alpha& A = *c.A;
          std::vector<int> profile(c.reference.begin(), c.reference.end());
-         if (!e.value.empty()) {
+         if (e.by_id) {
+            profile = sequence_at_primary_key(t, c, e.value);
+         } else if (!e.value.empty()) {
             if (e.value.size() != profile.size()) throw IllegalQuery("querySequence length does not match");
             for (size_t p = 0; p < profile.size(); ++p) {
                profile[p] = A.sym(e.value[p]);
@@ -1674,6 +1708,14 @@ int oracle_build(const ORawTable* raw, void** out) {
 }
 
 void oracle_free(void* t) { delete static_cast<Table*>(t); }
+
+int oracle_set_primary_key(void* t, const char* dict_column) {
+   return guard([&] {
+      Table& tab = *static_cast<Table*>(t);
+      tab.primary_key = dict_column ? tab.find_dict(dict_column) : -1;
+      if (dict_column && tab.primary_key < 0) throw IllegalQuery("no such dictionary column");
+   });
+}
 
 int oracle_count(void* t, const char* expr, uint64_t* out) {
    return guard([&] { *out = compute_filter(*static_cast<Table*>(t), expr).cardinality(); });

@@ -33,6 +33,7 @@ def lib():
             "oracle_mutations": (I, [P, C.c_char_p, U32, P, C.POINTER(U64)]),
             "oracle_mutation_rows": (I, [P, U32, P, D, P, P, P, P, P, P, SZ, C.POINTER(SZ)]),
             "oracle_local_reference": (I, [P, U32, C.c_char_p]),
+            "oracle_set_primary_key": (I, [P, C.c_char_p]),
             "oracle_vertical": (I, [P, U32, P, P, P, P, SZ, C.POINTER(SZ)]),
             "oracle_row_coverage": (I, [P, U32, U32, C.POINTER(U32), C.POINTER(U32), P, SZ, C.POINTER(SZ)]),
             "oracle_diff_string": (I, [I, C.c_char_p, C.c_char_p, C.POINTER(U32), C.POINTER(U32), P, C.POINTER(SZ), P,
@@ -112,6 +113,9 @@ class Oracle:
         _check(lib().oracle_mutation_rows(self._h, column, _p(counts), min_proportion, _p(pos), _p(frm), _p(to),
                                           _p(cnt), _p(cov), _p(prop), m, C.byref(n)))
         return [(int(pos[i]), chr(frm[i]), chr(to[i]), int(cnt[i]), int(cov[i]), float(prop[i])) for i in range(m)]
+
+    def set_primary_key(self, dict_column):
+        _check(lib().oracle_set_primary_key(self._h, None if dict_column is None else dict_column.encode()))
 
     def local_reference(self, column: int) -> str:
         L = self.columns[column][2]

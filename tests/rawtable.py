@@ -124,3 +124,41 @@ def date_days(iso: str) -> int:
     import datetime
 
     return (datetime.date.fromisoformat(iso) - datetime.date(1970, 1, 1)).days
+
+
+def accession_table(n_rows: int = 300, L: int = 120, seed: int = 5):
+    """A raw table with a primary-key dictionary column "accession": sequences drawn around a random
+    reference (substitutions, ambiguity codes, leading / trailing / inner N runs, gaps, null rows),
+    mostly unique accessions, two accessions shared by several rows (the first row counts), one
+    held by a null row, some rows without one. Returns (builder, raw, accessions)."""
+    rng = np.random.default_rng(seed)
+    ref = "".join(rng.choice(list("ACGT"), L))
+    rows = []
+    for i in range(n_rows):
+        if i % 37 == 5:
+            rows.append(None)
+            continue
+        s = list(ref)
+        for p in rng.choice(L, int(rng.integers(0, 12)), replace=False):
+            s[p] = "ACGTRYKMN-"[rng.integers(10)]
+        if rng.random() < 0.3:  # leading missing symbols
+            k = int(rng.integers(1, 20))
+            s[:k] = ["N"] * k
+        if rng.random() < 0.3:  # trailing
+            k = int(rng.integers(1, 20))
+            s[L - k:] = ["N"] * k
+        if rng.random() < 0.3:  # inside
+            a, k = int(rng.integers(0, L - 10)), int(rng.integers(2, 10))
+            s[a: a + k] = ["N"] * k
+        assert len(s) == L
+        rows.append("".join(s))
+    acc = [f"seq_{i:04d}" for i in range(n_rows)]
+    for i in (40, 41, 90):
+        acc[i] = "shared_a"
+    for i in (7, 200):
+        acc[i] = "shared_b"
+    acc[5] = "null_row"  # row 5 has no sequence
+    for i in (11, 12):
+        acc[i] = None
+    b = RawBuilder(n_rows).add_sequences("main", 0, ref, rows).add_dict("accession", acc)
+    return b, b.raw(), acc

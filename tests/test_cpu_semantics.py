@@ -5,6 +5,7 @@ import pytest
 
 import rhydb_gpu as R
 import semantic
+import oracle as oracle_mod
 from rawtable import oracle_for
 
 
@@ -64,3 +65,38 @@ def test_mutation_profile(small):
         expect = gid[sem.evaluate(q)]
         bits, cnt = orc.compute_filter(q)
         assert cnt == len(expect) and np.array_equal(R.bits_to_rows(bits), expect), q[:80]
+
+
+def test_mutation_profile_sequence_id():
+    """MutProfileSequenceId: the profile is the aligned sequence of the first row holding the
+    primary key (all missing for a row without a sequence); the oracle against the row-level
+    semantics, and the product's compile step (plan) for its error cases."""
+    from rawtable import accession_table
+
+    b, raw, acc = accession_table()
+    t = R.Table.from_raw(raw)
+    orc = oracle_mod.Oracle(raw, t.n_chunks, [(c.name, c.n_symbols, c.L) for c in t.columns])
+    sem = semantic.from_raw(raw)
+    col = sem.cols["main"]
+    L = len(col.reference)
+    with pytest.raises(R.RhyError):
+        t.plan("MutProfileSequenceId(main,1,seq_0003)")  # no primary key yet
+    t.set_primary_key("accession")
+    orc.set_primary_key("accession")
+    gid = np.arange(t.n_rows, dtype=np.uint32)
+    for key in ("seq_0003", "shared_a", "shared_b", "null_row", "seq_0299"):
+        row = acc.index(key)
+        seq = "N" * L if col.null[row] else "".join(col.alpha[x] for x in col.sym[row])
+        for d in (0, 1, 3, 10):
+            q = f"MutProfileSequenceId(main,{d},{key})"
+            expect = gid[sem.evaluate(f"MutProfile(main,{d},{seq})")]
+            bits, cnt = orc.compute_filter(q)
+            assert cnt == len(expect) and np.array_equal(R.bits_to_rows(bits), expect), q
+            tree, _, _ = t.plan(q)
+            assert "Profile" in tree
+    for bad in ("MutProfileSequenceId(main,1,nosuch)", "MutProfileSequenceId(main,-1,seq_0003)",
+                "MutProfileSequenceId(nosuch,1,seq_0003)"):
+        with pytest.raises(R.RhyError):
+            t.plan(bad)
+    with pytest.raises(R.RhyError):
+        t.set_primary_key("nosuch")

@@ -5,6 +5,7 @@ import pytest
 import rhydb_gpu as R
 import semantic
 import workloads
+import oracle as oracle_mod
 from rawtable import RawBuilder, oracle_for
 
 pytestmark = pytest.mark.gpu
@@ -506,5 +507,34 @@ def test_mutation_profile_long_genome():
         qs = [f"MutProfileMutations(main,{d},{muts})" for d in (10, 40)]
         counts, _ = dev.batch(qs, np.zeros(2, np.int32))
         assert list(counts) == [orc.count(q) for q in qs]
+    finally:
+        dev.close()
+
+
+def test_mutation_profile_sequence_id():
+    """MutProfileSequenceId: the profile is the sequence of the first row holding a primary key,
+    rebuilt on the host from the row index; the same row sets as the oracle's reconstruction from
+    its vertical and coverage indexes, alone and in a batch."""
+    from rawtable import accession_table
+
+    b, raw, acc = accession_table(n_rows=70000, L=300, seed=9)
+    t = R.Table.from_raw(raw)
+    orc = oracle_mod.Oracle(raw, t.n_chunks, [(c.name, c.n_symbols, c.L) for c in t.columns])
+    t.set_primary_key("accession")
+    orc.set_primary_key("accession")
+    dev = R.Device(t, 0)
+    try:
+        qs = [f"MutProfileSequenceId(main,{d},{k})" for k in ("seq_0003", "shared_a", "null_row", "seq_69999")
+              for d in (0, 2, 8)]
+        for q in qs:
+            check_filter(dev, orc, q)
+        act = np.array([1 if i % 3 == 1 else 0 for i in range(len(qs))], np.int32)
+        counts, muts = dev.batch(qs, act)
+        assert list(counts) == [orc.count(q) for q in qs]
+        for i in np.flatnonzero(act)[:3]:
+            om, _ = orc.mutations(qs[i], 0)
+            assert np.array_equal(muts[int(i)], om), qs[i]
+        with pytest.raises(R.RhyError):
+            dev.count("MutProfileSequenceId(main,1,nosuch)")
     finally:
         dev.close()
