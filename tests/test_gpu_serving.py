@@ -14,6 +14,11 @@ pytestmark = pytest.mark.gpu
 def setup():
     t = R.Table.generate(300000, seed=21, n_aa_genes=12, null_fraction=0.002)
     qs = t.queries(240, seed=22, use_aa=True, use_metadata=True)
+    # every 20th request filters by a MutationProfile (row-index pass before the filter programs)
+    muts = "241:T,3037:T,14408:T,23403:G,28881:A"
+    for j in range(0, len(qs), 20):
+        d = (0, 2, 5, 30)[(j // 20) % 4]
+        qs[j] = f"MutProfileMutations(main,{d},{muts})" if j % 40 else f"And({qs[j]},MutProfileMutations(main,{d},{muts}))"
     dev = R.Device(t, 0)
     rng = np.random.default_rng(23)
     acts = rng.choice([0, 1, 2], len(qs), p=[0.6, 0.25, 0.15])
