@@ -65,11 +65,11 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, 
 //   SU_BITSET  one bitset container; SU_RUN one run container.
 // Array and bitset payloads, and the first DESC_CAP descriptors of an array unit, are double-
 // buffered into shared memory by TMA bulk copies completing on one mbarrier (the copy of the next
-// unit is in flight while the current one is counted). For array units each warp tests 32
-// consecutive elements at a time against the filter tile of the chunk (staged in shared memory)
-// and ballots the membership bits; a block prefix sum over the unit's 128 membership words gives
-// every container its |F ∩ c| as the difference of two prefix values, added to
-// counts[symbol][position] (containers cut by a unit boundary add two partial counts). Full filters (|F| == rows) use the stored cardinalities
+// unit is in flight while the current one is counted). For array units thread t tests elements
+// EPT t .. EPT t + EPT - 1 against the filter tile of the chunk (staged in shared memory), a
+// block prefix sum over the membership bits gives every container its |F ∩ c| as the difference
+// of two prefix values, added to counts[symbol][position] (containers cut by a unit boundary add
+// two partial counts). Full filters (|F| == rows) use the stored cardinalities
 // (reference: mutations_node.cpp:139-190, full path :240-266).
 __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                         const uint32_t* __restrict__ filter,
@@ -151,35 +151,41 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
          } else {
             const uint4* sdesc = sm4 + b * BUF4 + SU / 8;
             const uint32_t n = U.e1 - U.e0;
-            const uint16_t* pay = reinterpret_cast<const uint16_t*>(sm4 + b * BUF4);
-            // element i = MT k + tid: a warp tests 32 consecutive elements at a time (neighbouring
-            // rows of one container share filter words), and its ballot is word i / 32 of the
-            // unit's membership bits
+            const uint4* q = sm4 + b * BUF4 + 2 * tid;
+            uint32_t m = 0;
+            // element r of the chunk sets mask bit k when row r is in F: the filter word holding r,
+            // rotated right by (r - k) mod 32, has that row's bit at position k
             if (n == SU) {
 #pragma unroll
-               for (uint32_t k = 0; k < EPT; ++k) {
-                  const uint32_t r = pay[MT * k + tid];
-                  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, (F[r >> 5] >> (r & 31u)) & 1u);
-                  if ((tid & 31u) == 0) msk[k * NW + (tid >> 5)] = bal;
+               for (uint32_t j = 0; j < 2; ++j) {
+                  const uint4 x = q[j];
+#pragma unroll
+                  for (uint32_t t = 0; t < 8; ++t) {
+                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
+                     const uint32_t w = F[r >> 5];
+                     m |= __funnelshift_r(w, w, r - k) & (1u << k);
+                  }
                }
             } else {
 #pragma unroll
-               for (uint32_t k = 0; k < EPT; ++k) {
-                  const uint32_t i = MT * k + tid;
-                  const uint32_t r = i < n ? pay[i] : 0u;
-                  const uint32_t bal = __ballot_sync(0xFFFFFFFFu, i < n && ((F[r >> 5] >> (r & 31u)) & 1u));
-                  if ((tid & 31u) == 0) msk[k * NW + (tid >> 5)] = bal;
+               for (uint32_t j = 0; j < 2; ++j) {
+                  const uint4 x = q[j];
+#pragma unroll
+                  for (uint32_t t = 0; t < 8; ++t) {
+                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
+                     const uint32_t w = F[r >> 5];
+                     if (EPT * tid + k < n) m |= __funnelshift_r(w, w, r - k) & (1u << k);
+                  }
                }
             }
-            __syncthreads();
-            constexpr uint32_t MW = SU / 32;  // membership words per unit
             uint32_t total;
-            const uint32_t ex = block_excl_scan(tid < MW ? __popc(msk[tid]) : 0u, wsum, &total);
-            if (tid < MW) exq[tid] = ex;
+            const uint32_t ex = block_excl_scan(__popc(m), wsum, &total);
+            msk[tid] = m;
+            exq[tid] = ex;
             __syncthreads();
             auto prefix = [&](uint32_t i) -> uint32_t {  // members among elements [0, i)
-               if (i >= SU) return total;
-               return exq[i >> 5] + __popc(msk[i >> 5] & ((1u << (i & 31u)) - 1u));
+               if (i / EPT >= MT) return total;
+               return exq[i / EPT] + __popc(msk[i / EPT] & ((1u << (i % EPT)) - 1u));
             };
             for (uint32_t c = U.c0 + tid; c < U.c1; c += MT) {
                const uint4 raw = c - U.c0 < DESC_CAP ? sdesc[c - U.c0] : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
