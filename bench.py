@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default filter schedule")
     ap.add_argument("--schedule", default="",
                     help="max_tile_bits,stack_kb,ctas_per_sm,query_major: this filter schedule instead of the autotuner's")
+    ap.add_argument("--shape-queries", type=int, default=4096,
+                    help="batching-shape leg: trees of 1-64 leaves, log-uniform selectivities (0: none)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
     ap.add_argument("--serve-rows", type=int, default=8_000_000,
@@ -354,8 +356,8 @@ def main():
     barrier(ws)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, ws)
     value = n * args.steps * ws / total_s
-    # a persistent filter launch per class of programs, then per column with Mutations queries: the
-    # slot split, transpose, container, coverage, row-index (when on) and final kernels
+    # one persistent filter launch for all classes of programs, then per column with Mutations
+    # queries: the slot split, transpose, container, coverage, row-index (when on) and final kernels
     per_col = 5 + (1 if dev.sparse_rows()[1] > 0 else 0)
     launches_per_step = info.n_filter_launches + per_col * len({int(c) for c, a in zip(columns, actions) if a == 1})
 
@@ -525,6 +527,39 @@ def main():
             p_ms.append(1000 * (time.perf_counter() - t0))
         profile["distances"][str(d)] = {"rows": int(pn), "ms_per_count": round(statistics.median(p_ms), 3)}
 
+    # ---------------- batching shape: trees of 1-64 leaves, selectivities log-uniform in [1e-5, 0.9] ----------------
+    shape = None
+    if args.shape_queries:
+        t0 = time.perf_counter()
+        s_qs = workloads.batching_workload(table, dev, n=args.shape_queries, seed=44,
+                                           candidates=10 * args.shape_queries)
+        pick_s = time.perf_counter() - t0
+        dev.batch_prepare(s_qs)
+        dev.batch_launch(sp, True, False)
+        dev.batch_capture_ex(sp, copy_in=False, copy_out=False)
+        for _ in range(3):
+            flush_l2()
+            dev.batch_replay(sp)
+        torch.cuda.synchronize()
+        s_ms = []
+        for _ in range(20):
+            flush_l2()
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            dev.batch_replay(sp)
+            e1.record(stream)
+            e1.synchronize()
+            s_ms.append(e0.elapsed_time(e1))
+        dev.batch_launch(sp, True, True)
+        torch.cuda.synchronize()
+        s_counts, _ = dev.batch_results()
+        sel = np.asarray(s_counts, np.float64) / table.n_rows
+        shape = {"queries": len(s_qs), "leaves": "1-64, NOf up to 64 children", "action": "Aggregated count",
+                 "selectivity_min": float(sel.min()), "selectivity_max": float(sel.max()),
+                 "queries_per_s": len(s_qs) / (statistics.median(s_ms) / 1000.0),
+                 "batch_ms_p50": float(np.percentile(s_ms, 50)), "batch_ms_p99": float(np.percentile(s_ms, 99)),
+                 "steps": len(s_ms), "l2": "flushed before every step", "pick_s": round(pick_s, 2)}
+
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)
     # queries whose filter is neither empty nor every row: the pass reads the whole column
@@ -584,6 +619,7 @@ def main():
             "autotune": autotune,
             "aggregate": aggregate,
             "mutation_profile": profile,
+            "batching_shape": shape,
             "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
