@@ -16,12 +16,15 @@
 //     VerticalSequenceIndex (storage/column/vertical_sequence_index.cpp:17-283),
 //   * expressions: SymbolEquals / HasMutation / SymbolInSet / And / Or / Negation / NOf / Maybe /
 //     Exact / Equals (indexed string) / DateBetween rewrite + compile (query_engine/scalar_expressions/),
+//     and MutationProfile's literal rewrite into Not(NOf(distance + 1, SymbolInSet per position))
+//     with all three profile inputs (scalar_expressions/mutation_profile.cpp:62-257),
 //   * operators: IndexScan, Intersection, Union, Complement, Threshold, Selection,
 //     IsInCoveredRegion, CompareToValueSelection, Empty, Full (query_engine/filter/operators/),
 //   * actions: CountFilterNode (operators/count_filter_node.cpp:35-71) and the Mutations action
 //     (operators/mutations_node.cpp:39-366).
 // The restatement is pinned against the reference's own known-answer tests, restated in
-// tests/test_oracle_known_answers.py (file:line of each test cited there).
+// tests/golden/reference_cases.py (file:line of each test cited there) and run by
+// tests/test_golden_reference.py.
 #include <algorithm>
 #include <array>
 #include <atomic>
