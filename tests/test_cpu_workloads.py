@@ -1,4 +1,5 @@
-"""The seeded workload helpers: leaf-limited trees and the log-uniform selectivity pick."""
+"""The seeded workload helpers: leaf-limited trees, the log-uniform selectivity pick and the
+MutationProfile query sequence."""
 import re
 
 import numpy as np
@@ -33,3 +34,17 @@ def test_log_uniform_pick():
     assert per_decade.min() > 300 and per_decade.max() < 500, per_decade
     with pytest.raises(ValueError):
         workloads.log_uniform_pick(counts[:10], rows, 2000)
+
+
+def test_profile_query_sequence():
+    """The benchmark's MutationProfile query sequence is the row's aligned sequence (its runs over the
+    reference), with exactly the seeded substitutions changed."""
+    import semantic
+
+    t = R.Table.generate(3000, seed=4, genome_len=600, pool_sites=120, n_aa_genes=0, null_fraction=0.0)
+    col = semantic.from_raw(t.raw()).cols["main"]
+    for row in (0, 1234, 2999):
+        own = "".join(col.alpha[x] for x in col.sym[row])
+        assert workloads.profile_query_sequence(t, row=row, substitutions=0) == own
+        changed = workloads.profile_query_sequence(t, row=row, substitutions=7, seed=3)
+        assert len(changed) == len(own) and sum(a != b for a, b in zip(own, changed)) <= 7
