@@ -98,7 +98,42 @@ NOF = {
     "errors": [],
 }
 
-DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF]
+# src/rhydb/query_engine/scalar_expressions/mutation_profile.test.cpp:23-62: six rows, the primary
+# key a metadata column; segment1 reference ATGCN, gene1 reference M* (gene2 has no sequences)
+MUTATION_PROFILE = {
+    "name": "mutation_profile.test.cpp:23-62",
+    "n_rows": 6,
+    "seq": [
+        ("segment1", 0, "ATGCN", ["ATGCN", "CTGCN", "CTCCN", "CTCTN", "NNNNN", "RTGCN"]),
+        ("gene1", 1, "M*", ["M*", "C*", "M*", "M*", "M*", "M*"]),
+        ("gene2", 1, "M*", [None] * 6),
+    ],
+    "dict": [("primaryKey", ["seq_ref", "seq_1mut", "seq_2mut", "seq_3mut", "seq_all_n", "seq_mixed_amb"])],
+    "primary_key": "primaryKey",
+    # expected row ids (rows in input order: seq_ref, seq_1mut, seq_2mut, seq_3mut, seq_all_n, seq_mixed_amb)
+    "row_cases": [
+        ("MutProfileMutations(segment1,0)", [0, 4, 5]),                 # :68-77
+        ("MutProfileMutations(segment1,1)", [0, 1, 4, 5]),              # :79-88
+        ("MutProfileMutations(segment1,2)", [0, 1, 2, 4, 5]),           # :90-99
+        ("MutProfileMutations(segment1,0,1:C)", [1, 4]),                # :103-111
+        ("MutProfile(segment1,0,ATGCN)", [0, 4, 5]),                    # :116-125
+        ("MutProfileSequenceId(segment1,0,seq_1mut)", [1, 4]),          # :141-149
+        ("MutProfileMutations(gene1,0)", [0, 2, 3, 4, 5]),              # :187-197
+        ("MutProfileMutations(gene1,1)", [0, 1, 2, 3, 4, 5]),           # :199-209
+        ("MutProfileMutations(gene1,0,1:C)", [1]),                      # :211-217
+        ("MutProfile(gene1,0,M*)", [0, 2, 3, 4, 5]),                    # :221-231
+        ("MutProfileSequenceId(gene1,0,seq_1mut)", [1]),                # :233-240
+    ],
+    "cases": [],
+    "errors": [
+        "MutProfile(segment1,0,ATG)",                      # :127-137, querySequence of the wrong length
+        "MutProfileSequenceId(segment1,0,nonexistent_id)", # :151-159
+        "MutProfileMutations(nonexistent_gene,0)",         # :242-249
+        "MutProfileMutations(gene1,0,123456:C)",           # :259-268, position out of bounds
+    ],
+}
+
+DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE]
 
 # Operator-level known answers: src/rhydb/query_engine/filter/operators/threshold.test.cpp:28-313.
 # (kind 0 = Threshold; non-negated row sets, negated row sets, n, exactly, expected)

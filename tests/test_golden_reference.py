@@ -19,7 +19,11 @@ def build(ds):
         b.add_dates(name, [date_days(v) if v else None for v in values])
     raw = b.raw()
     table = R.Table.from_raw(raw)
-    return b, raw, table, oracle_for(table, raw)
+    orc = oracle_for(table, raw)
+    if ds.get("primary_key"):
+        table.set_primary_key(ds["primary_key"])
+        orc.set_primary_key(ds["primary_key"])
+    return b, raw, table, orc
 
 
 @pytest.fixture(scope="module", params=G.DATASETS, ids=lambda d: d["name"])
