@@ -133,7 +133,31 @@ MUTATION_PROFILE = {
     ],
 }
 
-DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE]
+# src/rhydb/query_engine/scalar_expressions/date_between.test.cpp:10-47: one row, a sorted and an
+# unsorted date column (2020-12-24 = day 18620, 2023-01-20 = day 19377); the reference has no
+# sequence columns, a one-position sequence column stands in here
+DATE_BETWEEN = {
+    "name": "date_between.test.cpp:10-47",
+    "n_rows": 1,
+    "seq": [("segment1", 0, "A", ["A"])],
+    "dict": [("primaryKey", ["id"])],
+    "date": [("sorted_date", ["2020-12-24"]), ("unsorted_date", ["2023-01-20"])],
+    "row_cases": [
+        ("DateBetween(sorted_date,18620,18620)", [0]),    # :49-53
+        ("DateBetween(sorted_date,*,18620)", [0]),        # :55-59
+        ("DateBetween(sorted_date,18620,*)", [0]),        # :61-65
+        ("DateBetween(unsorted_date,19377,19377)", [0]),  # :67-71
+        ("DateBetween(unsorted_date,*,19377)", [0]),      # :73-77
+        ("DateBetween(unsorted_date,19377,*)", [0]),      # :79-83
+    ],
+    "cases": [],
+    "errors": [
+        "DateBetween(something_not_in_database,10957,*)",  # :85-90
+        "DateBetween(primaryKey,18262,*)",                 # :92-96, not a date column
+    ],
+}
+
+DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE, DATE_BETWEEN]
 
 # Operator-level known answers: src/rhydb/query_engine/filter/operators/threshold.test.cpp:28-313.
 # (kind 0 = Threshold; non-negated row sets, negated row sets, n, exactly, expected)
