@@ -157,7 +157,29 @@ DATE_BETWEEN = {
     ],
 }
 
-DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE, DATE_BETWEEN]
+# src/rhydb/query_engine/scalar_expressions/or.test.cpp:404-461: six rows with country and region
+# (USA -> Americas, else Europe)
+_OR_COUNTRIES = ["Switzerland", "Germany", "USA", "Switzerland", "France", "Germany"]
+OR = {
+    "name": "or.test.cpp:404-461",
+    "n_rows": 6,
+    "seq": [("segment1", 0, "ATGCN", ["ACGTN"] * 6)],
+    "dict": [("country", _OR_COUNTRIES), ("region", ["Americas" if c == "USA" else "Europe" for c in _OR_COUNTRIES])],
+    "row_cases": [
+        ("Or(Or(StrEq(country,Switzerland),StrEq(country,Germany)),StrEq(country,France))", [0, 1, 3, 4, 5]),  # :463-477
+        ("Or(StrEq(country,Switzerland),StrEq(country,Germany))", [0, 1, 3, 5]),                                # :479-492
+        ("Or(StrEq(country,Switzerland))", [0, 3]),                                                              # :494-500
+        ("Or(StrEq(country,Switzerland),StrEq(country,Germany),StrEq(country,France))", [0, 1, 3, 4, 5]),       # :502-516
+        ("Or(StrEq(country,USA),StrEq(region,Europe))", [0, 1, 2, 3, 4, 5]),                                    # :518-533
+        ("Or(And(StrEq(country,Switzerland),StrEq(region,Europe)),StrEq(country,USA))", [0, 2, 3]),            # :535-547
+        ("False", []),                                                                                           # :549-552
+        ("Or()", []),
+    ],
+    "cases": [],
+    "errors": [],
+}
+
+DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE, DATE_BETWEEN, OR]
 
 # Operator-level known answers: src/rhydb/query_engine/filter/operators/threshold.test.cpp:28-313.
 # (kind 0 = Threshold; non-negated row sets, negated row sets, n, exactly, expected)
