@@ -179,7 +179,24 @@ OR = {
     "errors": [],
 }
 
-DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE, DATE_BETWEEN, OR]
+# src/rhydb/query_engine/scalar_expressions/and.test.cpp:67-90: six rows with country and date
+# (2009-01-01 = day 14245, 2000-01-01 = day 10957)
+_AND_ROWS = [("Switzerland", "2020-01-01"), ("Germany", "2000-03-07"), ("Germany", "2009-06-07"),
+             ("Switzerland", "2003-07-02"), ("Switzerland", "2002-01-04"), ("Switzerland", "2001-12-07")]
+AND = {
+    "name": "and.test.cpp:67-90",
+    "n_rows": 6,
+    "seq": [("segment1", 0, "ATGCN", ["ACGTN"] * 6)],
+    "dict": [("country", [r[0] for r in _AND_ROWS])],
+    "date": [("date", [r[1] for r in _AND_ROWS])],
+    "row_cases": [
+        ("And(DateBetween(date,14245,*),DateBetween(date,10957,*),StrEq(country,Germany))", [2]),  # :79-88
+    ],
+    "cases": [],
+    "errors": [],
+}
+
+DATASETS = [SYMBOL_EQUALS_NUC, HAS_MUTATION, SYMBOL_EQUALS_AA, NOF, MUTATION_PROFILE, DATE_BETWEEN, OR, AND]
 
 # Operator-level known answers: src/rhydb/query_engine/filter/operators/threshold.test.cpp:28-313.
 # (kind 0 = Threshold; non-negated row sets, negated row sets, n, exactly, expected)
