@@ -135,11 +135,11 @@ MUTATION_PROFILE = {
 
 # src/rhydb/query_engine/scalar_expressions/date_between.test.cpp:10-47: one row, a sorted and an
 # unsorted date column (2020-12-24 = day 18620, 2023-01-20 = day 19377); the reference has no
-# sequence columns, a one-position sequence column stands in here
+# sequence columns, the five-position column of the other datasets stands in here
 DATE_BETWEEN = {
     "name": "date_between.test.cpp:10-47",
     "n_rows": 1,
-    "seq": [("segment1", 0, "A", ["A"])],
+    "seq": [("segment1", 0, "ATGCN", ["ACGTN"])],
     "dict": [("primaryKey", ["id"])],
     "date": [("sorted_date", ["2020-12-24"]), ("unsorted_date", ["2023-01-20"])],
     "row_cases": [
