@@ -19,6 +19,13 @@
  *   rhy_mutations_batch  many queries per launch (no reference counterpart: the reference runs one
  *                        query per worker thread, app/src/api.cpp:39-51).
  *
+ * Expressions are text, one function per node of the reference's expression tree (positions
+ * 1-based): SymEq(col,pos,C) with C = '.' for the reference symbol, HasMut(col,pos), And(...),
+ * Or(...), Not(x), NOf(n,exactly|atleast,...), Maybe(x), Exact(x), StrEq(col,value),
+ * DateBetween(col,from,to) in days since 1970-01-01 with '*' for an open end, True, False, and
+ * MutationProfile (scalar_expressions/mutation_profile.cpp) as MutProfile(col,distance,SEQUENCE),
+ * MutProfileMutations(col,distance,pos:C,...) or MutProfileSequenceId(col,distance,id).
+ *
  * Conventions: every function returns RHY_OK (0) or an error code and never throws; the message
  * of the last error on the calling thread is returned by rhy_last_error(). Output buffers are
  * owned by the caller. Calls on one device handle are serialised by the handle; `stream` is a
