@@ -170,6 +170,10 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
                       void* stream, uint32_t parts = MUT_PART_ALL | MUT_PART_SPARSE, uint64_t sparse_max = 0);
+// Testing the failure path of the container pass's bounded waits on the current device: while on,
+// each of its CTAs withholds the copy its first wait expects, so the wait gives up and the pass sets
+// error 7 (device error flag) instead of counting. Nothing is left in flight.
+void set_copy_withholding(bool on);
 
 // One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),
 // at most CTR_UNIT_CHUNKS chunks and, unless a single chunk exceeds it, CTR_UNIT_ELEMENTS elements.

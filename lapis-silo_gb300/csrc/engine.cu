@@ -333,19 +333,22 @@ void Engine::upload_program(const Program& p, Instr* dst, cudaStream_t stream) {
 }
 
 void Engine::launch_count(const Instr* code, const Program& p, unsigned long long* count, uint32_t* tiles,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, const uint32_t* const* literals) {
    uint32_t W = tile_bits;
    // shared memory: keep the stack under 200 KiB
    while (W > 4096 && static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) W >>= 1;
    if (static_cast<size_t>(p.max_depth) * (W / 8) > 200 * 1024) throw IllegalQuery("filter expression nests too deeply");
    cudaGetLastError();  // an error left by an unrelated earlier call must not be reported here
    const uint32_t* aux = nullptr;
+   if (p.n_literals > 0 && literals == nullptr) throw std::invalid_argument("the program reads caller row sets");
+   const size_t set_words = static_cast<size_t>(nchunks()) * CHUNK_WORDS;
+   if (!p.aux.empty() || p.n_literals > 0)
+      grow_device(d_aux_, aux_cap_, (p.aux.size() + p.n_literals) * set_words);
    if (!p.aux.empty()) {  // MutationProfile row sets, before the program that reads them
       const uint32_t n = static_cast<uint32_t>(p.aux.size());
       const size_t nw = profile_words(p.aux);
       grow_device(d_prof_, prof_cap_, n);
       grow_device(d_prof_data_, prof_data_cap_, nw);
-      grow_device(d_aux_, aux_cap_, static_cast<size_t>(n) * nchunks() * CHUNK_WORDS);
       std::vector<DevProfile> profs(n);
       std::vector<uint32_t> data(nw);
       pack_profiles(p.aux, d_prof_data_, profs.data(), data.data());
@@ -353,8 +356,12 @@ void Engine::launch_count(const Instr* code, const Program& p, unsigned long lon
       cuda_check(cudaMemcpyAsync(d_prof_data_, data.data(), nw * 4, cudaMemcpyHostToDevice, stream), "H2D");
       cuda_check(cudaStreamSynchronize(stream), "profile upload");  // the host arrays go out of scope
       launch_profiles(d_table_, nchunks(), d_prof_, n, profile_max_L(p.aux), d_aux_, stream);
-      aux = d_aux_;
    }
+   for (uint32_t k = 0; k < p.n_literals; ++k)  // the caller's row sets after the profiles' (the caller owns them)
+      cuda_check(cudaMemcpyAsync(d_aux_ + (p.aux.size() + k) * set_words, literals[k], set_words * 4,
+                                 cudaMemcpyHostToDevice, stream),
+                 "copy caller row set");
+   if (!p.aux.empty() || p.n_literals > 0) aux = d_aux_;
    const cudaError_t e = rhygpu::launch_filter(d_table_, nchunks(), code, static_cast<uint32_t>(p.code.size()),
                                                p.n_ctr_leaves | (p.n_cov_leaves << 16), W,
                                                p.max_depth, tiles, count, d_err, stream, nullptr, aux);
@@ -376,17 +383,23 @@ void Engine::check_error_flag() {
       const int e = *h_err_;
       *h_err_ = 0;
       cudaMemset(d_err, 0, sizeof(int));
-      throw CompilationError("device program error " + std::to_string(e));
+      throw_device_error(e);
    }
 }
 
-uint64_t Engine::count(const Program& p, cudaStream_t stream) {
+void throw_device_error(int code) {
+   if (code == DEVERR_WAIT_FILTER || code == DEVERR_WAIT_MUTATIONS)
+      throw CudaError("a bounded device wait for bulk copies gave up (device error " + std::to_string(code) + ")");
+   throw CompilationError("device program error " + std::to_string(code));
+}
+
+uint64_t Engine::count(const Program& p, cudaStream_t stream, const uint32_t* const* literals) {
    std::lock_guard<std::mutex> lock(mu);
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
    if (!stream) stream = stream_;
    upload_program(p, d_code, stream);
    cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream), "memset");
-   launch_count(d_code, p, d_count, nullptr, stream);
+   launch_count(d_code, p, d_count, nullptr, stream, literals);
    cuda_check(cudaMemcpyAsync(h_count_, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "copy count");
    cuda_check(cudaMemcpyAsync(h_err_, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream), "copy error flag");
    cuda_check(cudaStreamSynchronize(stream), "count");
@@ -394,13 +407,14 @@ uint64_t Engine::count(const Program& p, cudaStream_t stream) {
    return *h_count_;
 }
 
-void Engine::eval(const Program& p, uint32_t* host_bits, uint64_t* host_count, cudaStream_t stream) {
+void Engine::eval(const Program& p, uint32_t* host_bits, uint64_t* host_count, cudaStream_t stream,
+                  const uint32_t* const* literals) {
    std::lock_guard<std::mutex> lock(mu);
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
    if (!stream) stream = stream_;
    upload_program(p, d_code, stream);
    cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream), "memset");
-   launch_count(d_code, p, d_count, d_filter, stream);
+   launch_count(d_code, p, d_count, d_filter, stream, literals);
    if (host_bits)
       cuda_check(cudaMemcpyAsync(host_bits, d_filter, static_cast<size_t>(nchunks()) * CHUNK_WORDS * 4, cudaMemcpyDeviceToHost,
                                  stream),
@@ -412,7 +426,8 @@ void Engine::eval(const Program& p, uint32_t* host_bits, uint64_t* host_count, c
    if (host_count) *host_count = *h_count_;
 }
 
-void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint64_t* filter_count, cudaStream_t stream) {
+void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint64_t* filter_count, cudaStream_t stream,
+                       const uint32_t* const* literals) {
    if (column < 0 || static_cast<size_t>(column) >= table_.seq.size()) throw std::invalid_argument("no such sequence column");
    std::lock_guard<std::mutex> lock(mu);
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
@@ -423,7 +438,7 @@ void Engine::mutations(const Program& p, int column, uint32_t* host_counts, uint
    cuda_check(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream), "memset");
    cuda_check(cudaMemsetAsync(d_counts, 0, words * 4, stream), "memset");
    cuda_check(cudaMemsetAsync(d_scratch, 0, mut_scratch_words(c.L) * 4, stream), "memset");
-   launch_count(d_code, p, d_count, d_filter, stream);
+   launch_count(d_code, p, d_count, d_filter, stream, literals);
    launch_mutations(column, d_filter, d_count, d_counts, d_scratch, stream);
    cuda_check(cudaMemcpyAsync(h_count_, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "copy count");
    cuda_check(cudaMemcpyAsync(host_counts, d_counts, words * 4, cudaMemcpyDeviceToHost, stream), "copy counts");
@@ -500,6 +515,7 @@ void Engine::batch_prepare(BatchState& b, const std::vector<BatchQuery>& qs, uin
    uint32_t depth = 1;
    size_t ncode = 0;
    for (const auto& q : qs) {
+      if (q.prog.n_literals) throw std::invalid_argument("batched programs cannot read caller row sets");
       depth = std::max(depth, q.prog.max_depth);
       ncode += q.prog.code.size();
       if (q.action == 1 && (q.column < 0 || static_cast<size_t>(q.column) >= table_.seq.size()))
@@ -762,7 +778,7 @@ void Engine::check_batch_error(BatchState& b) {
    if (b.h_err && *b.h_err != 0) {
       const int e = *b.h_err;
       *b.h_err = 0;
-      throw CompilationError("device program error " + std::to_string(e));
+      throw_device_error(e);
    }
 }
 

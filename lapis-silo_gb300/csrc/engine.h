@@ -25,6 +25,13 @@ struct CudaError : std::runtime_error {
 
 void cuda_check(cudaError_t e, const char* what);
 
+// Device error flag values set by the kernels' bounded waits when they give up (the filter kernel's
+// leaf copies, the Mutations container pass's unit copies); other values are program errors.
+enum : int { DEVERR_WAIT_FILTER = 6, DEVERR_WAIT_MUTATIONS = 7 };
+// Throws the exception of a nonzero device error flag: CudaError for a wait that gave up,
+// CompilationError for a malformed program.
+[[noreturn]] void throw_device_error(int code);
+
 // One query of a batch. Actions: 0 = Aggregated count, 1 = Mutations of `column`, 2 = Details
 // (the first k row ids of the filter, ascending).
 struct BatchQuery {
@@ -158,10 +165,13 @@ class Engine {
    Program plan(const std::string& expr, const LowerOptions& opt = {}, std::string* tree = nullptr) const;
 
    // Plain single-query path: host in, host out, synchronous on `stream` (nullptr = engine stream).
-   uint64_t count(const Program& p, cudaStream_t stream);
-   void eval(const Program& p, uint32_t* host_bits /* nchunks * 2048 */, uint64_t* host_count, cudaStream_t stream);
+   // `literals`: the caller's row sets read by the program's ROWS leaves (host memory, nchunks * 2048
+   // words each; Program::n_literals of them), or nullptr for a program without them.
+   uint64_t count(const Program& p, cudaStream_t stream, const uint32_t* const* literals = nullptr);
+   void eval(const Program& p, uint32_t* host_bits /* nchunks * 2048 */, uint64_t* host_count, cudaStream_t stream,
+             const uint32_t* const* literals = nullptr);
    void mutations(const Program& p, int column, uint32_t* host_counts /* nsym * L */, uint64_t* filter_count,
-                  cudaStream_t stream);
+                  cudaStream_t stream, const uint32_t* const* literals = nullptr);
    // Grouped counts of the filter's rows (BitmapAggregation): one dimension per sequence position
    // (kind AGG_SEQUENCE, 0-based position) or dictionary column (AGG_DICTIONARY). Output rows in the
    // reference's order, groups[i * dims + d] = symbol index / value id / -1 for the null group.
@@ -174,7 +184,7 @@ class Engine {
    // Device-side building blocks (no host synchronisation); used by the timed benchmark legs.
    void upload_program(const Program& p, Instr* d_code, cudaStream_t stream);
    void launch_count(const Instr* d_code, const Program& p, unsigned long long* d_count, uint32_t* d_tiles,
-                     cudaStream_t stream);
+                     cudaStream_t stream, const uint32_t* const* literals = nullptr);
    void launch_mutations(int column, const uint32_t* d_filter, const unsigned long long* d_count, uint32_t* d_counts,
                          uint32_t* d_scratch, cudaStream_t stream, uint32_t parts = MUT_PART_ALL);
    void check_error_flag();

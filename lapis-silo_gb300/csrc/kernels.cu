@@ -164,17 +164,24 @@ __device__ __forceinline__ uint4 cover_ranges(const DevTable* __restrict__ tab, 
    return make_uint4(__ldg(xo + k0), __ldg(xo + k1), __ldg(no + k0), __ldg(no + k1));
 }
 
-// Waits (bounded) for phase `parity` of the copies' barrier; false if it gave up.
+// Waits for phase `parity` of the copies' barrier, bounded by 2 s on the GPU's global timer (a copy
+// lands in microseconds) and, as a second bound, by 2^26 polls of at most about 1 us each; false if
+// it gave up.
 __device__ __forceinline__ bool wait_copies(LeafCache& lc, uint32_t parity) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
-   for (uint32_t i = 0; i < (1u << 22); ++i) {
+   uint64_t t0 = 0;
+   for (uint32_t i = 0; i < (1u << 26); ++i) {
       uint32_t done;
       asm volatile(
-         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
          : "=r"(done)
-         : "r"(b), "r"(parity)
+         : "r"(b), "r"(parity), "r"(1000u)
          : "memory");
       if (done) return true;
+      uint64_t now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > 2000000000ull) return false;
    }
    return false;
 }

@@ -18,6 +18,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <stdexcept>
+#include <string>
 
 #include "device.h"
 #include "mutations_common.cuh"
@@ -25,6 +27,13 @@
 namespace rhygpu {
 
 namespace {
+
+// Testing the failure path of the bounded waits: when set (on the current device), every CTA of the
+// container pass announces the bytes of its first unit's copy on its barrier but never issues the
+// copy, so its wait gives up (after 1 ms) and the call reports error 7. No copy is left in
+// flight: the withheld copy never starts and the CTA waits for its other copy before it returns.
+// Off by default; set only through set_copy_withholding.
+__device__ uint32_t g_withhold_first_copy = 0;
 
 constexpr uint32_t MT = 256;
 constexpr uint32_t NW = MT / 32;
@@ -91,6 +100,8 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint16_t* __restrict__ payload = cs->payload;
    const uint32_t L = cs->L, tid = threadIdx.x;
+   const bool withhold = *static_cast<volatile uint32_t*>(&g_withhold_first_copy) != 0;
+   const uint64_t wait_limit = withhold ? WAIT_LIMIT_TEST_NS : WAIT_LIMIT_NS;
    uint32_t* F = reinterpret_cast<uint32_t*>(sm4 + 2 * BUF4);
    if (tid == 0) {
       mbar_init(&bar[0]);
@@ -111,7 +122,10 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
    {
       const StreamUnit U = unit(u0);
       if (copies(U)) {
-         if (tid == 0) issue(U, 0);
+         if (tid == 0) {
+            if (withhold) mbar_expect(&bar[0], 16u);  // announced, never issued: the wait gives up
+            else issue(U, 0);
+         }
          ++issued0;
       }
    }
@@ -133,7 +147,7 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
             else ++issued1;
          }
       }
-      if (copies(U)) ok = mbar_wait(&bar[b], ((b ? issued1 : issued0) - 1u) & 1u);
+      if (copies(U)) ok = mbar_wait(&bar[b], ((b ? issued1 : issued0) - 1u) & 1u, wait_limit);
       if (!__syncthreads_and(ok)) {
          ok = false;  // in every thread: the cleanup below has a barrier
          if (tid == 0) atomicExch(err, 7);
@@ -225,8 +239,8 @@ __global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __res
    }
    if (!ok) {  // let the copies still in flight land before the CTA's shared memory is released
       if (tid == 0) {
-         if (issued0) mbar_wait(&bar[0], (issued0 - 1u) & 1u);
-         if (issued1) mbar_wait(&bar[1], (issued1 - 1u) & 1u);
+         if (issued0) mbar_wait(&bar[0], (issued0 - 1u) & 1u, wait_limit);
+         if (issued1) mbar_wait(&bar[1], (issued1 - 1u) & 1u, wait_limit);
       }
       __syncthreads();
    }
@@ -333,6 +347,12 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __re
 }
 
 }  // namespace
+
+void set_copy_withholding(bool on) {
+   const uint32_t v = on ? 1u : 0u;
+   const cudaError_t e = cudaMemcpyToSymbol(g_withhold_first_copy, &v, sizeof(v));
+   if (e != cudaSuccess) throw std::runtime_error(std::string("set_copy_withholding: ") + cudaGetErrorString(e));
+}
 
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,

@@ -32,17 +32,35 @@ __device__ __forceinline__ void bulk_copy_g2s_tx(void* smem, const void* gmem, u
                 : "memory");
 }
 
-// Waits (bounded) for the phase with the given parity to complete. Returns false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ uint64_t global_ns() {
+   uint64_t t;
+   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+   return t;
+}
+
+// Limits of the bounded waits for bulk copies: normally 2 s (a copy lands in microseconds), 1 ms
+// while a test withholds copies on purpose.
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
+constexpr uint64_t WAIT_LIMIT_TEST_NS = 1000000ull;
+
+// Waits for the phase with the given parity to complete, bounded by time (limit_ns on the global
+// timer) and, as a second bound, by 2^26 polls of at most about 1 us each. Returns false if it gave
+// up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = WAIT_LIMIT_NS) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
-   for (uint32_t i = 0; i < (1u << 22); ++i) {
+   uint64_t t0 = 0;
+   for (uint32_t i = 0; i < (1u << 26); ++i) {
       uint32_t done;
       asm volatile(
-         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
          : "=r"(done)
-         : "r"(b), "r"(parity)
+         : "r"(b), "r"(parity), "r"(1000u)
          : "memory");
       if (done) return true;
+      const uint64_t now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > limit_ns) return false;
    }
    return false;
 }
