@@ -15,6 +15,10 @@
  *   rhy_mutations        calculateMutationsPerPosition
  *                        (src/rhydb/query_engine/operators/mutations_node.cpp:269-288);
  *   rhy_mutation_rows    addMutationsToOutput (mutations_node.cpp:292-366);
+ *   rhy_program_eval /
+ *   rhy_program_count /
+ *   rhy_program_mutations the same over an already compiled operator tree
+ *                        (src/rhydb/query_engine/filter/operators/operator.h:32);
  *   rhy_count_batch /
  *   rhy_mutations_batch  many queries per launch (no reference counterpart: the reference runs one
  *                        query per worker thread, app/src/api.cpp:39-51).
@@ -167,6 +171,78 @@ int rhy_count(RhyDevice* d, const char* expr, void* stream, uint64_t* out);
 int rhy_eval(RhyDevice* d, const char* expr, void* stream, uint32_t* out_bits, uint64_t* out_count);
 /* counts: n_symbols * L words, counts[symbol * L + position]; filter_count may be NULL. */
 int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream, uint32_t* counts, uint64_t* filter_count);
+/* ---- compiled operator trees (the reference's Operator::evaluate() -> CopyOnWriteBitmap,
+ * src/rhydb/query_engine/filter/operators/operator.h:32, and the actions consuming it) ----
+ * A caller that has compiled a filter into the reference's operator tree passes it as a postorder
+ * node list (children before their parent), each node popping its n_children operands. Node kinds
+ * follow the reference's Operator types (operator.h:11-22):
+ *   RHY_NODE_EMPTY / RHY_NODE_FULL        Empty, Full (every row of each chunk)
+ *   RHY_NODE_SCAN_SEQ     IndexScan over a sequence column's containers: column, position (0-based),
+ *                         symbols (bit s = symbol s in the column's alphabet order; the result is the
+ *                         union of the rows holding one of them, as getMatchingContainerViews)
+ *   RHY_NODE_SCAN_NULLS   IndexScan of the null rows of a sequence column: column
+ *   RHY_NODE_SCAN_DICT    IndexScan of a dictionary column's inverted index: column, value (id)
+ *   RHY_NODE_SCAN_ROWS    IndexScan over a row set the caller passes: value = its index in row_sets
+ *                         (any CopyOnWriteBitmap, e.g. of an index the device does not hold)
+ *   RHY_NODE_INTERSECTION Intersection: n_children operands, the last n_negated of them negated
+ *   RHY_NODE_UNION        Union: n_children operands (none: the empty set)
+ *   RHY_NODE_COMPLEMENT   Complement within each chunk's rows: one operand
+ *   RHY_NODE_THRESHOLD    Threshold: value = number_of_matchers, flags & 1 = match exactly;
+ *                         n_children operands, the last n_negated of them negated
+ *   RHY_NODE_SELECTION    Selection: n_children operands = its predicates and at most one child
+ *   RHY_NODE_PRED_COVERED predicate IsInCoveredRegion: column, position, flags & 1 = IS_NOT_COVERED
+ *   RHY_NODE_PRED_DATE    predicate CompareToValueSelection on a date column: column, date (days
+ *                         since 1970-01-01), flags & 7 = comparator (0 ==, 1 !=, 2 <, 3 <=, 4 >, 5 >=),
+ *                         flags & 8 = null dates match
+ * The reference's constructor checks apply (Intersection needs a non-negated child and two
+ * children, Threshold 0 < n < children): they and malformed lists return RHY_COMPILATION; unknown
+ * columns, positions, symbols or value ids RHY_ILLEGAL_QUERY. RangeSelection is passed as a row set.
+ * Row sets are dense bitmaps of n_chunks * 2048 words in host memory with no bit at or above the
+ * table's row count. */
+enum {
+   RHY_NODE_EMPTY = 0,
+   RHY_NODE_FULL = 1,
+   RHY_NODE_SCAN_SEQ = 2,
+   RHY_NODE_SCAN_NULLS = 3,
+   RHY_NODE_SCAN_DICT = 4,
+   RHY_NODE_SCAN_ROWS = 5,
+   RHY_NODE_INTERSECTION = 6,
+   RHY_NODE_UNION = 7,
+   RHY_NODE_COMPLEMENT = 8,
+   RHY_NODE_THRESHOLD = 9,
+   RHY_NODE_SELECTION = 10,
+   RHY_NODE_PRED_COVERED = 11,
+   RHY_NODE_PRED_DATE = 12
+};
+typedef struct {
+   uint32_t kind;
+   uint32_t n_children;
+   uint32_t n_negated;
+   uint32_t column;
+   uint32_t position;
+   uint32_t symbols;
+   uint32_t value;
+   uint32_t flags;
+   int32_t date;
+   uint32_t reserved;
+} RhyOpNode;
+typedef struct {
+   const RhyOpNode* nodes;
+   uint32_t n_nodes;
+   uint32_t n_row_sets;
+   const uint32_t* const* row_sets;
+} RhyOpProgram;
+/* The operator tree of rewrite(NONE) + compile of an expression as a node list (host only; the
+ * same tree rhy_plan prints). *n receives the node count; the first min(cap, *n) are copied.
+ * Expressions holding a MutationProfile have no node form (RHY_INVALID_ARGUMENT). */
+int rhy_program_from_expr(const RhyTable* t, const char* expr, RhyOpNode* nodes, size_t cap, size_t* n);
+/* Operator::evaluate (operator.h:32) -> dense row set and its cardinality (out_bits may be NULL). */
+int rhy_program_eval(RhyDevice* d, const RhyOpProgram* prog, void* stream, uint32_t* out_bits, uint64_t* out_count);
+/* CountFilterNode over an operator tree (count_filter_node.cpp:35-71). */
+int rhy_program_count(RhyDevice* d, const RhyOpProgram* prog, void* stream, uint64_t* out);
+/* calculateMutationsPerPosition over an operator tree's row set (mutations_node.cpp:269-288). */
+int rhy_program_mutations(RhyDevice* d, const RhyOpProgram* prog, uint32_t column, void* stream, uint32_t* counts,
+                          uint64_t* filter_count);
 /* Grouped counts of the filter's rows (replaces BitmapAggregationNode, reference
  * bitmap_aggregation_node.cpp:51-140): one dimension per sequence position (kind 0: column,
  * 1-based position; groups = the column's symbols in alphabet order, then null rows) or dictionary
@@ -276,16 +352,28 @@ int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_by
  * host memory). For callers that may not allocate during a query: a process whose device memory
  * is owned by its own pool allocator, or a latency-critical thread that must avoid the implicit
  * synchronisation of cudaMalloc / cudaFree. The caller passes device buffers it owns: the filter
- * row set (n_chunks * 2048 words, as written by the filter kernels), its cardinality, and the
- * output counts (n_symbols * L words, counts[symbol * L + position], overwritten). Working memory
- * is one fixed array in the library's device image (1.5 MiB, held on every GPU that loads the
- * library until the process exits), which limits the column to 131,072 positions; longer columns
- * fail with RHY_INVALID_ARGUMENT. The first call on a device looks up the array's address; make
- * that first call before any stream capture. All calls on a device share the array: calls that
- * overlap on the GPU race and must be serialised by the caller. The work is enqueued on `stream`
- * (NULL = the handle's stream); results are valid once that stream has been synchronised. */
+ * row set (n_chunks * 2048 words, as written by the filter kernels), its cardinality, the output
+ * counts (n_symbols * L words, counts[symbol * L + position], overwritten) and one int of status,
+ * which the call sets to 0 and the kernels set to a nonzero device error code if one of their
+ * bounded waits for bulk copies gave up (7: the counts are then incomplete). Read it after
+ * synchronising the stream. Working memory is one fixed array in the library's device image
+ * (1.5 MiB, held on every GPU that loads the library until the process exits), which limits the
+ * column to 131,072 positions; longer columns fail with RHY_INVALID_ARGUMENT. The first call on a
+ * device looks up the array's address; make that first call before any stream capture. All calls
+ * on a device share the array: calls that overlap on the GPU race and must be serialised by the
+ * caller. The enqueue itself is ordered with the handle's other calls. Filters of at most
+ * rhy_sparse_rows' single-query limit take the row-index pass, as in rhy_mutations. The work is
+ * enqueued on `stream` (NULL = the handle's stream); results are valid once that stream has been
+ * synchronised. */
 int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filter, const uint64_t* d_filter_count,
-                          uint32_t* d_counts, void* stream);
+                          uint32_t* d_counts, int* d_status, void* stream);
+/* Testing the failure path of the bounded device waits (no counterpart in the reference): while on
+ * (on = 1), every CTA of the Mutations container pass withholds the bulk copy its first wait
+ * expects, so that wait gives up after a short limit and the call reports device error 7
+ * (RHY_CUDA from rhy_mutations, the status word of rhy_mutations_noalloc). The withheld copy is
+ * never issued, so no copy is left in flight and the device stays usable. Synchronises the device;
+ * off (0) by default. Not for production use. */
+int rhy_test_withhold_copies(RhyDevice* d, int on);
 
 /* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */
 int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,

@@ -16,6 +16,7 @@
 #include "server.h"
 #include "expr.h"
 #include "noalloc.h"
+#include "op_program.h"
 #include "table.h"
 
 struct RhyTable {
@@ -425,6 +426,90 @@ int rhy_mutations(RhyDevice* d, const char* expr, uint32_t column, void* stream,
    });
 }
 
+namespace {
+
+// A caller's operator tree lowered to a device program, with its row sets (op_program.h).
+struct ProgramCall {
+   rhygpu::Program prog;
+   std::vector<const uint32_t*> sets;
+};
+
+ProgramCall plan_program(const RhyTable& table, const RhyOpProgram* prog) {
+   need(prog, "program");
+   if (prog->n_nodes) need(prog->nodes, "program nodes");
+   if (prog->n_row_sets) need(prog->row_sets, "program row sets");
+   const rhygpu::TableImage& t = table.image;
+   ProgramCall call;
+   std::vector<double> cards(prog->n_row_sets);
+   for (uint32_t k = 0; k < prog->n_row_sets; ++k) {
+      const uint32_t* rs = prog->row_sets[k];
+      need(rs, "row set");
+      uint64_t c = 0;
+      for (uint32_t v = 0; v < t.nchunks(); ++v) {
+         const uint32_t* w = rs + static_cast<size_t>(v) * rhygpu::CHUNK_WORDS;
+         const uint32_t rows = t.chunk_sizes[v];
+         for (uint32_t i = rows / 32; i < rhygpu::CHUNK_WORDS; ++i) {
+            const uint32_t keep = i == rows / 32 ? (rows % 32 ? (1u << (rows % 32)) - 1u : 0u) : 0u;
+            if (w[i] & ~keep)
+               throw std::invalid_argument("row set " + std::to_string(k) + " holds rows beyond chunk " + std::to_string(v) +
+                                           "'s " + std::to_string(rows) + " rows");
+         }
+         for (uint32_t i = 0; i < rhygpu::CHUNK_WORDS; ++i) c += static_cast<uint64_t>(__builtin_popcount(w[i]));
+      }
+      cards[k] = static_cast<double>(c);
+      call.sets.push_back(rs);
+   }
+   const rhygpu::OpPtr op = rhygpu::op_from_nodes(prog->nodes, prog->n_nodes, t, cards);
+   rhygpu::LowerOptions o;
+   o.rows = t.n_rows;
+   call.prog = rhygpu::lower(*op, rhygpu::rule_estimator(t), o);
+   return call;
+}
+
+}  // namespace
+
+int rhy_program_from_expr(const RhyTable* t, const char* expr, RhyOpNode* nodes, size_t cap, size_t* n) {
+   return guarded([&] {
+      need(t, "table");
+      need(expr, "expr");
+      need(n, "n");
+      const rhygpu::OpPtr op = rhygpu::compile_filter(expr, t->image);
+      std::vector<RhyOpNode> out;
+      rhygpu::op_to_nodes(*op, out);
+      *n = out.size();
+      if (nodes) std::memcpy(nodes, out.data(), std::min(cap, out.size()) * sizeof(RhyOpNode));
+   });
+}
+
+int rhy_program_eval(RhyDevice* d, const RhyOpProgram* prog, void* stream, uint32_t* out_bits, uint64_t* out_count) {
+   return guarded([&] {
+      need(d, "device");
+      const ProgramCall c = plan_program(*d->table, prog);
+      d->engine->eval(c.prog, out_bits, out_count, static_cast<cudaStream_t>(stream), c.sets.data());
+   });
+}
+
+int rhy_program_count(RhyDevice* d, const RhyOpProgram* prog, void* stream, uint64_t* out) {
+   return guarded([&] {
+      need(d, "device");
+      need(out, "out");
+      const ProgramCall c = plan_program(*d->table, prog);
+      *out = d->engine->count(c.prog, static_cast<cudaStream_t>(stream), c.sets.data());
+   });
+}
+
+int rhy_program_mutations(RhyDevice* d, const RhyOpProgram* prog, uint32_t column, void* stream, uint32_t* counts,
+                          uint64_t* filter_count) {
+   return guarded([&] {
+      need(d, "device");
+      need(counts, "counts");
+      if (column >= d->table->image.seq.size()) throw std::invalid_argument("no such sequence column");
+      const ProgramCall c = plan_program(*d->table, prog);
+      d->engine->mutations(c.prog, static_cast<int>(column), counts, filter_count, static_cast<cudaStream_t>(stream),
+                           c.sets.data());
+   });
+}
+
 int rhy_aggregate(RhyDevice* d, const char* expr, const RhyAggDimension* dims, uint32_t n_dims, void* stream,
                   int32_t* groups, uint64_t* counts, size_t cap, size_t* n_out, uint64_t* filter_count) {
    return guarded([&] {
@@ -732,12 +817,22 @@ int rhy_batch_launch_parts(RhyDevice* d, void* stream, uint32_t parts) {
 }
 
 int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filter, const uint64_t* d_filter_count,
-                          uint32_t* d_counts, void* stream) {
+                          uint32_t* d_counts, int* d_status, void* stream) {
    return guarded([&] {
       need(d, "device");
       rhygpu::mutations_noalloc(*d->engine, column, d_filter,
-                                reinterpret_cast<const unsigned long long*>(d_filter_count), d_counts,
+                                reinterpret_cast<const unsigned long long*>(d_filter_count), d_counts, d_status,
                                 static_cast<cudaStream_t>(stream));
+   });
+}
+
+int rhy_test_withhold_copies(RhyDevice* d, int on) {
+   return guarded([&] {
+      need(d, "device");
+      std::lock_guard<std::mutex> lock(d->engine->mu);
+      rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
+      rhygpu::cuda_check(cudaDeviceSynchronize(), "synchronise before switching copy withholding");
+      rhygpu::set_copy_withholding(on != 0);
    });
 }
 

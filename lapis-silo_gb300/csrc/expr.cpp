@@ -920,6 +920,7 @@ std::string Op::to_string() const {
       }
       case OpT::PROFILE:
          return "Profile(" + std::to_string(profile->col) + ",<=" + std::to_string(profile->distance) + ")";
+      case OpT::ROWS: return "Rows(" + std::to_string(rows_index) + ")";
    }
    return "?";
 }
@@ -968,6 +969,7 @@ double rule_node_estimate(const Op& op, const TableImage& t, const std::function
       case OpT::PROFILE:
          // no statistics of the profile distances: an even chance
          return 0.5 * rows;
+      case OpT::ROWS: return op.rows_card;
       case OpT::THRESHOLD: {
          // Poisson-binomial distribution of the number of matching children.
          std::vector<double> dist(1, 1.0);
@@ -1234,6 +1236,13 @@ struct Lowerer {
             push();
             ++prog.n_leaves;
             return;
+         case OpT::ROWS:
+            // numbered after the profiles once lowering is done (see lower)
+            emit(OP_PUSH_AUX, 0, AUX_LITERAL, op.rows_index);
+            prog.n_literals = std::max(prog.n_literals, op.rows_index + 1);
+            push();
+            ++prog.n_leaves;
+            return;
       }
    }
 };
@@ -1244,6 +1253,9 @@ Program lower(const Op& op, const Estimator& est, const LowerOptions& opt) {
    Lowerer l{est, opt, {}, 0};
    l.node(op);
    if (l.depth != 1) throw CompilationError("internal error: unbalanced filter program");
+   // caller row sets follow the MutationProfile row sets in the aux area
+   for (Instr& in : l.prog.code)
+      if (in.op == OP_PUSH_AUX && (in.flags & AUX_LITERAL)) in.a += static_cast<uint32_t>(l.prog.aux.size());
    return std::move(l.prog);
 }
 

@@ -67,7 +67,10 @@ ExprPtr parse_expression(const std::string& text, const TableImage& table);
 // ---------------------------------------------------------------------------------------------
 // Operator trees
 
-enum class OpT : uint8_t { EMPTY, FULL, INDEX_SCAN, INTERSECTION, UNION, COMPLEMENT, THRESHOLD, SELECTION, PROFILE };
+// ROWS: an IndexScan over a row set the caller supplies with the operator tree (the reference's
+// IndexScan over any CopyOnWriteBitmap, e.g. a column index the device does not hold).
+enum class OpT : uint8_t { EMPTY, FULL, INDEX_SCAN, INTERSECTION, UNION, COMPLEMENT, THRESHOLD, SELECTION, PROFILE,
+                           ROWS };
 
 // A MutationProfile as one operator: the rows with at most `distance` positions whose symbol is
 // not compatible with the profile's symbol there, which is the row set of the reference's rewrite
@@ -118,6 +121,8 @@ struct Op {
    int n = 0;                    // THRESHOLD
    bool exact = false;           // THRESHOLD
    std::shared_ptr<const ProfileSpec> profile;  // PROFILE
+   uint32_t rows_index = 0;                     // ROWS: index of the caller's row set
+   double rows_card = 0;                        // ROWS: its cardinality (estimates only)
    std::string to_string() const;
 };
 
@@ -148,6 +153,9 @@ struct Program {
    uint32_t n_cov_leaves = 0;  // PUSH_COVERED leaves, numbered 1.. in their c field
    // row sets computed before the program runs (PUSH_AUX leaves, numbered 0.. in their a field)
    std::vector<std::shared_ptr<const ProfileSpec>> aux;
+   // caller row sets read by ROWS leaves: PUSH_AUX leaves numbered aux.size() + the caller's index;
+   // the program reads the caller's sets 0 .. n_literals - 1
+   uint32_t n_literals = 0;
 };
 
 struct LowerOptions {

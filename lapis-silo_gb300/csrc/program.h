@@ -31,8 +31,11 @@ enum OpCode : uint8_t {
    OP_THR_END = 13,      // a = planes, b = n, flags&1 = exactly: pop planes, push count >= n (== n)
    OP_JZ = 14,           // a = target: jump if the top tile is all zero
    OP_JFULL = 15,        // a = target: jump if the top tile holds every valid row
-   OP_PUSH_AUX = 16,     // a = index of a row set computed before the program (a MutationProfile)
+   OP_PUSH_AUX = 16,     // a = index of a row set computed (a MutationProfile) or uploaded (a caller's row
+                         // set, flags & AUX_LITERAL) before the program runs
 };
+
+constexpr uint16_t AUX_LITERAL = 1;  // PUSH_AUX of a caller's row set
 
 // Comparators of the date predicate (reference: src/rhydb/query_engine/filter/operators/selection.h:40-72).
 enum CmpCode : uint32_t { CMP_EQ = 0, CMP_NE = 1, CMP_LT = 2, CMP_LE = 3, CMP_GT = 4, CMP_GE = 5 };

@@ -73,6 +73,32 @@ class AggDimension(C.Structure):
     _fields_ = [("kind", C.c_int), ("column", C.c_uint32), ("position", C.c_uint32)]
 
 
+class OpNode(C.Structure):
+    """One node of a compiled operator tree in postorder (RhyOpNode)."""
+    _fields_ = [("kind", C.c_uint32), ("n_children", C.c_uint32), ("n_negated", C.c_uint32), ("column", C.c_uint32),
+                ("position", C.c_uint32), ("symbols", C.c_uint32), ("value", C.c_uint32), ("flags", C.c_uint32),
+                ("date", C.c_int32), ("reserved", C.c_uint32)]
+
+
+class OpProgram(C.Structure):
+    _fields_ = [("nodes", C.POINTER(OpNode)), ("n_nodes", C.c_uint32), ("n_row_sets", C.c_uint32),
+                ("row_sets", C.POINTER(C.c_void_p))]
+
+
+# node kinds of the operator-tree entry points (the reference's Operator types)
+NODE_EMPTY, NODE_FULL, NODE_SCAN_SEQ, NODE_SCAN_NULLS, NODE_SCAN_DICT, NODE_SCAN_ROWS = range(6)
+NODE_INTERSECTION, NODE_UNION, NODE_COMPLEMENT, NODE_THRESHOLD, NODE_SELECTION = range(6, 11)
+NODE_PRED_COVERED, NODE_PRED_DATE = 11, 12
+
+
+def op_node(kind: int, **fields) -> OpNode:
+    nd = OpNode()
+    nd.kind = kind
+    for k, v in fields.items():
+        setattr(nd, k, v)
+    return nd
+
+
 class BatchSchedule(C.Structure):
     _fields_ = [("max_tile_bits", C.c_uint32), ("stack_kb", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("query_major", C.c_uint32)]
@@ -178,6 +204,10 @@ def lib():
         "rhy_count": (I, [P, C.c_char_p, P, C.POINTER(U64)]),
         "rhy_eval": (I, [P, C.c_char_p, P, P, C.POINTER(U64)]),
         "rhy_mutations": (I, [P, C.c_char_p, U32, P, P, C.POINTER(U64)]),
+        "rhy_program_from_expr": (I, [P, C.c_char_p, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_program_eval": (I, [P, P, P, P, C.POINTER(U64)]),
+        "rhy_program_count": (I, [P, P, P, C.POINTER(U64)]),
+        "rhy_program_mutations": (I, [P, P, U32, P, P, C.POINTER(U64)]),
         "rhy_mutation_rows": (I, [P, U32, P, C.c_double, C.POINTER(MutationRow), C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_batch": (I, [P, P, P, P, U32, U32, P, P, P]),
         "rhy_batch_rows": (I, [P, P, P, P, P, U32, U32, P, P, P, C.c_size_t, P, P, C.POINTER(C.c_size_t)]),
@@ -200,7 +230,8 @@ def lib():
         "rhy_mutation_bytes": (I, [P, U32, C.POINTER(U64), C.POINTER(U64)]),
         "rhy_batch_capture_ex": (I, [P, P, I, I]),
         "rhy_batch_launch_parts": (I, [P, P, U32]),
-        "rhy_mutations_noalloc": (I, [P, U32, P, P, P, P]),
+        "rhy_mutations_noalloc": (I, [P, U32, P, P, P, P, P]),
+        "rhy_test_withhold_copies": (I, [P, I]),
         "rhy_plan_features": (I, [P, C.c_char_p, P, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_planner_collect": (I, [P, P, U32, C.POINTER(C.c_size_t)]),
         "rhy_planner_train": (I, [P, U32, U32, C.c_float, U64, C.POINTER(PlannerStats)]),
@@ -358,6 +389,14 @@ class Table:
         _check(lib().rhy_plan(self._h, expr.encode(), buf, 1 << 20, C.byref(n), C.byref(d)))
         return buf.value.decode(), n.value, d.value
 
+    def program(self, expr: str) -> list:
+        """The compiled operator tree of an expression as postorder OpNodes (rhy_program_from_expr)."""
+        n = C.c_size_t()
+        _check(lib().rhy_program_from_expr(self._h, expr.encode(), None, 0, C.byref(n)))
+        nodes = (OpNode * max(1, n.value))()
+        _check(lib().rhy_program_from_expr(self._h, expr.encode(), nodes, n.value, C.byref(n)))
+        return list(nodes[: n.value])
+
     def plan_features(self, expr: str) -> np.ndarray:
         """Planner features of every operator node of the compiled expression (preorder)."""
         n = C.c_size_t()
@@ -422,6 +461,37 @@ class Device:
         _check(lib().rhy_mutations(self._h, expr.encode(), column, stream, _ptr(counts), C.byref(v)))
         return counts, v.value
 
+    # ---- compiled operator trees (Operator::evaluate and the actions over it) ----
+    def _program(self, nodes, row_sets):
+        arr = (OpNode * max(1, len(nodes)))(*nodes)
+        sets = [np.ascontiguousarray(r, dtype=np.uint32) for r in (row_sets or [])]
+        for r in sets:
+            if r.size != self.table.n_chunks * CHUNK_WORDS:
+                raise ValueError("a row set has n_chunks * 2048 words")
+        ptrs = (C.c_void_p * max(1, len(sets)))(*[r.ctypes.data for r in sets])
+        prog = OpProgram(C.cast(arr, C.POINTER(OpNode)), len(nodes), len(sets), C.cast(ptrs, C.POINTER(C.c_void_p)))
+        return prog, (arr, sets, ptrs)
+
+    def program_eval(self, nodes, row_sets=None, stream=None) -> tuple[np.ndarray, int]:
+        prog, keep = self._program(nodes, row_sets)
+        bits = np.zeros(self.table.n_chunks * CHUNK_WORDS, dtype=np.uint32)
+        v = C.c_uint64()
+        _check(lib().rhy_program_eval(self._h, C.byref(prog), stream, _ptr(bits), C.byref(v)))
+        return bits, v.value
+
+    def program_count(self, nodes, row_sets=None, stream=None) -> int:
+        prog, keep = self._program(nodes, row_sets)
+        v = C.c_uint64()
+        _check(lib().rhy_program_count(self._h, C.byref(prog), stream, C.byref(v)))
+        return v.value
+
+    def program_mutations(self, nodes, column: int = 0, row_sets=None, stream=None) -> tuple[np.ndarray, int]:
+        prog, keep = self._program(nodes, row_sets)
+        col = self.table.columns[column]
+        counts = np.zeros((col.n_symbols, col.L), dtype=np.uint32)
+        v = C.c_uint64()
+        _check(lib().rhy_program_mutations(self._h, C.byref(prog), column, stream, _ptr(counts), C.byref(v)))
+        return counts, v.value
 
     # ---- batched path ----
     @staticmethod
@@ -594,11 +664,18 @@ class Device:
     def batch_launch_parts(self, parts: int, stream=None):
         _check(lib().rhy_batch_launch_parts(self._h, stream, parts))
 
-    def mutations_noalloc(self, column: int, d_filter: int, d_filter_count: int, d_counts: int, stream=None):
+    def mutations_noalloc(self, column: int, d_filter: int, d_filter_count: int, d_counts: int, d_status: int,
+                          stream=None):
         """Mutations pass over caller-owned device buffers (addresses as ints); allocates nothing.
-        Enqueued on `stream`; synchronise it before reading d_counts."""
+        Enqueued on `stream`; synchronise it before reading d_counts and the int at d_status (0, or
+        the device error code of a bounded wait that gave up)."""
         _check(lib().rhy_mutations_noalloc(self._h, column, C.c_void_p(d_filter), C.c_void_p(d_filter_count),
-                                           C.c_void_p(d_counts), stream))
+                                           C.c_void_p(d_counts), C.c_void_p(d_status), stream))
+
+    def test_withhold_copies(self, on: bool):
+        """Testing only: the Mutations container pass withholds one bulk copy per CTA, so its bounded
+        wait gives up and the call reports device error 7 (nothing is left in flight)."""
+        _check(lib().rhy_test_withhold_copies(self._h, int(on)))
 
     # ---- learned planner ----
     def planner_collect(self, exprs) -> int:
@@ -753,3 +830,10 @@ def bits_to_rows(bits: np.ndarray) -> np.ndarray:
     """Global row ids (chunk << 16 | row) of a dense row-set bitmap."""
     b = np.unpackbits(bits.view(np.uint8), bitorder="little")
     return np.flatnonzero(b).astype(np.uint32)
+
+
+def rows_to_bits(rows, n_chunks: int) -> np.ndarray:
+    """Dense row-set bitmap (n_chunks * 2048 uint32 words) of global row ids."""
+    b = np.zeros(n_chunks * CHUNK_ROWS, np.uint8)
+    b[np.asarray(list(rows), dtype=np.int64)] = 1
+    return np.packbits(b, bitorder="little").view(np.uint32).copy()

@@ -35,6 +35,7 @@
 #include <iterator>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <optional>
 #include <stdexcept>
 #include <string>
@@ -1910,6 +1911,39 @@ int oracle_run_batch(void* t, const char* const* exprs, const int* action, const
       for (auto& th : pool) th.join();
       *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
       if (failed) throw std::runtime_error("a query failed in the batch");
+   });
+}
+
+// Many queries on `threads` worker threads (the checker of large parity runs): counts[i] receives
+// the filter cardinality of query i; for every i with tables[i] != NULL the Mutations counts of
+// column[i] (n_symbols * L words, counts[symbol * L + position]) are written there.
+int oracle_check_batch(void* t, const char* const* exprs, const uint32_t* column, uint32_t n, uint32_t threads,
+                       uint64_t* counts, uint32_t* const* tables) {
+   return guard([&] {
+      const Table& tab = *static_cast<Table*>(t);
+      std::atomic<uint32_t> next{0};
+      std::atomic<int> failed{0};
+      std::string first_error;
+      std::mutex err_mu;
+      auto body = [&]() {
+         for (uint32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+            try {
+               const RowSet r = compute_filter(tab, exprs[i]);
+               counts[i] = r.cardinality();
+               if (tables && tables[i]) {
+                  const auto c = mutation_counts(tab.seq.at(column[i]), r, tab.layout.num_rows);
+                  std::copy(c.begin(), c.end(), tables[i]);
+               }
+            } catch (const std::exception& e) {
+               std::lock_guard<std::mutex> lock(err_mu);
+               if (!failed.exchange(1)) first_error = std::string(exprs[i]) + ": " + e.what();
+            }
+         }
+      };
+      std::vector<std::thread> pool;
+      for (uint32_t k = 0; k < std::max(1u, threads); ++k) pool.emplace_back(body);
+      for (auto& th : pool) th.join();
+      if (failed) throw std::runtime_error("a query failed: " + first_error);
    });
 }
 

@@ -40,6 +40,7 @@ def lib():
                                        P, C.POINTER(SZ), SZ]),
             "oracle_operator": (I, [I, P, U32, P, P, U32, U32, U32, I, P, SZ, C.POINTER(SZ)]),
             "oracle_run_batch": (I, [P, P, P, P, U32, U32, P, P, C.POINTER(D)]),
+            "oracle_check_batch": (I, [P, P, P, U32, U32, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -154,6 +155,25 @@ class Oracle:
         _check(lib().oracle_run_batch(self._h, C.cast(arr, C.c_void_p), _p(act), _p(col), n, threads, _p(out),
                                       _p(ms), C.byref(secs)))
         return secs.value, ms, out
+
+    def check_batch(self, exprs, columns=None, tables=None, threads: int = 0):
+        """Counts of every expression and, for the indices in `tables`, the Mutations counts of
+        columns[i], on `threads` worker threads (0: all cores). Returns (counts, {i: table})."""
+        import os
+
+        n = len(exprs)
+        columns = np.zeros(n, np.uint32) if columns is None else np.asarray(columns, np.uint32)
+        arr = (C.c_char_p * n)(*[e.encode() for e in exprs])
+        counts = np.zeros(n, np.uint64)
+        out = {}
+        ptrs = (C.c_void_p * n)()
+        for i in tables or ():
+            _, nsym, L = self.columns[int(columns[i])]
+            out[int(i)] = np.zeros((nsym, L), np.uint32)
+            ptrs[int(i)] = out[int(i)].ctypes.data
+        _check(lib().oracle_check_batch(self._h, C.cast(arr, C.c_void_p), _p(columns), n,
+                                        threads or (os.cpu_count() or 1), _p(counts), C.cast(ptrs, C.c_void_p)))
+        return counts, out
 
 
 def diff_string(kind: int, seq: str, ref: str):
