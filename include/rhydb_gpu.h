@@ -236,6 +236,10 @@ typedef struct {
  * same tree rhy_plan prints). *n receives the node count; the first min(cap, *n) are copied.
  * Expressions holding a MutationProfile have no node form (RHY_INVALID_ARGUMENT). */
 int rhy_program_from_expr(const RhyTable* t, const char* expr, RhyOpNode* nodes, size_t cap, size_t* n);
+/* Checks and lowers an operator tree on the host (no device needed): the tree as rhy_plan prints
+ * it, the device program length and its stack depth. Fails as the evaluating calls would. */
+int rhy_program_plan(const RhyTable* t, const RhyOpProgram* prog, char* tree_buf, size_t cap, uint32_t* n_instr,
+                     uint32_t* depth);
 /* Operator::evaluate (operator.h:32) -> dense row set and its cardinality (out_bits may be NULL). */
 int rhy_program_eval(RhyDevice* d, const RhyOpProgram* prog, void* stream, uint32_t* out_bits, uint64_t* out_count);
 /* CountFilterNode over an operator tree (count_filter_node.cpp:35-71). */

@@ -434,7 +434,7 @@ struct ProgramCall {
    std::vector<const uint32_t*> sets;
 };
 
-ProgramCall plan_program(const RhyTable& table, const RhyOpProgram* prog) {
+ProgramCall plan_program(const RhyTable& table, const RhyOpProgram* prog, std::string* tree = nullptr) {
    need(prog, "program");
    if (prog->n_nodes) need(prog->nodes, "program nodes");
    if (prog->n_row_sets) need(prog->row_sets, "program row sets");
@@ -460,6 +460,7 @@ ProgramCall plan_program(const RhyTable& table, const RhyOpProgram* prog) {
       call.sets.push_back(rs);
    }
    const rhygpu::OpPtr op = rhygpu::op_from_nodes(prog->nodes, prog->n_nodes, t, cards);
+   if (tree) *tree = op->to_string();
    rhygpu::LowerOptions o;
    o.rows = t.n_rows;
    call.prog = rhygpu::lower(*op, rhygpu::rule_estimator(t), o);
@@ -478,6 +479,21 @@ int rhy_program_from_expr(const RhyTable* t, const char* expr, RhyOpNode* nodes,
       rhygpu::op_to_nodes(*op, out);
       *n = out.size();
       if (nodes) std::memcpy(nodes, out.data(), std::min(cap, out.size()) * sizeof(RhyOpNode));
+   });
+}
+
+int rhy_program_plan(const RhyTable* t, const RhyOpProgram* prog, char* tree_buf, size_t cap, uint32_t* n_instr,
+                     uint32_t* depth) {
+   return guarded([&] {
+      need(t, "table");
+      std::string tree;
+      const ProgramCall c = plan_program(*t, prog, &tree);
+      if (tree_buf) {
+         if (cap < tree.size() + 1) throw std::invalid_argument("buffer too small");
+         std::memcpy(tree_buf, tree.c_str(), tree.size() + 1);
+      }
+      if (n_instr) *n_instr = static_cast<uint32_t>(c.prog.code.size());
+      if (depth) *depth = c.prog.max_depth;
    });
 }
 

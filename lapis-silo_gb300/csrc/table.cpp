@@ -198,7 +198,10 @@ void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<
       uint32_t cursor = 0;
       for (uint64_t k = b; k < e; ++k) {
          const int s = A.sym(raw.run_char[k]);
-         if (s < 0) throw std::invalid_argument(std::string("illegal character '") + raw.run_char[k] + "' in column " + raw.name);
+         if (s < 0)  // the reference's message (aligned_sequence.cpp:38-41), then where
+            throw std::invalid_argument(std::string("illegal character '") + raw.run_char[k] + "' at position " +
+                                        std::to_string(raw.run_pos[k]) + " in the input sequence (column " + raw.name +
+                                        ", row " + std::to_string(row) + ")");
          const uint32_t p0 = raw.run_pos[k], len = raw.run_len[k];
          if (len == 0 || p0 < cursor || static_cast<uint64_t>(p0) + len > L)
             throw std::invalid_argument("runs must be sorted, non-overlapping and inside the genome in column " + raw.name);

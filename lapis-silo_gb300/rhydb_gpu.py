@@ -205,6 +205,7 @@ def lib():
         "rhy_eval": (I, [P, C.c_char_p, P, P, C.POINTER(U64)]),
         "rhy_mutations": (I, [P, C.c_char_p, U32, P, P, C.POINTER(U64)]),
         "rhy_program_from_expr": (I, [P, C.c_char_p, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_program_plan": (I, [P, P, C.c_char_p, C.c_size_t, C.POINTER(U32), C.POINTER(U32)]),
         "rhy_program_eval": (I, [P, P, P, P, C.POINTER(U64)]),
         "rhy_program_count": (I, [P, P, P, C.POINTER(U64)]),
         "rhy_program_mutations": (I, [P, P, U32, P, P, C.POINTER(U64)]),
@@ -397,6 +398,14 @@ class Table:
         _check(lib().rhy_program_from_expr(self._h, expr.encode(), nodes, n.value, C.byref(n)))
         return list(nodes[: n.value])
 
+    def program_plan(self, nodes, row_sets=None) -> tuple[str, int, int]:
+        """Checks and lowers an operator tree on the host: its text, program length and stack depth."""
+        prog, keep = _op_program(self, nodes, row_sets)
+        buf = C.create_string_buffer(1 << 20)
+        n, d = C.c_uint32(), C.c_uint32()
+        _check(lib().rhy_program_plan(self._h, C.byref(prog), buf, 1 << 20, C.byref(n), C.byref(d)))
+        return buf.value.decode(), n.value, d.value
+
     def plan_features(self, expr: str) -> np.ndarray:
         """Planner features of every operator node of the compiled expression (preorder)."""
         n = C.c_size_t()
@@ -463,14 +472,7 @@ class Device:
 
     # ---- compiled operator trees (Operator::evaluate and the actions over it) ----
     def _program(self, nodes, row_sets):
-        arr = (OpNode * max(1, len(nodes)))(*nodes)
-        sets = [np.ascontiguousarray(r, dtype=np.uint32) for r in (row_sets or [])]
-        for r in sets:
-            if r.size != self.table.n_chunks * CHUNK_WORDS:
-                raise ValueError("a row set has n_chunks * 2048 words")
-        ptrs = (C.c_void_p * max(1, len(sets)))(*[r.ctypes.data for r in sets])
-        prog = OpProgram(C.cast(arr, C.POINTER(OpNode)), len(nodes), len(sets), C.cast(ptrs, C.POINTER(C.c_void_p)))
-        return prog, (arr, sets, ptrs)
+        return _op_program(self.table, nodes, row_sets)
 
     def program_eval(self, nodes, row_sets=None, stream=None) -> tuple[np.ndarray, int]:
         prog, keep = self._program(nodes, row_sets)
@@ -837,3 +839,15 @@ def rows_to_bits(rows, n_chunks: int) -> np.ndarray:
     b = np.zeros(n_chunks * CHUNK_ROWS, np.uint8)
     b[np.asarray(list(rows), dtype=np.int64)] = 1
     return np.packbits(b, bitorder="little").view(np.uint32).copy()
+
+
+def _op_program(table, nodes, row_sets):
+    """An OpProgram over ctypes arrays; the second value keeps the arrays alive."""
+    arr = (OpNode * max(1, len(nodes)))(*nodes)
+    sets = [np.ascontiguousarray(r, dtype=np.uint32) for r in (row_sets or [])]
+    for r in sets:
+        if r.size != table.n_chunks * CHUNK_WORDS:
+            raise ValueError("a row set has n_chunks * 2048 words")
+    ptrs = (C.c_void_p * max(1, len(sets)))(*[r.ctypes.data for r in sets])
+    prog = OpProgram(C.cast(arr, C.POINTER(OpNode)), len(nodes), len(sets), C.cast(ptrs, C.POINTER(C.c_void_p)))
+    return prog, (arr, sets, ptrs)

@@ -537,6 +537,11 @@ struct Diff {
    std::vector<std::pair<uint32_t, int>> mutations;
 };
 
+// The reference's message for a character outside the alphabet (aligned_sequence.cpp:38-41).
+std::string illegal_character(char c, size_t position) {
+   return std::string("illegal character '") + c + "' at position " + std::to_string(position) + " in the input sequence";
+}
+
 Diff diff_runs(const ORawSeqColumn& raw, const Alpha& A, const std::vector<int>& ref, uint32_t row, bool ref_has_missing) {
    Diff d;
    const uint32_t L = raw.L;
@@ -550,7 +555,7 @@ Diff diff_runs(const ORawSeqColumn& raw, const Alpha& A, const std::vector<int>&
    };
    for (uint64_t k = raw.row_off[row]; k < raw.row_off[row + 1]; ++k) {
       const int s = A.sym(raw.run_char[k]);
-      if (s < 0) throw std::invalid_argument("illegal character");
+      if (s < 0) throw std::invalid_argument(illegal_character(raw.run_char[k], raw.run_pos[k]));
       if (ref_has_missing) reference_gap(cursor, raw.run_pos[k]);
       for (uint32_t p = raw.run_pos[k]; p < raw.run_pos[k] + raw.run_len[k]; ++p) {
          if (s == A.missing) d.missing.push_back(p);
@@ -583,7 +588,7 @@ Diff diff_string(const std::string& seq, const std::string& refs, const Alpha& A
    const bool ref_missing = refs.find(A.chars[A.missing]) != std::string::npos;
    auto one = [&](size_t i) {
       const int s = A.sym(seq[i]);
-      if (s < 0) throw std::invalid_argument("illegal character");
+      if (s < 0) throw std::invalid_argument(illegal_character(seq[i], i));
       if (s == A.missing) d.missing.push_back(static_cast<uint32_t>(i));
       else if (s != A.sym(refs[i])) d.mutations.emplace_back(static_cast<uint32_t>(i), s);
    };
