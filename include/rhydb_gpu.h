@@ -304,6 +304,9 @@ typedef struct {
    uint32_t n_queries, n_mutation_slots, n_items, n_instr, max_depth, tile_bits, grid;
    uint64_t device_bytes;
    uint32_t n_filter_launches; /* persistent filter launches per batch (one for all program classes) */
+   uint64_t filter_bytes;      /* algorithmic bytes of the batch's filter programs: container payloads and
+                                  descriptors of their index-scan leaves, coverage and date data their
+                                  leaves read, and their outputs (row sets of Mutations queries, counts) */
 } RhyBatchInfo;
 
 /* Split form of rhy_batch for callers that reuse one batch shape: prepare plans and stages the

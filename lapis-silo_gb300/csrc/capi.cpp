@@ -741,6 +741,7 @@ int rhy_batch_info(RhyDevice* d, RhyBatchInfo* out) {
       out->grid = b.grid;
       out->device_bytes = d->engine->device_bytes();
       out->n_filter_launches = b.n_items ? 1u : 0u;
+      out->filter_bytes = d->engine->batch_filter_bytes(b);
    });
 }
 

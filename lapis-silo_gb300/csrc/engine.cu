@@ -320,6 +320,57 @@ Engine::~Engine() {
 
 uint64_t Engine::mutation_payload_bytes(int column) const { return table_.seq.at(column).vertical.payload_bytes(); }
 
+namespace {
+// Payload bytes of one container: array 2 * card, bitset 8 KiB, run 4 * nruns.
+uint64_t container_bytes(const CtrDesc& d) {
+   if (d.type == CT_BITSET) return CHUNK_ROWS / 8;
+   if (d.type == CT_RUN) return 4ull * d.nruns;
+   return 2ull * (d.card_m1 + 1u);
+}
+// Payload and descriptor bytes of the containers of one key whose symbol is in `mask`, over all chunks.
+uint64_t key_bytes(const ContainerSet& cs, uint32_t nchunks, uint32_t key, uint32_t mask) {
+   uint64_t b = 0;
+   for (uint32_t v = 0; v < nchunks; ++v) {
+      const size_t k = static_cast<size_t>(v) * cs.nkeys + key;
+      for (uint32_t i = cs.off[k]; i < cs.off[k + 1]; ++i)
+         if (mask >> cs.ctrs[i].sym & 1u) b += container_bytes(cs.ctrs[i]) + sizeof(CtrDesc);
+   }
+   return b;
+}
+}  // namespace
+
+uint64_t Engine::instr_bytes(const Instr& in) const {
+   const uint32_t nv = nchunks();
+   const uint64_t set_bytes = static_cast<uint64_t>(nv) * (CHUNK_ROWS / 8);
+   switch (in.op) {
+      case OP_PUSH_SCAN: return key_bytes(table_.seq[in.col].vertical, nv, in.a, in.b);
+      case OP_PUSH_DICT: return key_bytes(table_.dict[in.col].inverted, nv, in.a, 0xFFFFFFFFu);
+      case OP_PUSH_NULLS:
+      case OP_PUSH_AUX: return set_bytes;
+      case OP_PUSH_COVERED: {
+         const SeqColumnImage& c = table_.seq[in.col];
+         const size_t blk = in.a / NBLOCK;
+         return c.cov_exc.size() * sizeof(CovExc) +
+                static_cast<uint64_t>(c.nblk_off[(blk + 1) * nv] - c.nblk_off[blk * nv]) * sizeof(NRunEntry);
+      }
+      case OP_PUSH_DATE: return static_cast<uint64_t>(view_.date[in.col].nbits + 1) * set_bytes;
+      default: return 0;
+   }
+}
+
+uint64_t Engine::program_bytes(const Program& p, bool writes_rows) const {
+   uint64_t b = writes_rows ? static_cast<uint64_t>(nchunks()) * (CHUNK_ROWS / 8) : sizeof(unsigned long long);
+   for (const Instr& in : p.code) b += instr_bytes(in);
+   return b;
+}
+
+uint64_t Engine::batch_filter_bytes(const BatchState& b) const {
+   uint64_t total = static_cast<uint64_t>(b.n_slots) * nchunks() * (CHUNK_ROWS / 8) +
+                    static_cast<uint64_t>(b.n_queries - b.n_slots) * sizeof(unsigned long long);
+   for (uint32_t i = 0; i < b.n_code; ++i) total += instr_bytes(b.h_code[i]);
+   return total;
+}
+
 Program Engine::plan(const std::string& expr, const LowerOptions& opt, std::string* tree) const {
    LowerOptions o = opt;
    if (o.rows <= 0) o.rows = table_.n_rows;  // early-exit tests where the estimates say they can fire
@@ -923,12 +974,26 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    batch_times = BatchTimes{};
    double plan_ms = 0, prepare_ms = 0;
    clk::time_point launched;
+   // learned planning: one network inference for the whole call, before any part is on the device
+   // (while a persistent filter kernel holds the SMs an inference would wait for it)
+   const bool learned = use_learned_;
+   LearnedPlans lp;
+   if (learned) {
+      const auto t0 = clk::now();
+      learned_compile(exprs, 0, lp);
+      plan_ms += ms(t0, clk::now());
+   }
    try {
       for (size_t p = 0; p < parts.size(); ++p) {
          const auto t0 = clk::now();
-         std::vector<std::string> texts(parts[p].size());
-         for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
-         std::vector<BatchQuery> qs = plan_batch(texts, 0);
+         std::vector<BatchQuery> qs;
+         if (learned) {
+            qs = learned_lower(lp, parts[p], 0);
+         } else {
+            std::vector<std::string> texts(parts[p].size());
+            for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
+            qs = plan_batch(texts, 0);
+         }
          for (size_t j = 0; j < parts[p].size(); ++j) {
             const uint32_t i = parts[p][j];
             qs[j].action = actions ? actions[i] : 0;
@@ -1184,7 +1249,6 @@ void Engine::set_planner_mode(int mode) {
 
 std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs, uint32_t threads) {
    const uint32_t n = static_cast<uint32_t>(exprs.size());
-   std::vector<BatchQuery> qs(n);
    // threads == 0: the engine's persistent workers; otherwise that many threads of their own
    auto each = [&](auto&& fn) {
       if (threads == 0) plan_pool_.run(n, fn);
@@ -1194,6 +1258,7 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
    auto t0 = clk::now();
    if (!use_learned_) {
+      std::vector<BatchQuery> qs(n);
       const Estimator est = rule_estimator(table_);
       LowerOptions lo;
       lo.rows = table_.n_rows;
@@ -1201,16 +1266,35 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
       batch_times.compile_ms += since(t0);
       return qs;
    }
-   // Learned: compile and featurise every expression, run the network once over every operator
-   // node of the batch (rows staged in pinned memory, each query's nodes at its own offset), then
-   // lower every expression with its nodes' predicted row counts.
+   LearnedPlans lp;
+   learned_compile(exprs, threads, lp);
+   std::vector<uint32_t> all(n);
+   for (uint32_t i = 0; i < n; ++i) all[i] = i;
+   return learned_lower(lp, all, threads);
+}
+
+// Learned planning, step 1: compile and featurise every expression, run the network once over every
+// operator node (rows staged in pinned memory, each query's nodes at its own offset) and keep each
+// query's estimates per node and its predicted cost.
+void Engine::learned_compile(const std::vector<std::string>& exprs, uint32_t threads, LearnedPlans& lp) {
+   const uint32_t n = static_cast<uint32_t>(exprs.size());
+   auto each = [&](auto&& fn) {
+      if (threads == 0) plan_pool_.run(n, fn);
+      else parallel_for(n, threads, fn);
+   };
+   using clk = std::chrono::steady_clock;
+   auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+   auto t0 = clk::now();
    const FeatureContext& ctx = fctx();
-   std::vector<OpPtr> ops(n);
+   lp.ops.clear();
+   lp.ops.resize(n);
+   lp.est.assign(n, {});
+   lp.cost.assign(n, 0.0);
    std::vector<std::vector<const Op*>> qnodes(n);
    std::vector<std::vector<std::array<float, PLAN_FEATURES>>> qx(n);
    each([&](uint32_t i) {
-      ops[i] = compile_filter(exprs[i], table_);
-      tree_features(*ops[i], ctx, qnodes[i], qx[i]);
+      lp.ops[i] = compile_filter(exprs[i], table_);
+      tree_features(*lp.ops[i], ctx, qnodes[i], qx[i]);
    });
    batch_times.compile_ms += since(t0);
    t0 = clk::now();
@@ -1229,13 +1313,36 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    const double rows = std::max(1u, table_.n_rows);
    each([&](uint32_t i) {
       // (node, estimated rows) sorted by node for lookup while lowering
-      std::vector<std::pair<const Op*, double>> est(qnodes[i].size());
+      auto& est = lp.est[i];
+      est.resize(qnodes[i].size());
       for (uint32_t k = 0; k < qnodes[i].size(); ++k) {
          const double sel = planner_.selectivity_of(qx[i][k].data(), Y + 2 * static_cast<size_t>(base[i] + k));
          est[k] = {qnodes[i][k], std::isfinite(sel) ? sel * rows : -1.0};
       }
       const double c = qnodes[i].empty() ? 0.0 : planner_.cost_of(Y + 2 * static_cast<size_t>(base[i]));
+      lp.cost[i] = std::isfinite(c) ? c : 0.0;
       std::sort(est.begin(), est.end());
+      std::vector<const Op*>().swap(qnodes[i]);
+      std::vector<std::array<float, PLAN_FEATURES>>().swap(qx[i]);
+   });
+   batch_times.lower_ms += since(t0);
+}
+
+// Learned planning, step 2: lowers the queries `idx` of a learned_compile with their estimates and
+// frees their trees (in parallel: a serial teardown of every tree costs as much as the planning).
+std::vector<BatchQuery> Engine::learned_lower(LearnedPlans& lp, const std::vector<uint32_t>& idx, uint32_t threads) {
+   const uint32_t n = static_cast<uint32_t>(idx.size());
+   std::vector<BatchQuery> qs(n);
+   auto each = [&](auto&& fn) {
+      if (threads == 0) plan_pool_.run(n, fn);
+      else parallel_for(n, threads, fn);
+   };
+   using clk = std::chrono::steady_clock;
+   const auto t0 = clk::now();
+   const FeatureContext& ctx = fctx();
+   each([&](uint32_t j) {
+      const uint32_t i = idx[j];
+      const auto& est = lp.est[i];
       const Estimator learned = [&](const Op& op) -> double {
          const auto it = std::lower_bound(est.begin(), est.end(), std::make_pair(&op, -2.0));
          if (it != est.end() && it->first == &op && it->second >= 0) return it->second;
@@ -1243,15 +1350,12 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
       };
       LowerOptions lo;
       lo.rows = table_.n_rows;
-      qs[i].prog = lower(*ops[i], learned, lo);
-      qs[i].cost = std::isfinite(c) ? c : 0.0;
-      // free the query's tree and features here, in parallel: a serial teardown of every tree on
-      // the calling thread costs as much as the planning
-      ops[i].reset();
-      std::vector<const Op*>().swap(qnodes[i]);
-      std::vector<std::array<float, PLAN_FEATURES>>().swap(qx[i]);
+      qs[j].prog = lower(*lp.ops[i], learned, lo);
+      qs[j].cost = lp.cost[i];
+      lp.ops[i].reset();
+      std::vector<std::pair<const Op*, double>>().swap(lp.est[i]);
    });
-   batch_times.lower_ms += since(t0);
+   batch_times.lower_ms += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
    return qs;
 }
 

@@ -269,10 +269,29 @@ class Engine {
    // Plans a batch: rule-based, or with the learned planner's estimates (one GPU inference over
    // all operator nodes of all expressions) and a predicted cost per query. The caller holds mu.
    std::vector<BatchQuery> plan_batch(const std::vector<std::string>& exprs, uint32_t threads);
+   // The learned planner in two steps: learned_compile compiles and featurises every expression and
+   // runs one network inference over all their operator nodes; learned_lower lowers a subset of
+   // them with those estimates (and frees their trees). The caller holds mu.
+   struct LearnedPlans {
+      std::vector<OpPtr> ops;
+      std::vector<std::vector<std::pair<const Op*, double>>> est;  // per query: (node, rows), by node
+      std::vector<double> cost;
+   };
+   void learned_compile(const std::vector<std::string>& exprs, uint32_t threads, LearnedPlans& lp);
+   std::vector<BatchQuery> learned_lower(LearnedPlans& lp, const std::vector<uint32_t>& idx, uint32_t threads);
 
    const EvItem* d_ev(int column) const { return d_ev_[column]; }
    uint32_t n_ev(int column) const { return n_ev_[column]; }
    uint64_t mutation_payload_bytes(int column) const;
+   // Algorithmic bytes of one filter program over the whole table: the payloads and descriptors of
+   // the containers its index-scan leaves read, the coverage exceptions and the missing intervals of
+   // the position's block its coverage leaves read, the bit planes its date leaves read, the dense
+   // row sets of null and aux leaves, and the output (a dense row set, or one count). Intermediates
+   // between operators are not counted.
+   uint64_t program_bytes(const Program& p, bool writes_rows) const;
+   uint64_t instr_bytes(const Instr& in) const;  // one leaf's share of program_bytes
+   // program_bytes over every program of a prepared batch (its slot queries write row sets)
+   uint64_t batch_filter_bytes(const BatchState& b) const;
 
    // scratch of the single-query path
    uint32_t* d_filter = nullptr;      // nchunks * CHUNK_WORDS

@@ -129,7 +129,7 @@ class SeqColumnInfo(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [("n_queries", C.c_uint32), ("n_mutation_slots", C.c_uint32), ("n_items", C.c_uint32),
                 ("n_instr", C.c_uint32), ("max_depth", C.c_uint32), ("tile_bits", C.c_uint32), ("grid", C.c_uint32),
-                ("device_bytes", C.c_uint64), ("n_filter_launches", C.c_uint32)]
+                ("device_bytes", C.c_uint64), ("n_filter_launches", C.c_uint32), ("filter_bytes", C.c_uint64)]
 
 
 class PlannerStats(C.Structure):
