@@ -17,8 +17,17 @@ plain      the plain single-query path over the same queries, one query at a tim
 roofline   the plain container pass of the Mutations action (mut_stream_kernel), the kernel that
            streams the whole vertical index: algorithmic bytes = container payloads + descriptors
            + the filter tiles it stages, divided by its CUDA-event duration.
+roofline_batch  the batched filter and container kernels: the algorithmic bytes of one batch
+           (rhy_batch_info's filter bytes; per dense pass every container and the query masks)
+           divided by their CUDA-event durations.
 cpu_baseline  the CPU oracle (a restatement of the reference's operators) on a bounded sample of
            the same queries, one query per host thread as the reference serves them.
+parity_oracle  the same leg as checker, outside every timed region: the oracle's count of every
+           query of the batch and its Mutations tables and rows for the sample's Mutations queries,
+           against the batched path's counts and tables and the rows built on the device.
+planner    rule-based vs learned ordering: device time of the captured batch and end to end.
+serving    Poisson arrivals at 2,000 and 20,000 requests/s on an 8M-sequence table: continuous
+           batching (learned planner) against the plain single-query path, p50 / p99 and the rate.
 
 `python bench.py --impl reference` times that CPU implementation alone on the same workload.
 """
@@ -57,7 +66,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--qseed", type=int, default=43)
     ap.add_argument("--plain-queries", type=int, default=256)
-    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--cpu-sample", type=int, default=256,
+                    help="queries of the batch the CPU oracle times (one Mutations query in four)")
     ap.add_argument("--tile-bits", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--planner-samples", type=int, default=200_000,
@@ -76,6 +86,11 @@ def parse():
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
     ap.add_argument("--serve-rows", type=int, default=8_000_000,
                     help="sequences of the serving table (its own seeded table when it differs from --rows)")
+    ap.add_argument("--profile-workload", default="", choices=["", "plain-mutations", "batch", "profile"],
+                    help="run one workload for a profiler and exit: plain-mutations (the single-query path for "
+                         "Mutations queries whose filter is neither empty nor every row; --plain-queries of them), "
+                         "batch (the batched path, --steps launches), profile (MutationProfile counts at "
+                         "distances 0, 5, 50, 200)")
     return ap.parse_args()
 
 
@@ -160,6 +175,40 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(args, n, n_mut, ws):
+    """The workload both arms run, identical in their JSON lines."""
+    return {"workload": f"{args.rows} sequences x {args.batch}-query batches "
+                        f"({n - n_mut} Aggregated count + {n_mut} nucleotide Mutations)",
+            "rows": args.rows, "batch": n, "mutations_per_batch": n_mut, "aa_genes": 12,
+            "seeds": {"table": args.seed, "queries": args.qseed},
+            "l2": "flushed before every timed step (256 MiB write, outside the events)",
+            "parallelism": f"replicas x{ws}"}
+
+
+def oracle_build_info():
+    """Compiler flags of the oracle library and the host CPU, for the CPU baseline's record."""
+    flags = ""
+    for line in (ROOT / "oracle" / "Makefile").read_text().splitlines():
+        if line.startswith("CXXFLAGS"):
+            flags = line.split("=", 1)[1].strip()
+    model = ""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu part", "hardware") and not model:
+                model = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"compile_flags": flags, "cpu_model": model or "unknown", "machine": os.uname().machine}
+
+
 def build_workload(R, args):
     table = R.Table.generate(args.rows, seed=args.seed, n_aa_genes=12)
     queries = table.queries(args.batch, seed=args.qseed, use_aa=True, use_metadata=True)
@@ -169,7 +218,8 @@ def build_workload(R, args):
 
 
 def cpu_leg(table, queries, actions, columns, n_sample: int, threads: int):
-    """Times the CPU oracle on a sample of the workload; returns (queries/s, sample description, p50, p99)."""
+    """Times the CPU oracle on a sample of the workload; returns (queries/s, sample description, p50,
+    p99, seconds, the oracle)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as oracle_mod
 
@@ -182,7 +232,25 @@ def cpu_leg(table, queries, actions, columns, n_sample: int, threads: int):
     qps = len(idx) / secs
     desc = (f"first {len(idx)} queries of the batch ({int(sum(actions[i] for i in idx))} Mutations), "
             f"{threads} worker threads, one query per thread; oracle ingestion {build_s:.1f} s not timed")
-    return qps, desc, float(np.percentile(ms, 50)), float(np.percentile(ms, 99)), secs
+    return qps, desc, float(np.percentile(ms, 50)), float(np.percentile(ms, 99)), secs, orc
+
+
+def oracle_parity(orc, table, queries, actions, columns, n_sample, b_counts, b_muts, rows, r_begin, r_cnt):
+    """The CPU leg as checker (outside every timed region): the oracle's count of every query of the
+    batch, and its Mutations tables and rows for the Mutations queries of the timed sample, against
+    the batched path's counts and tables and the rows rhy_batch_rows built on the device."""
+    t0 = time.perf_counter()
+    mut = [i for i in range(min(n_sample, len(queries))) if actions[i] == 1]
+    o_counts, o_tables = orc.check_batch(queries, columns, tables=mut)
+    count_bad = int(np.sum(np.asarray(b_counts, np.uint64) != o_counts))
+    table_bad = sum(int(not np.array_equal(b_muts[i], o_tables[i])) for i in mut)
+    rows_bad = 0
+    for i in mut:
+        got = [(int(r["position"]), r["from_"].decode(), r["to"].decode(), int(r["count"]), int(r["coverage"]),
+                float(r["proportion"])) for r in rows[int(r_begin[i]):int(r_begin[i]) + int(r_cnt[i])]]
+        rows_bad += int(got != orc.mutation_rows(int(columns[i]), o_tables[i], MIN_PROPORTION))
+    return {"counts_checked": len(queries), "tables_checked": len(mut), "rows_checked": len(mut),
+            "mismatches": count_bad + table_bad + rows_bad, "seconds": round(time.perf_counter() - t0, 1)}
 
 
 def reference_arm(args, ws, rank):
@@ -214,15 +282,41 @@ def reference_arm(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic (seeded generator)",
-        "config": {"workload": f"{args.rows} sequences, 12 aa genes; {n}-query samples of the {args.batch}-query "
-                               f"batch (1 in {args.mut_every} Mutations)", "rows": args.rows},
+        "data": "synthetic (seeded generator: 2M sequences, Zipf(1.1) substitutions, N-runs, gaps, 12 aa genes)",
+        "config": workload_config(args, len(queries), int(actions.sum()), ws),
         "p50_ms": float(np.percentile(all_ms, 50)), "p99_ms": float(np.percentile(all_ms, 99)),
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} queries per step, one query per worker thread ({threads} threads)"},
+                         "sample": f"{n} consecutive queries of the batch per step (a rotating window, "
+                                   f"1 in {args.mut_every} Mutations), one query per worker thread",
+                         **oracle_build_info()},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def profile_workload(args, R, workloads, table, dev, queries, actions, columns, sp, stream):
+    """One workload for a profiler (no timing of its own): see --profile-workload."""
+    if args.profile_workload == "plain-mutations":
+        counts, _ = dev.batch(queries, actions, columns)
+        idx = [i for i in range(len(queries)) if actions[i] == 1 and 0 < counts[i] < table.n_rows][:args.plain_queries]
+        dev.plain_prepare(queries, actions, columns)
+        for i in idx:
+            dev.plain_launch(i, sp)
+        stream.synchronize()
+        print(f"plain-mutations: {len(idx)} queries over {table.n_rows} rows")
+    elif args.profile_workload == "profile":
+        seq = workloads.profile_query_sequence(table, row=123457, substitutions=20, seed=17)
+        for d in (0, 5, 50, 200):
+            print(f"profile: distance {d}: {dev.count(f'MutProfile(main,{d},{seq})', sp)} of {table.n_rows} rows")
+    else:
+        if args.schedule:
+            w, kb, cps, qm = (int(x) for x in args.schedule.split(","))
+            dev.batch_schedule(max_tile_bits=w, stack_kb=kb, ctas_per_sm=cps, query_major=qm)
+        dev.batch_prepare(queries, actions, columns)
+        for _ in range(args.steps):
+            dev.batch_launch(sp, True, True)
+        stream.synchronize()
+        print(f"batch: {args.steps} x {len(queries)} queries over {table.n_rows} rows")
 
 
 def main():
@@ -245,6 +339,10 @@ def main():
     n_mut = int(actions.sum())
     stream = torch.cuda.Stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
+    if args.profile_workload:
+        profile_workload(args, R, workloads, table, dev, queries, actions, columns, sp, stream)
+        dev.close()
+        return
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev_index}")
 
     def flush_l2():
@@ -322,10 +420,34 @@ def main():
                     "default_filter_ms": next((round(ms, 3) for sc, ms in tried if sc == default_sched), None),
                     "worst_filter_ms": round(tried[-1][1], 3)}
 
+    min_props = np.full(n, MIN_PROPORTION)
+
+    def e2e_run(steps):
+        """rhy_batch_rows end to end (planning, copies, kernels, rows): one untimed call, then `steps`
+        timed calls; queries/s of the median call and that call's phases."""
+        dev.batch_rows(queries, actions, columns, min_props, tile_bits=args.tile_bits, stream=sp)
+        secs, phases, last = [], [], None
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            last = dev.batch_rows(queries, actions, columns, min_props, tile_bits=args.tile_bits, stream=sp)
+            secs.append(time.perf_counter() - t0)
+            phases.append(dev.batch_times())
+        mid = sorted(range(len(secs)), key=lambda i: secs[i])[len(secs) // 2]
+        ph = {k: round(v, 3) for k, v in phases[mid].items()}
+        top = ("plan_ms", "prepare_ms", "device_ms", "output_ms")  # the rest split plan_ms
+        ph["other_ms"] = round(1000 * secs[mid] - sum(phases[mid][k] for k in top), 3)
+        return n * ws / max_over_ranks(statistics.median(secs), ws), ph, last
+
     if planner["mode"] == "learned":
-        planner["rule_ms_per_step"] = time_batch(10, 3)  # the same batch and schedule, rule-based plans
+        # the same batch and schedule under both orderings: device time of the captured batch, and
+        # end to end through rhy_batch_rows (planning included)
+        planner["rule_ms_per_step"] = time_batch(10, 3)
+        planner["rule_e2e_qps"], planner["rule_e2e_phases_ms"], _ = e2e_run(5)
         dev.planner_mode(1)
         planner["learned_ms_per_step"] = time_batch(10, 3)
+        planner["learned_e2e_qps"], planner["learned_e2e_phases_ms"], _ = e2e_run(5)
+        planner["device_speedup"] = planner["rule_ms_per_step"] / planner["learned_ms_per_step"]
+        planner["e2e_speedup"] = planner["learned_e2e_qps"] / planner["rule_e2e_qps"]
 
     # ---------------- batched path: device-resident ----------------
     dev.batch_prepare(queries, actions, columns, tile_bits=args.tile_bits)
@@ -426,23 +548,9 @@ def main():
     plain_e2e_qps = m / (time.perf_counter() - t0)
 
     # ---------------- batched e2e through the C-ABI ----------------
-    # rows of the Mutations action built on the device; the dense-count variant is kept for context
-    e2e_s, e2e_phases = [], []
-    min_props = np.full(n, 0.05)
-    # one untimed call sizes the two parts' buffers, then timed calls
-    dev.batch_rows(queries, actions, columns, min_props, tile_bits=args.tile_bits, stream=sp)
-    for step in range(max(3, min(args.steps, 10))):
-        t0 = time.perf_counter()
-        r_counts, rows, r_begin, r_cnt = dev.batch_rows(queries, actions, columns, min_props,
-                                                        tile_bits=args.tile_bits, stream=sp)
-        e2e_s.append(time.perf_counter() - t0)
-        e2e_phases.append(dev.batch_times())
-    e2e_qps = n * ws / max_over_ranks(statistics.median(e2e_s), ws)
-    # host wall time per phase of the median step; "other" is the binding's own time
-    mid = sorted(range(len(e2e_s)), key=lambda i: e2e_s[i])[len(e2e_s) // 2]
-    e2e_phase_ms = {k: round(v, 3) for k, v in e2e_phases[mid].items()}
-    top = ("plan_ms", "prepare_ms", "device_ms", "output_ms")  # the rest split plan_ms
-    e2e_phase_ms["other_ms"] = round(1000 * e2e_s[mid] - sum(e2e_phases[mid][k] for k in top), 3)
+    # rows of the Mutations action built on the device; the dense-count variant is kept for context.
+    # Host wall time per phase of the median step; "other" is the binding's own time.
+    e2e_qps, e2e_phase_ms, (r_counts, rows, r_begin, r_cnt) = e2e_run(max(3, min(args.steps, 10)))
     dense_s = []
     for step in range(2):
         t0 = time.perf_counter()
@@ -461,37 +569,49 @@ def main():
     prog_bytes = info.n_instr * 16 + n * 16 + info.n_items * 8 + n_mut * 12
     d2h = n * 8 + n * 12 + len(rows) * 24
 
-    # ---------------- serving: Poisson arrivals, continuous batching ----------------
+    # ---------------- serving: Poisson arrivals, continuous batching vs the plain path ----------------
     serving = None
     if args.serve_seconds > 0:
         t_setup = time.perf_counter()
-        s_table, s_dev, s_queries, s_planner = table, dev, queries, planner["mode"]
+        s_table, s_dev, s_queries = table, dev, queries
         if args.serve_rows != args.rows:
             s_table = R.Table.generate(args.serve_rows, seed=args.seed, n_aa_genes=12)
             s_dev = R.Device(s_table, dev_index)
             s_queries = s_table.queries(n, seed=args.qseed, use_aa=True, use_metadata=True)
-            s_planner = "rule-based ordering"
+            if planner["mode"] == "learned":  # the model trained on its own table plans here too
+                s_dev.planner_import(dev.planner_export())  # with the verdict judged on this table
+                s_dev.planner_mode(1)
+        s_planner = "learned" if planner["mode"] == "learned" else "rule-based ordering"
         setup_s = time.perf_counter() - t_setup
-        srv = R.Server(s_dev, max_batch=512, streams=3)
         rng = np.random.default_rng(args.qseed + 7)
-        runs = []
-        for rate in [float(x) for x in args.serve_rates.split(",") if x]:
+        rates = [float(x) for x in args.serve_rates.split(",") if x]
+        traces = []
+        for rate in rates:
             nreq = max(1, int(rate * args.serve_seconds))
-            arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-            mix = rng.choice(3, nreq, p=[0.70, 0.25, 0.05]).astype(np.int32)
-            pick = rng.integers(0, n, nreq)
-            lat, wall = srv.replay([s_queries[i] for i in pick], mix, np.zeros(nreq, np.uint32), np.full(nreq, 0.05),
-                                   np.full(nreq, 1000, np.uint32), arrivals)
-            ok = lat[np.isfinite(lat)]
-            runs.append({"arrival_qps": rate, "requests": nreq, "achieved_qps": nreq / wall,
-                         "p50_ms": float(np.percentile(ok, 50)), "p99_ms": float(np.percentile(ok, 99)),
-                         "failed": int(nreq - len(ok))})
-        st = srv.stats()
-        srv.stop()
+            traces.append((rate, np.cumsum(rng.exponential(1.0 / rate, nreq)),
+                           rng.choice(3, nreq, p=[0.70, 0.25, 0.05]).astype(np.int32), rng.integers(0, n, nreq)))
+        arms = {}
+        # continuous batching, then the plain arm (one request at a time through the single-query
+        # path, the reference's one-query-per-request model). The plain arm saturates far below the
+        # high rates, so its traces are cut to the first 4,000 requests (the same arrival times).
+        for arm, kw in (("batched", {"max_batch": 512, "streams": 3}), ("plain", {"plain": True})):
+            srv = R.Server(s_dev, **kw)
+            runs = []
+            for rate, arrivals, mix, pick in traces:
+                m = len(arrivals) if arm == "batched" else min(len(arrivals), 4000)
+                lat, wall = srv.replay([s_queries[i] for i in pick[:m]], mix[:m], np.zeros(m, np.uint32),
+                                       np.full(m, MIN_PROPORTION), np.full(m, 1000, np.uint32), arrivals[:m])
+                ok = lat[np.isfinite(lat)]
+                runs.append({"arrival_qps": rate, "requests": m, "achieved_qps": m / wall,
+                             "p50_ms": float(np.percentile(ok, 50)), "p99_ms": float(np.percentile(ok, 99)),
+                             "failed": int(m - len(ok))})
+            st = srv.stats()
+            srv.stop()
+            arms[arm] = {"runs": runs, "mean_batch": st["mean_batch"], "batches": st["batches"],
+                         "peak_device_bytes": st["peak_bytes"]}
         serving = {"mix": "70% count / 25% mutations (nucleotide, min proportion 0.05) / 5% details (first 1000 ids)",
                    "arrivals": "Poisson, open loop (native submitter thread)", "rows": s_table.n_rows,
-                   "table_setup_s": round(setup_s, 1), "runs": runs, "mean_batch": st["mean_batch"],
-                   "batches": st["batches"], "peak_device_bytes": st["peak_bytes"], "planner": s_planner}
+                   "table_setup_s": round(setup_s, 1), "planner": s_planner, **arms}
         if s_dev is not dev:
             s_dev.close()
             del s_table
@@ -587,13 +707,40 @@ def main():
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
 
-    # ---------------- CPU baseline ----------------
-    cpu = None
+    # ---------------- roofline of the batched kernels ----------------
+    # filter_batch_kernel: the algorithmic bytes of the batch's programs (container payloads and
+    # descriptors of their index-scan leaves, coverage and date data, outputs) per launch.
+    # mut_ctr_batch_kernel: per dense pass (up to 256 slots) every container payload and descriptor
+    # plus the 32-byte query-mask sector of every row, and the count tables of the dense slots.
+    sparse_b = dev.sparse_rows()[1]
+    dense_slots = sum(1 for i in range(n) if actions[i] == 1 and int(b_counts[i]) > max(sparse_b, 0)
+                      and int(b_counts[i]) > 0)
+    passes = -(-dense_slots // 256)
+    col0 = table.columns[0]
+    ctr_alg = passes * (payload_b + desc_b + table.n_chunks * 65536 * 32) + dense_slots * col0.n_symbols * col0.L * 4
+    roofline_batch = {
+        "filter_batch_kernel": {"algorithmic_bytes_per_launch": int(info.filter_bytes),
+                                "launch_ms": kernels_ms["filter_batch"],
+                                "achieved": info.filter_bytes / (kernels_ms["filter_batch"] / 1000.0) / 1e9,
+                                "unit": "GB/s", "peak": peak},
+        "mut_ctr_batch_kernel": {"algorithmic_bytes_per_launch": int(ctr_alg), "dense_slots": dense_slots,
+                                 "passes": passes, "launch_ms": kernels_ms["mut_ctr_batch"],
+                                 "achieved": ctr_alg / (kernels_ms["mut_ctr_batch"] / 1000.0) / 1e9,
+                                 "unit": "GB/s", "peak": peak},
+    }
+    for v in roofline_batch.values():
+        v["frac"] = v["achieved"] / peak
+
+    # ---------------- CPU baseline, then the oracle as checker of the batch ----------------
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        cqps, cdesc, cp50, cp99, csecs = cpu_leg(table, queries, actions, columns, args.cpu_sample, threads)
+        cqps, cdesc, cp50, cp99, csecs, orc = cpu_leg(table, queries, actions, columns, args.cpu_sample, threads)
         cpu = {"value": cqps, "unit": "queries/s", "cores": threads, "kind": "port", "sample": cdesc,
-               "p50_ms": cp50, "p99_ms": cp99, "seconds": csecs}
+               "p50_ms": cp50, "p99_ms": cp99, "seconds": csecs, **oracle_build_info()}
+        parity = oracle_parity(orc, table, queries, actions, columns, args.cpu_sample, b_counts, b_muts, rows,
+                               r_begin, r_cnt)
+        del orc
 
     if rank == 0:
         line = {
@@ -601,13 +748,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded generator: 2M sequences, Zipf(1.1) substitutions, N-runs, gaps, 12 aa genes)",
-            "config": {"workload": f"{args.rows} sequences x {args.batch}-query batches "
-                                   f"({n - n_mut} Aggregated count + {n_mut} nucleotide Mutations)",
-                       "rows": args.rows, "batch": n, "mutations_per_batch": n_mut, "aa_genes": 12,
-                       "tile_bits": info.tile_bits, "grid": info.grid, "planner": planner["mode"],
-                       "schedule": dev.batch_schedule(),
-                       "l2": "flushed before every timed step (256 MiB write, outside the events)",
-                       "parallelism": f"replicas x{ws}"},
+            "config": workload_config(args, n, n_mut, ws),
+            "schedule": {"tile_bits": info.tile_bits, "grid": info.grid, "planner": planner["mode"],
+                         **dev.batch_schedule()},
             "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
             "latency_note": "batched: every query of a batch completes with its batch",
             "plain": {"qps": plain_qps, "p50_ms": float(np.percentile(plain_ms, 50)),
@@ -622,6 +765,8 @@ def main():
             "batching_shape": shape,
             "serving": serving,
             "parity_plain_vs_batched_mismatches": mismatches,
+            "parity_oracle": parity,
+            "parity_oracle_mismatches": parity["mismatches"] if parity else None,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(prog_bytes),
                     "d2h_bytes_per_step": int(d2h), "output": "Mutations rows (min proportion 0.05) + counts",
                     "rows_per_step": int(len(rows)), "rows_mismatches": rows_mismatches,
@@ -633,6 +778,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": ctr_avg_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"},
+            "roofline_batch": roofline_batch,
             "cpu_baseline": cpu,
             "clocks": clk,
             "wall_s_timed_region": wall,

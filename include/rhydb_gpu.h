@@ -53,7 +53,8 @@ enum {
    RHY_CUDA = 3,
    RHY_INVALID_ARGUMENT = 4,
    RHY_INTERNAL = 5,
-   RHY_TIMEOUT = 6          /* rhy_server_result: not done within the timeout */
+   RHY_TIMEOUT = 6,         /* rhy_server_result: not done within the timeout */
+   RHY_CANCELLED = 7        /* rhy_server_result: the request was cancelled */
 };
 
 typedef struct RhyTable RhyTable;
@@ -451,12 +452,16 @@ typedef struct {
    uint32_t max_inflight;    /* admitted, unfinished queries (default 4096) */
    uint64_t memory_budget;   /* device bytes of in-flight work; 0 = a quarter of the free memory */
    double max_wait_ms;       /* default 0.25 */
+   uint32_t plain;           /* 1: no batching; each request runs alone through the single-query path
+                                (rhy_count / rhy_mutations / rhy_eval) in arrival order, the way the
+                                reference serves one query per request; 0 (default): continuous batching */
 } RhyServerConfig;
 typedef struct {
    uint64_t submitted, completed, rejected, batches;
    double p50_ms, p99_ms, mean_batch, qps;
    uint64_t peak_bytes, budget_bytes;
    uint32_t peak_inflight;
+   uint64_t cancelled;
 } RhyServerStats;
 int rhy_server_start(RhyDevice* d, const RhyServerConfig* cfg /* NULL: defaults */, RhyServer** out);
 /* Validates and queues a request (user errors are returned here). */
@@ -469,6 +474,11 @@ int rhy_server_submit(RhyServer* s, const char* expr, int action, uint32_t colum
 int rhy_server_result(RhyServer* s, uint64_t id, double timeout_ms, uint64_t* count, RhyMutationRow* rows,
                       size_t rows_cap, size_t* n_rows, uint32_t* ids, size_t ids_cap, size_t* n_ids, double* latency_ms);
 int rhy_server_stats(RhyServer* s, RhyServerStats* out);
+/* Cancels a request that is not done (reference: the plan-stop guard of a query that is abandoned,
+ * query_plan.cpp:66-123): a queued request is dropped before admission, one already on the device
+ * finishes there and its result is discarded. rhy_server_result then returns RHY_CANCELLED.
+ * *was_pending (may be NULL) is 1 if the request was cancelled, 0 if it had already finished. */
+int rhy_server_cancel(RhyServer* s, uint64_t id, int* was_pending);
 /* Open-loop replay of a request trace: request i is submitted by a native thread at arrival_s[i]
  * seconds after the call starts; then all are awaited. latency_ms[i] receives each latency (NaN if
  * the request failed), *wall_s the time from the start to the last result. */

@@ -166,6 +166,8 @@ int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out)
          need(s.reference, "reference");
          need(s.is_null, "is_null");
          need(s.row_off, "row_off");
+         if (s.kind != 0 && s.kind != 1)
+            throw std::invalid_argument("column " + std::string(s.name) + ": kind must be 0 (nucleotide) or 1 (amino acid)");
          rhygpu::RawSeqColumn col;
          col.name = s.name;
          col.kind = s.kind == 0 ? rhygpu::SymKind::NUC : rhygpu::SymKind::AA;
@@ -195,10 +197,21 @@ int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out)
       }
       for (uint32_t c = 0; c < raw->n_dict; ++c) {
          const RhyRawDictColumn& s = raw->dict[c];
+         need(s.name, "column name");
+         need(s.ids, "ids");
+         if (s.n_values) need(s.values, "values");
          rhygpu::RawDictColumn col;
          col.name = s.name;
-         for (uint32_t i = 0; i < s.n_values; ++i) col.values.emplace_back(s.values[i]);
+         for (uint32_t i = 0; i < s.n_values; ++i) {
+            need(s.values[i], "dictionary value");
+            col.values.emplace_back(s.values[i]);
+         }
          col.ids.assign(s.ids, s.ids + raw->n_rows);
+         for (uint32_t row = 0; row < raw->n_rows; ++row)
+            if (col.ids[row] != UINT32_MAX && col.ids[row] >= s.n_values)
+               throw std::invalid_argument("column " + col.name + ": row " + std::to_string(row) + " has value id " +
+                                           std::to_string(col.ids[row]) + " of a dictionary of " +
+                                           std::to_string(s.n_values) + " values");
          r.dict.push_back(std::move(col));
       }
       for (uint32_t c = 0; c < raw->n_date; ++c) {
@@ -856,37 +869,13 @@ int rhy_test_withhold_copies(RhyDevice* d, int on) {
 int rhy_mutation_rows(const RhyTable* t, uint32_t column, const uint32_t* counts, double min_proportion,
                       RhyMutationRow* rows, size_t cap, size_t* n_rows) {
    // reference: mutations_node.cpp:292-366
+   static_assert(sizeof(RhyMutationRow) == sizeof(rhygpu::DevMutationRow), "row layout");
    return guarded([&] {
       need(t, "table");
       need(counts, "counts");
       need(n_rows, "n_rows");
-      const auto& c = t->image.seq.at(column);
-      const rhygpu::Alphabet& A = rhygpu::alphabet(c.kind);
-      size_t n = 0;
-      for (uint32_t pos = 0; pos < c.L; ++pos) {
-         uint32_t total = 0;
-         for (uint32_t s = 0; s < A.count; ++s)
-            if (A.valid_mask >> s & 1) total += counts[static_cast<size_t>(s) * c.L + pos];
-         if (total == 0) continue;
-         const uint32_t threshold =
-            min_proportion == 0 ? 0 : static_cast<uint32_t>(std::ceil(static_cast<double>(total) * min_proportion) - 1);
-         const uint32_t ref = c.global_ref[pos];
-         for (uint32_t s = 0; s < A.count; ++s) {
-            if (!(A.valid_mask >> s & 1) || s == ref) continue;
-            const uint32_t count = counts[static_cast<size_t>(s) * c.L + pos];
-            if (count <= threshold) continue;
-            if (rows && n < cap) {
-               rows[n].position = pos + 1;
-               rows[n].from = A.chars[ref];
-               rows[n].to = A.chars[s];
-               rows[n].count = count;
-               rows[n].coverage = total;
-               rows[n].proportion = static_cast<double>(count) / static_cast<double>(total);
-            }
-            ++n;
-         }
-      }
-      *n_rows = n;
+      *n_rows = rhygpu::mutation_rows_host(t->image.seq.at(column), counts, min_proportion,
+                                           reinterpret_cast<rhygpu::DevMutationRow*>(rows), rows ? cap : 0);
    });
 }
 
@@ -1103,6 +1092,7 @@ int rhy_server_start(RhyDevice* d, const RhyServerConfig* cfg, RhyServer** out) 
          if (cfg->max_inflight) c.max_inflight = cfg->max_inflight;
          c.memory_budget = cfg->memory_budget;
          if (cfg->max_wait_ms >= 0) c.max_wait_ms = cfg->max_wait_ms;
+         c.plain = cfg->plain != 0;
       }
       auto s = std::make_unique<RhyServer>();
       s->server = std::make_unique<rhygpu::Server>(*d->engine, c);
@@ -1132,7 +1122,9 @@ int rhy_server_result(RhyServer* s, uint64_t id, double timeout_ms, uint64_t* co
       }
       if (!r->error.empty()) {
          s->server->release(id);
-         code = r->error.find("device program error") != std::string::npos ? RHY_COMPILATION : RHY_CUDA;
+         code = r->cancelled                                          ? RHY_CANCELLED
+                : r->error.find("device program error") != std::string::npos ? RHY_COMPILATION
+                                                                              : RHY_CUDA;
          throw std::runtime_error(r->error);
       }
       if (n_rows) *n_rows = r->rows.size();
@@ -1165,6 +1157,15 @@ int rhy_server_stats(RhyServer* s, RhyServerStats* out) {
       out->peak_bytes = st.peak_bytes;
       out->budget_bytes = st.budget_bytes;
       out->peak_inflight = st.peak_inflight;
+      out->cancelled = st.cancelled;
+   });
+}
+
+int rhy_server_cancel(RhyServer* s, uint64_t id, int* was_pending) {
+   return guarded([&] {
+      need(s, "server");
+      const bool c = s->server->cancel(id);
+      if (was_pending) *was_pending = c ? 1 : 0;
    });
 }
 

@@ -318,6 +318,37 @@ Engine::~Engine() {
    if (stream_) cudaStreamDestroy(stream_);
 }
 
+size_t mutation_rows_host(const SeqColumnImage& c, const uint32_t* counts, double min_proportion, DevMutationRow* out,
+                          size_t cap) {
+   const Alphabet& A = alphabet(c.kind);
+   size_t n = 0;
+   for (uint32_t pos = 0; pos < c.L; ++pos) {
+      uint32_t total = 0;
+      for (uint32_t s = 0; s < A.count; ++s)
+         if (A.valid_mask >> s & 1) total += counts[static_cast<size_t>(s) * c.L + pos];
+      if (total == 0) continue;
+      const uint32_t threshold =
+         min_proportion == 0 ? 0 : static_cast<uint32_t>(std::ceil(static_cast<double>(total) * min_proportion) - 1);
+      const uint32_t ref = c.global_ref[pos];
+      for (uint32_t s = 0; s < A.count; ++s) {
+         if (!(A.valid_mask >> s & 1) || s == ref) continue;
+         const uint32_t count = counts[static_cast<size_t>(s) * c.L + pos];
+         if (count <= threshold) continue;
+         if (out && n < cap) {
+            out[n].position = pos + 1;
+            out[n].from = A.chars[ref];
+            out[n].to = A.chars[s];
+            out[n].pad = 0;
+            out[n].count = count;
+            out[n].coverage = total;
+            out[n].proportion = static_cast<double>(count) / static_cast<double>(total);
+         }
+         ++n;
+      }
+   }
+   return n;
+}
+
 uint64_t Engine::mutation_payload_bytes(int column) const { return table_.seq.at(column).vertical.payload_bytes(); }
 
 namespace {

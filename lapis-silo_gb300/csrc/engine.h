@@ -32,6 +32,14 @@ enum : int { DEVERR_WAIT_FILTER = 6, DEVERR_WAIT_MUTATIONS = 7 };
 // CompilationError for a malformed program.
 [[noreturn]] void throw_device_error(int code);
 
+// addMutationsToOutput on the host (reference: mutations_node.cpp:292-366): the rows of a column's
+// dense counts (counts[symbol * L + position]) whose count exceeds ceil(total * min_proportion) - 1
+// (any count > 0 when min_proportion is 0), total over the valid symbols, the global reference
+// symbol skipped; proportion = count / total. Rows go to `out` (when not null) up to `cap`; returns
+// their number.
+size_t mutation_rows_host(const SeqColumnImage& c, const uint32_t* counts, double min_proportion, DevMutationRow* out,
+                          size_t cap);
+
 // One query of a batch. Actions: 0 = Aggregated count, 1 = Mutations of `column`, 2 = Details
 // (the first k row ids of the filter, ascending).
 struct BatchQuery {

@@ -104,6 +104,48 @@ void Server::release(uint64_t id) {
    all_.erase(id);
 }
 
+bool Server::cancel(uint64_t id) {
+   std::lock_guard<std::mutex> lock(mu_);
+   auto it = all_.find(id);
+   if (it == all_.end()) throw std::invalid_argument("no such request");
+   ServeRequest& r = *it->second;
+   if (r.done) return false;
+   r.cancelled = true;
+   const auto q = std::find(pending_.begin(), pending_.end(), it->second);
+   if (q != pending_.end()) {  // not admitted yet: it never reaches the device
+      pending_.erase(q);
+      r.error = "request cancelled";
+      r.t_done = now_s();
+      r.done = true;
+      ++st_.cancelled;
+      cv_done_.notify_all();
+   }
+   return true;
+}
+
+void Server::run_plain(ServeRequest& r, cudaStream_t stream) {
+   const Program p = engine_.plan(r.expr);
+   if (r.action == 0) {
+      r.count = engine_.count(p, stream);
+   } else if (r.action == 1) {
+      const SeqColumnImage& c = engine_.table().seq.at(static_cast<size_t>(r.column));
+      std::vector<uint32_t> counts(static_cast<size_t>(alphabet(c.kind).count) * c.L);
+      uint64_t n = 0;
+      engine_.mutations(p, r.column, counts.data(), &n, stream);
+      r.count = n;
+      r.rows.resize(mutation_rows_host(c, counts.data(), r.min_proportion, nullptr, 0));
+      mutation_rows_host(c, counts.data(), r.min_proportion, r.rows.data(), r.rows.size());
+   } else {
+      std::vector<uint32_t> bits(static_cast<size_t>(engine_.nchunks()) * CHUNK_WORDS);
+      uint64_t n = 0;
+      engine_.eval(p, bits.data(), &n, stream);
+      r.count = n;
+      for (size_t w = 0; w < bits.size() && r.ids.size() < r.k; ++w)
+         for (uint32_t x = bits[w]; x && r.ids.size() < r.k; x &= x - 1)
+            r.ids.push_back(static_cast<uint32_t>(w * 32 + static_cast<uint32_t>(__builtin_ctz(x))));
+   }
+}
+
 ServerStats Server::stats() {
    std::lock_guard<std::mutex> lock(mu_);
    ServerStats s = st_;
@@ -130,6 +172,42 @@ void Server::stop() {
 
 void Server::loop() {
    cudaSetDevice(engine_.device());
+   while (cfg_.plain) {  // one request at a time through the single-query path
+      std::shared_ptr<ServeRequest> r;
+      {
+         std::unique_lock<std::mutex> lock(mu_);
+         cv_work_.wait(lock, [&] { return stop_ || !pending_.empty(); });
+         if (pending_.empty()) return;  // stopped and drained
+         r = pending_.front();
+         pending_.pop_front();
+         ++inflight_;
+         ++st_.batches;
+         ++batched_queries_;
+      }
+      std::string error;
+      try {
+         run_plain(*r, slots_[0].stream);
+      } catch (const std::exception& e) {
+         error = e.what();
+      }
+      const double t = now_s();
+      std::lock_guard<std::mutex> lock(mu_);
+      --inflight_;
+      r->t_done = t;
+      t_last_ = t;
+      if (r->cancelled) {
+         r->error = "request cancelled";
+         ++st_.cancelled;
+      } else if (!error.empty()) {
+         r->error = error;
+         ++st_.rejected;
+      } else {
+         latencies_ms_.push_back(1000.0 * (r->t_done - r->t_submit));
+         ++st_.completed;
+      }
+      r->done = true;
+      cv_done_.notify_all();
+   }
    for (;;) {
       bool progressed = false;
       for (Slot& s : slots_) {
@@ -245,6 +323,13 @@ void Server::finish(Slot& slot) {
    for (size_t i = 0; i < slot.reqs.size(); ++i) {
       ServeRequest& r = *slot.reqs[i];
       const uint32_t q = static_cast<uint32_t>(i);
+      if (r.cancelled) {  // ran on the device, the result is discarded
+         r.error = "request cancelled";
+         r.t_done = t;
+         r.done = true;
+         ++st_.cancelled;
+         continue;
+      }
       r.count = engine_.batch_state_count(slot.b, q);
       if (r.action == 1) {
          uint64_t begin;

@@ -40,6 +40,7 @@ struct ServeRequest {
    std::string error;
    double t_submit = 0, t_done = 0;  // seconds, steady clock
    bool done = false;
+   bool cancelled = false;  // cancel() was called before the result was ready
 };
 
 struct ServerConfig {
@@ -48,10 +49,13 @@ struct ServerConfig {
    uint32_t max_inflight = 4096;  // admitted, unfinished queries
    uint64_t memory_budget = 0;    // device bytes of in-flight micro-batches; 0 = a quarter of free memory
    double max_wait_ms = 0.25;     // a partial micro-batch launches once its oldest request waited this long
+   // Plain serving: every request runs alone through the single-query path (rhy_count /
+   // rhy_mutations / rhy_eval), one after the other in arrival order; no batching.
+   bool plain = false;
 };
 
 struct ServerStats {
-   uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0;
+   uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0, cancelled = 0;
    double p50_ms = 0, p99_ms = 0, mean_batch = 0, qps = 0;
    uint64_t peak_bytes = 0, budget_bytes = 0;
    uint32_t peak_inflight = 0;
@@ -69,6 +73,10 @@ class Server {
    // Blocks until the request is done (timeout_ms < 0: no limit); nullptr on timeout.
    std::shared_ptr<ServeRequest> wait(uint64_t id, double timeout_ms);
    void release(uint64_t id);
+   // Cancels a request that is not done: a queued one is dropped before it is admitted, one already
+   // on the device finishes there but its result is discarded. Either way its result reports
+   // "request cancelled". Returns false when the request was already done.
+   bool cancel(uint64_t id);
    ServerStats stats();
    void stop();
    // Open-loop replay of a request trace: every request is submitted at its arrival time (seconds
@@ -92,6 +100,7 @@ class Server {
    void advance(Slot& slot);
    void finish(Slot& slot);
    void fail(Slot& slot, const std::string& what);
+   void run_plain(ServeRequest& r, cudaStream_t stream);
    size_t request_bytes(const ServeRequest& r) const;
 
    Engine& engine_;

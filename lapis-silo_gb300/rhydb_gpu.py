@@ -150,14 +150,14 @@ class PlannerModel(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("max_batch", C.c_uint32), ("streams", C.c_uint32), ("max_inflight", C.c_uint32),
-                ("memory_budget", C.c_uint64), ("max_wait_ms", C.c_double)]
+                ("memory_budget", C.c_uint64), ("max_wait_ms", C.c_double), ("plain", C.c_uint32)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
                 ("batches", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_batch", C.c_double), ("qps", C.c_double), ("peak_bytes", C.c_uint64),
-                ("budget_bytes", C.c_uint64), ("peak_inflight", C.c_uint32)]
+                ("budget_bytes", C.c_uint64), ("peak_inflight", C.c_uint32), ("cancelled", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -249,6 +249,7 @@ def lib():
         "rhy_server_result": (I, [P, U64, C.c_double, C.POINTER(U64), P, C.c_size_t, C.POINTER(C.c_size_t), P,
                                   C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_double)]),
         "rhy_server_stats": (I, [P, C.POINTER(ServerStats)]),
+        "rhy_server_cancel": (I, [P, U64, C.POINTER(I)]),
         "rhy_server_replay": (I, [P, P, P, P, P, P, P, U32, P, C.POINTER(C.c_double)]),
         "rhy_server_stop": (None, [P]),
         "rhy_close": (None, [P]),
@@ -753,8 +754,8 @@ class Server:
     """Continuous-batching request loop over a Device (rhy_server_*)."""
 
     def __init__(self, device: "Device", max_batch: int = 0, streams: int = 0, max_inflight: int = 0,
-                 memory_budget: int = 0, max_wait_ms: float = -1.0):
-        cfg = ServerConfig(max_batch, streams, max_inflight, memory_budget, max_wait_ms)
+                 memory_budget: int = 0, max_wait_ms: float = -1.0, plain: bool = False):
+        cfg = ServerConfig(max_batch, streams, max_inflight, memory_budget, max_wait_ms, int(plain))
         h = C.c_void_p()
         _check(lib().rhy_server_start(device._h, C.byref(cfg), C.byref(h)))
         self._h = h
@@ -793,6 +794,12 @@ class Server:
         _check(lib().rhy_server_replay(self._h, C.cast(arr, C.c_void_p), _ptr(act), _ptr(col), _ptr(mp), _ptr(k),
                                        _ptr(at), n, _ptr(lat), C.byref(wall)))
         return lat[:n], wall.value
+
+    def cancel(self, rid: int) -> bool:
+        """Cancels a request that is not done; False if it had already finished."""
+        v = C.c_int()
+        _check(lib().rhy_server_cancel(self._h, rid, C.byref(v)))
+        return bool(v.value)
 
     def stats(self) -> dict:
         st = ServerStats()

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import rhydb_gpu as R
+from rawtable import oracle_for
 
 pytestmark = pytest.mark.gpu
 
@@ -73,6 +74,74 @@ def test_each_result_same_alone_and_in_the_mix(setup):
             bits, n = dev.compute_filter(qs[i])
             assert n == c
             assert ids == tuple(R.bits_to_rows(bits)[:int(ks[i])].tolist()), qs[i]
+
+
+@pytest.fixture(scope="module")
+def oracle_results(setup):
+    """The oracle's answer to every request of the mix: its count, its Mutations rows and its first
+    k row ids."""
+    t, dev, qs, acts, cols, props, ks = setup
+    orc = oracle_for(t)
+    mut = [i for i in range(len(qs)) if acts[i] == 1]
+    counts, tables = orc.check_batch(qs, cols, tables=mut)
+    out = []
+    for i in range(len(qs)):
+        rows = tuple(orc.mutation_rows(int(cols[i]), tables[i], float(props[i]))) if acts[i] == 1 else ()
+        ids = ()
+        if acts[i] == 2:
+            bits, _ = orc.compute_filter(qs[i])
+            ids = tuple(R.bits_to_rows(bits)[:int(ks[i])].tolist())
+        out.append((int(counts[i]), rows, ids))
+    return out
+
+
+def canon_rows(res):
+    rows = tuple((int(r["position"]), r["from_"].decode(), r["to"].decode(), int(r["count"]), int(r["coverage"]),
+                  float(r["proportion"])) for r in res["rows"])
+    return res["count"], rows, tuple(res["ids"].tolist())
+
+
+def test_served_results_equal_the_oracle(setup, oracle_results):
+    """Counts, Mutations rows and Details ids served by continuous batching and by the plain arm
+    (one request at a time through the single-query path) equal the oracle's."""
+    t, dev, qs, acts, cols, props, ks = setup
+    for plain in (False, True):
+        srv = R.Server(dev, max_batch=64, streams=3, plain=plain)
+        rids = [submit(srv, setup, i) for i in range(len(qs))]
+        got = [canon_rows(srv.result(r)) for r in rids]
+        st = srv.stats()
+        srv.stop()
+        for i in range(len(qs)):
+            assert got[i] == oracle_results[i], (plain, qs[i], acts[i])
+        assert st["completed"] == len(qs)
+        if plain:
+            assert st["batches"] == len(qs)  # no batching
+
+
+def test_cancel_and_timeout(setup):
+    """Requests queued behind others report RHY_TIMEOUT for a wait that runs out; cancelled requests
+    report RHY_CANCELLED and the others complete with their own results."""
+    t, dev, qs, acts, cols, props, ks = setup
+    srv = R.Server(dev, max_batch=4, streams=1)
+    mut = [i for i in range(len(qs)) if acts[i] == 1]
+    order = (mut * 4)[:200]
+    rids = [srv.submit(qs[i], 1, int(cols[i]), 0.05) for i in order]
+    with pytest.raises(R.RhyError) as e:
+        srv.result(rids[-1], timeout_ms=0)
+    assert e.value.code == 6
+    cancelled = [srv.cancel(r) for r in rids[100:]]
+    assert any(cancelled)
+    for j, r in enumerate(rids):
+        if j >= 100 and cancelled[j - 100]:
+            with pytest.raises(R.RhyError) as e:
+                srv.result(r)
+            assert e.value.code == 7
+        else:
+            assert srv.result(r)["count"] == dev.count(qs[order[j]])
+    st = srv.stats()
+    srv.stop()
+    assert st["cancelled"] == sum(cancelled)
+    assert st["completed"] + st["cancelled"] == len(rids)
 
 
 def test_admission_by_device_memory(setup):
