@@ -654,22 +654,32 @@ def main():
         s_qs = workloads.batching_workload(table, dev, n=args.shape_queries, seed=44,
                                            candidates=10 * args.shape_queries)
         pick_s = time.perf_counter() - t0
-        dev.batch_prepare(s_qs)
-        dev.batch_launch(sp, True, False)
-        dev.batch_capture_ex(sp, copy_in=False, copy_out=False)
-        for _ in range(3):
-            flush_l2()
-            dev.batch_replay(sp)
-        torch.cuda.synchronize()
-        s_ms = []
-        for _ in range(20):
-            flush_l2()
-            e0, e1 = ev(), ev()
-            e0.record(stream)
-            dev.batch_replay(sp)
-            e1.record(stream)
-            e1.synchronize()
-            s_ms.append(e0.elapsed_time(e1))
+
+        def shape_steps():
+            dev.batch_prepare(s_qs)
+            dev.batch_launch(sp, True, False)
+            dev.batch_capture_ex(sp, copy_in=False, copy_out=False)
+            for _ in range(3):
+                flush_l2()
+                dev.batch_replay(sp)
+            torch.cuda.synchronize()
+            out = []
+            for _ in range(20):
+                flush_l2()
+                e0, e1 = ev(), ev()
+                e0.record(stream)
+                dev.batch_replay(sp)
+                e1.record(stream)
+                e1.synchronize()
+                out.append(e0.elapsed_time(e1))
+            return out
+
+        shape_rule_ms = None
+        if planner["mode"] == "learned":  # the same trees under the rule-based ordering
+            dev.planner_mode(0)
+            shape_rule_ms = statistics.median(shape_steps())
+            dev.planner_mode(1)
+        s_ms = shape_steps()
         dev.batch_launch(sp, True, True)
         torch.cuda.synchronize()
         s_counts, _ = dev.batch_results()
@@ -678,7 +688,8 @@ def main():
                  "selectivity_min": float(sel.min()), "selectivity_max": float(sel.max()),
                  "queries_per_s": len(s_qs) / (statistics.median(s_ms) / 1000.0),
                  "batch_ms_p50": float(np.percentile(s_ms, 50)), "batch_ms_p99": float(np.percentile(s_ms, 99)),
-                 "steps": len(s_ms), "l2": "flushed before every step", "pick_s": round(pick_s, 2)}
+                 "steps": len(s_ms), "l2": "flushed before every step", "pick_s": round(pick_s, 2),
+                 "planner": planner["mode"], "rule_batch_ms_p50": shape_rule_ms}
 
     # ---------------- roofline: plain container pass ----------------
     payload_b, desc_b = dev.mutation_bytes(0)

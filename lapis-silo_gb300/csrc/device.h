@@ -23,17 +23,23 @@ constexpr int MAX_SEQ_COLS = 32;
 constexpr int MAX_DICT_COLS = 8;
 constexpr int MAX_DATE_COLS = 8;
 
-// One unit of the Mutations container pass (see mut_stream_kernel). e0/e1: payload-arena element
-// range (SU_ARRAYS: up to SU elements of one chunk's array payloads; SU_BITSET: the bitset's 4096
-// u16); c0/c1: descriptor range (arrays: every descriptor overlapping [e0, e1); bitset / run: one).
+// One unit of the Mutations container pass (see mut_chunk_kernel). e0/e1: payload-arena element
+// range (SU_ARRAYS: at most WU elements of one chunk's array payloads, e0 a multiple of 8 so the
+// unit is read with 16-byte loads; elements below the chunk's first array belong to no container
+// of the unit; SU_BITSET: the bitset's 4096 u16); c0/c1: descriptor range (arrays: every
+// descriptor overlapping [e0, e1); bitset / run: one).
 enum : uint32_t { SU_ARRAYS = 0, SU_BITSET = 1, SU_RUN = 2 };
-constexpr uint32_t SU = 4096;
+constexpr uint32_t WU = 1024;
 struct StreamUnit {
    uint32_t kind;
    uint32_t v;
    uint32_t e0, e1;
    uint32_t c0, c1;
    uint32_t pad[2];
+};
+// Units [u0, u1) of one chunk v: the work of one CTA of the container pass.
+struct ChunkTask {
+   uint32_t v, u0, u1, pad;
 };
 
 struct DevSeqCol {
@@ -45,6 +51,7 @@ struct DevSeqCol {
    const NRunEntry* nblk;
    const uint32_t* nblk_off;   // nblocks * nchunks + 1
    const StreamUnit* su;       // units of the Mutations container pass, chunk-major
+   const ChunkTask* tasks;     // CTAs of the container pass: unit ranges within one chunk
    const uint32_t* exc_toff;   // nchunks * TOFF_N: tile row-range offsets into exc
    const uint32_t* nblk_toff;  // nblocks * nchunks * TOFF_N: the same into each nblk bucket
    const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
@@ -60,6 +67,7 @@ struct DevSeqCol {
    uint32_t nsym;
    uint32_t nctrs;
    uint32_t nsu;
+   uint32_t ntasks;
    uint32_t valid_mask;        // symbols counted in a position's coverage (valid mutation symbols)
    const uint8_t* global_ref;  // L: the column's reference symbols (the "from" of a mutation)
    char chars[32];             // symbol -> character
@@ -170,9 +178,9 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
                       void* stream, uint32_t parts = MUT_PART_ALL | MUT_PART_SPARSE, uint64_t sparse_max = 0);
-// Testing the failure path of the container pass's bounded waits on the current device: while on,
-// each of its CTAs withholds the copy its first wait expects, so the wait gives up and the pass sets
-// error 7 (device error flag) instead of counting. Nothing is left in flight.
+// Testing the failure path of the filter kernels' bounded waits on the current device: while on,
+// the leaf payload copies they announce are never issued, so their waits give up and the kernels
+// set error 6 (DEVERR_WAIT_FILTER) instead of evaluating. Nothing is left in flight.
 void set_copy_withholding(bool on);
 
 // One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),

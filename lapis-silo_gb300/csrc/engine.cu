@@ -106,12 +106,15 @@ std::vector<CtrUnit> container_units(const SeqColumnImage& s, uint32_t nchunks) 
 }
 
 // Units of the Mutations container pass, chunk by chunk: the chunk's array payloads (back to back in
-// descriptor order) cut into SU-element pieces, each with the descriptors that overlap it, then one
-// unit per bitset and per run container.
-std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks) {
+// descriptor order) cut into pieces of at most WU elements starting on 8-element (16-byte)
+// boundaries, each with the descriptors that overlap it, then one unit per bitset and per run
+// container. first[v] is the first unit of chunk v (first[nchunks] = the number of units).
+std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks, std::vector<uint32_t>& first) {
    const ContainerSet& cs = s.vertical;
    std::vector<StreamUnit> out;
+   first.assign(nchunks + 1, 0);
    for (uint32_t v = 0; v < nchunks; ++v) {
+      first[v] = static_cast<uint32_t>(out.size());
       const uint32_t cb = cs.off[static_cast<size_t>(v) * s.L], ce = cs.off[static_cast<size_t>(v + 1) * s.L];
       std::vector<uint32_t> arr;
       for (uint32_t i = cb; i < ce; ++i)
@@ -119,10 +122,10 @@ std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks) 
       if (!arr.empty()) {
          const uint32_t A0 = cs.ctrs[arr.front()].payload;
          const uint32_t A1 = cs.ctrs[arr.back()].payload + cs.ctrs[arr.back()].card_m1 + 1u;
+         auto end_of = [&](size_t k) { return cs.ctrs[arr[k]].payload + cs.ctrs[arr[k]].card_m1 + 1u; };
          size_t lo = 0;  // first array ending after e0
-         for (uint32_t e0 = A0; e0 < A1; e0 += SU) {
-            const uint32_t e1 = std::min(e0 + SU, A1);
-            auto end_of = [&](size_t k) { return cs.ctrs[arr[k]].payload + cs.ctrs[arr[k]].card_m1 + 1u; };
+         for (uint32_t e0 = A0 & ~7u; e0 < A1; e0 += WU) {
+            const uint32_t e1 = std::min(e0 + WU, A1);
             while (lo < arr.size() && end_of(lo) <= e0) ++lo;
             size_t hi = lo;  // one past the last array starting before e1
             while (hi < arr.size() && cs.ctrs[arr[hi]].payload < e1) ++hi;
@@ -133,6 +136,37 @@ std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks) 
          const CtrDesc& d = cs.ctrs[i];
          if (d.type == CT_BITSET) out.push_back(StreamUnit{SU_BITSET, v, d.payload, d.payload + 4096, i, i + 1, {0, 0}});
          else if (d.type == CT_RUN) out.push_back(StreamUnit{SU_RUN, v, 0, 0, i, i + 1, {0, 0}});
+      }
+   }
+   first[nchunks] = static_cast<uint32_t>(out.size());
+   return out;
+}
+
+// CTAs of the container pass: each chunk's units cut into ranges of about the same bytes (payload
+// and descriptors), `ctas` ranges over the whole column, none spanning two chunks.
+std::vector<ChunkTask> chunk_tasks(const SeqColumnImage& s, const std::vector<StreamUnit>& units,
+                                   const std::vector<uint32_t>& first, uint32_t ctas) {
+   const ContainerSet& cs = s.vertical;
+   auto weight = [&](const StreamUnit& u) -> uint64_t {
+      const uint64_t desc = 16ull * (u.c1 - u.c0);
+      if (u.kind == SU_ARRAYS) return 2ull * (u.e1 - u.e0) + desc;
+      if (u.kind == SU_BITSET) return CHUNK_ROWS / 8 + desc;
+      return 4ull * cs.ctrs[u.c0].nruns + desc;
+   };
+   uint64_t total = 0;
+   for (const StreamUnit& u : units) total += weight(u);
+   const uint64_t per_task = std::max<uint64_t>(1, total / std::max(1u, ctas));
+   std::vector<ChunkTask> out;
+   for (uint32_t v = 0; v + 1 < first.size(); ++v) {
+      uint32_t u0 = first[v];
+      uint64_t acc = 0;
+      for (uint32_t u = first[v]; u < first[v + 1]; ++u) {
+         acc += weight(units[u]);
+         if (acc >= per_task || u + 1 == first[v + 1]) {
+            out.push_back(ChunkTask{v, u0, u + 1, 0});
+            u0 = u + 1;
+            acc = 0;
+         }
       }
    }
    return out;
@@ -198,9 +232,16 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
          d.nblk = upload(s.nblk);
          d.nblk_off = upload(s.nblk_off);
          {
-            const std::vector<StreamUnit> su = stream_units(s, nchunks);
+            std::vector<uint32_t> first;
+            const std::vector<StreamUnit> su = stream_units(s, nchunks, first);
             d.su = upload(su);
             d.nsu = static_cast<uint32_t>(su.size());
+            // one wave of the container pass's CTAs (five per SM)
+            int sms = 0;
+            cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), "SM count");
+            const std::vector<ChunkTask> tasks = chunk_tasks(s, su, first, static_cast<uint32_t>(std::max(sms, 1)) * 5u);
+            d.tasks = upload(tasks);
+            d.ntasks = static_cast<uint32_t>(tasks.size());
          }
          d.exc_toff = upload(s.exc_toff);
          d.nblk_toff = upload(s.nblk_toff);
@@ -1005,26 +1046,12 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    batch_times = BatchTimes{};
    double plan_ms = 0, prepare_ms = 0;
    clk::time_point launched;
-   // learned planning: one network inference for the whole call, before any part is on the device
-   // (while a persistent filter kernel holds the SMs an inference would wait for it)
-   const bool learned = use_learned_;
-   LearnedPlans lp;
-   if (learned) {
-      const auto t0 = clk::now();
-      learned_compile(exprs, 0, lp);
-      plan_ms += ms(t0, clk::now());
-   }
    try {
       for (size_t p = 0; p < parts.size(); ++p) {
          const auto t0 = clk::now();
-         std::vector<BatchQuery> qs;
-         if (learned) {
-            qs = learned_lower(lp, parts[p], 0);
-         } else {
-            std::vector<std::string> texts(parts[p].size());
-            for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
-            qs = plan_batch(texts, 0);
-         }
+         std::vector<std::string> texts(parts[p].size());
+         for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
+         std::vector<BatchQuery> qs = plan_batch(texts, 0);
          for (size_t j = 0; j < parts[p].size(); ++j) {
             const uint32_t i = parts[p][j];
             qs[j].action = actions ? actions[i] : 0;
@@ -1329,25 +1356,38 @@ void Engine::learned_compile(const std::vector<std::string>& exprs, uint32_t thr
    });
    batch_times.compile_ms += since(t0);
    t0 = clk::now();
-   std::vector<uint32_t> base(n + 1, 0);  // query i's nodes are rows base[i] .. base[i + 1]
-   for (uint32_t i = 0; i < n; ++i) base[i + 1] = base[i] + static_cast<uint32_t>(qnodes[i].size());
+   // network rows: every query's root (its predicted cost) and the nodes whose rule estimate is not
+   // exact (index scans keep their exact rule estimate and need no inference)
+   std::vector<uint32_t> base(n + 1, 0);  // query i's rows are base[i] .. base[i + 1]
+   std::vector<std::vector<uint32_t>> row_of(n);
+   each([&](uint32_t i) {
+      row_of[i].assign(qnodes[i].size(), UINT32_MAX);
+      uint32_t r = 0;
+      for (uint32_t k = 0; k < qnodes[i].size(); ++k)
+         if (k == 0 || !exact_by_rule(qx[i][k].data())) row_of[i][k] = r++;
+      base[i + 1] = r;
+   });
+   for (uint32_t i = 0; i < n; ++i) base[i + 1] += base[i];
    const uint32_t total = base[n];
    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
    float* X = planner_.net.staged_input(total);
    each([&](uint32_t i) {
       for (uint32_t k = 0; k < qnodes[i].size(); ++k)
-         planner_.normalize(qx[i][k].data(), X + static_cast<size_t>(base[i] + k) * PLAN_FEATURES);
+         if (row_of[i][k] != UINT32_MAX)
+            planner_.normalize(qx[i][k].data(), X + static_cast<size_t>(base[i] + row_of[i][k]) * PLAN_FEATURES);
    });
    const float* Y = total ? planner_.net.predict_staged(total) : nullptr;
    batch_times.predict_ms += since(t0);
    t0 = clk::now();
    const double rows = std::max(1u, table_.n_rows);
+   const float no_output[2] = {0.0f, 0.0f};  // exact nodes: the rule estimate, no network output read
    each([&](uint32_t i) {
       // (node, estimated rows) sorted by node for lookup while lowering
       auto& est = lp.est[i];
       est.resize(qnodes[i].size());
       for (uint32_t k = 0; k < qnodes[i].size(); ++k) {
-         const double sel = planner_.selectivity_of(qx[i][k].data(), Y + 2 * static_cast<size_t>(base[i] + k));
+         const float* y = row_of[i][k] != UINT32_MAX ? Y + 2 * static_cast<size_t>(base[i] + row_of[i][k]) : no_output;
+         const double sel = planner_.selectivity_of(qx[i][k].data(), y);
          est[k] = {qnodes[i][k], std::isfinite(sel) ? sel * rows : -1.0};
       }
       const double c = qnodes[i].empty() ? 0.0 : planner_.cost_of(Y + 2 * static_cast<size_t>(base[i]));

@@ -11,6 +11,9 @@
 // All arithmetic is integer; results are bit-exact with the CPU operators.
 #include <cuda_runtime.h>
 
+#include <stdexcept>
+#include <string>
+
 #include "device.h"
 
 namespace rhygpu {
@@ -164,10 +167,17 @@ __device__ __forceinline__ uint4 cover_ranges(const DevTable* __restrict__ tab, 
    return make_uint4(__ldg(xo + k0), __ldg(xo + k1), __ldg(no + k0), __ldg(no + k1));
 }
 
-// Waits for phase `parity` of the copies' barrier, bounded by 2 s on the GPU's global timer (a copy
-// lands in microseconds) and, as a second bound, by 2^26 polls of at most about 1 us each; false if
-// it gave up.
-__device__ __forceinline__ bool wait_copies(LeafCache& lc, uint32_t parity) {
+// Testing the failure path of the bounded waits: while set (on the current device), the threads that
+// stage leaf payloads announce their bytes on the item's barrier but never issue the bulk copies,
+// so the item's wait gives up (after 1 ms) and the kernel sets error 6 (DEVERR_WAIT_FILTER). No
+// copy is left in flight: the withheld copies never start. Off by default; set only through
+// set_copy_withholding.
+__device__ uint32_t g_withhold_leaf_copies = 0;
+
+// Waits for phase `parity` of the copies' barrier, bounded by `limit_ns` on the GPU's global timer
+// (2 s: a copy lands in microseconds) and, as a second bound, by 2^26 polls of at most about 1 us
+// each; false if it gave up.
+__device__ __forceinline__ bool wait_copies(LeafCache& lc, uint32_t parity, uint64_t limit_ns) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(&lc.bar));
    uint64_t t0 = 0;
    for (uint32_t i = 0; i < (1u << 26); ++i) {
@@ -181,7 +191,7 @@ __device__ __forceinline__ bool wait_copies(LeafCache& lc, uint32_t parity) {
       uint64_t now;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
       if (t0 == 0) t0 = now;
-      else if (now - t0 > 2000000000ull) return false;
+      else if (now - t0 > limit_ns) return false;
    }
    return false;
 }
@@ -195,6 +205,7 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
                              uint32_t& phase, int* err) {
    const DevTable* __restrict__ tab = c.tab;
    const uint32_t nl = lc.nl, ncov = lc.ncov;
+   const bool withhold = *static_cast<volatile uint32_t*>(&g_withhold_leaf_copies) != 0;
    // this thread's earlier shared-memory accesses (stack tiles, staged payloads of the previous
    // item) are ordered before the bulk copies into the same memory issued after the next barrier
    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -293,10 +304,11 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
          if (po != LC_NOPAY) {
             lc.poff[j] = static_cast<uint16_t>(po);
             asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-            asm volatile(
-               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(a0), "r"(bytes), "r"(bar)
-               : "memory");
+            if (!withhold)
+               asm volatile(
+                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                  "l"(a0), "r"(bytes), "r"(bar)
+                  : "memory");
             continue;
          }
       }
@@ -308,8 +320,9 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
    if (lc.pay_used == 0 && lc.ext_used == 0) return true;  // no copies this item
    if (threadIdx.x == 0)
       asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar) : "memory");
-   bool ok = wait_copies(lc, phase);
-   if (!ok) ok = wait_copies(lc, phase);  // once more before giving up with copies possibly in flight
+   const uint64_t limit = withhold ? 1000000ull : 2000000000ull;
+   bool ok = wait_copies(lc, phase, limit);
+   if (!ok) ok = wait_copies(lc, phase, limit);  // once more before giving up with copies possibly in flight
    phase ^= 1u;
    if (!__syncthreads_and(ok)) {
       if (threadIdx.x == 0) atomicExch(err, 6);
@@ -613,21 +626,20 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                return false;
             }
             const uint4* x4 = stk4 + (sp - 1) * W4;
-            uint32_t* planes = stk + (sp - 1 - P) * WW;
+            uint4* planes4 = stk4 + (sp - 1 - P) * W4;
             const bool neg = in.flags & 1;
+            // ripple-carry add of one bit per row into the bit-sliced counter, four words at a time
             for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) {
-               const uint4 xv = neg ? andnot4(valid4(w4, c), x4[w4]) : x4[w4];
-#pragma unroll
-               for (uint32_t j = 0; j < 4; ++j) {
-                  const uint32_t w = 4 * w4 + j;
-                  uint32_t carry = get4(xv, j);
-                  for (uint32_t i = 0; i < P && carry; ++i) {
-                     const uint32_t p = planes[i * WW + w];
-                     planes[i * WW + w] = p ^ carry;
-                     carry &= p;
-                  }
-                  if (carry) {  // saturate at 2^P - 1
-                     for (uint32_t i = 0; i < P; ++i) planes[i * WW + w] |= carry;
+               uint4 carry = neg ? andnot4(valid4(w4, c), x4[w4]) : x4[w4];
+               for (uint32_t i = 0; i < P && (carry.x | carry.y | carry.z | carry.w); ++i) {
+                  const uint4 p = planes4[i * W4 + w4];
+                  planes4[i * W4 + w4] = make_uint4(p.x ^ carry.x, p.y ^ carry.y, p.z ^ carry.z, p.w ^ carry.w);
+                  carry = make_uint4(carry.x & p.x, carry.y & p.y, carry.z & p.z, carry.w & p.w);
+               }
+               if (carry.x | carry.y | carry.z | carry.w) {  // saturate at 2^P - 1
+                  for (uint32_t i = 0; i < P; ++i) {
+                     const uint4 p = planes4[i * W4 + w4];
+                     planes4[i * W4 + w4] = make_uint4(p.x | carry.x, p.y | carry.y, p.z | carry.z, p.w | carry.w);
                   }
                }
             }
@@ -641,23 +653,23 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
                if (threadIdx.x == 0) atomicExch(err, 2);
                return false;
             }
-            uint32_t* planes = stk + (sp - P) * WW;
+            uint4* planes4 = stk4 + (sp - P) * W4;
             const bool exact = in.flags & 1;
+            // compare the counter with n from the top plane down, four words at a time
             for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) {
-               const uint4 vm = valid4(w4, c);
-#pragma unroll
-               for (uint32_t j = 0; j < 4; ++j) {
-                  const uint32_t w = 4 * w4 + j;
-                  uint32_t gt = 0, eq = 0xFFFFFFFFu;
-                  for (int i = static_cast<int>(P) - 1; i >= 0; --i) {
-                     const uint32_t p = planes[i * WW + w];
-                     const uint32_t nb = ((n >> i) & 1u) ? 0xFFFFFFFFu : 0u;
-                     gt |= eq & p & ~nb;
-                     eq &= ~(p ^ nb);
-                  }
-                  if (n >> P) eq = 0;  // n does not fit: the saturated count can only be below it
-                  planes[w] = (exact ? eq : (gt | eq)) & get4(vm, j);
+               uint4 gt = make_uint4(0, 0, 0, 0), eq = make_uint4(~0u, ~0u, ~0u, ~0u);
+               for (int i = static_cast<int>(P) - 1; i >= 0; --i) {
+                  const uint4 p = planes4[i * W4 + w4];
+                  const uint32_t nb = ((n >> i) & 1u) ? 0xFFFFFFFFu : 0u;
+                  gt = make_uint4(gt.x | (eq.x & p.x & ~nb), gt.y | (eq.y & p.y & ~nb), gt.z | (eq.z & p.z & ~nb),
+                                  gt.w | (eq.w & p.w & ~nb));
+                  eq = make_uint4(eq.x & ~(p.x ^ nb), eq.y & ~(p.y ^ nb), eq.z & ~(p.z ^ nb), eq.w & ~(p.w ^ nb));
                }
+               if (n >> P) eq = make_uint4(0, 0, 0, 0);  // n does not fit: the saturated count is below it
+               const uint4 vm = valid4(w4, c);
+               planes4[w4] = exact ? make_uint4(eq.x & vm.x, eq.y & vm.y, eq.z & vm.z, eq.w & vm.w)
+                                   : make_uint4((gt.x | eq.x) & vm.x, (gt.y | eq.y) & vm.y, (gt.z | eq.z) & vm.z,
+                                                (gt.w | eq.w) & vm.w);
             }
             sp = sp - P + 1;
             synced = false;
@@ -882,6 +894,12 @@ cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const
    filter_batch_kernel<<<grid, FT, smem, static_cast<cudaStream_t>(stream)>>>(
       d_table, d_code, d_queries, d_items, n_items, stack_bytes / 4, d_out_tiles, d_counts, d_next, d_err, d_aux);
    return cudaGetLastError();
+}
+
+void set_copy_withholding(bool on) {
+   const uint32_t v = on ? 1u : 0u;
+   const cudaError_t e = cudaMemcpyToSymbol(g_withhold_leaf_copies, &v, sizeof(v));
+   if (e != cudaSuccess) throw std::runtime_error(std::string("set_copy_withholding: ") + cudaGetErrorString(e));
 }
 
 }  // namespace rhygpu

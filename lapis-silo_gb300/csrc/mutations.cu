@@ -1,9 +1,9 @@
 // Mutations action kernels of the plain single-query path.
 //
-//  mut_stream_kernel every vertical container once: |F ∩ container| against the filter tile of its
+//  mut_chunk_kernel  every vertical container once: |F ∩ container| against the filter tile of its
 //                    chunk staged in shared memory; integer counts per (symbol, position)
-//                    (reference: mutations_node.cpp:139-189). The payload arena is streamed in
-//                    units of 16 KiB by TMA bulk copies into double-buffered shared memory.
+//                    (reference: mutations_node.cpp:139-189). Warps stream units of at most WU
+//                    array elements (or one bitset / run container) into registers.
 //  mut_cov_kernel    rows of F outside their covered region and inside missing intervals, from
 //                    position-sorted start / end events aggregated per position with warp ballots
 //                    (reference: mutations_node.cpp:51-136).
@@ -28,221 +28,142 @@ namespace rhygpu {
 
 namespace {
 
-// Testing the failure path of the bounded waits: when set (on the current device), every CTA of the
-// container pass announces the bytes of its first unit's copy on its barrier but never issues the
-// copy, so its wait gives up (after 1 ms) and the call reports error 7. No copy is left in
-// flight: the withheld copy never starts and the CTA waits for its other copy before it returns.
-// Off by default; set only through set_copy_withholding.
-__device__ uint32_t g_withhold_first_copy = 0;
-
 constexpr uint32_t MT = 256;
 constexpr uint32_t NW = MT / 32;
+constexpr uint32_t WU_VEC = WU / 8;         // uint4 of payload per array unit
+constexpr uint32_t WU_GROUPS = WU_VEC / 32;  // groups of 32 uint4 (one per lane) per array unit
 
-constexpr uint32_t STAGED_UNITS = 64;  // units of one CTA staged in shared memory
-constexpr uint32_t EPT = SU / MT;      // array elements per thread in a unit (16)
-constexpr uint32_t DESC_CAP = 256;     // descriptors of an array unit copied beside its payload
-constexpr uint32_t BUF4 = SU / 8 + DESC_CAP;  // uint4 per buffer: payload, then descriptors
-static_assert(EPT == 16, "units hold 16 elements per thread");
-
-// Block-wide exclusive prefix sum of one value per thread; *total receives the sum. Contains
-// one barrier; the caller separates consecutive calls with another.
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t* wsum, uint32_t* total) {
-   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   uint32_t incl = x;
-#pragma unroll
-   for (uint32_t o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= o) incl += y;
-   }
-   if (lane == 31) wsum[warp] = incl;
-   __syncthreads();
-   uint32_t before = 0, all = 0;
-#pragma unroll
-   for (uint32_t w = 0; w < NW; ++w) {
-      const uint32_t v = wsum[w];
-      before += w < warp ? v : 0u;
-      all += v;
-   }
-   *total = all;
-   return before + incl - x;
-}
-
-// Container pass of the Mutations action, streaming the payload arena. Persistent CTAs walk a
-// contiguous range of the column's stream units (chunk-major), staged in shared memory:
-//   SU_ARRAYS  up to SU consecutive elements of a chunk's array payloads (arrays are stored back to
-//              back in descriptor order), with the descriptor range [c0, c1) overlapping them;
-//   SU_BITSET  one bitset container; SU_RUN one run container.
-// Array and bitset payloads, and the first DESC_CAP descriptors of an array unit, are double-
-// buffered into shared memory by TMA bulk copies completing on one mbarrier (the copy of the next
-// unit is in flight while the current one is counted). For array units thread t tests elements
-// EPT t .. EPT t + EPT - 1 against the filter tile of the chunk (staged in shared memory), a
-// block prefix sum over the membership bits gives every container its |F ∩ c| as the difference
-// of two prefix values, added to counts[symbol][position] (containers cut by a unit boundary add
-// two partial counts). Full filters (|F| == rows) use the stored cardinalities
-// (reference: mutations_node.cpp:139-190, full path :240-266).
-__global__ void __launch_bounds__(MT, 6) mut_stream_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                        const uint32_t* __restrict__ filter,
-                                                        const unsigned long long* __restrict__ fcount,
-                                                        unsigned long long sparse_max, uint32_t* counts, int* err) {
-   extern __shared__ __align__(128) uint4 sm4[];  // two buffers (payload + descriptors), then the filter tile
-   __shared__ __align__(8) uint64_t bar[2];
-   __shared__ uint32_t wsum[NW], msk[MT], exq[MT];
-   __shared__ StreamUnit su[STAGED_UNITS];  // this CTA's units, staged once
+// Container pass of the Mutations action (reference: mutations_node.cpp:139-190, full path
+// :240-266). One CTA per task: a range of units of one chunk (host-built, ChunkTask). The CTA
+// stages the chunk's filter tile in shared memory once; then every warp claims units of the range
+// from a shared counter and counts them on its own, with no further CTA barrier:
+//   SU_ARRAYS  up to WU elements of the chunk's array payloads (arrays lie back to back in
+//              descriptor order), read by 16-byte loads straight into registers, lane l holding
+//              uint4 l + 32 g of group g. Each element (a row of the chunk) is tested against the
+//              tile; a warp prefix sum over the lanes' membership counts gives every container its
+//              |F ∩ c| as the difference of two prefix values (a container cut by a unit boundary
+//              adds two partial counts).
+//   SU_BITSET  one bitset: AND with the tile and popcount, 16 uint4 per lane.
+//   SU_RUN     one run container: the tile's popcount over each run.
+// Full filters (|F| == rows) add the stored cardinalities and read no payload.
+__global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __restrict__ tab, uint32_t col,
+                                                       const uint32_t* __restrict__ filter,
+                                                       const unsigned long long* __restrict__ fcount,
+                                                       unsigned long long sparse_max, uint32_t* counts) {
+   __shared__ __align__(16) uint32_t F[CHUNK_WORDS];
+   __shared__ uint32_t next_unit;
+   __shared__ uint16_t pre[NW][WU_GROUPS][32];  // per warp: lane's exclusive prefix within a group
+   __shared__ uint8_t msk[NW][WU_GROUPS][32];   // per warp: lane's 8 membership bits within a group
+   __shared__ uint32_t gpre[NW][WU_GROUPS + 1]; // per warp: exclusive prefix of the groups, then the total
    const unsigned long long fc = *fcount;
    if (fc == 0 || fc <= sparse_max) return;  // empty, or counted by the row-index pass
    const bool full = fc == tab->n_rows;
    const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t n_units = cs->nsu;
-   const uint32_t u0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * n_units / gridDim.x);
-   const uint32_t u1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * n_units / gridDim.x);
-   if (u0 >= u1) return;
-   const StreamUnit* __restrict__ gunits = cs->su;
-   const CtrDesc* __restrict__ ctrs = cs->ctrs;
-   const uint16_t* __restrict__ payload = cs->payload;
-   const uint32_t L = cs->L, tid = threadIdx.x;
-   const bool withhold = *static_cast<volatile uint32_t*>(&g_withhold_first_copy) != 0;
-   const uint64_t wait_limit = withhold ? WAIT_LIMIT_TEST_NS : WAIT_LIMIT_NS;
-   uint32_t* F = reinterpret_cast<uint32_t*>(sm4 + 2 * BUF4);
-   if (tid == 0) {
-      mbar_init(&bar[0]);
-      mbar_init(&bar[1]);
+   const ChunkTask task = cs->tasks[blockIdx.x];
+   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, L = cs->L;
+   if (!full) {
+      const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(task.v) * CHUNK_WORDS);
+      for (uint32_t i = tid; i < CHUNK_WORDS / 4; i += MT) reinterpret_cast<uint4*>(F)[i] = __ldg(src + i);
    }
-   for (uint32_t i = tid; i < u1 - u0 && i < STAGED_UNITS; i += MT) su[i] = gunits[u0 + i];
+   if (tid == 0) next_unit = task.u0;
    __syncthreads();
-   auto unit = [&](uint32_t u) { return u - u0 < STAGED_UNITS ? su[u - u0] : gunits[u]; };
-   auto copies = [&](const StreamUnit& U) { return !full && U.kind != SU_RUN; };
-   auto issue = [&](const StreamUnit& U, uint32_t b) {  // thread 0: payload and descriptors on one barrier
-      const uint32_t bytes = U.kind == SU_BITSET ? CHUNK_ROWS / 8 : ((U.e1 - U.e0) * 2u + 15u) & ~15u;
-      const uint32_t nd = U.kind == SU_ARRAYS ? min(U.c1 - U.c0, DESC_CAP) : 0u;
-      mbar_expect(&bar[b], bytes + nd * 16u);
-      bulk_copy_g2s_tx(sm4 + b * BUF4, payload + U.e0, bytes, &bar[b]);
-      if (nd) bulk_copy_g2s_tx(sm4 + b * BUF4 + SU / 8, ctrs + U.c0, nd * 16u, &bar[b]);
-   };
-   uint32_t issued0 = 0, issued1 = 0;  // copies issued into each buffer (the same in every thread)
-   {
-      const StreamUnit U = unit(u0);
-      if (copies(U)) {
-         if (tid == 0) {
-            if (withhold) mbar_expect(&bar[0], 16u);  // announced, never issued: the wait gives up
-            else issue(U, 0);
-         }
-         ++issued0;
-      }
-   }
-   uint32_t cur_v = 0xFFFFFFFFu;
-   bool ok = true;
-   for (uint32_t u = u0; u < u1 && ok; ++u) {
-      const uint32_t b = (u - u0) & 1u;
-      const StreamUnit U = unit(u);
-      if (!full && U.v != cur_v) {
-         const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(U.v) * CHUNK_WORDS);
-         for (uint32_t i = tid; i < CHUNK_WORDS / 4; i += MT) reinterpret_cast<uint4*>(F)[i] = __ldg(src + i);
-         cur_v = U.v;
-      }
-      if (u + 1 < u1) {
-         const StreamUnit N = unit(u + 1);
-         if (copies(N)) {
-            if (tid == 0) issue(N, b ^ 1u);
-            if (b) ++issued0;
-            else ++issued1;
-         }
-      }
-      if (copies(U)) ok = mbar_wait(&bar[b], ((b ? issued1 : issued0) - 1u) & 1u, wait_limit);
-      if (!__syncthreads_and(ok)) {
-         ok = false;  // in every thread: the cleanup below has a barrier
-         if (tid == 0) atomicExch(err, 7);
-         break;
-      }
+   const StreamUnit* __restrict__ units = cs->su;
+   const CtrDesc* __restrict__ ctrs = cs->ctrs;
+   const uint4* __restrict__ pay4 = reinterpret_cast<const uint4*>(cs->payload);
+   for (;;) {
+      uint32_t u = 0;
+      if (lane == 0) u = atomicAdd(&next_unit, 1u);
+      u = __shfl_sync(0xFFFFFFFFu, u, 0);
+      if (u >= task.u1) break;
+      const StreamUnit U = units[u];
       if (U.kind == SU_ARRAYS) {
          if (full) {
-            for (uint32_t c = U.c0 + tid; c < U.c1; c += MT) {
+            for (uint32_t c = U.c0 + lane; c < U.c1; c += 32) {
                const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
                const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
                if (d.type != CT_ARRAY) continue;
                const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
                if (s < e) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], e - s);
             }
-         } else {
-            const uint4* sdesc = sm4 + b * BUF4 + SU / 8;
-            const uint32_t n = U.e1 - U.e0;
-            const uint4* q = sm4 + b * BUF4 + 2 * tid;
-            uint32_t m = 0;
-            // element r of the chunk sets mask bit k when row r is in F: the filter word holding r,
-            // rotated right by (r - k) mod 32, has that row's bit at position k
-            if (n == SU) {
-#pragma unroll
-               for (uint32_t j = 0; j < 2; ++j) {
-                  const uint4 x = q[j];
-#pragma unroll
-                  for (uint32_t t = 0; t < 8; ++t) {
-                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
-                     const uint32_t w = F[r >> 5];
-                     m |= __funnelshift_r(w, w, r - k) & (1u << k);
-                  }
-               }
-            } else {
-#pragma unroll
-               for (uint32_t j = 0; j < 2; ++j) {
-                  const uint4 x = q[j];
-#pragma unroll
-                  for (uint32_t t = 0; t < 8; ++t) {
-                     const uint32_t r = u16_of(x, t), k = 8 * j + t;
-                     const uint32_t w = F[r >> 5];
-                     if (EPT * tid + k < n) m |= __funnelshift_r(w, w, r - k) & (1u << k);
-                  }
-               }
-            }
-            uint32_t total;
-            const uint32_t ex = block_excl_scan(__popc(m), wsum, &total);
-            msk[tid] = m;
-            exq[tid] = ex;
-            __syncthreads();
-            auto prefix = [&](uint32_t i) -> uint32_t {  // members among elements [0, i)
-               if (i / EPT >= MT) return total;
-               return exq[i / EPT] + __popc(msk[i / EPT] & ((1u << (i % EPT)) - 1u));
-            };
-            for (uint32_t c = U.c0 + tid; c < U.c1; c += MT) {
-               const uint4 raw = c - U.c0 < DESC_CAP ? sdesc[c - U.c0] : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
-               const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
-               if (d.type != CT_ARRAY) continue;
-               const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
-               if (s >= e) continue;
-               const uint32_t k = prefix(e - U.e0) - prefix(s - U.e0);
-               if (k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
-            }
+            continue;
          }
+         const uint32_t n = U.e1 - U.e0;  // U.e0 is a multiple of 8 (16-byte aligned), n <= WU
+         uint4 x[WU_GROUPS];
+#pragma unroll
+         for (uint32_t g = 0; g < WU_GROUPS; ++g) {
+            const uint32_t i = 32 * g + lane;
+            x[g] = 8 * i < n ? __ldg(pay4 + U.e0 / 8 + i) : make_uint4(0, 0, 0, 0);
+         }
+         uint32_t run = 0;  // members in the groups before g (the same in every lane)
+#pragma unroll
+         for (uint32_t g = 0; g < WU_GROUPS; ++g) {
+            const uint32_t i = 32 * g + lane;
+            uint32_t m = 0;
+#pragma unroll
+            for (uint32_t t = 0; t < 8; ++t) {
+               const uint32_t r = u16_of(x[g], t);
+               m |= ((F[r >> 5] >> (r & 31)) & 1u) << t;
+            }
+            if (8 * i + 8 > n) m &= 8 * i < n ? (1u << (n - 8 * i)) - 1u : 0u;  // past the unit's end
+            const uint32_t c = __popc(m);
+            uint32_t incl = c;
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+               const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+               if (lane >= o) incl += y;
+            }
+            pre[warp][g][lane] = static_cast<uint16_t>(incl - c);
+            msk[warp][g][lane] = static_cast<uint8_t>(m);
+            if (lane == 0) gpre[warp][g] = run;
+            run += __shfl_sync(0xFFFFFFFFu, incl, 31);
+         }
+         if (lane == 0) gpre[warp][WU_GROUPS] = run;
+         __syncwarp();
+         auto prefix = [&](uint32_t i) -> uint32_t {  // members among the unit's elements [0, i)
+            if (i >= WU) return gpre[warp][WU_GROUPS];
+            const uint32_t g = i / 256, k = (i / 8) % 32, t = i % 8;
+            return gpre[warp][g] + pre[warp][g][k] + __popc(msk[warp][g][k] & ((1u << t) - 1u));
+         };
+         for (uint32_t c = U.c0 + lane; c < U.c1; c += 32) {
+            const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
+            const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
+            if (d.type != CT_ARRAY) continue;
+            const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);
+            if (s >= e) continue;
+            const uint32_t k = prefix(e - U.e0) - prefix(s - U.e0);
+            if (k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
+         }
+         __syncwarp();  // the prefix arrays are rewritten by the warp's next unit
       } else {
          const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + U.c0);
          const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
          uint32_t k = 0;
          if (full) {
-            k = tid == 0 ? d.card_m1 + 1u : 0u;
+            k = lane == 0 ? d.card_m1 + 1u : 0u;
          } else if (U.kind == SU_BITSET) {
-            const uint4* x = sm4 + b * BUF4;
-            const uint4* f = reinterpret_cast<const uint4*>(F);
+            const uint4* f4 = reinterpret_cast<const uint4*>(F);
+            constexpr uint32_t BV = CHUNK_WORDS / 4 / 32, BB = 4;  // uint4 per lane; loads in flight
 #pragma unroll
-            for (uint32_t j = 0; j < CHUNK_WORDS / 4 / MT; ++j) {
-               const uint4 a = x[tid + j * MT], y = f[tid + j * MT];
-               k += __popc(a.x & y.x) + __popc(a.y & y.y) + __popc(a.z & y.z) + __popc(a.w & y.w);
+            for (uint32_t j0 = 0; j0 < BV; j0 += BB) {
+               uint4 a[BB];
+#pragma unroll
+               for (uint32_t j = 0; j < BB; ++j) a[j] = __ldg(pay4 + U.e0 / 8 + lane + 32 * (j0 + j));
+#pragma unroll
+               for (uint32_t j = 0; j < BB; ++j) {
+                  const uint4 y = f4[lane + 32 * (j0 + j)];
+                  k += __popc(a[j].x & y.x) + __popc(a[j].y & y.y) + __popc(a[j].z & y.z) + __popc(a[j].w & y.w);
+               }
             }
          } else {
-            const uint16_t* r = payload + d.payload;
-            for (uint32_t i = tid; i < d.nruns; i += MT) {
+            const uint16_t* r = cs->payload + d.payload;
+            for (uint32_t i = lane; i < d.nruns; i += 32) {
                const uint32_t s = __ldg(r + 2 * i);
                k += count_range(F, s, s + __ldg(r + 2 * i + 1) + 1u);
             }
          }
          k = __reduce_add_sync(0xFFFFFFFFu, k);
-         if ((tid & 31) == 0 && k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
+         if (lane == 0 && k) atomicAdd(&counts[static_cast<size_t>(d.sym) * L + d.key], k);
       }
-      __syncthreads();
-   }
-   if (!ok) {  // let the copies still in flight land before the CTA's shared memory is released
-      if (tid == 0) {
-         if (issued0) mbar_wait(&bar[0], (issued0 - 1u) & 1u, wait_limit);
-         if (issued1) mbar_wait(&bar[1], (issued1 - 1u) & 1u, wait_limit);
-      }
-      __syncthreads();
    }
 }
 
@@ -348,16 +269,11 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_kernel(const DevTable* __re
 
 }  // namespace
 
-void set_copy_withholding(bool on) {
-   const uint32_t v = on ? 1u : 0u;
-   const cudaError_t e = cudaMemcpyToSymbol(g_withhold_first_copy, &v, sizeof(v));
-   if (e != cudaSuccess) throw std::runtime_error(std::string("set_copy_withholding: ") + cudaGetErrorString(e));
-}
-
 void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
                       const EvItem* d_ev, uint32_t n_ev, const uint32_t* d_filter,
                       const unsigned long long* d_filter_count, uint32_t* d_counts, uint32_t* d_scratch, int* d_err,
                       void* stream, uint32_t parts, uint64_t sparse_max) {
+   (void)d_err;  // no kernel of this pass waits on anything: none reports a device error
    cudaStream_t s = static_cast<cudaStream_t>(stream);
    if (!(parts & MUT_PART_SPARSE)) sparse_max = 0;  // the dense passes count every filter
    if (sparse_max) {
@@ -365,26 +281,9 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
       mut_sparse_kernel<<<std::max(1u, std::min(groups / NW, 2048u)), MT, 0, s>>>(
          d_table, col, d_filter, d_filter_count, static_cast<unsigned long long>(sparse_max), d_counts, d_scratch);
    }
-   if ((parts & MUT_PART_CTR) && col_host.nsu > 0) {
-      const size_t smem = 2 * BUF4 * 16 + CHUNK_WORDS * 4;
-      // resident CTAs per device, computed once per device
-      static std::atomic<uint32_t> resident[64];
-      int dev = 0;
-      cudaGetDevice(&dev);
-      uint32_t res = dev >= 0 && dev < 64 ? resident[dev].load(std::memory_order_relaxed) : 0u;
-      if (res == 0) {
-         int sms = 0, per_sm = 0;
-         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mut_stream_kernel, MT, smem) != cudaSuccess ||
-             per_sm < 1)
-            per_sm = 1;
-         res = static_cast<uint32_t>(std::max(sms, 1) * per_sm);
-         if (dev >= 0 && dev < 64) resident[dev].store(res, std::memory_order_relaxed);
-      }
-      const uint32_t grid = std::min<uint32_t>(col_host.nsu, res);
-      mut_stream_kernel<<<grid, MT, smem, s>>>(d_table, col, d_filter, d_filter_count,
-                                               static_cast<unsigned long long>(sparse_max), d_counts, d_err);
-   }
+   if ((parts & MUT_PART_CTR) && col_host.ntasks > 0)
+      mut_chunk_kernel<<<col_host.ntasks, MT, 0, s>>>(d_table, col, d_filter, d_filter_count,
+                                                      static_cast<unsigned long long>(sparse_max), d_counts);
    if ((parts & MUT_PART_COV) && n_ev > 0)
       mut_cov_kernel<<<n_ev, MT, 0, s>>>(d_table, col, d_ev, d_filter, d_filter_count,
                                          static_cast<unsigned long long>(sparse_max), d_scratch);

@@ -14,9 +14,9 @@
 // NOALLOC_MAX_POSITIONS positions; longer columns are rejected. Every call on a device uses the
 // same array, so calls whose work overlaps on that GPU (other streams, other threads, other
 // handles) race and must be serialised by the caller. The array keeps the last call's contents;
-// each call clears the part it uses before its kernels run. Device errors (a bounded wait for bulk
-// copies that gave up) go to the caller's status word, never to the handle's own error flag, so
-// they neither pass unseen nor fall on a later call.
+// each call clears the part it uses before its kernels run. A device error of the pass would go to
+// the caller's status word, never to the handle's own error flag, so it could neither pass unseen
+// nor fall on a later call (the pass's kernels wait on nothing, so a completed pass leaves it 0).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -73,8 +73,7 @@ void mutations_noalloc(Engine& engine, uint32_t column, const uint32_t* d_filter
    cuda_check(cudaSetDevice(engine.device()), "cudaSetDevice");
    uint32_t* scratch = scratch_address(engine.device());
    cudaStream_t s = engine.stream_for(stream);
-   // the pass accumulates into both buffers, so they start from zero; the status starts clear and
-   // the kernels' bounded waits set it if they give up
+   // the pass accumulates into both buffers, so they start from zero; the status starts clear
    cuda_check(cudaMemsetAsync(scratch, 0, mut_scratch_words(col.L) * sizeof(uint32_t), s), "clear scratch");
    cuda_check(cudaMemsetAsync(d_counts, 0, static_cast<size_t>(col.nsym) * col.L * sizeof(uint32_t), s), "clear counts");
    cuda_check(cudaMemsetAsync(d_status, 0, sizeof(int), s), "clear status");

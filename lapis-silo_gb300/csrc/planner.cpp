@@ -41,13 +41,12 @@ float log2p(double x) { return static_cast<float>(std::log2(1.0 + x)); }
 
 constexpr double MIN_SEL = 1e-7;
 
-// The rule estimate's ln(selectivity) as encoded in feature 8, and whether the node is an index
-// scan (features 0 / 1), whose rule estimate is its exact cardinality (the containers of the
-// symbols of one position are disjoint, so their cardinalities add up to the rows).
+// The rule estimate's ln(selectivity) as encoded in feature 8.
 double rule_log_sel_of(const float* x) { return static_cast<double>(x[8]) * -std::log(MIN_SEL); }
-bool exact_by_rule(const float* x) { return x[0] > 0.5f || x[1] > 0.5f; }
 
 }  // namespace
+
+bool exact_by_rule(const float* x) { return x[0] > 0.5f || x[1] > 0.5f; }
 
 FeatureContext feature_context(const TableImage& t) {
    FeatureContext c;

@@ -25,6 +25,11 @@
 
 namespace rhygpu {
 
+// Whether a node (by its features) is an index scan (features 0 / 1), whose rule estimate is its
+// exact cardinality: the containers of the symbols of one position are disjoint, so their
+// cardinalities add up to the rows. The network's selectivity is not used for such nodes.
+bool exact_by_rule(const float* x);
+
 constexpr uint32_t PLAN_FEATURES = MLP_IN;
 
 // Table statistics the features are relative to.

@@ -670,14 +670,15 @@ class Device:
     def mutations_noalloc(self, column: int, d_filter: int, d_filter_count: int, d_counts: int, d_status: int,
                           stream=None):
         """Mutations pass over caller-owned device buffers (addresses as ints); allocates nothing.
-        Enqueued on `stream`; synchronise it before reading d_counts and the int at d_status (0, or
-        the device error code of a bounded wait that gave up)."""
+        Enqueued on `stream`; synchronise it before reading d_counts and the int at d_status (0
+        after a completed pass)."""
         _check(lib().rhy_mutations_noalloc(self._h, column, C.c_void_p(d_filter), C.c_void_p(d_filter_count),
                                            C.c_void_p(d_counts), C.c_void_p(d_status), stream))
 
     def test_withhold_copies(self, on: bool):
-        """Testing only: the Mutations container pass withholds one bulk copy per CTA, so its bounded
-        wait gives up and the call reports device error 7 (nothing is left in flight)."""
+        """Testing only: the filter kernels withhold the leaf payload copies their bounded waits
+        expect, so those waits give up and the calls report device error 6 (nothing is left in
+        flight)."""
         _check(lib().rhy_test_withhold_copies(self._h, int(on)))
 
     # ---- learned planner ----

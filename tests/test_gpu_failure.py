@@ -1,6 +1,7 @@
 """Failure paths on the GPU in the form this pool allows: a bounded device wait is made to run out
-(the bulk copy it waits for is withheld, so nothing is left in flight), the call returns an error
-status instead of hanging or trapping, and the handle's next calls succeed with correct results."""
+(the filter kernel's leaf payload copies are announced but withheld, so nothing is left in flight),
+the call returns an error status instead of hanging or trapping, and the handle's next calls
+succeed with correct results."""
 import numpy as np
 import pytest
 
@@ -18,41 +19,50 @@ def setup():
     dev.close()
 
 
-def _dense_query(table, dev):
-    """A filter of neither few rows nor every row: its Mutations action runs the container pass."""
-    return next(q for q in table.queries(200, seed=31) if 0.2 * table.n_rows < dev.count(q) < 0.8 * table.n_rows)
+def _queries(table):
+    return table.queries(40, seed=31)
 
 
 def test_wait_that_gives_up_returns_an_error_and_the_handle_recovers(setup):
     table, dev, orc = setup
-    q = _dense_query(table, dev)
+    qs = _queries(table)
+    failed = []
     dev.test_withhold_copies(True)
     try:
-        with pytest.raises(R.RhyError) as e:
-            dev.mutations(q, 0)
+        for q in qs:
+            try:
+                dev.mutations(q, 0)
+            except R.RhyError as e:
+                assert e.code == 3 and "gave up" in str(e), str(e)
+                failed.append(q)
     finally:
         dev.test_withhold_copies(False)
-    assert e.value.code == 3 and "gave up" in str(e.value)
+    assert failed  # programs whose leaves stage payload copies wait on them
     # the next calls on the same handle succeed and agree with the oracle
-    m, n = dev.mutations(q, 0)
-    om, on = orc.mutations(q, 0)
-    assert n == on and np.array_equal(m, om)
-    assert dev.count(q) == orc.count(q)
+    for q in failed[:5] + qs[:5]:
+        m, n = dev.mutations(q, 0)
+        om, on = orc.mutations(q, 0)
+        assert n == on and np.array_equal(m, om), q
+        assert dev.count(q) == orc.count(q)
 
 
-def test_wait_failure_does_not_touch_filter_only_calls(setup):
-    """Withholding affects only the container pass: counts and row sets are unaffected, and the
-    error flag of a failed Mutations call is not reported again by a later call."""
+def test_wait_failure_is_reported_once(setup):
+    """A failed count and a failed row set report the error on their own call; the error flag is
+    cleared, so the next call does not report it again."""
     table, dev, orc = setup
-    q = _dense_query(table, dev)
+    qs = _queries(table)
     dev.test_withhold_copies(True)
     try:
-        assert dev.count(q) == orc.count(q)
-        bits, n = dev.compute_filter(q)
-        obits, on = orc.compute_filter(q)
-        assert n == on and np.array_equal(bits, obits)
-        with pytest.raises(R.RhyError):
-            dev.mutations(q, 0)
+        errors = 0
+        for q in qs:
+            for call in (lambda: dev.count(q), lambda: dev.compute_filter(q)):
+                try:
+                    call()
+                except R.RhyError as e:
+                    assert e.code == 3
+                    errors += 1
     finally:
         dev.test_withhold_copies(False)
-    assert dev.count(q) == orc.count(q)
+    assert errors > 0
+    for q in qs:
+        assert dev.count(q) == orc.count(q), q
