@@ -138,7 +138,17 @@ const char* rhy_last_error(void);
 /* ---- tables (host) ---- */
 int rhy_generate(const RhyGenConfig* cfg, RhyTable** out);
 int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out);
+/* rhy_table_from_raw with the sequence columns built on GPU `device` (reference:
+ * SequenceColumn::appendChunk + finalize, src/rhydb/storage/column/sequence_column.cpp:100-212;
+ * TableInserter, src/rhydb/append/table_inserter.cpp:279-343): every row's coverage, missing
+ * intervals and stored symbols, the local-reference flips, and the containers are computed on the
+ * device; the rest of the image is finished on the host. The table equals rhy_table_from_raw's,
+ * byte for byte (rhy_seq_column_checksum). The device memory it uses is freed before it returns. */
+int rhy_table_from_raw_gpu(const RhyRawTable* raw, int device, uint32_t threads, RhyTable** out);
 int rhy_table_info(const RhyTable* t, RhyTableInfo* out);
+/* A 64-bit checksum of a sequence column's whole storage image (local reference, containers and
+ * payload, coverage, missing intervals, events, row index), to compare two builds of a table. */
+int rhy_seq_column_checksum(const RhyTable* t, uint32_t column, uint64_t* out);
 /* Names the dictionary column holding the table's primary key (the schema's primary_key, used by
  * MutProfileSequenceId; reference: src/rhydb/query_engine/scalar_expressions/mutation_profile.cpp:127-150).
  * NULL clears it. Call it before queries that use it run, not concurrently with them. */

@@ -15,6 +15,7 @@
 #include "engine.h"
 #include "server.h"
 #include "expr.h"
+#include "ingest.h"
 #include "noalloc.h"
 #include "op_program.h"
 #include "table.h"
@@ -151,14 +152,13 @@ int rhy_generate(const RhyGenConfig* cfg, RhyTable** out) {
    });
 }
 
-int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out) {
-   return guarded([&] {
-      need(raw, "raw");
-      need(out, "out");
-      *out = nullptr;
-      if (raw->n_rows == 0) throw std::invalid_argument("n_rows must be positive");
-      auto t = std::make_unique<RhyTable>();
-      rhygpu::RawTable& r = t->gen.table;
+namespace {
+
+// Copies and checks a caller's raw partition (the run order, dictionary ids, sequence kinds).
+void import_raw(const RhyRawTable* raw, rhygpu::RawTable& r) {
+   need(raw, "raw");
+   if (raw->n_rows == 0) throw std::invalid_argument("n_rows must be positive");
+   {
       r.n_rows = raw->n_rows;
       for (uint32_t c = 0; c < raw->n_seq; ++c) {
          const RhyRawSeqColumn& s = raw->seq[c];
@@ -221,9 +221,75 @@ int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out)
          col.days.assign(s.days, s.days + raw->n_rows);
          r.date.push_back(std::move(col));
       }
-      t->image = rhygpu::build_table(r, threads);
+   }
+}
+
+}  // namespace
+
+int rhy_table_from_raw(const RhyRawTable* raw, uint32_t threads, RhyTable** out) {
+   return guarded([&] {
+      need(out, "out");
+      *out = nullptr;
+      auto t = std::make_unique<RhyTable>();
+      import_raw(raw, t->gen.table);
+      t->image = rhygpu::build_table(t->gen.table, threads);
       make_views(*t);
       *out = t.release();
+   });
+}
+
+int rhy_table_from_raw_gpu(const RhyRawTable* raw, int device, uint32_t threads, RhyTable** out) {
+   return guarded([&] {
+      need(out, "out");
+      *out = nullptr;
+      auto t = std::make_unique<RhyTable>();
+      import_raw(raw, t->gen.table);
+      t->image = rhygpu::build_table_gpu(t->gen.table, device, threads);
+      make_views(*t);
+      *out = t.release();
+   });
+}
+
+int rhy_seq_column_checksum(const RhyTable* t, uint32_t column, uint64_t* out) {
+   return guarded([&] {
+      need(t, "table");
+      need(out, "out");
+      const rhygpu::SeqColumnImage& c = t->image.seq.at(column);
+      uint64_t h = 1469598103934665603ull;  // FNV-1a over every array of the column's image
+      auto bytes = [&](const void* p, size_t n) {
+         const auto* b = static_cast<const unsigned char*>(p);
+         for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+      };
+      auto vec = [&](const auto& v) {
+         const uint64_t n = v.size();
+         bytes(&n, sizeof n);
+         if (n) bytes(v.data(), v.size() * sizeof(v[0]));
+      };
+      vec(c.local_ref);
+      vec(c.vertical.ctrs);
+      vec(c.vertical.payload);
+      vec(c.vertical.off);
+      vec(c.vertical.stats);
+      vec(c.null_rows);
+      vec(c.cov_exc);
+      vec(c.cov_exc_off);
+      vec(c.nrow_off);
+      vec(c.nrow_start);
+      vec(c.nrow_end);
+      vec(c.nblk);
+      vec(c.nblk_off);
+      vec(c.exc_toff);
+      vec(c.nblk_toff);
+      vec(c.mstart);
+      vec(c.mend);
+      vec(c.mstart_off);
+      vec(c.mend_off);
+      vec(c.cstart);
+      vec(c.cend);
+      vec(c.hrow_off);
+      vec(c.hent);
+      bytes(&c.flipped_positions, sizeof c.flipped_positions);
+      *out = h;
    });
 }
 

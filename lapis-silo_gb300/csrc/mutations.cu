@@ -32,14 +32,17 @@ constexpr uint32_t MT = 256;
 constexpr uint32_t NW = MT / 32;
 constexpr uint32_t WU_VEC = WU / 8;         // uint4 of payload per array unit
 constexpr uint32_t WU_GROUPS = WU_VEC / 32;  // groups of 32 uint4 (one per lane) per array unit
+constexpr uint32_t TASK_UNITS = 128;         // units of a task staged in shared memory (the rest read from global)
 
 // Container pass of the Mutations action (reference: mutations_node.cpp:139-190, full path
 // :240-266). One CTA per task: a range of units of one chunk (host-built, ChunkTask). The CTA
-// stages the chunk's filter tile in shared memory once; then every warp claims units of the range
-// from a shared counter and counts them on its own, with no further CTA barrier:
+// stages the chunk's filter tile and the task's unit records in shared memory once; then every warp
+// claims units of the range from a shared counter and counts them on its own, with no further CTA
+// barrier:
 //   SU_ARRAYS  up to WU elements of the chunk's array payloads (arrays lie back to back in
 //              descriptor order), read by 16-byte loads straight into registers, lane l holding
-//              uint4 l + 32 g of group g. Each element (a row of the chunk) is tested against the
+//              uint4 l + 32 g of group g, with the unit's first 32 descriptors loaded beside
+//              them. Each element (a row of the chunk) is tested against the
 //              tile; a warp prefix sum over the lanes' membership counts gives every container its
 //              |F ∩ c| as the difference of two prefix values (a container cut by a unit boundary
 //              adds two partial counts).
@@ -51,6 +54,7 @@ __global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __rest
                                                        const unsigned long long* __restrict__ fcount,
                                                        unsigned long long sparse_max, uint32_t* counts) {
    __shared__ __align__(16) uint32_t F[CHUNK_WORDS];
+   __shared__ __align__(16) StreamUnit su[TASK_UNITS];
    __shared__ uint32_t next_unit;
    __shared__ uint16_t pre[NW][WU_GROUPS][32];  // per warp: lane's exclusive prefix within a group
    __shared__ uint8_t msk[NW][WU_GROUPS][32];   // per warp: lane's 8 membership bits within a group
@@ -65,9 +69,10 @@ __global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __rest
       const uint4* src = reinterpret_cast<const uint4*>(filter + static_cast<size_t>(task.v) * CHUNK_WORDS);
       for (uint32_t i = tid; i < CHUNK_WORDS / 4; i += MT) reinterpret_cast<uint4*>(F)[i] = __ldg(src + i);
    }
+   const StreamUnit* __restrict__ units = cs->su;
+   for (uint32_t i = tid; i < task.u1 - task.u0 && i < TASK_UNITS; i += MT) su[i] = units[task.u0 + i];
    if (tid == 0) next_unit = task.u0;
    __syncthreads();
-   const StreamUnit* __restrict__ units = cs->su;
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint4* __restrict__ pay4 = reinterpret_cast<const uint4*>(cs->payload);
    for (;;) {
@@ -75,7 +80,7 @@ __global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __rest
       if (lane == 0) u = atomicAdd(&next_unit, 1u);
       u = __shfl_sync(0xFFFFFFFFu, u, 0);
       if (u >= task.u1) break;
-      const StreamUnit U = units[u];
+      const StreamUnit U = u - task.u0 < TASK_UNITS ? su[u - task.u0] : units[u];
       if (U.kind == SU_ARRAYS) {
          if (full) {
             for (uint32_t c = U.c0 + lane; c < U.c1; c += 32) {
@@ -94,6 +99,9 @@ __global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __rest
             const uint32_t i = 32 * g + lane;
             x[g] = 8 * i < n ? __ldg(pay4 + U.e0 / 8 + i) : make_uint4(0, 0, 0, 0);
          }
+         // the unit's first 32 descriptors, loaded beside the payload (one round trip for both)
+         const uint4 d0 = U.c0 + lane < U.c1 ? __ldg(reinterpret_cast<const uint4*>(ctrs) + U.c0 + lane)
+                                             : make_uint4(0, 0, 0, 0);
          uint32_t run = 0;  // members in the groups before g (the same in every lane)
 #pragma unroll
          for (uint32_t g = 0; g < WU_GROUPS; ++g) {
@@ -125,7 +133,7 @@ __global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __rest
             return gpre[warp][g] + pre[warp][g][k] + __popc(msk[warp][g][k] & ((1u << t) - 1u));
          };
          for (uint32_t c = U.c0 + lane; c < U.c1; c += 32) {
-            const uint4 raw = __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
+            const uint4 raw = c - U.c0 < 32 ? d0 : __ldg(reinterpret_cast<const uint4*>(ctrs) + c);
             const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&raw);
             if (d.type != CT_ARRAY) continue;
             const uint32_t s = max(d.payload, U.e0), e = min(d.payload + d.card_m1 + 1u, U.e1);

@@ -1,5 +1,6 @@
 // Ingestion of a raw table into the storage image (see table.h for the layout).
 #include "table.h"
+#include "table_build.h"
 
 #include <algorithm>
 #include <cstring>
@@ -138,6 +139,13 @@ void assemble(std::vector<ChunkContainers>& chunks, uint32_t nkeys, ContainerSet
    // 16-byte loads that may cover up to seven u16 past a container's last element
    while (cs.payload.size() % 8) cs.payload.push_back(0);
    cs.payload.insert(cs.payload.end(), 8, 0);
+   finish_container_set(cs, static_cast<uint32_t>(chunks.size()));
+}
+
+}  // namespace
+
+void finish_container_set(ContainerSet& cs, uint32_t nchunks) {
+   const uint32_t nkeys = cs.nkeys;
    cs.stats.assign(static_cast<size_t>(nkeys) * STAT_SYMS, KeyStats{});
    for (const auto& d : cs.ctrs) {
       KeyStats& st = cs.stats[static_cast<size_t>(d.key) * STAT_SYMS + d.sym];
@@ -145,19 +153,13 @@ void assemble(std::vector<ChunkContainers>& chunks, uint32_t nkeys, ContainerSet
       ++st.nctr;
       st.nbits += d.type == CT_BITSET;
    }
-   const uint64_t nslots = static_cast<uint64_t>(chunks.size()) * nkeys;
+   const uint64_t nslots = static_cast<uint64_t>(nchunks) * nkeys;
    cs.off.assign(nslots + 1, 0);
    for (const auto& d : cs.ctrs) cs.off[static_cast<uint64_t>(d.v) * nkeys + d.key + 1]++;
    for (uint64_t i = 0; i < nslots; ++i) cs.off[i + 1] += cs.off[i];
 }
 
-struct ChunkRows {
-   std::vector<uint64_t> keys;
-   std::vector<CovExc> exc;
-   std::vector<uint32_t> nr_off;  // chunk_size + 1
-   std::vector<uint32_t> nr_s, nr_e;
-   std::vector<uint32_t> nulls;
-};
+namespace {
 
 void ingest_chunk(const RawSeqColumn& raw, const Alphabet& A, const std::vector<uint8_t>& ref_sym, uint32_t L,
                   uint32_t v, uint32_t size, ChunkRows& out) {
@@ -368,8 +370,9 @@ void build_row_index(SeqColumnImage& col, const std::vector<uint32_t>& chunk_siz
    });
 }
 
-SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
-   SeqColumnImage col;
+}  // namespace
+
+void init_seq_column(const RawSeqColumn& raw, SeqColumnImage& col) {
    col.name = raw.name;
    col.kind = raw.kind;
    const Alphabet& A = alphabet(raw.kind);
@@ -384,6 +387,15 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
       col.global_ref[p] = static_cast<uint8_t>(s);
    }
    col.local_ref = col.global_ref;
+}
+
+namespace {
+
+SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
+   SeqColumnImage col;
+   init_seq_column(raw, col);
+   const Alphabet& A = alphabet(raw.kind);
+   const uint32_t L = col.L;
    const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
    const uint32_t nsym = A.count;
 
@@ -492,7 +504,16 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
       std::vector<uint64_t>().swap(chunks[v].keys);
    });
    assemble(enc, L, col.vertical);
+   finish_seq_column(col, chunks, chunk_sizes, threads);
+   return col;
+}
 
+}  // namespace
+
+void finish_seq_column(SeqColumnImage& col, const std::vector<ChunkRows>& chunks, const std::vector<uint32_t>& chunk_sizes,
+                       uint32_t threads) {
+   const uint32_t nchunks = static_cast<uint32_t>(chunk_sizes.size());
+   const uint32_t L = col.L;
    // ---- coverage, nulls, missing intervals ----
    col.cov_exc_off.assign(1, 0);
    for (uint32_t v = 0; v < nchunks; ++v) {
@@ -559,8 +580,9 @@ SeqColumnImage build_seq_column(const RawSeqColumn& raw, const std::vector<uint3
            [&](uint32_t i) { return col.nblk[i].row & 0xFFFFu; });
    build_mutation_events(col, chunks, chunk_sizes);
    build_row_index(col, chunk_sizes, threads);
-   return col;
 }
+
+namespace {
 
 DictColumnImage build_dict_column(const RawDictColumn& raw, const std::vector<uint32_t>& chunk_sizes, uint32_t threads) {
    DictColumnImage col;
@@ -587,8 +609,7 @@ DictColumnImage build_dict_column(const RawDictColumn& raw, const std::vector<ui
 
 }  // namespace
 
-TableImage build_table(const RawTable& raw, uint32_t threads) {
-   TableImage t;
+void build_table_frame(const RawTable& raw, TableImage& t) {
    t.n_rows = raw.n_rows;
    if (raw.n_rows == 0) throw std::invalid_argument("a partition needs at least one row");
    for (uint32_t left = raw.n_rows; left > 0;) {
@@ -597,11 +618,12 @@ TableImage build_table(const RawTable& raw, uint32_t threads) {
       left -= s;
    }
    if (t.chunk_sizes.size() >= 65535) throw std::invalid_argument("too many chunks");
-   for (const auto& c : raw.seq) {
+   for (const auto& c : raw.seq)
       if (c.is_null.size() != raw.n_rows || c.row_off.size() != raw.n_rows + 1ull)
          throw std::invalid_argument("row count mismatch in column " + c.name);
-      t.seq.push_back(build_seq_column(c, t.chunk_sizes, threads));
-   }
+}
+
+void build_metadata_columns(const RawTable& raw, TableImage& t, uint32_t threads) {
    for (const auto& c : raw.dict) {
       if (c.ids.size() != raw.n_rows) throw std::invalid_argument("row count mismatch in column " + c.name);
       t.dict.push_back(build_dict_column(c, t.chunk_sizes, threads));
@@ -614,6 +636,13 @@ TableImage build_table(const RawTable& raw, uint32_t threads) {
       for (uint32_t i = 0; i < raw.n_rows; ++i) d.days[i] = c.days[i];  // full chunks: global id == row index
       t.date.push_back(std::move(d));
    }
+}
+
+TableImage build_table(const RawTable& raw, uint32_t threads) {
+   TableImage t;
+   build_table_frame(raw, t);
+   for (const auto& c : raw.seq) t.seq.push_back(build_seq_column(c, t.chunk_sizes, threads));
+   build_metadata_columns(raw, t, threads);
    return t;
 }
 

@@ -189,6 +189,8 @@ def lib():
         "rhy_generate": (I, [C.POINTER(GenConfig), C.POINTER(P)]),
         "rhy_table_from_raw": (I, [C.POINTER(RawTable), U32, C.POINTER(P)]),
         "rhy_table_info": (I, [P, C.POINTER(TableInfo)]),
+        "rhy_table_from_raw_gpu": (I, [C.POINTER(RawTable), I, U32, C.POINTER(P)]),
+        "rhy_seq_column_checksum": (I, [P, U32, C.POINTER(U64)]),
         "rhy_table_set_primary_key": (I, [P, C.c_char_p]),
         "rhy_seq_column_info": (I, [P, U32, C.POINTER(SeqColumnInfo)]),
         "rhy_seq_column_name": (I, [P, U32, C.c_char_p, C.c_size_t]),
@@ -329,6 +331,19 @@ class Table:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.rhy_table_free(self._h)
             self._h = None
+
+    @classmethod
+    def from_raw_gpu(cls, raw: RawTable, device: int = 0, threads: int = 0) -> "Table":
+        """The same table as from_raw, its sequence columns built on a GPU."""
+        h = C.c_void_p()
+        _check(lib().rhy_table_from_raw_gpu(C.byref(raw), device, threads, C.byref(h)))
+        return cls(h)
+
+    def checksum(self, column: int) -> int:
+        """64-bit checksum of a sequence column's whole storage image."""
+        v = C.c_uint64()
+        _check(lib().rhy_seq_column_checksum(self._h, column, C.byref(v)))
+        return v.value
 
     def set_primary_key(self, dict_column: str | None) -> None:
         """Names the dictionary column holding the primary key (MutProfileSequenceId)."""
