@@ -295,8 +295,9 @@ int rhy_batch(RhyDevice* d, const char* const* exprs, const int* actions, const 
  * which are copied when *n_rows <= rows_cap (otherwise rhy_batch_rows_fetch copies them without
  * recomputing). Query i's rows are rows[row_begin[i] .. row_begin[i] + row_count[i]).
  * min_proportions may be NULL (0.05 for every query); each must lie in [0, 1]. The batch is planned
- * and run in parts (the Mutations and Details queries about 256 at a time, then the counts) so that
- * planning a part overlaps the device work of the ones before it; results do not depend on it. */
+ * and run in parts (the Mutations and Details queries up to 1,024 at a time, then the counts) so
+ * that planning a part overlaps the device work of the ones before it; the first part is planned by
+ * the rule even when the learned planner is on. Results do not depend on it. */
 int rhy_batch_rows(RhyDevice* d, const char* const* exprs, const int* actions, const uint32_t* columns,
                    const double* min_proportions, uint32_t n, uint32_t tile_bits, void* stream, uint64_t* counts,
                    RhyMutationRow* rows, size_t rows_cap, uint64_t* row_begin, uint32_t* row_count, size_t* n_rows);

@@ -1013,9 +1013,11 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
    s = stream_for(s);
    const uint32_t n = static_cast<uint32_t>(exprs.size());
-   // first the Mutations and Details queries, in parts of about PIPELINE_PART (one dense pass each)
-   // so that the device starts after the first of them is planned (without any: the first quarter
-   // of the counts); then the counts, planned while the first parts run
+   // first the Mutations and Details queries, in parts of at most PIPELINE_HEAVY (the device splits
+   // a part's dense Mutations queries into passes of 256, and sparse ones take no pass, so one part
+   // reads the containers as few times as the whole batch would), so that the device starts after
+   // they are planned (without any: the first quarter of the counts); then the counts, planned
+   // while the first part runs
    std::vector<std::vector<uint32_t>> parts(1);
    std::vector<uint32_t> light, heavy;
    for (uint32_t i = 0; i < n; ++i) {
@@ -1024,7 +1026,7 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
       (a == 0 ? light : heavy).push_back(i);
    }
    {
-      const size_t k = std::max<size_t>(1, heavy.size() / PIPELINE_PART);  // heavy parts
+      const size_t k = std::max<size_t>(1, (heavy.size() + PIPELINE_HEAVY - 1) / PIPELINE_HEAVY);  // heavy parts
       parts.assign(k, {});
       for (size_t j = 0; j < k; ++j)
          parts[j].assign(heavy.begin() + heavy.size() * j / k, heavy.begin() + heavy.size() * (j + 1) / k);
@@ -1051,7 +1053,9 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
          const auto t0 = clk::now();
          std::vector<std::string> texts(parts[p].size());
          for (size_t j = 0; j < parts[p].size(); ++j) texts[j] = exprs[parts[p][j]];
-         std::vector<BatchQuery> qs = plan_batch(texts, 0);
+         // the device is idle until the first part launches: that part is planned by the rule, the
+         // later ones (learned planner on) with the network's inference while the device runs
+         std::vector<BatchQuery> qs = plan_batch(texts, 0, p == 0);
          for (size_t j = 0; j < parts[p].size(); ++j) {
             const uint32_t i = parts[p][j];
             qs[j].action = actions ? actions[i] : 0;
@@ -1305,7 +1309,7 @@ void Engine::set_planner_mode(int mode) {
    use_learned_ = mode == 1;
 }
 
-std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs, uint32_t threads) {
+std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs, uint32_t threads, bool rule_only) {
    const uint32_t n = static_cast<uint32_t>(exprs.size());
    // threads == 0: the engine's persistent workers; otherwise that many threads of their own
    auto each = [&](auto&& fn) {
@@ -1315,7 +1319,7 @@ std::vector<BatchQuery> Engine::plan_batch(const std::vector<std::string>& exprs
    using clk = std::chrono::steady_clock;
    auto since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
    auto t0 = clk::now();
-   if (!use_learned_) {
+   if (!use_learned_ || rule_only) {
       std::vector<BatchQuery> qs(n);
       const Estimator est = rule_estimator(table_);
       LowerOptions lo;

@@ -239,11 +239,12 @@ class Engine {
    void batch_rows_fetch(cudaStream_t stream, DevMutationRow* rows, size_t cap);
    // batch_rows of a whole batch given as text, planned and run in parts so that the host plans a
    // part while the device runs the ones before it: first the Mutations and Details queries in
-   // parts of about PIPELINE_PART (a dense Mutations pass takes up to 256 queries; the first
-   // quarter of the counts when there are none), then the Aggregated counts. Results equal
-   // batch_rows of the whole batch; the rows come in part order. A counts part of fewer than
-   // PIPELINE_PART queries joins the part before it. The caller holds mu.
+   // parts of at most PIPELINE_HEAVY (the first quarter of the counts when there are none), then
+   // the Aggregated counts. Results equal batch_rows of the whole batch; the rows come in part
+   // order. A counts part of fewer than PIPELINE_PART queries joins the part before it. The caller
+   // holds mu.
    static constexpr uint32_t PIPELINE_PART = 256;
+   static constexpr uint32_t PIPELINE_HEAVY = 1024;
    size_t batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
                                const double* min_proportions, uint32_t tile_bits, cudaStream_t stream,
                                DevMutationRow* rows, size_t cap, uint64_t* counts, uint64_t* row_begin,
@@ -270,13 +271,15 @@ class Engine {
    // them against the rule; the verdict replaces the planner's acceptance (a rejected network
    // leaves the learned mode).
    PlannerStats planner_evaluate(const std::vector<std::string>& exprs);
-   // 0: rule-based ordering; 1: learned (only once a trained network was accepted by the judge).
+   // 0: rule-based ordering; 1: learned (only once a trained network was accepted against the
+   // rule-based ordering on held-out traces).
    void set_planner_mode(int mode);
    int planner_mode() const { return use_learned_ ? 1 : 0; }
    Planner& planner() { return planner_; }
    // Plans a batch: rule-based, or with the learned planner's estimates (one GPU inference over
-   // all operator nodes of all expressions) and a predicted cost per query. The caller holds mu.
-   std::vector<BatchQuery> plan_batch(const std::vector<std::string>& exprs, uint32_t threads);
+   // all operator nodes of all expressions) and a predicted cost per query. `rule_only` plans with
+   // the rule even when the learned planner is on. The caller holds mu.
+   std::vector<BatchQuery> plan_batch(const std::vector<std::string>& exprs, uint32_t threads, bool rule_only = false);
    // The learned planner in two steps: learned_compile compiles and featurises every expression and
    // runs one network inference over all their operator nodes; learned_lower lowers a subset of
    // them with those estimates (and frees their trees). The caller holds mu.
