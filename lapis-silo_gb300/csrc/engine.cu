@@ -236,10 +236,10 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
             const std::vector<StreamUnit> su = stream_units(s, nchunks, first);
             d.su = upload(su);
             d.nsu = static_cast<uint32_t>(su.size());
-            // one wave of the container pass's CTAs (five per SM)
+            // one wave of the container pass's CTAs (six per SM: 40 registers per thread)
             int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), "SM count");
-            const std::vector<ChunkTask> tasks = chunk_tasks(s, su, first, static_cast<uint32_t>(std::max(sms, 1)) * 5u);
+            const std::vector<ChunkTask> tasks = chunk_tasks(s, su, first, static_cast<uint32_t>(std::max(sms, 1)) * 6u);
             d.tasks = upload(tasks);
             d.ntasks = static_cast<uint32_t>(tasks.size());
          }

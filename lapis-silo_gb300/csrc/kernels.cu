@@ -95,6 +95,8 @@ constexpr uint32_t LC_NONE = 0xFFFFFFFFu;
 constexpr uint32_t LC_PAY = 2048;   // u16 of small-array payloads copied into shared memory per item
 constexpr uint32_t LC_SMALL = 64;   // arrays up to this cardinality are copied
 constexpr uint16_t LC_NOPAY = 0xFFFF;
+constexpr uint32_t LC_BIG = 0x80000000u;
+constexpr uint32_t LC_OWNER_MAX = 256;  // leaves of at most this many copied rows are set by their words' owners
 
 struct LeafCache {
    uint4 desc[LC_DESCS];
@@ -113,6 +115,8 @@ struct LeafCache {
    uint32_t n[LC_LEAVES];
    uint32_t symmask[LC_LEAVES];  // symbols the leaf ORs (every container for dictionary leaves)
    uint32_t match[LC_LEAVES];    // staged leaves of at most 32 descriptors: bit i = descriptor i matches
+   uint32_t tot[LC_LEAVES];      // rows of the leaf's matching containers copied into shared memory;
+                                 // LC_BIG set when a matching container was not copied
    uint32_t beg[LC_LEAVES];  // LC_NONE: not staged (the leaf reads its descriptors from global memory)
    uint4 cov[LC_COV];        // exception range (x, y) and missing-interval range (z, w) of the tile
    uint32_t nl;              // container leaves 1..nl are described by the table
@@ -153,6 +157,7 @@ __device__ __forceinline__ void clear_leaves(LeafCache& lc, uint32_t nl, uint32_
       lc.n[k] = 0;
       lc.src[k] = nullptr;
       lc.match[k] = 0;
+      lc.tot[k] = 0;
    }
    for (uint32_t k = threadIdx.x; k < ncov; k += blockDim.x) lc.cov[k] = make_uint4(0, 0, 0, 0);
 }
@@ -303,6 +308,7 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
          }
          if (po != LC_NOPAY) {
             lc.poff[j] = static_cast<uint16_t>(po);
+            atomicAdd(&lc.tot[k], d.card_m1 + 1u);
             asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
             if (!withhold)
                asm volatile(
@@ -312,6 +318,7 @@ __device__ bool stage_leaves(LeafCache& lc, const TileCtx& c, const Instr* __res
             continue;
          }
       }
+      atomicOr(&lc.tot[k], LC_BIG);
       if (d.type == CT_ARRAY) prefetch_l2(p, p + d.card_m1 + 1u);
       else if (d.type == CT_BITSET) prefetch_l2(p + (c.row0 >> 4), p + ((c.row0 + c.W) >> 4));
       else prefetch_l2(p, p + 2u * d.nruns);
@@ -372,10 +379,41 @@ __device__ void push_containers(uint32_t* t, const TileCtx& c, const CtrDesc* __
    }
 }
 
+// A staged leaf of at most 32 descriptors whose matching containers are arrays copied into shared
+// memory, LC_OWNER_MAX rows at most: set by the owners of its words (see below), with no CTA
+// barrier. Each thread clears the words it owns; each warp then reads every row of the leaf and sets
+// those in the words its lanes own (shared-memory atomics: two lanes may hit one word), fenced by
+// __syncwarp on both sides. Returns false (nothing done) for any other leaf.
+__device__ __forceinline__ bool push_owned(uint4* t4, uint32_t* t, const TileCtx& c, const LeafCache& lc, uint32_t leaf) {
+   if (leaf < 1 || leaf > lc.nl) return false;
+   const uint32_t k = leaf - 1;
+   if (lc.beg[k] == LC_NONE || lc.n[k] > 32 || lc.tot[k] > LC_OWNER_MAX) return false;
+   const uint32_t W4 = c.W >> 7, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = make_uint4(0, 0, 0, 0);
+   __syncwarp();
+   uint32_t todo = lc.match[k];
+   while (todo) {
+      const uint32_t i = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t j = lc.beg[k] + i;
+      const CtrDesc d = *reinterpret_cast<const CtrDesc*>(&lc.desc[j]);
+      const uint16_t po = lc.poff[j];
+      const uint16_t* sp = po < LC_PAY ? reinterpret_cast<const uint16_t*>(lc.pay4) + po : lc.ext + (po - LC_PAY);
+      const uint32_t card = d.card_m1 + 1u;
+      for (uint32_t e = lane; e < card; e += 32) {
+         const uint32_t r = static_cast<uint32_t>(sp[e]) - c.row0;
+         if (r < c.W && (((r >> 7) % FT) >> 5) == warp) atomicOr(&t[r >> 5], 1u << (r & 31));
+      }
+   }
+   __syncwarp();
+   return true;
+}
+
 // Word-parallel tile operations use one fixed mapping: thread i owns the uint4 words i, i +
 // blockDim.x, ... of every tile. Consecutive word-parallel operations therefore need no barrier
 // between them; leaves that scatter with shared-memory atomics (or write per warp) are fenced by
-// barriers on both sides.
+// barriers on both sides, except the small staged leaves that only their words' owning warps write
+// (push_owned, fenced per warp).
 __device__ __forceinline__ uint4 valid4(uint32_t w4, const TileCtx& c) {
    if (c.nvalid == c.W) return make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
    return make_uint4(valid_word(4 * w4, c.nvalid), valid_word(4 * w4 + 1, c.nvalid), valid_word(4 * w4 + 2, c.nvalid),
@@ -560,6 +598,8 @@ __device__ bool run_program(const TileCtx& c, const Instr* __restrict__ code, ui
             } else if (in.op == OP_PUSH_DATE) {
                push_date(t4, c, &c.tab->date[in.col], static_cast<int32_t>(in.a), static_cast<int32_t>(in.b), in.flags & 2,
                          in.flags & 1);
+               synced = false;
+            } else if (push_owned(t4, t, c, lc, in.c)) {
                synced = false;
             } else {
                for (uint32_t w4 = threadIdx.x; w4 < W4; w4 += blockDim.x) t4[w4] = make_uint4(0, 0, 0, 0);

@@ -49,7 +49,7 @@ constexpr uint32_t TASK_UNITS = 128;         // units of a task staged in shared
 //   SU_BITSET  one bitset: AND with the tile and popcount, 16 uint4 per lane.
 //   SU_RUN     one run container: the tile's popcount over each run.
 // Full filters (|F| == rows) add the stored cardinalities and read no payload.
-__global__ void __launch_bounds__(MT, 5) mut_chunk_kernel(const DevTable* __restrict__ tab, uint32_t col,
+__global__ void __launch_bounds__(MT, 6) mut_chunk_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                        const uint32_t* __restrict__ filter,
                                                        const unsigned long long* __restrict__ fcount,
                                                        unsigned long long sparse_max, uint32_t* counts) {
