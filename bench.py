@@ -28,6 +28,8 @@ parity_oracle  the same leg as checker, outside every timed region: the oracle's
 planner    rule-based vs learned ordering: device time of the captured batch and end to end.
 serving    Poisson arrivals at 2,000 and 20,000 requests/s on an 8M-sequence table: continuous
            batching (learned planner) against the plain single-query path, p50 / p99 and the rate.
+ingestion  the serving table's raw partition built on the host (all host threads) and on the GPU:
+           seconds of each and whether the two images are identical.
 
 `python bench.py --impl reference` times that CPU implementation alone on the same workload.
 """
@@ -84,6 +86,8 @@ def parse():
                     help="batching-shape leg: trees of 1-64 leaves, log-uniform selectivities (0: none)")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="length of each serving run (0: none)")
     ap.add_argument("--serve-rates", default="2000,20000", help="Poisson arrival rates (requests/s) of the serving runs")
+    ap.add_argument("--no-ingest", action="store_true",
+                    help="skip the ingestion leg (host vs GPU build of the serving table's raw partition)")
     ap.add_argument("--serve-rows", type=int, default=8_000_000,
                     help="sequences of the serving table (its own seeded table when it differs from --rows)")
     ap.add_argument("--profile-workload", default="", choices=["", "plain-mutations", "batch", "profile"],
@@ -292,6 +296,26 @@ def reference_arm(args, ws, rank):
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def ingestion_leg(R, table, dev_index):
+    """Ingestion of one raw partition (the rows of `table`) on the host (rhy_table_from_raw, all host
+    threads) and on the GPU (rhy_table_from_raw_gpu): wall seconds of each, and whether every
+    sequence column's image is identical (checksum over all of its arrays)."""
+    raw = table.raw()
+    t0 = time.perf_counter()
+    host = R.Table.from_raw(raw)
+    host_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gpu = R.Table.from_raw_gpu(raw, dev_index)
+    gpu_s = time.perf_counter() - t0
+    same = all(host.checksum(c) == gpu.checksum(c) and host.local_reference(c) == gpu.local_reference(c)
+               for c in range(host.n_seq))
+    out = {"rows": table.n_rows, "sequence_columns": host.n_seq, "host_build_s": round(host_s, 2),
+           "host_threads": os.cpu_count() or 1, "gpu_build_s": round(gpu_s, 2), "speedup": host_s / gpu_s,
+           "images_identical": bool(same)}
+    del host, gpu
+    return out
 
 
 def profile_workload(args, R, workloads, table, dev, queries, actions, columns, sp, stream):
@@ -573,7 +597,7 @@ def main():
     d2h = n * 8 + n * 12 + len(rows) * 24
 
     # ---------------- serving: Poisson arrivals, continuous batching vs the plain path ----------------
-    serving = None
+    serving, ingestion = None, None
     if args.serve_seconds > 0:
         t_setup = time.perf_counter()
         s_table, s_dev, s_queries = table, dev, queries
@@ -615,6 +639,8 @@ def main():
         serving = {"mix": "70% count / 25% mutations (nucleotide, min proportion 0.05) / 5% details (first 1000 ids)",
                    "arrivals": "Poisson, open loop (native submitter thread)", "rows": s_table.n_rows,
                    "table_setup_s": round(setup_s, 1), "planner": s_planner, **arms}
+        if not args.no_ingest:
+            ingestion = ingestion_leg(R, s_table, dev_index)
         if s_dev is not dev:
             s_dev.close()
             del s_table
@@ -778,6 +804,7 @@ def main():
             "mutation_profile": profile,
             "batching_shape": shape,
             "serving": serving,
+            "ingestion": ingestion,
             "parity_plain_vs_batched_mismatches": mismatches,
             "parity_oracle": parity,
             "parity_oracle_mismatches": parity["mismatches"] if parity else None,
