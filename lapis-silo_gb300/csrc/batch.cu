@@ -22,6 +22,7 @@
 
 #include "device.h"
 #include "mutations_common.cuh"
+#include "rows_rule.cuh"
 
 namespace rhygpu {
 
@@ -426,18 +427,38 @@ __global__ void __launch_bounds__(BT) mut_sparse_batch_kernel(const DevTable* __
       row_index_pass32(cs, F, w, words, cnt, sc, list[warp]);
 }
 
-// grid (ceil(L / MUT_SEG), nq): reference counts of slot blockIdx.y.
+// grid (ceil(L / MUT_SEG), nq): reference counts of slot blockIdx.y. With rowblk (the Mutations
+// rows are wanted), the CTA then counts the output rows of its MUT_SEG (= ROWS_BLOCK) positions
+// under the slot's minimum proportion into rowblk[slot * gridDim.x + blockIdx.x], the entry
+// rows_count_kernel would write, from the counts its threads just completed.
 __global__ void __launch_bounds__(MUT_SEG) mut_final_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                                   const unsigned long long* __restrict__ fcounts,
                                                                   const uint32_t* __restrict__ slot_query,
                                                                   uint32_t* __restrict__ counts,
-                                                                  const uint32_t* __restrict__ scratch) {
+                                                                  const uint32_t* __restrict__ scratch,
+                                                                  const double* __restrict__ min_prop,
+                                                                  uint32_t* __restrict__ rowblk) {
+   static_assert(MUT_SEG == ROWS_BLOCK, "a final CTA covers one block of the row counts");
    __shared__ uint32_t red[MUT_SEG / 32];
    const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t q = blockIdx.y;
+   const uint32_t q = blockIdx.y, L = cs->L;
    const uint32_t total = static_cast<uint32_t>(fcounts[slot_query[q]]);
-   final_position_counts(cs, total, counts + static_cast<size_t>(q) * cs->nsym * cs->L,
-                         scratch + static_cast<size_t>(q) * mut_scratch_words(cs->L), red);
+   uint32_t* c = counts + static_cast<size_t>(q) * cs->nsym * L;
+   final_position_counts(cs, total, c, scratch + static_cast<size_t>(q) * mut_scratch_words(L), red);
+   if (rowblk == nullptr) return;
+   // each thread reads back its own position's counts (plain loads: it has just written one)
+   const uint32_t p = blockIdx.x * MUT_SEG + threadIdx.x;
+   const uint32_t n =
+      p < L ? position_rows(cs, p, min_prop[q], [&](uint32_t s) { return c[static_cast<size_t>(s) * L + p]; }).n : 0u;
+   const uint32_t wn = __reduce_add_sync(0xFFFFFFFFu, n);
+   __syncthreads();  // red is free again (final_position_counts' scans are done)
+   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wn;
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      uint32_t sum = 0;
+      for (uint32_t w = 0; w < MUT_SEG / 32; ++w) sum += red[w];
+      rowblk[static_cast<size_t>(q) * gridDim.x + blockIdx.x] = sum;
+   }
 }
 
 }  // namespace
@@ -451,7 +472,8 @@ void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, 
                             const uint32_t* d_filters, uint32_t nq, const unsigned long long* d_fcounts,
                             const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
                             uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
-                            uint32_t* d_lists, uint64_t sparse_max, void* stream, uint32_t parts) {
+                            uint32_t* d_lists, uint64_t sparse_max, void* stream, uint32_t parts,
+                            const double* d_min_prop, uint32_t* d_rowblk) {
    if (nq == 0) return;
    cudaStream_t s = static_cast<cudaStream_t>(stream);
    const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP;  // grids for the largest dense list
@@ -477,7 +499,8 @@ void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, 
    }
    if (parts & BMUT_PART_FINAL) {
       dim3 fin((col_host.L + MUT_SEG - 1) / MUT_SEG, nq);
-      mut_final_batch_kernel<<<fin, MUT_SEG, 0, s>>>(d_table, col, d_fcounts, d_slot_query, d_counts, d_scratch);
+      mut_final_batch_kernel<<<fin, MUT_SEG, 0, s>>>(d_table, col, d_fcounts, d_slot_query, d_counts, d_scratch,
+                                                     d_min_prop, d_rowblk);
    }
 }
 

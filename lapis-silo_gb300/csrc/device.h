@@ -199,7 +199,9 @@ constexpr uint32_t CTR_UNIT_ELEMENTS = 4096;
 // On the device, once the filters are known, the slots split by their filter's cardinality: empty
 // filters need no pass, filters of at most sparse_max rows (0: none) take the row-index pass (part
 // BMUT_PART_SPARSE), the others the dense passes over the slots listed in d_lists (2 * nq + 2 u32
-// of scratch: the dense and the sparse slot lists and their lengths).
+// of scratch: the dense and the sparse slot lists and their lengths). With d_rowblk, the final
+// pass also counts every slot's Mutations output rows (minimum proportion d_min_prop[slot]) per
+// block of ROWS_BLOCK positions into d_rowblk, as launch_rows_count would.
 enum : uint32_t { BMUT_PART_SPARSE = 16 };
 size_t mutations_batch_mask_bytes(uint32_t nq, uint32_t nchunks);
 void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, uint32_t nchunks,
@@ -207,7 +209,8 @@ void launch_mutations_batch(const DevTable* d_table, const DevSeqCol& col_host, 
                             const uint32_t* d_slot_query, const EvItem* d_ev, uint32_t n_ev, const CtrUnit* d_units,
                             uint32_t n_units, uint16_t* d_masks, uint32_t* d_counts, uint32_t* d_scratch,
                             uint32_t* d_lists, uint64_t sparse_max, void* stream,
-                            uint32_t parts = BMUT_PART_ALL | BMUT_PART_SPARSE);
+                            uint32_t parts = BMUT_PART_ALL | BMUT_PART_SPARSE, const double* d_min_prop = nullptr,
+                            uint32_t* d_rowblk = nullptr);
 
 // Output rows of the Mutations action (same layout as RhyMutationRow in the C-ABI header).
 struct DevMutationRow {
@@ -221,13 +224,12 @@ struct DevMutationRow {
 static_assert(sizeof(DevMutationRow) == 24, "row layout");
 
 // Rows of nq query slots whose dense counts lie at d_counts + slot * nsym * L, with per-slot minimum
-// proportions. Count pass: d_blk[slot * rows_blocks(L) + b] = rows of position block b; the scan
-// turns n entries into exclusive offsets with the total at d_blk[n]; the write pass emits the rows
-// at their offsets in (slot, position, symbol) order.
+// proportions. The batched final pass counts them (launch_mutations_batch with d_rowblk):
+// d_blk[slot * rows_blocks(L) + b] = rows of position block b; the scan turns n entries into
+// exclusive offsets with the total at d_blk[n]; the write pass emits the rows at their offsets in
+// (slot, position, symbol) order, skipping the blocks without rows.
 constexpr uint32_t ROWS_BLOCK = 1024;
 uint32_t rows_blocks(uint32_t L);
-void launch_rows_count(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, const uint32_t* d_counts,
-                       uint32_t nq, const double* d_min_prop, uint32_t* d_blk, void* stream);
 void launch_rows_scan(uint32_t* d_blk, uint32_t n, void* stream);
 void launch_rows_write(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, const uint32_t* d_counts,
                        uint32_t nq, const double* d_min_prop, const uint32_t* d_blk, DevMutationRow* d_rows,

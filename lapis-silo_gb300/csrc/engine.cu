@@ -873,7 +873,9 @@ void Engine::batch_enqueue(BatchState& b, cudaStream_t s, bool copy_in, bool cop
                              b.d_slot_query + g.slot_begin, d_ev_[g.column], n_ev_[g.column], d_cu_[g.column],
                              n_cu_[g.column], b.d_masks, b.d_mcounts + g.counts_off, b.d_mscratch + g.scratch_off,
                              b.d_lists + g.lists_off, sparse_rows_batch, s,
-                             (parts >> 1) & (BMUT_PART_ALL | BMUT_PART_SPARSE));
+                             (parts >> 1) & (BMUT_PART_ALL | BMUT_PART_SPARSE),
+                             b.rows_in_final ? b.d_minprop + g.slot_begin : nullptr,
+                             b.rows_in_final ? b.d_rowblk + g.blk_off : nullptr);
       cuda_check(cudaGetLastError(), "mutations batch launch");
    }
    if (b.n_details && (parts & 1)) {
@@ -908,14 +910,18 @@ void Engine::check_batch_error(BatchState& b) {
 void Engine::rows_phase1(BatchState& b, cudaStream_t s) {
    s = stream_for(s);
    if (b.n_queries == 0) return;
-   batch_enqueue(b, s, true, false);
+   b.rows_in_final = true;  // the final pass counts the rows per block (no separate counting pass)
+   try {
+      batch_enqueue(b, s, true, false);
+   } catch (...) {
+      b.rows_in_final = false;
+      throw;
+   }
+   b.rows_in_final = false;
    cuda_check(cudaMemcpyAsync(b.h_counts, b.d_counts, b.n_queries * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
               "D2H");
    copy_details(b, s);
    cuda_check(cudaMemcpyAsync(b.h_err, b.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
-   for (const auto& g : b.groups)
-      launch_rows_count(d_table_, view_.seq[g.column], static_cast<uint32_t>(g.column), b.d_mcounts + g.counts_off, g.n,
-                        b.d_minprop + g.slot_begin, b.d_rowblk + g.blk_off, s);
    if (b.n_mut_slots) {
       launch_rows_scan(b.d_rowblk, b.n_blk, s);
       cuda_check(cudaMemcpyAsync(b.h_rowblk, b.d_rowblk, (static_cast<size_t>(b.n_blk) + 1) * sizeof(uint32_t),

@@ -115,6 +115,7 @@ struct BatchState {
    uint32_t* d_nids = nullptr;        // Details: ids per slot
    uint32_t* h_nids = nullptr;
    uint32_t n_blk = 0;                // row-block table entries (Mutations slots)
+   bool rows_in_final = false;        // the final Mutations pass also counts the rows per block
    size_t n_rows = 0;                 // rows of the last row pass
    uint32_t n_mut_slots = 0, n_details = 0, n_ids = 0;
    // MutationProfile row sets of the batch's programs (QueryDesc.aux_base numbers them)

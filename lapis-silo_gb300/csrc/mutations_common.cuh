@@ -144,10 +144,11 @@ __device__ __forceinline__ void final_position_counts(const DevSeqCol* cs, uint3
    const uint32_t sl = block_incl_scan_u32(in ? start_hist[p] : 0u, red) + pre[0];
    const uint32_t el = block_incl_scan_u32(in ? end_hist[p] : 0u, red) + pre[1];
    const uint32_t nl = block_incl_scan_u32(in ? ndiff[p] : 0u, red) + pre[2];
-   if (!in) return;
-   uint32_t ref = total - (pre[3] - sl) - el - nl;
-   for (uint32_t s = 0; s < nsym; ++s) ref -= counts[static_cast<size_t>(s) * L + p];
-   counts[static_cast<size_t>(cs->local_ref[p]) * L + p] += ref;
+   if (in) {  // no early return: a caller may follow with barriers
+      uint32_t ref = total - (pre[3] - sl) - el - nl;
+      for (uint32_t s = 0; s < nsym; ++s) ref -= counts[static_cast<size_t>(s) * L + p];
+      counts[static_cast<size_t>(cs->local_ref[p]) * L + p] += ref;
+   }
 }
 
 // Row-index pass over 32 words [w, w + 32) of a dense filter F (words in all): every row of F there

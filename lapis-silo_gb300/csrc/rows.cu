@@ -7,15 +7,18 @@
 // proportion = count / total). The double operations are single IEEE operations (a product, ceil,
 // a quotient), so the values equal the host's bit for bit.
 //
-// Three passes keep the output packed and in (slot, position, symbol) order:
-//   rows_count_kernel  rows per block of ROWS_BLOCK positions of every slot
+// Three steps keep the output packed and in (slot, position, symbol) order:
+//   the batched final pass (mut_final_batch_kernel) counts the rows per block of ROWS_BLOCK
+//                      positions of every slot, from the counts it has just completed
 //   rows_scan_kernel   exclusive prefix over all (slot, block) counts; the total follows them
-//   rows_write_kernel  recomputes the rows of each block and writes them at their offsets
+//   rows_write_kernel  recomputes the rows of each block that has any and writes them at their
+//                      offsets (blocks without rows, most of them, read no counts)
 #include <cuda_runtime.h>
 
 #include <cmath>
 
 #include "device.h"
+#include "rows_rule.cuh"
 
 namespace rhygpu {
 
@@ -23,25 +26,10 @@ namespace {
 
 constexpr uint32_t RT = ROWS_BLOCK;  // one thread per position
 
-struct PosRows {
-   uint32_t n;       // rows of this position
-   uint32_t total;   // coverage
-   uint32_t thr;     // counts above it are reported
-   uint32_t ref;     // global reference symbol
-};
-
 __device__ __forceinline__ PosRows position_rows(const DevSeqCol* __restrict__ cs, const uint32_t* __restrict__ c,
                                                  uint32_t p, double min_prop) {
-   PosRows r{0, 0, 0, 0};
-   const uint32_t L = cs->L, nsym = cs->nsym, valid = cs->valid_mask;
-   for (uint32_t s = 0; s < nsym; ++s)
-      if ((valid >> s) & 1u) r.total += __ldg(c + static_cast<size_t>(s) * L + p);
-   if (r.total == 0) return r;
-   r.thr = min_prop == 0.0 ? 0u : static_cast<uint32_t>(ceil(static_cast<double>(r.total) * min_prop) - 1.0);
-   r.ref = __ldg(cs->global_ref + p);
-   for (uint32_t s = 0; s < nsym; ++s)
-      if (((valid >> s) & 1u) && s != r.ref && __ldg(c + static_cast<size_t>(s) * L + p) > r.thr) ++r.n;
-   return r;
+   const uint32_t L = cs->L;
+   return position_rows(cs, p, min_prop, [&](uint32_t s) { return __ldg(c + static_cast<size_t>(s) * L + p); });
 }
 
 __device__ __forceinline__ uint32_t block_scan_excl(uint32_t x, uint32_t* wsum, uint32_t* total) {
@@ -62,20 +50,6 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t x, uint32_t* wsum, 
    }
    *total = all;
    return before + incl - x;
-}
-
-// grid (blocks of positions, slots)
-__global__ void __launch_bounds__(RT) rows_count_kernel(const DevTable* __restrict__ tab, uint32_t col,
-                                                        const uint32_t* __restrict__ counts,
-                                                        const double* __restrict__ min_prop, uint32_t* blk) {
-   __shared__ uint32_t wsum[RT / 32];
-   const DevSeqCol* cs = &tab->seq[col];
-   const uint32_t q = blockIdx.y, p = blockIdx.x * RT + threadIdx.x;
-   const uint32_t* c = counts + static_cast<size_t>(q) * cs->nsym * cs->L;
-   const uint32_t n = p < cs->L ? position_rows(cs, c, p, min_prop[q]).n : 0u;
-   uint32_t total;
-   block_scan_excl(n, wsum, &total);
-   if (threadIdx.x == 0) blk[static_cast<size_t>(q) * gridDim.x + blockIdx.x] = total;
 }
 
 // One CTA: exclusive prefix sum over n entries in place, the total written to blk[n].
@@ -100,6 +74,9 @@ __global__ void __launch_bounds__(RT) rows_write_kernel(const DevTable* __restri
                                                         const double* __restrict__ min_prop,
                                                         const uint32_t* __restrict__ blk, DevMutationRow* rows) {
    __shared__ uint32_t wsum[RT / 32];
+   const size_t bi = static_cast<size_t>(blockIdx.y) * gridDim.x + blockIdx.x;
+   const uint32_t at0 = blk[bi];
+   if (blk[bi + 1] == at0) return;  // a block without rows (the scan's next entry, or its total, is equal)
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t q = blockIdx.y, p = blockIdx.x * RT + threadIdx.x;
    const uint32_t L = cs->L;
@@ -107,7 +84,7 @@ __global__ void __launch_bounds__(RT) rows_write_kernel(const DevTable* __restri
    PosRows r{0, 0, 0, 0};
    if (p < L) r = position_rows(cs, c, p, min_prop[q]);
    uint32_t total;
-   uint32_t at = blk[static_cast<size_t>(q) * gridDim.x + blockIdx.x] + block_scan_excl(r.n, wsum, &total);
+   uint32_t at = at0 + block_scan_excl(r.n, wsum, &total);
    if (r.n == 0) return;
    const uint32_t valid = cs->valid_mask;
    for (uint32_t s = 0; s < cs->nsym; ++s) {
@@ -129,13 +106,6 @@ __global__ void __launch_bounds__(RT) rows_write_kernel(const DevTable* __restri
 }  // namespace
 
 uint32_t rows_blocks(uint32_t L) { return (L + RT - 1) / RT; }
-
-void launch_rows_count(const DevTable* d_table, const DevSeqCol& col_host, uint32_t col, const uint32_t* d_counts,
-                       uint32_t nq, const double* d_min_prop, uint32_t* d_blk, void* stream) {
-   if (nq == 0) return;
-   rows_count_kernel<<<dim3(rows_blocks(col_host.L), nq), RT, 0, static_cast<cudaStream_t>(stream)>>>(
-      d_table, col, d_counts, d_min_prop, d_blk);
-}
 
 void launch_rows_scan(uint32_t* d_blk, uint32_t n, void* stream) {
    rows_scan_kernel<<<1, RT, 0, static_cast<cudaStream_t>(stream)>>>(d_blk, n);
