@@ -14,7 +14,7 @@ e2e        the same through the C-ABI call rhy_batch_rows with host buffers: pla
            copies, kernels, the Mutations output rows built on the device (minimum proportion
            0.05) and the device->host copy of every count and row.
 plain      the plain single-query path over the same queries, one query at a time.
-roofline   the plain container pass of the Mutations action (mut_chunk_kernel), the kernel that
+roofline   the plain container pass of the Mutations action (mut_ring_kernel), the kernel that
            streams the whole vertical index: algorithmic bytes = container payloads + descriptors
            + the filter tiles it stages, divided by its CUDA-event duration.
 roofline_batch  the batched filter and container kernels: the algorithmic bytes of one batch
@@ -743,7 +743,7 @@ def main():
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (ctr_avg_ms / 1000.0) / 1e9
     traffic = None
-    prof = ROOT / "profiles" / "mut_chunk_kernel_2M.traffic.json"
+    prof = ROOT / "profiles" / "mut_ring_kernel_2M.traffic.json"
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
 
@@ -814,7 +814,7 @@ def main():
                     "dense_counts_qps": dense_qps, "phases_ms": e2e_phase_ms},
             "gpu_launches": launches_per_step * args.steps,
             "kernels_ms": kernels_ms,
-            "roofline": {"kernel": "mut_chunk_kernel (plain Mutations container pass, nucleotide column)",
+            "roofline": {"kernel": "mut_ring_kernel (plain Mutations container pass, nucleotide column)",
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": ctr_avg_ms,

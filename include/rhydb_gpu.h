@@ -373,9 +373,9 @@ int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_by
  * synchronisation of cudaMalloc / cudaFree. The caller passes device buffers it owns: the filter
  * row set (n_chunks * 2048 words, as written by the filter kernels), its cardinality, the output
  * counts (n_symbols * L words, counts[symbol * L + position], overwritten) and one int of status,
- * which the call clears and a kernel of the pass would set to a nonzero device error code (none of
- * the pass's kernels waits on anything, so a completed pass leaves it 0). Read it after
- * synchronising the stream. Working memory is one fixed array in the library's device image
+ * which the call clears and a kernel of the pass sets to a nonzero device error code (7: a bounded
+ * wait of the container pass for its bulk copies gave up); a completed pass leaves it 0. Read it
+ * after synchronising the stream. Working memory is one fixed array in the library's device image
  * (1.5 MiB, held on every GPU that loads the library until the process exits), which limits the
  * column to 131,072 positions; longer columns fail with RHY_INVALID_ARGUMENT. The first call on a
  * device looks up the array's address; make that first call before any stream capture. All calls
@@ -386,12 +386,13 @@ int rhy_mutation_bytes(const RhyDevice* d, uint32_t column, uint64_t* payload_by
  * synchronised. */
 int rhy_mutations_noalloc(RhyDevice* d, uint32_t column, const uint32_t* d_filter, const uint64_t* d_filter_count,
                           uint32_t* d_counts, int* d_status, void* stream);
-/* Testing the failure path of the bounded device waits (no counterpart in the reference): while on
- * (on = 1), the filter kernels announce the leaf payload copies their waits expect but never issue
- * them, so a wait gives up after 1 ms and the call reports RHY_CUDA ("a bounded device wait for
- * bulk copies gave up", device error 6). The withheld copies never start, so no copy is left in
- * flight and the device stays usable. Synchronises the device; off (0) by default. Not for
- * production use. */
+/* Testing the failure path of the bounded device waits (no counterpart in the reference): while bit
+ * 0 of `on` is set, the filter kernels announce the leaf payload copies their waits expect but never
+ * issue them, so a wait gives up after 1 ms and the call reports RHY_CUDA ("a bounded device wait
+ * for bulk copies gave up", device error 6); bit 1 does the same for the Mutations container pass's
+ * ring copies (device error 7; rhy_mutations_noalloc reports it in its status word). The withheld
+ * copies never start, so no copy is left in flight and the device stays usable. Synchronises the
+ * device; off (0) by default. Not for production use. */
 int rhy_test_withhold_copies(RhyDevice* d, int on);
 
 /* Formats counts like the reference's Mutations action; returns the number of rows in *n_rows. */

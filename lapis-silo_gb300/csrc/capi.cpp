@@ -928,7 +928,8 @@ int rhy_test_withhold_copies(RhyDevice* d, int on) {
       std::lock_guard<std::mutex> lock(d->engine->mu);
       rhygpu::cuda_check(cudaSetDevice(d->engine->device()), "cudaSetDevice");
       rhygpu::cuda_check(cudaDeviceSynchronize(), "synchronise before switching copy withholding");
-      rhygpu::set_copy_withholding(on != 0);
+      rhygpu::set_copy_withholding((on & 1) != 0);
+      rhygpu::set_ring_withholding((on & 2) != 0);
    });
 }
 

@@ -23,24 +23,36 @@ constexpr int MAX_SEQ_COLS = 32;
 constexpr int MAX_DICT_COLS = 8;
 constexpr int MAX_DATE_COLS = 8;
 
-// One unit of the Mutations container pass (see mut_chunk_kernel). e0/e1: payload-arena element
-// range (SU_ARRAYS: at most WU elements of one chunk's array payloads, e0 a multiple of 8 so the
-// unit is read with 16-byte loads; elements below the chunk's first array belong to no container
-// of the unit; SU_BITSET: the bitset's 4096 u16); c0/c1: descriptor range (arrays: every
-// descriptor overlapping [e0, e1); bitset / run: one).
-enum : uint32_t { SU_ARRAYS = 0, SU_BITSET = 1, SU_RUN = 2 };
+// Units of the Mutations container pass (see mut_ring_kernel).
+// An array unit: n <= WU elements [e0, e0 + n) of one chunk's array payloads (arrays lie back to
+// back in descriptor order; e0 is a multiple of 8, so the unit starts on a 16-byte boundary;
+// elements below the chunk's first array belong to no container of the unit) and the nd
+// descriptors [c0, c0 + nd) that cover every array overlapping it (bitset and run descriptors
+// between them are skipped). The host cuts units so that nd <= WU_DESC wherever it can.
 constexpr uint32_t WU = 1024;
-struct StreamUnit {
+constexpr uint32_t WU_DESC = 64;
+struct ArrUnit {
+   uint32_t e0;
+   uint32_t c0;
+   uint16_t n, nd;
+   uint32_t v;
+};
+static_assert(sizeof(ArrUnit) == 16, "array unit record");
+// A bitset (kind SU_BITSET: its 4096 u16 at e0) or run container (SU_RUN), descriptor c.
+enum : uint32_t { SU_BITSET = 1, SU_RUN = 2 };
+struct OtherUnit {
    uint32_t kind;
    uint32_t v;
-   uint32_t e0, e1;
-   uint32_t c0, c1;
-   uint32_t pad[2];
+   uint32_t e0;
+   uint32_t c;
 };
-// Units [u0, u1) of one chunk v: the work of one CTA of the container pass.
-struct ChunkTask {
-   uint32_t v, u0, u1, pad;
+// The work of one CTA of the container pass: array units [a0, a1) and other units [o0, o1), all
+// of chunks v0 and v1 (v1 == v0 for one chunk).
+struct StreamRange {
+   uint32_t a0, a1, o0, o1, v0, v1, pad[2];
 };
+// CTAs of the container pass per SM (its shared-memory ring sets this); one range per CTA.
+constexpr uint32_t RING_CTAS_PER_SM = 3;
 
 struct DevSeqCol {
    const CtrDesc* ctrs;
@@ -50,8 +62,9 @@ struct DevSeqCol {
    const uint32_t* exc_off;    // nchunks + 1
    const NRunEntry* nblk;
    const uint32_t* nblk_off;   // nblocks * nchunks + 1
-   const StreamUnit* su;       // units of the Mutations container pass, chunk-major
-   const ChunkTask* tasks;     // CTAs of the container pass: unit ranges within one chunk
+   const ArrUnit* au;          // array units of the Mutations container pass, chunk-major
+   const OtherUnit* ou;        // its bitset and run units, chunk-major
+   const StreamRange* ranges;  // its CTAs
    const uint32_t* exc_toff;   // nchunks * TOFF_N: tile row-range offsets into exc
    const uint32_t* nblk_toff;  // nblocks * nchunks * TOFF_N: the same into each nblk bucket
    const uint32_t* null_tiles; // nchunks * CHUNK_WORDS
@@ -66,8 +79,8 @@ struct DevSeqCol {
    uint32_t nblocks;
    uint32_t nsym;
    uint32_t nctrs;
-   uint32_t nsu;
-   uint32_t ntasks;
+   uint32_t nau;
+   uint32_t nranges;
    uint32_t valid_mask;        // symbols counted in a position's coverage (valid mutation symbols)
    const uint8_t* global_ref;  // L: the column's reference symbols (the "from" of a mutation)
    char chars[32];             // symbol -> character
@@ -164,6 +177,14 @@ cudaError_t launch_filter_batch(const DevTable* d_table, uint32_t nchunks, const
                          uint32_t* d_out_tiles /* per query nchunks*CHUNK_WORDS */, unsigned long long* d_counts,
                          uint32_t* d_next, uint32_t grid, int* d_err, void* stream, const uint32_t* d_aux = nullptr);
 
+// Device error codes the kernels set in their error word: a bounded wait for bulk copies gave up
+// in a filter kernel (6) or in the Mutations container pass (7).
+enum : int { DEVERR_WAIT_FILTER = 6, DEVERR_WAIT_MUTATIONS = 7 };
+
+// Sets the container pass's shared-memory size on the current device (once per device, before
+// its first launch).
+void mutations_setup();
+
 // Kernel selection masks (all bits set = the whole pass); used to time the kernels one by one.
 enum : uint32_t { MUT_PART_CTR = 1, MUT_PART_COV = 2, MUT_PART_FINAL = 4, MUT_PART_ALL = 7 };
 enum : uint32_t { BMUT_PART_TRANSPOSE = 1, BMUT_PART_CTR = 2, BMUT_PART_COV = 4, BMUT_PART_FINAL = 8, BMUT_PART_ALL = 15 };
@@ -182,6 +203,9 @@ void launch_mutations(const DevTable* d_table, const DevSeqCol& col_host, uint32
 // the leaf payload copies they announce are never issued, so their waits give up and the kernels
 // set error 6 (DEVERR_WAIT_FILTER) instead of evaluating. Nothing is left in flight.
 void set_copy_withholding(bool on);
+// The same for the Mutations container pass (mutations.cu): while on, its slot copies are announced
+// but withheld, so its consumers' waits give up and it sets DEVERR_WAIT_MUTATIONS.
+void set_ring_withholding(bool on);
 
 // One unit of the batched container pass: the containers of position `pos` in chunks [v0, v1),
 // at most CTR_UNIT_CHUNKS chunks and, unless a single chunk exceeds it, CTR_UNIT_ELEMENTS elements.

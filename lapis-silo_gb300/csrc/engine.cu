@@ -105,69 +105,118 @@ std::vector<CtrUnit> container_units(const SeqColumnImage& s, uint32_t nchunks) 
    return out;
 }
 
-// Units of the Mutations container pass, chunk by chunk: the chunk's array payloads (back to back in
-// descriptor order) cut into pieces of at most WU elements starting on 8-element (16-byte)
-// boundaries, each with the descriptors that overlap it, then one unit per bitset and per run
-// container. first[v] is the first unit of chunk v (first[nchunks] = the number of units).
-std::vector<StreamUnit> stream_units(const SeqColumnImage& s, uint32_t nchunks, std::vector<uint32_t>& first) {
+// Units of the Mutations container pass, chunk by chunk: the chunk's array payloads (back to back
+// in descriptor order) cut into pieces of at most WU elements starting on 8-element (16-byte)
+// boundaries, each with the descriptors that cover the arrays overlapping it, then one unit per
+// bitset and run container. A piece ends early, before the first array whose descriptor would not
+// fit, where more than WU_DESC descriptors would be needed. afirst[v] / ofirst[v]: the first array /
+// other unit of chunk v (nchunks + 1 entries).
+struct PassUnits {
+   std::vector<ArrUnit> au;
+   std::vector<OtherUnit> ou;
+   std::vector<uint32_t> afirst, ofirst;
+};
+PassUnits pass_units(const SeqColumnImage& s, uint32_t nchunks) {
    const ContainerSet& cs = s.vertical;
-   std::vector<StreamUnit> out;
-   first.assign(nchunks + 1, 0);
+   PassUnits P;
+   P.afirst.assign(nchunks + 1, 0);
+   P.ofirst.assign(nchunks + 1, 0);
    for (uint32_t v = 0; v < nchunks; ++v) {
-      first[v] = static_cast<uint32_t>(out.size());
+      P.afirst[v] = static_cast<uint32_t>(P.au.size());
+      P.ofirst[v] = static_cast<uint32_t>(P.ou.size());
       const uint32_t cb = cs.off[static_cast<size_t>(v) * s.L], ce = cs.off[static_cast<size_t>(v + 1) * s.L];
       std::vector<uint32_t> arr;
       for (uint32_t i = cb; i < ce; ++i)
          if (cs.ctrs[i].type == CT_ARRAY) arr.push_back(i);
       if (!arr.empty()) {
-         const uint32_t A0 = cs.ctrs[arr.front()].payload;
-         const uint32_t A1 = cs.ctrs[arr.back()].payload + cs.ctrs[arr.back()].card_m1 + 1u;
+         auto start_of = [&](size_t k) { return cs.ctrs[arr[k]].payload; };
          auto end_of = [&](size_t k) { return cs.ctrs[arr[k]].payload + cs.ctrs[arr[k]].card_m1 + 1u; };
+         const uint32_t A1 = end_of(arr.size() - 1);
          size_t lo = 0;  // first array ending after e0
-         for (uint32_t e0 = A0 & ~7u; e0 < A1; e0 += WU) {
-            const uint32_t e1 = std::min(e0 + WU, A1);
+         for (uint32_t e0 = start_of(0) & ~7u; e0 < A1;) {
             while (lo < arr.size() && end_of(lo) <= e0) ++lo;
+            uint32_t e1 = std::min(e0 + WU, A1);
             size_t hi = lo;  // one past the last array starting before e1
-            while (hi < arr.size() && cs.ctrs[arr[hi]].payload < e1) ++hi;
-            out.push_back(StreamUnit{SU_ARRAYS, v, e0, e1, arr[lo], arr[hi - 1] + 1, {0, 0}});
+            while (hi < arr.size() && start_of(hi) < e1) ++hi;
+            if (arr[hi - 1] + 1 - arr[lo] > WU_DESC) {
+               size_t h = lo + 1;  // arrays [lo, h) fit
+               while (h < hi && arr[h] + 1 - arr[lo] <= WU_DESC) ++h;
+               e1 = std::min(std::max(start_of(h) & ~7u, e0 + 8), A1);
+               while (hi > lo + 1 && start_of(hi - 1) >= e1) --hi;
+            }
+            P.au.push_back(ArrUnit{e0, arr[lo], static_cast<uint16_t>(e1 - e0),
+                                   static_cast<uint16_t>(arr[hi - 1] + 1 - arr[lo]), v});
+            e0 = e1;
          }
       }
       for (uint32_t i = cb; i < ce; ++i) {
          const CtrDesc& d = cs.ctrs[i];
-         if (d.type == CT_BITSET) out.push_back(StreamUnit{SU_BITSET, v, d.payload, d.payload + 4096, i, i + 1, {0, 0}});
-         else if (d.type == CT_RUN) out.push_back(StreamUnit{SU_RUN, v, 0, 0, i, i + 1, {0, 0}});
+         if (d.type == CT_BITSET) P.ou.push_back(OtherUnit{SU_BITSET, v, d.payload, i});
+         else if (d.type == CT_RUN) P.ou.push_back(OtherUnit{SU_RUN, v, 0, i});
       }
    }
-   first[nchunks] = static_cast<uint32_t>(out.size());
-   return out;
+   P.afirst[nchunks] = static_cast<uint32_t>(P.au.size());
+   P.ofirst[nchunks] = static_cast<uint32_t>(P.ou.size());
+   return P;
 }
 
-// CTAs of the container pass: each chunk's units cut into ranges of about the same bytes (payload
-// and descriptors), `ctas` ranges over the whole column, none spanning two chunks.
-std::vector<ChunkTask> chunk_tasks(const SeqColumnImage& s, const std::vector<StreamUnit>& units,
-                                   const std::vector<uint32_t>& first, uint32_t ctas) {
+// CTAs of the container pass: the units of each chunk, its bitset and run units spread evenly among
+// its array units, cut into at most `ctas` ranges of about the same counting time, none spanning
+// more than two chunks. The weights are a consumer warp's cycles per unit, measured on the 2M-row
+// benchmark table: an array unit costs a fixed part plus its elements and descriptors; a bitset,
+// read by one warp straight from global memory, costs about one and a half array units.
+std::vector<StreamRange> pass_ranges(const SeqColumnImage& s, const PassUnits& P, uint32_t nchunks, uint32_t ctas) {
    const ContainerSet& cs = s.vertical;
-   auto weight = [&](const StreamUnit& u) -> uint64_t {
-      const uint64_t desc = 16ull * (u.c1 - u.c0);
-      if (u.kind == SU_ARRAYS) return 2ull * (u.e1 - u.e0) + desc;
-      if (u.kind == SU_BITSET) return CHUNK_ROWS / 8 + desc;
-      return 4ull * cs.ctrs[u.c0].nruns + desc;
+   auto aw = [&](const ArrUnit& u) -> uint64_t { return 2400ull + u.n + 20ull * u.nd; };
+   auto ow = [&](const OtherUnit& u) -> uint64_t {
+      return u.kind == SU_BITSET ? 6000ull : 600ull + 40ull * cs.ctrs[u.c].nruns;
    };
    uint64_t total = 0;
-   for (const StreamUnit& u : units) total += weight(u);
-   const uint64_t per_task = std::max<uint64_t>(1, total / std::max(1u, ctas));
-   std::vector<ChunkTask> out;
-   for (uint32_t v = 0; v + 1 < first.size(); ++v) {
-      uint32_t u0 = first[v];
+   for (const ArrUnit& u : P.au) total += aw(u);
+   for (const OtherUnit& u : P.ou) total += ow(u);
+   ctas = std::max(1u, ctas);
+   std::vector<StreamRange> out;
+   for (uint64_t per = std::max<uint64_t>(1, total / ctas);; per += per / 32 + 1) {
+      out.clear();
+      StreamRange cur{};
+      bool open = false;
       uint64_t acc = 0;
-      for (uint32_t u = first[v]; u < first[v + 1]; ++u) {
-         acc += weight(units[u]);
-         if (acc >= per_task || u + 1 == first[v + 1]) {
-            out.push_back(ChunkTask{v, u0, u + 1, 0});
-            u0 = u + 1;
-            acc = 0;
+      uint32_t ai = 0, oi = 0;
+      auto close = [&]() {
+         cur.a1 = ai;
+         cur.o1 = oi;
+         out.push_back(cur);
+         open = false;
+         acc = 0;
+      };
+      auto add = [&](uint32_t v, uint64_t w, bool array) {
+         if (open && v != cur.v0 && v != cur.v1 && cur.v1 != cur.v0) close();  // a third chunk
+         if (!open) {
+            cur = StreamRange{ai, 0, oi, 0, v, v, {0, 0}};
+            open = true;
+         }
+         cur.v1 = v;
+         (array ? ai : oi)++;
+         acc += w;
+         if (acc >= per) close();
+      };
+      for (uint32_t v = 0; v < nchunks; ++v) {
+         // merge the chunk's two lists so that other unit j follows array unit (j + 1/2) * na / no
+         const uint64_t na = P.afirst[v + 1] - P.afirst[v], no = P.ofirst[v + 1] - P.ofirst[v];
+         uint64_t ka = 0, ko = 0;
+         while (ka < na || ko < no) {
+            if (ko < no && (ka >= na || 2 * ka * no >= (2 * ko + 1) * na)) {
+               add(v, ow(P.ou[P.ofirst[v] + ko]), false);
+               ++ko;
+            } else {
+               add(v, aw(P.au[P.afirst[v] + ka]), true);
+               ++ka;
+            }
          }
       }
+      if (open) close();
+      // one wave; a table of more than 2 * ctas chunks needs more ranges than that (two chunks each)
+      if (out.size() <= ctas || per >= total) break;
    }
    return out;
 }
@@ -216,6 +265,7 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
    cuda_check(cudaSetDevice(device), "cudaSetDevice");
    try {
       cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+      mutations_setup();
       const uint32_t nchunks = t.nchunks();
       view_.nchunks = nchunks;
       view_.n_rows = t.n_rows;
@@ -232,16 +282,17 @@ Engine::Engine(const TableImage& t, int device) : table_(t), device_(device), pl
          d.nblk = upload(s.nblk);
          d.nblk_off = upload(s.nblk_off);
          {
-            std::vector<uint32_t> first;
-            const std::vector<StreamUnit> su = stream_units(s, nchunks, first);
-            d.su = upload(su);
-            d.nsu = static_cast<uint32_t>(su.size());
-            // one wave of the container pass's CTAs (six per SM: 40 registers per thread)
+            const PassUnits P = pass_units(s, nchunks);
+            d.au = upload(P.au);
+            d.ou = upload(P.ou);
+            d.nau = static_cast<uint32_t>(P.au.size());
+            // one wave of the container pass's CTAs
             int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), "SM count");
-            const std::vector<ChunkTask> tasks = chunk_tasks(s, su, first, static_cast<uint32_t>(std::max(sms, 1)) * 6u);
-            d.tasks = upload(tasks);
-            d.ntasks = static_cast<uint32_t>(tasks.size());
+            const std::vector<StreamRange> ranges =
+               pass_ranges(s, P, nchunks, static_cast<uint32_t>(std::max(sms, 1)) * RING_CTAS_PER_SM);
+            d.ranges = upload(ranges);
+            d.nranges = static_cast<uint32_t>(ranges.size());
          }
          d.exc_toff = upload(s.exc_toff);
          d.nblk_toff = upload(s.nblk_toff);

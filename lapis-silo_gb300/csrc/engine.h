@@ -25,11 +25,8 @@ struct CudaError : std::runtime_error {
 
 void cuda_check(cudaError_t e, const char* what);
 
-// Device error flag values set by the kernels' bounded waits when they give up (the filter kernel's
-// leaf copies, the Mutations container pass's unit copies); other values are program errors.
-enum : int { DEVERR_WAIT_FILTER = 6, DEVERR_WAIT_MUTATIONS = 7 };
-// Throws the exception of a nonzero device error flag: CudaError for a wait that gave up,
-// CompilationError for a malformed program.
+// Throws the exception of a nonzero device error flag: CudaError for a bounded wait that gave up
+// (DEVERR_WAIT_FILTER, DEVERR_WAIT_MUTATIONS), CompilationError for a malformed program.
 [[noreturn]] void throw_device_error(int code);
 
 // addMutationsToOutput on the host (reference: mutations_node.cpp:292-366): the rows of a column's

@@ -14,9 +14,10 @@
 // NOALLOC_MAX_POSITIONS positions; longer columns are rejected. Every call on a device uses the
 // same array, so calls whose work overlaps on that GPU (other streams, other threads, other
 // handles) race and must be serialised by the caller. The array keeps the last call's contents;
-// each call clears the part it uses before its kernels run. A device error of the pass would go to
-// the caller's status word, never to the handle's own error flag, so it could neither pass unseen
-// nor fall on a later call (the pass's kernels wait on nothing, so a completed pass leaves it 0).
+// each call clears the part it uses before its kernels run. A device error of the pass (a bounded
+// wait of the container pass for its bulk copies that gave up: 7) goes to the caller's status word,
+// never to the handle's own error flag, so it can neither pass unseen nor fall on a later call; a
+// completed pass leaves it 0.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -690,11 +690,11 @@ class Device:
         _check(lib().rhy_mutations_noalloc(self._h, column, C.c_void_p(d_filter), C.c_void_p(d_filter_count),
                                            C.c_void_p(d_counts), C.c_void_p(d_status), stream))
 
-    def test_withhold_copies(self, on: bool):
-        """Testing only: the filter kernels withhold the leaf payload copies their bounded waits
-        expect, so those waits give up and the calls report device error 6 (nothing is left in
-        flight)."""
-        _check(lib().rhy_test_withhold_copies(self._h, int(on)))
+    def test_withhold_copies(self, on: bool, container_pass: bool = False):
+        """Testing only: the filter kernels (on) and the Mutations container pass (container_pass)
+        withhold the bulk copies their bounded waits expect, so those waits give up and the calls
+        report device error 6 (filter) or 7 (container pass); nothing is left in flight."""
+        _check(lib().rhy_test_withhold_copies(self._h, (1 if on else 0) | (2 if container_pass else 0)))
 
     # ---- learned planner ----
     def planner_collect(self, exprs) -> int:
