@@ -27,6 +27,9 @@ cudaError_t mlp_forward(const __nv_bfloat16* d_w, const float* d_X, uint32_t n, 
 // and the loss to *d_loss.
 cudaError_t mlp_gradient(const __nv_bfloat16* d_w, const float* d_X, const float* d_T, uint32_t n, float* d_grad,
                          float* d_loss, cudaStream_t s);
+// A device error of the gradient kernel since the last call (1: a bounded wait for its tensor-core
+// products gave up; -1: the flag could not be read), cleared on reading; 0 if none.
+int mlp_take_error();
 // One Adam step (beta 0.9 / 0.999, eps 1e-8, bias-corrected at `step` >= 1) on the master weights;
 // refreshes the BF16 copy and clears the gradient.
 cudaError_t mlp_adam(float* d_master, __nv_bfloat16* d_w, float* d_grad, float* d_m, float* d_v, float lr, uint32_t step,

@@ -262,6 +262,7 @@ void PlannerNet::gradient(const float* X, const float* T, uint32_t n, float* gra
    if (loss) cuda_check(cudaMemcpyAsync(loss, d_loss_, sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
    if (Y) cuda_check(cudaMemcpyAsync(Y, d_Y_, static_cast<size_t>(n) * MLP_OUT * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
    cuda_check(cudaStreamSynchronize(s), "mlp gradient");
+   if (mlp_take_error() != 0) throw std::runtime_error("planner network: a bounded wait of the gradient kernel gave up");
    cuda_check(cudaMemsetAsync(d_grad_, 0, MLP_NPARAM * sizeof(float), s), "memset");
    cuda_check(cudaStreamSynchronize(s), "mlp gradient");
 }
@@ -299,6 +300,7 @@ float PlannerNet::train(const std::vector<float>& X, const std::vector<float>& T
       float loss = 0.0f;
       cuda_check(cudaMemcpyAsync(&loss, d_loss_, sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
       cuda_check(cudaStreamSynchronize(s), "train epoch");
+      if (mlp_take_error() != 0) throw std::runtime_error("planner network: a bounded wait of the gradient kernel gave up");
       last = loss / static_cast<float>(std::max(1u, nb));
    }
    return last;
