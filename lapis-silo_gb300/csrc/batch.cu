@@ -2,8 +2,8 @@
 //
 // The plain path streams every container once per query. Here the filters of a batch are
 // transposed into 16-bit query masks per row (bit q of group g = row in filter 16 g + q) and every
-// container element and event is read once per pass of up to 256 queries: a warp's lanes are the
-// query groups, each lane gathers its group's mask of the element's row and counts 16 queries in
+// container element and event is read once per pass of up to 256 queries. The container pass counts
+// 32 queries per lane in bit-sliced counters; the event pass gives each lane one 16-query group in
 // nibble counters. Results are bit-identical to the single-query kernels.
 //
 //   transpose_kernel       filter row sets -> masks, pass-major rows (32 B per row and pass)
@@ -115,32 +115,71 @@ struct NibbleCounter {
    }
 };
 
-// Counts the rows rowbase + x_t, t < cnt, of a window held one per lane in x (warp-uniform cnt
-// <= 32). Sub-warp `sub` of spw takes elements sub, sub + spw, ...; every lane adds its group's
-// masks, read from Rg (its group's column of the pass, `stride` u16 per row).
-__device__ __forceinline__ void count_window(NibbleCounter& k, uint32_t x, uint32_t cnt, uint32_t rowbase,
-                                             const uint16_t* __restrict__ Rg, uint32_t stride, bool gvalid,
-                                             uint32_t sub, uint32_t spw) {
-   constexpr uint32_t U = 8;  // gathers in flight per lane
-   const uint32_t per_lane = (cnt + spw - 1) / spw;
-   for (uint32_t i0 = 0; i0 < per_lane; i0 += U) {
-      uint32_t m[U];
+// Per-lane counters of the 32 queries of one mask word, as carry-save bit planes: bit q of ones,
+// twos and fours holds bits 0..2 of query q's count, and byte j of eb[k] counts the eights of query
+// 4k + j. Rows are added eight at a time by a Harley-Seal tree of carry-save adders (one LOP3 for
+// the sum and one for the carry of three words); the tree's carry-out word, the queries whose count
+// passed another multiple of eight, is spread into the byte counters (4 bits to 4 bytes by one
+// multiply). At most 255 blocks of eight rows fit the bytes; the caller flushes before that.
+struct BitCounter {
+   uint32_t ones, twos, fours;
+   uint32_t eb[8];
+   uint32_t blocks;
+
+   __device__ __forceinline__ void clear() {
+      ones = twos = fours = 0;
 #pragma unroll
-      for (uint32_t u = 0; u < U; ++u) {
-         const uint32_t t = (i0 + u) * spw + sub;
-         const uint32_t e = __shfl_sync(0xFFFFFFFFu, x, t & 31u);
-         m[u] = (t < cnt && gvalid) ? __ldg(Rg + static_cast<size_t>(rowbase + e) * stride) : 0u;
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < U; u += 2) k.add(__byte_perm(m[u], m[u + 1], 0x5410));
+      for (uint32_t k = 0; k < 8; ++k) eb[k] = 0;
+      blocks = 0;
    }
+   __device__ __forceinline__ static void csa(uint32_t& carry, uint32_t& sum, uint32_t a, uint32_t b, uint32_t c) {
+      const uint32_t u = a ^ b;
+      carry = (a & b) | (u & c);
+      sum = u ^ c;
+   }
+   __device__ __forceinline__ void add8(const uint32_t (&m)[8]) {
+      uint32_t twos_a, twos_b, fours_a, fours_b, eights;
+      csa(twos_a, ones, ones, m[0], m[1]);
+      csa(twos_b, ones, ones, m[2], m[3]);
+      csa(fours_a, twos, twos, twos_a, twos_b);
+      csa(twos_a, ones, ones, m[4], m[5]);
+      csa(twos_b, ones, ones, m[6], m[7]);
+      csa(fours_b, twos, twos, twos_a, twos_b);
+      csa(eights, fours, fours, fours_a, fours_b);
+#pragma unroll
+      for (uint32_t k = 0; k < 8; ++k) eb[k] += (((eights >> (4 * k)) & 0xFu) * 0x00204081u) & 0x01010101u;
+      ++blocks;
+   }
+   // query q's count: the three low planes plus eight times its byte counter
+   __device__ __forceinline__ uint32_t count(uint32_t q) const {
+      const uint32_t low = ((ones >> q) & 1u) | (((twos >> q) & 1u) << 1) | (((fours >> q) & 1u) << 2);
+      return low + 8u * ((eb[q >> 2] >> (8 * (q & 3))) & 0xFFu);
+   }
+};
+
+// Counts the rows rowbase + x_t, t < cnt, of a window held one per lane in x (warp-uniform cnt
+// <= 32). Lane group g = lane / 8 takes elements g, g + 4, ..., g + 28; every lane reads word
+// lane % 8 of each of its rows' masks (wp words per row, zero past wp) and adds the eight words.
+__device__ __forceinline__ void count_window_bits(BitCounter& k, uint32_t x, uint32_t cnt, uint32_t rowbase,
+                                                  const uint32_t* __restrict__ Rp, uint32_t wp, uint32_t lane) {
+   const uint32_t g = lane >> 3, w = lane & 7u;
+   uint32_t m[8];
+#pragma unroll
+   for (uint32_t i = 0; i < 8; ++i) {
+      const uint32_t t = 4 * i + g;
+      const uint32_t e = __shfl_sync(0xFFFFFFFFu, x, t);
+      m[i] = (t < cnt && w < wp) ? __ldg(Rp + static_cast<size_t>(rowbase + e) * wp + w) : 0u;
+   }
+   k.add8(m);
 }
 
 // One warp per (unit, pass): for every symbol present at the unit's position, the containers of
-// the unit's chunks are counted by all query groups of the pass (one lane per group in each of spw
-// sub-warps); the sub-warps' counts are summed with shuffles and added to counts once per symbol.
-// Bitset containers are expanded 1024 rows at a time into a per-warp row list in shared memory.
-__global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
+// the unit's chunks are counted for all queries of the pass. Lane (g, w) = (lane / 8, lane % 8)
+// adds mask word w (queries 32w .. 32w + 31 of the pass) of every fourth row of each 32-element
+// window into its bit-sliced counters; the four groups' counts are summed with shuffles and added
+// to counts once per symbol. Bitset containers are expanded 1024 rows at a time into a per-warp row
+// list in shared memory.
+__global__ void __launch_bounds__(BT, 4) mut_ctr_batch_kernel(const DevTable* __restrict__ tab, uint32_t col,
                                                            const CtrUnit* __restrict__ units, uint32_t n_units,
                                                            const uint16_t* __restrict__ R,
                                                            const uint32_t* __restrict__ lists, uint32_t nq_max,
@@ -156,16 +195,10 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
    const CtrDesc* __restrict__ ctrs = cs->ctrs;
    const uint16_t* __restrict__ payload = cs->payload;
    const uint32_t pass = blockIdx.y;
-   const uint32_t ngroups = (nq + MUT_GROUP - 1) / MUT_GROUP, nqc = (nq + 31) / 32;
-   const uint32_t gp = ngroups - PASS_GROUPS * pass < PASS_GROUPS ? ngroups - PASS_GROUPS * pass : PASS_GROUPS;
-   uint32_t gsz = 1;
-   while (gsz < gp) gsz <<= 1;
-   const uint32_t spw = 32 / gsz, sub = lane / gsz, gl = lane & (gsz - 1);
-   const bool gvalid = gl < gp;
-   const uint32_t g = PASS_GROUPS * pass + gl;
+   const uint32_t nqc = (nq + 31) / 32;
    const size_t rows = static_cast<size_t>(tab->nchunks) * CHUNK_ROWS;
-   const uint32_t stride = 2 * pass_width_u32(nqc, pass);
-   const uint16_t* Rg = R + static_cast<size_t>(pass) * rows * 16 + gl;
+   const uint32_t wp = pass_width_u32(nqc, pass);  // mask words per row in this pass
+   const uint32_t* Rp = reinterpret_cast<const uint32_t*>(R + static_cast<size_t>(pass) * rows * 16);
 
    const CtrUnit unit = units[u];
    const uint32_t p = unit.pos, v0 = unit.v0, nv = unit.v1 - unit.v0;
@@ -178,6 +211,7 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
    for (uint32_t i = cb; i < ce; ++i) symmask |= 1u << __ldg(&ctrs[i].sym);
    symmask = __reduce_or_sync(0xFFFFFFFFu, symmask);
    uint16_t* wl = list[warp];
+   const uint32_t g = lane >> 3, w = lane & 7u;
    while (symmask) {
       const uint32_t s = __ffs(symmask) - 1;
       symmask &= symmask - 1;
@@ -185,8 +219,26 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
       for (uint32_t i = cb; i < ce; ++i)
          if (__ldg(&ctrs[i].sym) == s) idx = i;
       uint32_t have = __ballot_sync(0xFFFFFFFFu, idx != 0xFFFFFFFFu);
-      NibbleCounter k;
+      BitCounter k;
       k.clear();
+      // adds the counters of the four lane groups and the counts of this word's 32 queries to the
+      // query tables, then clears (at the end of a symbol, or before the byte counters could wrap)
+      auto flush = [&]() {
+#pragma unroll
+         for (uint32_t q = 0; q < 32; ++q) {  // unrolled: the byte counters stay in registers
+            uint32_t c = k.count(q);
+            c += __shfl_xor_sync(0xFFFFFFFFu, c, 8);
+            c += __shfl_xor_sync(0xFFFFFFFFu, c, 16);
+            const uint32_t slot = 256 * pass + 32 * w + q;
+            if (g == 0 && w < wp && c && slot < nq)
+               atomicAdd(counts + static_cast<size_t>(lists[slot]) * per_query + static_cast<size_t>(s) * L + p, c);
+         }
+         k.clear();
+      };
+      auto window = [&](uint32_t x, uint32_t cnt, uint32_t rowbase) {
+         count_window_bits(k, x, cnt, rowbase, Rp, wp, lane);
+         if (k.blocks == 255) flush();
+      };
       while (have) {
          const uint32_t j = __ffs(have) - 1;
          have &= have - 1;
@@ -197,14 +249,16 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
          if (d.type == CT_ARRAY) {
             const uint32_t n = d.card_m1 + 1u;
             const uint16_t* a = payload + d.payload;
+            // container payloads stream through once: read them evict-first so that the masks the
+            // gathers reuse stay in L2
             for (uint32_t base = 0; base < n; base += 32) {
-               const uint32_t x = base + lane < n ? __ldg(a + base + lane) : 0u;
-               count_window(k, x, n - base < 32 ? n - base : 32u, rowbase, Rg, stride, gvalid, sub, spw);
+               const uint32_t x = base + lane < n ? __ldcs(a + base + lane) : 0u;
+               window(x, n - base < 32 ? n - base : 32u, rowbase);
             }
          } else if (d.type == CT_BITSET) {
             const uint32_t* bits = reinterpret_cast<const uint32_t*>(payload + d.payload);
             for (uint32_t wb = 0; wb < CHUNK_WORDS; wb += 32) {
-               uint32_t x = __ldg(bits + wb + lane);
+               uint32_t x = __ldcs(bits + wb + lane);
                const uint32_t c = __popc(x);
                uint32_t incl = c;
 #pragma unroll
@@ -222,7 +276,7 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
                __syncwarp();
                for (uint32_t base = 0; base < total; base += 32) {
                   const uint32_t y = base + lane < total ? wl[base + lane] : 0u;
-                  count_window(k, y, total - base < 32 ? total - base : 32u, rowbase, Rg, stride, gvalid, sub, spw);
+                  window(y, total - base < 32 ? total - base : 32u, rowbase);
                }
                __syncwarp();
             }
@@ -230,23 +284,11 @@ __global__ void __launch_bounds__(BT) mut_ctr_batch_kernel(const DevTable* __res
             const uint16_t* r = payload + d.payload;
             for (uint32_t i = 0; i < d.nruns; ++i) {
                const uint32_t s0 = __ldg(r + 2 * i), n = __ldg(r + 2 * i + 1) + 1u;
-               for (uint32_t base = 0; base < n; base += 32)
-                  count_window(k, s0 + base + lane, n - base < 32 ? n - base : 32u, rowbase, Rg, stride, gvalid, sub,
-                               spw);
+               for (uint32_t base = 0; base < n; base += 32) window(s0 + base + lane, n - base < 32 ? n - base : 32u, rowbase);
             }
          }
       }
-      k.drain();
-#pragma unroll
-      for (uint32_t q = 0; q < MUT_GROUP; ++q)
-         for (uint32_t o = 16; o >= gsz; o >>= 1) k.c[q] += __shfl_down_sync(0xFFFFFFFFu, k.c[q], o);
-      if (sub == 0 && gvalid) {
-#pragma unroll
-         for (uint32_t q = 0; q < MUT_GROUP; ++q)
-            if (k.c[q] && MUT_GROUP * g + q < nq)
-               atomicAdd(counts + static_cast<size_t>(lists[MUT_GROUP * g + q]) * per_query + static_cast<size_t>(s) * L + p,
-                         k.c[q]);
-      }
+      if (k.blocks) flush();
    }
 }
 
