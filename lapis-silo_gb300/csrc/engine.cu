@@ -1073,8 +1073,8 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
    // first the Mutations and Details queries, in parts of at most PIPELINE_HEAVY (the device splits
    // a part's dense Mutations queries into passes of 256, and sparse ones take no pass, so one part
    // reads the containers as few times as the whole batch would), so that the device starts after
-   // they are planned (without any: the first quarter of the counts); then the counts, planned
-   // while the first part runs
+   // they are planned (without any: the first quarter of the counts); then the counts, in parts
+   // planned while the parts before them run
    std::vector<std::vector<uint32_t>> parts(1);
    std::vector<uint32_t> light, heavy;
    for (uint32_t i = 0; i < n; ++i) {
@@ -1094,8 +1094,16 @@ size_t Engine::batch_rows_pipelined(const std::vector<std::string>& exprs, const
       parts[0].assign(light.begin(), light.begin() + first);
    }
    if (first < light.size()) {
-      if (light.size() - first < PIPELINE_PART) parts.back().insert(parts.back().end(), light.begin() + first, light.end());
-      else parts.emplace_back(light.begin() + first, light.end());
+      const size_t rest = light.size() - first;
+      if (rest < PIPELINE_PART) {
+         parts.back().insert(parts.back().end(), light.begin() + first, light.end());
+      } else {
+         // counts in parts of about PIPELINE_COUNTS, so that the planning of each overlaps the
+         // device work of the part before it
+         const size_t k = std::max<size_t>(1, (rest + PIPELINE_COUNTS / 2) / PIPELINE_COUNTS);
+         for (size_t j = 0; j < k; ++j)
+            parts.emplace_back(light.begin() + first + rest * j / k, light.begin() + first + rest * (j + 1) / k);
+      }
    }
    while (parts_.size() + 1 < parts.size()) parts_.push_back(std::make_unique<BatchState>());
    std::vector<BatchState*> states(parts.size());

@@ -238,11 +238,12 @@ class Engine {
    // batch_rows of a whole batch given as text, planned and run in parts so that the host plans a
    // part while the device runs the ones before it: first the Mutations and Details queries in
    // parts of at most PIPELINE_HEAVY (the first quarter of the counts when there are none), then
-   // the Aggregated counts. Results equal batch_rows of the whole batch; the rows come in part
-   // order. A counts part of fewer than PIPELINE_PART queries joins the part before it. The caller
-   // holds mu.
+   // the Aggregated counts in parts of about PIPELINE_COUNTS. Results equal batch_rows of the whole
+   // batch; the rows come in part order. Counts fewer than PIPELINE_PART join the part before them.
+   // The caller holds mu.
    static constexpr uint32_t PIPELINE_PART = 256;
    static constexpr uint32_t PIPELINE_HEAVY = 1024;
+   static constexpr uint32_t PIPELINE_COUNTS = 768;
    size_t batch_rows_pipelined(const std::vector<std::string>& exprs, const int* actions, const uint32_t* columns,
                                const double* min_proportions, uint32_t tile_bits, cudaStream_t stream,
                                DevMutationRow* rows, size_t cap, uint64_t* counts, uint64_t* row_begin,
