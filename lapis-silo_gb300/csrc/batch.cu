@@ -485,6 +485,10 @@ __global__ void __launch_bounds__(MUT_SEG) mut_final_batch_kernel(const DevTable
    const DevSeqCol* cs = &tab->seq[col];
    const uint32_t q = blockIdx.y, L = cs->L;
    const uint32_t total = static_cast<uint32_t>(fcounts[slot_query[q]]);
+   if (total == 0) {  // an empty filter: its counts stay zero and it has no rows
+      if (rowblk != nullptr && threadIdx.x == 0) rowblk[static_cast<size_t>(q) * gridDim.x + blockIdx.x] = 0;
+      return;
+   }
    uint32_t* c = counts + static_cast<size_t>(q) * cs->nsym * L;
    final_position_counts(cs, total, c, scratch + static_cast<size_t>(q) * mut_scratch_words(L), red);
    if (rowblk == nullptr) return;
