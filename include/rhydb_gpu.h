@@ -163,6 +163,15 @@ int rhy_local_reference(const RhyTable* t, uint32_t column, char* out, size_t ca
  * chunk, symbol, cardinality and encoding (0 array, 1 bitset, 2 run). Pass cap = 0 to size. */
 int rhy_seq_containers(const RhyTable* t, uint32_t column, uint32_t* pos, uint16_t* chunk, uint8_t* sym, uint32_t* card,
                        uint8_t* type, size_t cap, size_t* n);
+/* The plan of the Mutations container pass over sequence column `column` (no counterpart in the
+ * reference; for tests and tuning), for `ctas` CTAs. Array units as 5 u32 each: first payload element
+ * (a multiple of 8), element count (at most 1,024), first descriptor (index in storage order, as
+ * rhy_seq_containers lists them), descriptor count, chunk. Bitset and run units as 4 u32 each: kind
+ * (1 bitset, 2 run), chunk, first payload element, descriptor. CTA ranges as 6 u32 each: array
+ * units [a0, a1), other units [o0, o1), chunks v0 and v1. Pass all caps 0 to size. */
+int rhy_container_pass_plan(const RhyTable* t, uint32_t column, uint32_t ctas, uint32_t* array_units, size_t array_cap,
+                            size_t* n_array, uint32_t* other_units, size_t other_cap, size_t* n_other, uint32_t* ranges,
+                            size_t range_cap, size_t* n_ranges);
 /* Newline-separated seeded random filter expressions (trees of at most max_leaves leaves, 0 = no
  * limit); *needed receives the byte count (incl. NUL). */
 int rhy_generate_queries(const RhyTable* t, uint64_t seed, uint32_t n, uint32_t max_depth, uint32_t max_nof_children,

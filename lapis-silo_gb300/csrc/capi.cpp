@@ -18,6 +18,7 @@
 #include "ingest.h"
 #include "noalloc.h"
 #include "op_program.h"
+#include "pass_plan.h"
 #include "table.h"
 
 struct RhyTable {
@@ -397,6 +398,57 @@ int rhy_seq_containers(const RhyTable* t, uint32_t column, uint32_t* pos, uint16
          sym[i] = ctrs[i].sym;
          card[i] = ctrs[i].card_m1 + 1u;
          type[i] = ctrs[i].type;
+      }
+   });
+}
+
+int rhy_container_pass_plan(const RhyTable* t, uint32_t column, uint32_t ctas, uint32_t* array_units, size_t array_cap,
+                            size_t* n_array, uint32_t* other_units, size_t other_cap, size_t* n_other, uint32_t* ranges,
+                            size_t range_cap, size_t* n_ranges) {
+   return guarded([&] {
+      need(t, "table");
+      need(n_array, "n_array");
+      need(n_other, "n_other");
+      need(n_ranges, "n_ranges");
+      const rhygpu::SeqColumnImage& col = t->image.seq.at(column);
+      const uint32_t nchunks = t->image.nchunks();
+      const rhygpu::PassUnits P = rhygpu::pass_units(col, nchunks);
+      const std::vector<rhygpu::StreamRange> R = rhygpu::pass_ranges(col, P, nchunks, ctas);
+      *n_array = P.au.size();
+      *n_other = P.ou.size();
+      *n_ranges = R.size();
+      if (array_cap == 0 && other_cap == 0 && range_cap == 0) return;
+      if (array_cap < P.au.size() || other_cap < P.ou.size() || range_cap < R.size())
+         throw std::invalid_argument("buffer too small");
+      need(array_units, "array_units");
+      need(other_units, "other_units");
+      need(ranges, "ranges");
+      for (size_t i = 0; i < P.au.size(); ++i) {
+         const rhygpu::ArrUnit& u = P.au[i];
+         uint32_t* o = array_units + 5 * i;
+         o[0] = u.e0;
+         o[1] = u.n;
+         o[2] = u.c0;
+         o[3] = u.nd;
+         o[4] = u.v;
+      }
+      for (size_t i = 0; i < P.ou.size(); ++i) {
+         const rhygpu::OtherUnit& u = P.ou[i];
+         uint32_t* o = other_units + 4 * i;
+         o[0] = u.kind;
+         o[1] = u.v;
+         o[2] = u.e0;
+         o[3] = u.c;
+      }
+      for (size_t i = 0; i < R.size(); ++i) {
+         const rhygpu::StreamRange& r = R[i];
+         uint32_t* o = ranges + 6 * i;
+         o[0] = r.a0;
+         o[1] = r.a1;
+         o[2] = r.o0;
+         o[3] = r.o1;
+         o[4] = r.v0;
+         o[5] = r.v1;
       }
    });
 }

@@ -10,6 +10,7 @@
 #include <numeric>
 #include <unordered_map>
 
+#include "pass_plan.h"
 #include "util.h"
 
 namespace rhygpu {
@@ -105,17 +106,6 @@ std::vector<CtrUnit> container_units(const SeqColumnImage& s, uint32_t nchunks) 
    return out;
 }
 
-// Units of the Mutations container pass, chunk by chunk: the chunk's array payloads (back to back
-// in descriptor order) cut into pieces of at most WU elements starting on 8-element (16-byte)
-// boundaries, each with the descriptors that cover the arrays overlapping it, then one unit per
-// bitset and run container. A piece ends early, before the first array whose descriptor would not
-// fit, where more than WU_DESC descriptors would be needed. afirst[v] / ofirst[v]: the first array /
-// other unit of chunk v (nchunks + 1 entries).
-struct PassUnits {
-   std::vector<ArrUnit> au;
-   std::vector<OtherUnit> ou;
-   std::vector<uint32_t> afirst, ofirst;
-};
 PassUnits pass_units(const SeqColumnImage& s, uint32_t nchunks) {
    const ContainerSet& cs = s.vertical;
    PassUnits P;
@@ -160,9 +150,7 @@ PassUnits pass_units(const SeqColumnImage& s, uint32_t nchunks) {
    return P;
 }
 
-// CTAs of the container pass: the units of each chunk, its bitset and run units spread evenly among
-// its array units, cut into at most `ctas` ranges of about the same counting time, none spanning
-// more than two chunks. The weights are a consumer warp's cycles per unit, measured on the 2M-row
+// The weights of the ranges are a consumer warp's cycles per unit, measured on the 2M-row
 // benchmark table: an array unit costs a fixed part plus its elements and descriptors; a bitset,
 // read by one warp straight from global memory, costs about one and a half array units.
 std::vector<StreamRange> pass_ranges(const SeqColumnImage& s, const PassUnits& P, uint32_t nchunks, uint32_t ctas) {

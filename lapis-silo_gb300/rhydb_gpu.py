@@ -197,6 +197,8 @@ def lib():
         "rhy_table_raw": (I, [P, C.POINTER(RawTable)]),
         "rhy_local_reference": (I, [P, U32, C.c_char_p, C.c_size_t]),
         "rhy_seq_containers": (I, [P, U32, P, P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rhy_container_pass_plan": (I, [P, U32, U32, P, C.c_size_t, C.POINTER(C.c_size_t), P, C.c_size_t,
+                                        C.POINTER(C.c_size_t), P, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_generate_queries": (I, [P, U64, U32, U32, U32, U32, I, I, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rhy_table_free": (None, [P]),
         "rhy_plan": (I, [P, C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(U32), C.POINTER(U32)]),
@@ -387,6 +389,20 @@ class Table:
             _check(lib().rhy_seq_containers(self._h, column, _ptr(pos), _ptr(chunk), _ptr(sym), _ptr(card), _ptr(typ),
                                             m, C.byref(n)))
         return pos, chunk, sym, card, typ
+
+    def container_pass_plan(self, column: int, ctas: int):
+        """The Mutations container pass's plan for `ctas` CTAs: array units (n x 5: first element,
+        elements, first descriptor, descriptors, chunk), bitset / run units (n x 4: kind, chunk,
+        first element, descriptor) and CTA ranges (n x 6: a0, a1, o0, o1, v0, v1), as uint32 arrays."""
+        na, no, nr = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        _check(lib().rhy_container_pass_plan(self._h, column, ctas, None, 0, C.byref(na), None, 0, C.byref(no), None, 0,
+                                             C.byref(nr)))
+        au = np.zeros((na.value, 5), np.uint32)
+        ou = np.zeros((no.value, 4), np.uint32)
+        rg = np.zeros((nr.value, 6), np.uint32)
+        _check(lib().rhy_container_pass_plan(self._h, column, ctas, _ptr(au), max(na.value, 1), C.byref(na), _ptr(ou),
+                                             max(no.value, 1), C.byref(no), _ptr(rg), max(nr.value, 1), C.byref(nr)))
+        return au, ou, rg
 
     def queries(self, n: int, seed: int = 43, max_depth: int = 4, max_nof_children: int = 8, use_aa: bool = False,
                 use_metadata: bool = False, max_leaves: int = 0) -> list[str]:
