@@ -55,9 +55,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(b) : "memory");
 }
 
-// Waits for the phase of `bar` with the given parity like mbar_wait, but polls without a suspend
-// hint and sleeps between polls (backing off up to max_sleep_ns), so that a warp waiting on the
-// ring takes few issue slots from the warps that count. Bounded by limit_ns; false if it gave up.
+// Waits for the phase of `bar` with the given parity to complete. It polls without a suspend hint
+// and sleeps between polls (backing off up to max_sleep_ns), so that a warp waiting on the ring
+// takes few issue slots from the warps that count. Bounded by limit_ns on the global timer and by
+// 2^26 polls; false if it gave up.
 __device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity, uint32_t max_sleep_ns, uint64_t limit_ns) {
    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
    uint64_t t0 = 0;

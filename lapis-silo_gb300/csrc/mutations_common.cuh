@@ -44,27 +44,6 @@ __device__ __forceinline__ uint64_t global_ns() {
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
 constexpr uint64_t WAIT_LIMIT_TEST_NS = 1000000ull;
 
-// Waits for the phase with the given parity to complete, bounded by time (limit_ns on the global
-// timer) and, as a second bound, by 2^26 polls of at most about 1 us each. Returns false if it gave
-// up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = WAIT_LIMIT_NS) {
-   const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
-   uint64_t t0 = 0;
-   for (uint32_t i = 0; i < (1u << 26); ++i) {
-      uint32_t done;
-      asm volatile(
-         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
-         : "=r"(done)
-         : "r"(b), "r"(parity), "r"(1000u)
-         : "memory");
-      if (done) return true;
-      const uint64_t now = global_ns();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > limit_ns) return false;
-   }
-   return false;
-}
-
 // popcount of F in [a, b)
 __device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, uint32_t b) {
    if (a >= b) return 0;
@@ -77,12 +56,6 @@ __device__ __forceinline__ uint32_t count_range(const uint32_t* F, uint32_t a, u
       s += __popc(F[w] & m);
    }
    return s;
-}
-
-// element t (0..7) of eight packed u16 values
-__device__ __forceinline__ uint32_t u16_of(const uint4& w, uint32_t t) {
-   const uint32_t x = t < 2 ? w.x : t < 4 ? w.y : t < 6 ? w.z : w.w;
-   return (t & 1u) ? (x >> 16) : (x & 0xFFFFu);
 }
 
 __device__ __forceinline__ uint32_t block_incl_scan_u32(uint32_t v, uint32_t* red) {
